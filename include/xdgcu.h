@@ -1,0 +1,225 @@
+/*
+ * xdgcu.h -- C ABI of the GB300 (sm_103a) ray-query engine for XDG.
+ *
+ * This is the boundary a CUDA backend of XDG's RayTracer plugin API binds
+ * (include/xdg/ray_tracing_interface.h:16-147 in the reference).  Each entry
+ * point below names the reference interface it replaces.  Plain C types
+ * only: pointers, sizes, int32 ids.  No exceptions cross it; every function
+ * returns an xdgcu_status and xdgcu_last_error() describes the last failure.
+ *
+ * Conventions (reference semantics):
+ *   - ids are int32 (constants.h:73-87); ID_NONE = TREE_NONE = -1;
+ *   - surface and element tree ids are separate counters starting at 1
+ *     (ray_tracing_interface.cpp:10-18);
+ *   - a miss is {t = INFTY (DBL_MAX), surface = ID_NONE} (embree/ray_tracer.cpp:320-321);
+ *   - positions/directions are n x 3 doubles (AoS), as Position/Direction.
+ *
+ * Batched queries take `n` rays and either one tree (`tree` > 0,
+ * `ray_trees` = NULL) or one tree per ray (`ray_trees` != NULL, `tree`
+ * ignored).  Input and output pointers may be device memory (the fast path:
+ * the work is enqueued on `stream` and the call returns without
+ * synchronising) or host memory (the call stages through pinned buffers and
+ * returns when the results are in the caller's arrays).  The two kinds may
+ * not be mixed within one call.
+ *
+ * Precision: XDGCU_FP64 evaluates everything in double precision (the plain
+ * drop-in); XDGCU_MIXED runs FP32 box tests and an FP32 Plucker pre-filter
+ * with a proven error bound, escalating to the FP64 test wherever the FP32
+ * answer is not certain.  Both return bit-identical ids and distances.
+ *
+ * Tie rule: when two accepted candidates are at exactly the same distance,
+ * the lowest mesh id wins (face id for ray_fire / point_in_volume / closest,
+ * element id for find_element).  The reference leaves this to Embree's
+ * traversal order.
+ */
+#ifndef XDGCU_H
+#define XDGCU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct xdgcu_ctx xdgcu_ctx;
+
+typedef enum {
+  XDGCU_OK = 0,
+  XDGCU_ERR_INVALID_ARG = 1,
+  XDGCU_ERR_CUDA = 2,
+  XDGCU_ERR_NOT_FOUND = 3,
+  XDGCU_ERR_OUT_OF_MEMORY = 4,
+  XDGCU_ERR_STATE = 5
+} xdgcu_status;
+
+/* per-ray status codes written to the optional `status` arrays */
+enum {
+  XDGCU_RAY_OK = 0,
+  XDGCU_RAY_INVALID = 1,        /* NaN/inf origin or direction, or bad tree id */
+  XDGCU_RAY_STACK_OVERFLOW = 2, /* traversal stack exhausted (result incomplete) */
+  XDGCU_RAY_WALK_LIMIT = 4,     /* walk stopped at max_segs (output truncated) */
+  XDGCU_RAY_NO_EXIT_FACE = 5    /* next_element found no exiting face */
+};
+
+/* shared_enums.h:11-15 */
+enum { XDGCU_ANY = -1, XDGCU_EXITING = 0, XDGCU_ENTERING = 1 };
+
+enum { XDGCU_FP64 = 0, XDGCU_MIXED = 1 };
+
+/* ------------------------------------------------------------------------
+ * Context
+ * ------------------------------------------------------------------------ */
+
+/* Replaces the backend constructor (embree/ray_tracer.cpp:15-19).  Binds the
+ * context to CUDA device `device`. */
+int xdgcu_create(xdgcu_ctx** ctx, int device);
+
+/* Replaces the backend destructor (embree/ray_tracer.cpp:21-24). */
+int xdgcu_destroy(xdgcu_ctx* ctx);
+
+/* Human-readable description of the last failed call on this context (never
+ * NULL; "" when none).  The pointer stays valid until the next call. */
+const char* xdgcu_last_error(const xdgcu_ctx* ctx);
+
+/* Library version (major*10000 + minor*100 + patch). */
+int xdgcu_version(void);
+
+/* ------------------------------------------------------------------------
+ * Geometry registration and tree builds
+ * ------------------------------------------------------------------------ */
+
+/* Uploads one surface's triangles: tri_xyz holds 9 doubles per face (the
+ * face's three vertices in mesh order, as MeshManager::face_vertices returns
+ * them), face_ids the mesh face ids.  Replaces the first-visit branch of
+ * EmbreeRayTracer::register_surface (embree/ray_tracer.cpp:107-147).  A
+ * surface may be registered once. */
+int xdgcu_register_surface(xdgcu_ctx* ctx, int32_t surface_id, int64_t n_faces,
+                           const double* tri_xyz, const int32_t* face_ids);
+
+/* Builds a surface tree over the given registered surfaces and returns its
+ * tree id.  sense[i] = 0 when the tree's volume is surface i's forward
+ * volume, 1 when it is the reverse volume (normals are flipped for that tree,
+ * triangle_intersect.cpp:84-87).  bump is the box dilation
+ * (ray_tracing_interface.cpp:20-24); the tree's boxes use, per surface, the
+ * largest bump of any tree the surface belongs to, as
+ * embree/ray_tracer.cpp:76-89 does.  Replaces
+ * RayTracer::create_surface_tree (embree/ray_tracer.cpp:49-105). */
+int xdgcu_create_surface_tree(xdgcu_ctx* ctx, const int32_t* surface_ids, const int32_t* sense,
+                              int32_t n_surfaces, double bump, int32_t* tree_out);
+
+/* Builds the global surface tree over every registered surface (no normal
+ * flips).  Replaces create_global_surface_tree (embree/ray_tracer.cpp:190-206). */
+int xdgcu_create_global_surface_tree(xdgcu_ctx* ctx, int32_t* tree_out);
+
+/* Uploads the tet mesh used by find_element and the element walk: vertex
+ * coordinates (3 per vertex), connectivity (4 vertex indices per tet),
+ * adjacency (4 neighbour tet indices per tet, -1 on the boundary, in face
+ * order), the per-element mesh ids, and the 4x3 local face table of the mesh
+ * library's ElementFaceAccessor (e.g. MOAB's {0,1,3},{1,2,3},{2,0,3},{0,2,1},
+ * moab/direct_access.h:181-183).  Replaces what MeshManager::next_element
+ * reads through ElementFaceAccessor / adjacent_element
+ * (mesh_manager_interface.cpp:149-200).  May be called once. */
+int xdgcu_set_tet_mesh(xdgcu_ctx* ctx, int64_t n_vertices, const double* xyz, int64_t n_tets,
+                       const int32_t* conn, const int32_t* adj, const int32_t* elem_ids,
+                       const int32_t face_table[12]);
+
+/* Builds an element tree over the given tet indices (of the mesh above) and
+ * returns its tree id.  Replaces RayTracer::create_element_tree
+ * (embree/ray_tracer.cpp:149-188). */
+int xdgcu_create_element_tree(xdgcu_ctx* ctx, const int32_t* tet_indices, int64_t n,
+                              int32_t* tree_out);
+
+/* Builds the global element tree over all tets in every element tree.
+ * Replaces create_global_element_tree (embree/ray_tracer.cpp:208-224). */
+int xdgcu_create_global_element_tree(xdgcu_ctx* ctx, int32_t* tree_out);
+
+/* Number of surface / element trees built so far (num_registered_*_trees,
+ * ray_tracing_interface.h:121-123). */
+int xdgcu_num_surface_trees(const xdgcu_ctx* ctx);
+int xdgcu_num_element_trees(const xdgcu_ctx* ctx);
+
+/* ------------------------------------------------------------------------
+ * Batched queries
+ * ------------------------------------------------------------------------ */
+
+/* RayTracer::ray_fire (ray_tracing_interface.h:81-86; embree/ray_tracer.cpp:
+ * 289-326; triangle_intersect.cpp:52-109).  dist_limit: n doubles or NULL
+ * (INFTY).  Exclusions in CSR form: excl_offsets (n+1) and excl_ids, or both
+ * NULL.  Outputs: t_out (INFTY on a miss), surface_out (ID_NONE on a miss),
+ * face_out (the hit face id the reference appends to its exclude list;
+ * may be NULL), status (may be NULL). */
+int xdgcu_ray_fire(xdgcu_ctx* ctx, int32_t tree, const int32_t* ray_trees, int64_t n,
+                   const double* origins, const double* directions, const double* dist_limit,
+                   int32_t orientation, const int32_t* excl_offsets, const int32_t* excl_ids,
+                   double* t_out, int32_t* surface_out, int32_t* face_out, int32_t* status,
+                   int32_t precision, void* stream);
+
+/* RayTracer::point_in_volume (ray_tracing_interface.h:76-79;
+ * embree/ray_tracer.cpp:259-287).  directions may be NULL: the reference's
+ * default direction (1/sqrt(2), 1/sqrt(2), 0) is used.  inside_out: 1/0. */
+int xdgcu_point_in_volume(xdgcu_ctx* ctx, int32_t tree, const int32_t* ray_trees, int64_t n,
+                          const double* points, const double* directions,
+                          const int32_t* excl_offsets, const int32_t* excl_ids,
+                          int32_t* inside_out, int32_t* status, int32_t precision, void* stream);
+
+/* RayTracer::occluded (ray_tracing_interface.h:112-115; embree/ray_tracer.cpp:
+ * 347-370).  occluded_out: 1/0; dist_out (may be NULL): -INFTY when occluded,
+ * INFTY otherwise, the value the reference writes through its `dist`. */
+int xdgcu_occluded(xdgcu_ctx* ctx, int32_t tree, const int32_t* ray_trees, int64_t n,
+                   const double* origins, const double* directions, int32_t* occluded_out,
+                   double* dist_out, int32_t* status, int32_t precision, void* stream);
+
+/* RayTracer::closest (ray_tracing_interface.h:109-110; embree/ray_tracer.cpp:
+ * 328-345).  Outputs the distance and the nearest face id. */
+int xdgcu_closest(xdgcu_ctx* ctx, int32_t tree, const int32_t* ray_trees, int64_t n,
+                  const double* points, double* dist_out, int32_t* face_out, int32_t* status,
+                  int32_t precision, void* stream);
+
+/* RayTracer::find_element (ray_tracing_interface.h:98-107; embree/ray_tracer.cpp:
+ * 226-257).  tree = an element tree id.  Outputs the element mesh id
+ * (ID_NONE when no element contains the point) and/or its tet index. */
+int xdgcu_find_element(xdgcu_ctx* ctx, int32_t tree, const int32_t* ray_trees, int64_t n,
+                       const double* points, int32_t* elem_id_out, int32_t* elem_index_out,
+                       int32_t* status, int32_t precision, void* stream);
+
+/* MeshManager::next_element (mesh_manager_interface.cpp:149-200) for n rays:
+ * elem_index = tet index; outputs the next tet index (-1 when leaving the
+ * mesh) and the exit distance. */
+int xdgcu_next_element(xdgcu_ctx* ctx, int64_t n, const int32_t* elem_index,
+                       const double* positions, const double* directions, int32_t* next_out,
+                       double* dist_out, int32_t* status, int32_t precision, void* stream);
+
+/* MeshManager::walk_elements (mesh_manager_interface.cpp:106-136) for n
+ * tracks starting in tet start_index[i] at start[i], direction u[i] (unit),
+ * length distance[i].  Output is track-major with stride max_segs:
+ * seg_elem[i*max_segs + k] (element MESH ids) and seg_len[...]; seg_count[i]
+ * = number of segments (zero-length ones included, as the reference keeps
+ * them); status[i] = XDGCU_RAY_WALK_LIMIT when the track needed more than
+ * max_segs segments. */
+int xdgcu_walk_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
+                        const double* start, const double* u, const double* distance,
+                        int32_t max_segs, int32_t* seg_elem, double* seg_len,
+                        int32_t* seg_count, int32_t* status, int32_t precision, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Diagnostics
+ * ------------------------------------------------------------------------ */
+
+/* Per-launch work counters of the last query run with counting enabled:
+ * counters[0] = box tests, [1] = node fetches, [2] = primitive tests,
+ * [3] = FP64 escalations, [4] = rays, [5] = walk steps.  Counting is enabled
+ * with xdgcu_set_counting(ctx, 1) and slows queries down; it exists to
+ * compute algorithmic bytes for roofline reports. */
+int xdgcu_set_counting(xdgcu_ctx* ctx, int32_t enable);
+int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
+
+/* Tree statistics: out[0] = nodes, [1] = primitives, [2] = depth,
+ * [3] = bytes of FP32 nodes, [4] = bytes of FP64 nodes. */
+int xdgcu_surface_tree_info(const xdgcu_ctx* ctx, int32_t tree, int64_t out[8]);
+int xdgcu_element_tree_info(const xdgcu_ctx* ctx, int32_t tree, int64_t out[8]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XDGCU_H */

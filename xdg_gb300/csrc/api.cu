@@ -1,0 +1,1054 @@
+// api.cu -- the C ABI declared in include/xdgcu.h.
+//
+// A context owns every device copy of the geometry: the registered surface
+// triangles (FP64, mesh vertex order), the tet mesh (FP64 + FP32 vertices,
+// connectivity, adjacency), and one 4-wide BVH per tree with its primitives
+// re-laid out in leaf order.  Callers keep ownership of their own arrays; they
+// are only read during the call.
+//
+// Query calls accept device pointers (enqueued on the caller's stream, no
+// synchronisation) or host pointers (staged through a per-thread device
+// workspace and stream, synchronised before returning), so the scalar,
+// one-ray-per-call use of the reference API can run concurrently from many
+// host threads.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/xdgcu.h"
+#include "bvh.h"
+#include "queries.h"
+#include "walk.h"
+
+using namespace xdgcu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct SurfaceRec {
+  int32_t id;
+  int64_t first;
+  int64_t count;
+  int32_t fwd_tree = -1;
+  int32_t rev_tree = -1;
+  double bump = 0.0;
+};
+
+struct TreeHost {
+  int32_t id = -1;
+  int32_t kind = TREE_SURFACE;
+  Node32* n32 = nullptr;
+  Node64* n64 = nullptr;
+  DevMem<float4> prim32;
+  DevMem<double> prim64;
+  DevMem<int32_t> prim_ref;
+  int32_t n_nodes = 0;
+  int32_t depth = 0;
+  TreeDev dev{};
+  std::vector<int32_t> members;  // surfaces (surface tree) or tet indices (element tree)
+  ~TreeHost() {
+    if (n32) cudaFree(n32);
+    if (n64) cudaFree(n64);
+  }
+};
+
+struct Slot {
+  cudaStream_t stream = nullptr;
+  DevMem<char> buf;
+  ~Slot() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+int set_err(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_err(cudaError_t e, const char* what) {
+  return set_err(XDGCU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define API_CUDA(x, what)                         \
+  do {                                            \
+    cudaError_t e_ = (x);                         \
+    if (e_ != cudaSuccess) return cuda_err(e_, what); \
+  } while (0)
+
+constexpr int32_t kLeafMax = 4;
+const int32_t kMoabFaces[12] = {0, 1, 3, 1, 2, 3, 2, 0, 3, 0, 2, 1};
+
+// ---------------------------------------------------------------------------
+// build-time kernels
+// ---------------------------------------------------------------------------
+
+__global__ void k_tri_boxes(const double* __restrict__ tri_xyz, const int32_t* __restrict__ tris,
+                            const double* __restrict__ bump, int32_t n, double* __restrict__ box) {
+  int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* v = tri_xyz + 9 * (int64_t)tris[i];
+  for (int c = 0; c < 3; ++c) {
+    // bbox.h:104-111 + triangle_intersect.cpp:36-50
+    const double lo = fmin(fmin(v[c], v[3 + c]), v[6 + c]);
+    const double hi = fmax(fmax(v[c], v[3 + c]), v[6 + c]);
+    box[6 * (int64_t)i + c] = lo - bump[i];
+    box[6 * (int64_t)i + 3 + c] = hi + bump[i];
+  }
+}
+
+__global__ void k_tri_gather(const double* __restrict__ tri_xyz, const int32_t* __restrict__ tris,
+                             const int32_t* __restrict__ order, int32_t n,
+                             float4* __restrict__ prim32, double* __restrict__ prim64,
+                             int32_t* __restrict__ prim_ref) {
+  int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int32_t g = tris[order[j]];
+  const double* v = tri_xyz + 9 * (int64_t)g;
+  double* o = prim64 + kPrim64Stride * (int64_t)j;
+  for (int k = 0; k < 9; ++k) o[k] = v[k];
+  o[9] = 0.0;
+  prim_ref[j] = g;
+  const double e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+  const double e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+  double emax = 0.0;
+  for (int c = 0; c < 3; ++c) {
+    emax = fmax(emax, fabs(e1[c]));
+    emax = fmax(emax, fabs(e2[c]));
+    emax = fmax(emax, fabs(e2[c] - e1[c]));
+  }
+  const float v0x = __double2float_rn(v[0]), v0y = __double2float_rn(v[1]),
+              v0z = __double2float_rn(v[2]);
+  const float v0abs = fmaxf(fabsf(v0x), fmaxf(fabsf(v0y), fabsf(v0z)));
+  // the edge bound must cover the exact edges and the FP32 difference of the
+  // stored edges, hence the 1 + 2^-20 margin on the upward rounding
+  const float emaxf = __double2float_ru(emax * (1.0 + 9.5367431640625e-07));
+  prim32[3 * (int64_t)j] = make_float4(v0x, v0y, v0z, v0abs);
+  prim32[3 * (int64_t)j + 1] = make_float4(__double2float_rn(e1[0]), __double2float_rn(e1[1]),
+                                           __double2float_rn(e1[2]), emaxf);
+  prim32[3 * (int64_t)j + 2] = make_float4(__double2float_rn(e2[0]), __double2float_rn(e2[1]),
+                                           __double2float_rn(e2[2]), 0.0f);
+}
+
+__global__ void k_tet_boxes(const double* __restrict__ xyz, const int4* __restrict__ conn,
+                            const int32_t* __restrict__ tets, int32_t n, double* __restrict__ box) {
+  int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int4 c = conn[tets[i]];
+  const int32_t ci[4] = {c.x, c.y, c.z, c.w};
+  double lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = INFINITY;
+    hi[a] = -INFINITY;
+  }
+  for (int k = 0; k < 4; ++k)
+    for (int a = 0; a < 3; ++a) {
+      const double x = xyz[3 * (int64_t)ci[k] + a];
+      lo[a] = fmin(lo[a], x);
+      hi[a] = fmax(hi[a], x);
+    }
+  // bbox.h:85-102: dilation = |width| * FP_BOX_TOL (tetrahedron_contain.cpp:47-63)
+  const double wx = hi[0] - lo[0], wy = hi[1] - lo[1], wz = hi[2] - lo[2];
+  const double bump = sqrt(wx * wx + wy * wy + wz * wz) * 1e-6;
+  for (int a = 0; a < 3; ++a) {
+    box[6 * (int64_t)i + a] = lo[a] - bump;
+    box[6 * (int64_t)i + 3 + a] = hi[a] + bump;
+  }
+}
+
+__global__ void k_tet_gather(const double* __restrict__ xyz, const int4* __restrict__ conn,
+                             const int32_t* __restrict__ tets, const int32_t* __restrict__ order,
+                             int32_t n, double* __restrict__ prim64, int32_t* __restrict__ prim_ref) {
+  int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int32_t t = tets[order[j]];
+  const int4 c = conn[t];
+  const int32_t ci[4] = {c.x, c.y, c.z, c.w};
+  double* o = prim64 + 12 * (int64_t)j;
+  for (int k = 0; k < 4; ++k)
+    for (int a = 0; a < 3; ++a) o[3 * k + a] = xyz[3 * (int64_t)ci[k] + a];
+  prim_ref[j] = t;
+}
+
+__global__ void k_vert32(const double* __restrict__ xyz, int64_t n, float4* __restrict__ out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float x = __double2float_rn(xyz[3 * i]), y = __double2float_rn(xyz[3 * i + 1]),
+              z = __double2float_rn(xyz[3 * i + 2]);
+  out[i] = make_float4(x, y, z, fmaxf(fabsf(x), fmaxf(fabsf(y), fabsf(z))));
+}
+
+inline unsigned grid(int64_t n, int b = 256) { return (unsigned)((n + b - 1) / b); }
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+struct xdgcu_ctx {
+  int device = 0;
+  std::mutex mu;
+  // surfaces
+  std::vector<SurfaceRec> surfs;
+  std::unordered_map<int32_t, int32_t> surf_index;
+  std::vector<double> h_tri_xyz;
+  std::vector<int32_t> h_tri_face, h_tri_surf;
+  DevMem<double> d_tri_xyz;
+  DevMem<int32_t> d_tri_face, d_tri_surf, d_surf_id, d_surf_rev;
+  bool tri_dirty = true, surf_dirty = true;
+  // tet mesh
+  bool has_tets = false;
+  int64_t n_vert = 0, n_tet = 0;
+  DevMem<double> d_xyz;
+  DevMem<float4> d_xyz32;
+  DevMem<int4> d_conn, d_adj;
+  DevMem<int32_t> d_elem_ids;
+  int32_t face[12] = {0};
+  int face_order = 0;
+  // trees
+  std::vector<std::unique_ptr<TreeHost>> surf_trees, elem_trees;
+  DevMem<TreeDev> d_surf_trees, d_elem_trees;
+  bool surf_trees_dirty = true, elem_trees_dirty = true;
+  // diagnostics
+  bool counting = false;
+  DevMem<unsigned long long> d_counters;
+  cudaStream_t counter_stream = nullptr;
+  // per-thread staging for host-pointer calls
+  std::mutex slot_mu;
+  std::unordered_map<std::thread::id, std::unique_ptr<Slot>> slots;
+  cudaStream_t build_stream = nullptr;
+};
+
+namespace {
+
+int sync_surfaces(xdgcu_ctx* c) {
+  if (c->tri_dirty) {
+    const int64_t nt = (int64_t)c->h_tri_face.size();
+    API_CUDA(c->d_tri_xyz.alloc(std::max<int64_t>(1, 9 * nt)), "alloc triangles");
+    API_CUDA(c->d_tri_face.alloc(std::max<int64_t>(1, nt)), "alloc face ids");
+    API_CUDA(c->d_tri_surf.alloc(std::max<int64_t>(1, nt)), "alloc surface index");
+    if (nt) {
+      API_CUDA(cudaMemcpy(c->d_tri_xyz.p, c->h_tri_xyz.data(), sizeof(double) * 9 * nt,
+                          cudaMemcpyHostToDevice), "upload triangles");
+      API_CUDA(cudaMemcpy(c->d_tri_face.p, c->h_tri_face.data(), sizeof(int32_t) * nt,
+                          cudaMemcpyHostToDevice), "upload face ids");
+      API_CUDA(cudaMemcpy(c->d_tri_surf.p, c->h_tri_surf.data(), sizeof(int32_t) * nt,
+                          cudaMemcpyHostToDevice), "upload surface index");
+    }
+    c->tri_dirty = false;
+  }
+  if (c->surf_dirty) {
+    const int64_t ns = (int64_t)c->surfs.size();
+    std::vector<int32_t> ids(std::max<int64_t>(1, ns)), rev(std::max<int64_t>(1, ns));
+    for (int64_t s = 0; s < ns; ++s) {
+      ids[s] = c->surfs[s].id;
+      rev[s] = c->surfs[s].rev_tree;
+    }
+    API_CUDA(c->d_surf_id.alloc(std::max<int64_t>(1, ns)), "alloc surfaces");
+    API_CUDA(c->d_surf_rev.alloc(std::max<int64_t>(1, ns)), "alloc surfaces");
+    API_CUDA(cudaMemcpy(c->d_surf_id.p, ids.data(), sizeof(int32_t) * ids.size(),
+                        cudaMemcpyHostToDevice), "upload surfaces");
+    API_CUDA(cudaMemcpy(c->d_surf_rev.p, rev.data(), sizeof(int32_t) * rev.size(),
+                        cudaMemcpyHostToDevice), "upload surfaces");
+    c->surf_dirty = false;
+  }
+  return XDGCU_OK;
+}
+
+int sync_tree_tables(xdgcu_ctx* c) {
+  if (c->surf_trees_dirty) {
+    std::vector<TreeDev> t;
+    for (auto& p : c->surf_trees) t.push_back(p->dev);
+    if (t.empty()) t.push_back(TreeDev{});
+    API_CUDA(c->d_surf_trees.alloc((int64_t)t.size()), "alloc tree table");
+    API_CUDA(cudaMemcpy(c->d_surf_trees.p, t.data(), sizeof(TreeDev) * t.size(),
+                        cudaMemcpyHostToDevice), "upload tree table");
+    c->surf_trees_dirty = false;
+  }
+  if (c->elem_trees_dirty) {
+    std::vector<TreeDev> t;
+    for (auto& p : c->elem_trees) t.push_back(p->dev);
+    if (t.empty()) t.push_back(TreeDev{});
+    API_CUDA(c->d_elem_trees.alloc((int64_t)t.size()), "alloc tree table");
+    API_CUDA(cudaMemcpy(c->d_elem_trees.p, t.data(), sizeof(TreeDev) * t.size(),
+                        cudaMemcpyHostToDevice), "upload tree table");
+    c->elem_trees_dirty = false;
+  }
+  return XDGCU_OK;
+}
+
+void fill_dev(TreeHost& t, const BuiltTree& b, double min_bump) {
+  t.n32 = b.n32;
+  t.n64 = b.n64;
+  t.n_nodes = b.n_nodes;
+  t.depth = b.depth;
+  TreeDev& d = t.dev;
+  d.n32 = b.n32;
+  d.n64 = b.n64;
+  d.prim32 = t.prim32.p;
+  d.prim64 = t.prim64.p;
+  d.prim_ref = t.prim_ref.p;
+  d.root = b.root;
+  d.n_prims = (int32_t)t.prim_ref.n;
+  d.depth = b.depth;
+  d.tree_id = t.id;
+  d.kind = t.kind;
+  double m = 0.0;
+  for (int k = 0; k < 6; ++k) m = std::max(m, std::fabs(b.bounds[k]));
+  d.max_abs = (float)(m * (1.0 + 1e-6));
+  // FP32 safety check compares against the smallest dilation in the tree
+  float bf = (float)min_bump;
+  if ((double)bf > min_bump) bf = std::nextafter(bf, 0.0f);
+  d.bump = bf;
+}
+
+// Build the BVH over `tris` (global triangle indices) with per-triangle bumps.
+int build_surface_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tris,
+                      const std::vector<double>& bumps) {
+  const int32_t n = (int32_t)tris.size();
+  cudaStream_t st = c->build_stream;
+  DevMem<int32_t> d_tris(std::max(1, n));
+  DevMem<double> d_bump(std::max(1, n)), d_box(6 * (int64_t)std::max(1, n));
+  API_CUDA(d_tris.alloc(), "alloc");
+  API_CUDA(d_bump.alloc(), "alloc");
+  API_CUDA(d_box.alloc(), "alloc");
+  double min_bump = INFTY;
+  for (double b : bumps) min_bump = std::min(min_bump, b);
+  if (n > 0) {
+    API_CUDA(cudaMemcpyAsync(d_tris.p, tris.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
+             "upload");
+    API_CUDA(cudaMemcpyAsync(d_bump.p, bumps.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st),
+             "upload");
+    k_tri_boxes<<<grid(n), 256, 0, st>>>(c->d_tri_xyz.p, d_tris.p, d_bump.p, n, d_box.p);
+    API_CUDA(cudaGetLastError(), "triangle boxes");
+  }
+  BuiltTree b;
+  API_CUDA(build_wide_bvh(d_box.p, n, kLeafMax, st, &b), "bvh build");
+  API_CUDA(t.prim32.alloc(3 * (int64_t)std::max(1, n)), "alloc prims");
+  API_CUDA(t.prim64.alloc(kPrim64Stride * (int64_t)std::max(1, n)), "alloc prims");
+  API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
+  if (n > 0) {
+    k_tri_gather<<<grid(n), 256, 0, st>>>(c->d_tri_xyz.p, d_tris.p, b.order, n, t.prim32.p,
+                                          t.prim64.p, t.prim_ref.p);
+    API_CUDA(cudaGetLastError(), "gather");
+  }
+  API_CUDA(cudaStreamSynchronize(st), "build sync");
+  if (b.order) cudaFree(b.order);
+  t.prim_ref.n = n;
+  fill_dev(t, b, n > 0 ? min_bump : 1e-3);
+  return XDGCU_OK;
+}
+
+int build_element_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tets) {
+  const int32_t n = (int32_t)tets.size();
+  cudaStream_t st = c->build_stream;
+  DevMem<int32_t> d_tets(std::max(1, n));
+  DevMem<double> d_box(6 * (int64_t)std::max(1, n));
+  API_CUDA(d_tets.alloc(), "alloc");
+  API_CUDA(d_box.alloc(), "alloc");
+  if (n > 0) {
+    API_CUDA(cudaMemcpyAsync(d_tets.p, tets.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
+             "upload");
+    k_tet_boxes<<<grid(n), 256, 0, st>>>(c->d_xyz.p, c->d_conn.p, d_tets.p, n, d_box.p);
+    API_CUDA(cudaGetLastError(), "tet boxes");
+  }
+  BuiltTree b;
+  API_CUDA(build_wide_bvh(d_box.p, n, kLeafMax, st, &b), "bvh build");
+  API_CUDA(t.prim64.alloc(12 * (int64_t)std::max(1, n)), "alloc prims");
+  API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
+  if (n > 0) {
+    k_tet_gather<<<grid(n), 256, 0, st>>>(c->d_xyz.p, c->d_conn.p, d_tets.p, b.order, n,
+                                          t.prim64.p, t.prim_ref.p);
+    API_CUDA(cudaGetLastError(), "gather");
+  }
+  API_CUDA(cudaStreamSynchronize(st), "build sync");
+  if (b.order) cudaFree(b.order);
+  t.prim_ref.n = n;
+  fill_dev(t, b, 0.0);
+  return XDGCU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host/device staging
+// ---------------------------------------------------------------------------
+
+struct Arr {
+  const void* host_in = nullptr;  // input to copy H2D
+  void* host_out = nullptr;       // output to copy D2H
+  size_t bytes = 0;
+  void* dev = nullptr;
+};
+
+// Decide the pointer kind of a call: 1 device, 0 host, -1 mixed (error).
+int classify(std::initializer_list<const void*> ptrs) {
+  int kind = -2;
+  for (const void* p : ptrs) {
+    if (!p) continue;
+    const int k = is_device_ptr(p) ? 1 : 0;
+    if (kind == -2) kind = k;
+    else if (kind != k) return -1;
+  }
+  return kind == -2 ? 1 : kind;
+}
+
+Slot* get_slot(xdgcu_ctx* c) {
+  std::lock_guard<std::mutex> g(c->slot_mu);
+  auto& s = c->slots[std::this_thread::get_id()];
+  if (!s) {
+    s.reset(new Slot());
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      s.reset();
+      return nullptr;
+    }
+  }
+  return s.get();
+}
+
+// Allocate device images of the arrays in the slot's workspace, upload inputs.
+int stage_in(Slot* s, std::vector<Arr*> arrs, cudaStream_t st) {
+  size_t total = 0;
+  for (Arr* a : arrs) total += (a->bytes + 255) & ~(size_t)255;
+  if ((int64_t)total > s->buf.n) {
+    API_CUDA(s->buf.alloc((int64_t)std::max<size_t>(total, 1 << 20)), "workspace");
+  }
+  size_t off = 0;
+  for (Arr* a : arrs) {
+    if (a->bytes == 0) continue;
+    a->dev = s->buf.p + off;
+    off += (a->bytes + 255) & ~(size_t)255;
+    if (a->host_in)
+      API_CUDA(cudaMemcpyAsync(a->dev, a->host_in, a->bytes, cudaMemcpyHostToDevice, st), "H2D");
+  }
+  return XDGCU_OK;
+}
+
+int stage_out(std::vector<Arr*> arrs, cudaStream_t st) {
+  for (Arr* a : arrs)
+    if (a->host_out && a->bytes)
+      API_CUDA(cudaMemcpyAsync(a->host_out, a->dev, a->bytes, cudaMemcpyDeviceToHost, st), "D2H");
+  API_CUDA(cudaStreamSynchronize(st), "sync");
+  return XDGCU_OK;
+}
+
+int begin_query(xdgcu_ctx* c, cudaStream_t st, unsigned long long** counters) {
+  *counters = nullptr;
+  if (c->counting) {
+    if (!c->d_counters.p) API_CUDA(c->d_counters.alloc(CNT_N), "counters");
+    API_CUDA(cudaMemsetAsync(c->d_counters.p, 0, sizeof(unsigned long long) * CNT_N, st), "counters");
+    *counters = c->d_counters.p;
+    c->counter_stream = st;
+  }
+  return XDGCU_OK;
+}
+
+#define CHECK_CTX(c)                                                            \
+  do {                                                                          \
+    if (!(c)) return set_err(XDGCU_ERR_INVALID_ARG, "null context");            \
+    if (cudaSetDevice((c)->device) != cudaSuccess)                             \
+      return set_err(XDGCU_ERR_CUDA, "cudaSetDevice failed");                   \
+  } while (0)
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+int xdgcu_version(void) { return 100; }
+
+const char* xdgcu_last_error(const xdgcu_ctx*) { return g_last_error.c_str(); }
+
+int xdgcu_create(xdgcu_ctx** out, int device) {
+  if (!out) return set_err(XDGCU_ERR_INVALID_ARG, "null output pointer");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return set_err(XDGCU_ERR_CUDA, "no CUDA device available");
+  if (device < 0 || device >= n) return set_err(XDGCU_ERR_INVALID_ARG, "device out of range");
+  API_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  auto* c = new xdgcu_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->build_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return set_err(XDGCU_ERR_CUDA, "stream creation failed");
+  }
+  *out = c;
+  return XDGCU_OK;
+}
+
+int xdgcu_destroy(xdgcu_ctx* c) {
+  if (!c) return XDGCU_OK;
+  cudaSetDevice(c->device);
+  cudaDeviceSynchronize();
+  if (c->build_stream) cudaStreamDestroy(c->build_stream);
+  delete c;
+  return XDGCU_OK;
+}
+
+int xdgcu_register_surface(xdgcu_ctx* c, int32_t surface_id, int64_t n_faces, const double* tri_xyz,
+                           const int32_t* face_ids) {
+  CHECK_CTX(c);
+  std::lock_guard<std::mutex> g(c->mu);
+  if (n_faces < 0 || (n_faces > 0 && (!tri_xyz || !face_ids)))
+    return set_err(XDGCU_ERR_INVALID_ARG, "register_surface: bad arrays");
+  if (c->surf_index.count(surface_id))
+    return set_err(XDGCU_ERR_STATE, "register_surface: surface already registered");
+  if ((int64_t)c->h_tri_face.size() + n_faces > (int64_t)(1 << 27))
+    return set_err(XDGCU_ERR_INVALID_ARG, "register_surface: more than 2^27 triangles");
+  SurfaceRec r;
+  r.id = surface_id;
+  r.first = (int64_t)c->h_tri_face.size();
+  r.count = n_faces;
+  const int32_t sidx = (int32_t)c->surfs.size();
+  c->surf_index[surface_id] = sidx;
+  c->surfs.push_back(r);
+  c->h_tri_xyz.insert(c->h_tri_xyz.end(), tri_xyz, tri_xyz + 9 * n_faces);
+  c->h_tri_face.insert(c->h_tri_face.end(), face_ids, face_ids + n_faces);
+  c->h_tri_surf.insert(c->h_tri_surf.end(), (size_t)n_faces, sidx);
+  c->tri_dirty = true;
+  c->surf_dirty = true;
+  return XDGCU_OK;
+}
+
+static int create_surface_tree_impl(xdgcu_ctx* c, const std::vector<int32_t>& sidx,
+                                    const std::vector<int32_t>& sense, double bump, bool global,
+                                    int32_t* tree_out) {
+  auto t = std::make_unique<TreeHost>();
+  t->id = (int32_t)c->surf_trees.size() + 1;
+  t->kind = TREE_SURFACE;
+  t->members = sidx;
+  // parent tree ids and box dilation (embree/ray_tracer.cpp:76-99)
+  if (!global) {
+    for (size_t k = 0; k < sidx.size(); ++k) {
+      SurfaceRec& s = c->surfs[sidx[k]];
+      s.bump = std::max(s.bump, bump);
+      if (sense[k] == 0) s.fwd_tree = t->id;
+      else s.rev_tree = t->id;
+    }
+    c->surf_dirty = true;
+  }
+  int rc = sync_surfaces(c);
+  if (rc) return rc;
+  std::vector<int32_t> tris;
+  std::vector<double> bumps;
+  for (int32_t s : sidx) {
+    const SurfaceRec& r = c->surfs[s];
+    const double b = r.bump > 0 ? r.bump : (bump > 0 ? bump : 1e-3);
+    for (int64_t k = 0; k < r.count; ++k) {
+      tris.push_back((int32_t)(r.first + k));
+      bumps.push_back(b);
+    }
+  }
+  rc = build_surface_bvh(c, *t, tris, bumps);
+  if (rc) return rc;
+  *tree_out = t->id;
+  c->surf_trees.push_back(std::move(t));
+  c->surf_trees_dirty = true;
+  return sync_tree_tables(c);
+}
+
+int xdgcu_create_surface_tree(xdgcu_ctx* c, const int32_t* surface_ids, const int32_t* sense,
+                              int32_t n_surfaces, double bump, int32_t* tree_out) {
+  CHECK_CTX(c);
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!tree_out || n_surfaces < 0 || (n_surfaces > 0 && (!surface_ids || !sense)))
+    return set_err(XDGCU_ERR_INVALID_ARG, "create_surface_tree: bad arguments");
+  if (!(bump >= 0.0) || !std::isfinite(bump))
+    return set_err(XDGCU_ERR_INVALID_ARG, "create_surface_tree: bump must be finite and >= 0");
+  std::vector<int32_t> sidx, sn;
+  for (int32_t k = 0; k < n_surfaces; ++k) {
+    auto it = c->surf_index.find(surface_ids[k]);
+    if (it == c->surf_index.end())
+      return set_err(XDGCU_ERR_NOT_FOUND, "create_surface_tree: surface " +
+                                              std::to_string(surface_ids[k]) + " not registered");
+    if (sense[k] != 0 && sense[k] != 1)
+      return set_err(XDGCU_ERR_INVALID_ARG, "create_surface_tree: sense must be 0 or 1");
+    sidx.push_back(it->second);
+    sn.push_back(sense[k]);
+  }
+  return create_surface_tree_impl(c, sidx, sn, bump, false, tree_out);
+}
+
+int xdgcu_create_global_surface_tree(xdgcu_ctx* c, int32_t* tree_out) {
+  CHECK_CTX(c);
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!tree_out) return set_err(XDGCU_ERR_INVALID_ARG, "null tree_out");
+  std::vector<int32_t> sidx(c->surfs.size()), sn(c->surfs.size(), 0);
+  for (size_t k = 0; k < sidx.size(); ++k) sidx[k] = (int32_t)k;
+  return create_surface_tree_impl(c, sidx, sn, 0.0, true, tree_out);
+}
+
+int xdgcu_set_tet_mesh(xdgcu_ctx* c, int64_t n_vertices, const double* xyz, int64_t n_tets,
+                       const int32_t* conn, const int32_t* adj, const int32_t* elem_ids,
+                       const int32_t face_table[12]) {
+  CHECK_CTX(c);
+  std::lock_guard<std::mutex> g(c->mu);
+  if (c->has_tets) return set_err(XDGCU_ERR_STATE, "set_tet_mesh: mesh already set");
+  if (n_vertices < 0 || n_tets < 0 || n_tets >= (1ll << 31) || !face_table ||
+      (n_vertices > 0 && !xyz) || (n_tets > 0 && (!conn || !adj || !elem_ids)))
+    return set_err(XDGCU_ERR_INVALID_ARG, "set_tet_mesh: bad arrays");
+  for (int k = 0; k < 12; ++k)
+    if (face_table[k] < 0 || face_table[k] > 3)
+      return set_err(XDGCU_ERR_INVALID_ARG, "set_tet_mesh: face table entries must be 0..3");
+  for (int64_t i = 0; i < 4 * n_tets; ++i) {
+    if (conn[i] < 0 || conn[i] >= n_vertices)
+      return set_err(XDGCU_ERR_INVALID_ARG, "set_tet_mesh: connectivity out of range");
+    if (adj[i] < -1 || adj[i] >= n_tets)
+      return set_err(XDGCU_ERR_INVALID_ARG, "set_tet_mesh: adjacency out of range");
+  }
+  c->n_vert = n_vertices;
+  c->n_tet = n_tets;
+  API_CUDA(c->d_xyz.alloc(std::max<int64_t>(1, 3 * n_vertices)), "alloc vertices");
+  API_CUDA(c->d_xyz32.alloc(std::max<int64_t>(1, n_vertices)), "alloc vertices");
+  API_CUDA(c->d_conn.alloc(std::max<int64_t>(1, n_tets)), "alloc tets");
+  API_CUDA(c->d_adj.alloc(std::max<int64_t>(1, n_tets)), "alloc tets");
+  API_CUDA(c->d_elem_ids.alloc(std::max<int64_t>(1, n_tets)), "alloc tets");
+  if (n_vertices) {
+    API_CUDA(cudaMemcpy(c->d_xyz.p, xyz, sizeof(double) * 3 * n_vertices, cudaMemcpyHostToDevice),
+             "upload vertices");
+    k_vert32<<<grid(n_vertices), 256, 0, c->build_stream>>>(c->d_xyz.p, n_vertices, c->d_xyz32.p);
+    API_CUDA(cudaGetLastError(), "vertices");
+    API_CUDA(cudaStreamSynchronize(c->build_stream), "vertices");
+  }
+  if (n_tets) {
+    API_CUDA(cudaMemcpy(c->d_conn.p, conn, sizeof(int32_t) * 4 * n_tets, cudaMemcpyHostToDevice),
+             "upload tets");
+    API_CUDA(cudaMemcpy(c->d_adj.p, adj, sizeof(int32_t) * 4 * n_tets, cudaMemcpyHostToDevice),
+             "upload tets");
+    API_CUDA(cudaMemcpy(c->d_elem_ids.p, elem_ids, sizeof(int32_t) * n_tets, cudaMemcpyHostToDevice),
+             "upload tets");
+  }
+  std::memcpy(c->face, face_table, sizeof(c->face));
+  c->face_order = std::memcmp(face_table, kMoabFaces, sizeof(kMoabFaces)) == 0 ? 0 : 1;
+  c->has_tets = true;
+  return XDGCU_OK;
+}
+
+int xdgcu_create_element_tree(xdgcu_ctx* c, const int32_t* tet_indices, int64_t n, int32_t* tree_out) {
+  CHECK_CTX(c);
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!tree_out || n < 0 || (n > 0 && !tet_indices))
+    return set_err(XDGCU_ERR_INVALID_ARG, "create_element_tree: bad arguments");
+  if (!c->has_tets) return set_err(XDGCU_ERR_STATE, "create_element_tree: no tet mesh set");
+  if (n > (1 << 27)) return set_err(XDGCU_ERR_INVALID_ARG, "create_element_tree: too many tets");
+  std::vector<int32_t> tets(tet_indices, tet_indices + n);
+  for (int32_t t : tets)
+    if (t < 0 || t >= c->n_tet)
+      return set_err(XDGCU_ERR_INVALID_ARG, "create_element_tree: tet index out of range");
+  auto t = std::make_unique<TreeHost>();
+  t->id = (int32_t)c->elem_trees.size() + 1;
+  t->kind = TREE_ELEMENT;
+  t->members = tets;
+  int rc = build_element_bvh(c, *t, tets);
+  if (rc) return rc;
+  *tree_out = t->id;
+  c->elem_trees.push_back(std::move(t));
+  c->elem_trees_dirty = true;
+  return sync_tree_tables(c);
+}
+
+int xdgcu_create_global_element_tree(xdgcu_ctx* c, int32_t* tree_out) {
+  CHECK_CTX(c);
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!tree_out) return set_err(XDGCU_ERR_INVALID_ARG, "null tree_out");
+  if (!c->has_tets) {
+    // the reference builds an empty global scene (embree/ray_tracer.cpp:208-224)
+  }
+  std::vector<int32_t> tets;
+  for (auto& t : c->elem_trees) tets.insert(tets.end(), t->members.begin(), t->members.end());
+  auto t = std::make_unique<TreeHost>();
+  t->id = (int32_t)c->elem_trees.size() + 1;
+  t->kind = TREE_ELEMENT;
+  t->members = tets;
+  int rc = build_element_bvh(c, *t, tets);
+  if (rc) return rc;
+  *tree_out = t->id;
+  c->elem_trees.push_back(std::move(t));
+  c->elem_trees_dirty = true;
+  return sync_tree_tables(c);
+}
+
+int xdgcu_num_surface_trees(const xdgcu_ctx* c) { return c ? (int)c->surf_trees.size() : 0; }
+int xdgcu_num_element_trees(const xdgcu_ctx* c) { return c ? (int)c->elem_trees.size() : 0; }
+
+static int tree_info(const std::vector<std::unique_ptr<TreeHost>>& v, int32_t tree, int64_t out[8]) {
+  if (!out) return set_err(XDGCU_ERR_INVALID_ARG, "null output");
+  if (tree < 1 || tree > (int32_t)v.size()) return set_err(XDGCU_ERR_NOT_FOUND, "no such tree");
+  const TreeHost& t = *v[tree - 1];
+  for (int k = 0; k < 8; ++k) out[k] = 0;
+  out[0] = t.n_nodes;
+  out[1] = t.prim_ref.n;
+  out[2] = t.depth;
+  out[3] = (int64_t)sizeof(Node32) * t.n_nodes;
+  out[4] = (int64_t)sizeof(Node64) * t.n_nodes;
+  return XDGCU_OK;
+}
+
+int xdgcu_surface_tree_info(const xdgcu_ctx* c, int32_t tree, int64_t out[8]) {
+  if (!c) return set_err(XDGCU_ERR_INVALID_ARG, "null context");
+  return tree_info(c->surf_trees, tree, out);
+}
+int xdgcu_element_tree_info(const xdgcu_ctx* c, int32_t tree, int64_t out[8]) {
+  if (!c) return set_err(XDGCU_ERR_INVALID_ARG, "null context");
+  return tree_info(c->elem_trees, tree, out);
+}
+
+int xdgcu_set_counting(xdgcu_ctx* c, int32_t enable) {
+  if (!c) return set_err(XDGCU_ERR_INVALID_ARG, "null context");
+  c->counting = enable != 0;
+  return XDGCU_OK;
+}
+
+int xdgcu_get_counters(xdgcu_ctx* c, int64_t counters[8]) {
+  CHECK_CTX(c);
+  if (!counters) return set_err(XDGCU_ERR_INVALID_ARG, "null output");
+  for (int k = 0; k < 8; ++k) counters[k] = 0;
+  if (!c->d_counters.p) return XDGCU_OK;
+  if (c->counter_stream) API_CUDA(cudaStreamSynchronize(c->counter_stream), "sync");
+  unsigned long long h[CNT_N];
+  API_CUDA(cudaMemcpy(h, c->d_counters.p, sizeof h, cudaMemcpyDeviceToHost), "counters");
+  for (int k = 0; k < 8; ++k) counters[k] = (int64_t)h[k];
+  return XDGCU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// surface queries
+// ---------------------------------------------------------------------------
+
+static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ray_trees, int64_t n,
+                         const double* org, const double* dir, const double* tmax,
+                         int32_t orientation, const int32_t* excl_off, const int32_t* excl_ids,
+                         double* t_out, int32_t* surf_out, int32_t* face_out, int32_t* flag_out,
+                         double* dist_out, int32_t* status, int32_t precision, void* stream) {
+  CHECK_CTX(c);
+  if (n < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative ray count");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (n == 0) return XDGCU_OK;
+  if (!org || (!dir && mode != MODE_PIV))
+    return set_err(XDGCU_ERR_INVALID_ARG, "null origins/directions");
+  if (mode == MODE_RAY_FIRE && (!t_out || !surf_out))
+    return set_err(XDGCU_ERR_INVALID_ARG, "ray_fire: t_out and surface_out are required");
+  if (mode != MODE_RAY_FIRE && !flag_out) return set_err(XDGCU_ERR_INVALID_ARG, "null output");
+  if ((excl_off == nullptr) != (excl_ids == nullptr))
+    return set_err(XDGCU_ERR_INVALID_ARG, "exclusions need both offsets and ids");
+  if (mode == MODE_RAY_FIRE && orientation != XDGCU_ANY && orientation != XDGCU_EXITING &&
+      orientation != XDGCU_ENTERING)
+    return set_err(XDGCU_ERR_INVALID_ARG, "bad orientation");
+  if (!ray_trees && (tree < 1 || tree > (int32_t)c->surf_trees.size()))
+    return set_err(XDGCU_ERR_NOT_FOUND, "no such surface tree");
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    int rc = sync_surfaces(c);
+    if (rc) return rc;
+    rc = sync_tree_tables(c);
+    if (rc) return rc;
+  }
+  const int kind = classify({ray_trees, org, dir, tmax, excl_off, excl_ids, t_out, surf_out,
+                             face_out, flag_out, dist_out, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  SurfArgs a{};
+  a.trees = c->d_surf_trees.p;
+  a.n_trees = (int32_t)c->surf_trees.size();
+  a.tree = tree;
+  a.n = n;
+  a.orientation = orientation;
+  a.tri_face = c->d_tri_face.p;
+  a.tri_surf = c->d_tri_surf.p;
+  a.surf_id = c->d_surf_id.p;
+  a.surf_rev_tree = c->d_surf_rev.p;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 1) {
+    a.ray_trees = ray_trees;
+    a.org = org;
+    a.dir = dir;
+    a.tmax = tmax;
+    a.excl_off = excl_off;
+    a.excl_ids = excl_ids;
+    a.t_out = t_out;
+    a.surf_out = surf_out;
+    a.face_out = face_out;
+    a.flag_out = flag_out;
+    a.dist_out = dist_out;
+    a.status = status;
+    int rc = begin_query(c, st, &a.counters);
+    if (rc) return rc;
+    API_CUDA(launch_surface_query(mode, precision == XDGCU_MIXED, a, st), "query launch");
+    return XDGCU_OK;
+  }
+  Slot* s = get_slot(c);
+  if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  if (!st) st = s->stream;
+  const size_t n3 = sizeof(double) * 3 * (size_t)n;
+  int64_t n_excl = 0;
+  if (excl_off) n_excl = excl_off[n];
+  if (n_excl < 0) return set_err(XDGCU_ERR_INVALID_ARG, "bad exclusion offsets");
+  Arr A_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) * n : 0};
+  Arr A_org{org, nullptr, n3}, A_dir{dir, nullptr, dir ? n3 : 0};
+  Arr A_tmax{tmax, nullptr, tmax ? sizeof(double) * n : 0};
+  Arr A_eo{excl_off, nullptr, excl_off ? sizeof(int32_t) * (n + 1) : 0};
+  Arr A_ei{excl_ids, nullptr, excl_ids ? sizeof(int32_t) * std::max<int64_t>(1, n_excl) : 0};
+  Arr A_t{nullptr, t_out, t_out ? sizeof(double) * n : 0};
+  Arr A_s{nullptr, surf_out, surf_out ? sizeof(int32_t) * n : 0};
+  Arr A_f{nullptr, face_out, face_out ? sizeof(int32_t) * n : 0};
+  Arr A_fl{nullptr, flag_out, flag_out ? sizeof(int32_t) * n : 0};
+  Arr A_d{nullptr, dist_out, dist_out ? sizeof(double) * n : 0};
+  Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
+  if (excl_off && n_excl == 0) A_ei.host_in = nullptr;
+  std::vector<Arr*> all = {&A_trees, &A_org, &A_dir, &A_tmax, &A_eo, &A_ei,
+                           &A_t, &A_s, &A_f, &A_fl, &A_d, &A_st};
+  int rc = stage_in(s, all, st);
+  if (rc) return rc;
+  a.ray_trees = (const int32_t*)A_trees.dev;
+  a.org = (const double*)A_org.dev;
+  a.dir = (const double*)A_dir.dev;
+  a.tmax = (const double*)A_tmax.dev;
+  a.excl_off = (const int32_t*)A_eo.dev;
+  a.excl_ids = (const int32_t*)A_ei.dev;
+  a.t_out = (double*)A_t.dev;
+  a.surf_out = (int32_t*)A_s.dev;
+  a.face_out = (int32_t*)A_f.dev;
+  a.flag_out = (int32_t*)A_fl.dev;
+  a.dist_out = (double*)A_d.dev;
+  a.status = (int32_t*)A_st.dev;
+  rc = begin_query(c, st, &a.counters);
+  if (rc) return rc;
+  API_CUDA(launch_surface_query(mode, precision == XDGCU_MIXED, a, st), "query launch");
+  return stage_out(all, st);
+}
+
+int xdgcu_ray_fire(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,
+                   const double* origins, const double* directions, const double* dist_limit,
+                   int32_t orientation, const int32_t* excl_offsets, const int32_t* excl_ids,
+                   double* t_out, int32_t* surface_out, int32_t* face_out, int32_t* status,
+                   int32_t precision, void* stream) {
+  return surface_query(c, MODE_RAY_FIRE, tree, ray_trees, n, origins, directions, dist_limit,
+                       orientation, excl_offsets, excl_ids, t_out, surface_out, face_out, nullptr,
+                       nullptr, status, precision, stream);
+}
+
+int xdgcu_point_in_volume(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,
+                          const double* points, const double* directions,
+                          const int32_t* excl_offsets, const int32_t* excl_ids, int32_t* inside_out,
+                          int32_t* status, int32_t precision, void* stream) {
+  return surface_query(c, MODE_PIV, tree, ray_trees, n, points, directions, nullptr, XDGCU_ANY,
+                       excl_offsets, excl_ids, nullptr, nullptr, nullptr, inside_out, nullptr,
+                       status, precision, stream);
+}
+
+int xdgcu_occluded(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,
+                   const double* origins, const double* directions, int32_t* occluded_out,
+                   double* dist_out, int32_t* status, int32_t precision, void* stream) {
+  return surface_query(c, MODE_OCCLUDED, tree, ray_trees, n, origins, directions, nullptr,
+                       XDGCU_ANY, nullptr, nullptr, nullptr, nullptr, nullptr, occluded_out,
+                       dist_out, status, precision, stream);
+}
+
+// ---------------------------------------------------------------------------
+// point queries
+// ---------------------------------------------------------------------------
+
+static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* ray_trees,
+                       int64_t n, const double* pts, double* dist_out, int32_t* id_out,
+                       int32_t* index_out, int32_t* status, int32_t precision, void* stream) {
+  CHECK_CTX(c);
+  if (n < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative point count");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (n == 0) return XDGCU_OK;
+  if (!pts) return set_err(XDGCU_ERR_INVALID_ARG, "null points");
+  if (closest && !dist_out) return set_err(XDGCU_ERR_INVALID_ARG, "closest: dist_out required");
+  if (!closest && !id_out && !index_out)
+    return set_err(XDGCU_ERR_INVALID_ARG, "find_element: an output is required");
+  const int32_t ntrees = (int32_t)(closest ? c->surf_trees.size() : c->elem_trees.size());
+  if (!ray_trees && (tree < 1 || tree > ntrees))
+    return set_err(XDGCU_ERR_NOT_FOUND, closest ? "no such surface tree" : "no such element tree");
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    int rc = sync_surfaces(c);
+    if (rc) return rc;
+    rc = sync_tree_tables(c);
+    if (rc) return rc;
+  }
+  const int kind = classify({ray_trees, pts, dist_out, id_out, index_out, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  PointArgs a{};
+  a.trees = closest ? c->d_surf_trees.p : c->d_elem_trees.p;
+  a.n_trees = ntrees;
+  a.tree = tree;
+  a.n = n;
+  a.tri_face = c->d_tri_face.p;
+  a.elem_ids = c->d_elem_ids.p;
+  cudaStream_t st = (cudaStream_t)stream;
+  auto launch = [&]() -> cudaError_t {
+    return closest ? launch_closest(precision == XDGCU_MIXED, a, st)
+                   : launch_find_element(precision == XDGCU_MIXED, a, st);
+  };
+  if (kind == 1) {
+    a.ray_trees = ray_trees;
+    a.pts = pts;
+    a.dist_out = dist_out;
+    a.id_out = id_out;
+    a.index_out = index_out;
+    a.status = status;
+    int rc = begin_query(c, st, &a.counters);
+    if (rc) return rc;
+    API_CUDA(launch(), "query launch");
+    return XDGCU_OK;
+  }
+  Slot* s = get_slot(c);
+  if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  if (!st) st = s->stream;
+  Arr A_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) * n : 0};
+  Arr A_p{pts, nullptr, sizeof(double) * 3 * n};
+  Arr A_d{nullptr, dist_out, dist_out ? sizeof(double) * n : 0};
+  Arr A_i{nullptr, id_out, id_out ? sizeof(int32_t) * n : 0};
+  Arr A_x{nullptr, index_out, index_out ? sizeof(int32_t) * n : 0};
+  Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
+  std::vector<Arr*> all = {&A_trees, &A_p, &A_d, &A_i, &A_x, &A_st};
+  int rc = stage_in(s, all, st);
+  if (rc) return rc;
+  a.ray_trees = (const int32_t*)A_trees.dev;
+  a.pts = (const double*)A_p.dev;
+  a.dist_out = (double*)A_d.dev;
+  a.id_out = (int32_t*)A_i.dev;
+  a.index_out = (int32_t*)A_x.dev;
+  a.status = (int32_t*)A_st.dev;
+  rc = begin_query(c, st, &a.counters);
+  if (rc) return rc;
+  API_CUDA(launch(), "query launch");
+  return stage_out(all, st);
+}
+
+int xdgcu_closest(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,
+                  const double* points, double* dist_out, int32_t* face_out, int32_t* status,
+                  int32_t precision, void* stream) {
+  return point_query(c, true, tree, ray_trees, n, points, dist_out, face_out, nullptr, status,
+                     precision, stream);
+}
+
+int xdgcu_find_element(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,
+                       const double* points, int32_t* elem_id_out, int32_t* elem_index_out,
+                       int32_t* status, int32_t precision, void* stream) {
+  return point_query(c, false, tree, ray_trees, n, points, nullptr, elem_id_out, elem_index_out,
+                     status, precision, stream);
+}
+
+// ---------------------------------------------------------------------------
+// element walk
+// ---------------------------------------------------------------------------
+
+static int walk_query(xdgcu_ctx* c, bool walk, int64_t n, const int32_t* start, const double* org,
+                      const double* dir, const double* dist, int32_t max_segs, int32_t* seg_elem,
+                      double* seg_len, int32_t* seg_count, int32_t* next_out, double* dist_out,
+                      int32_t* status, int32_t precision, void* stream) {
+  CHECK_CTX(c);
+  if (n < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative track count");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (!c->has_tets) return set_err(XDGCU_ERR_STATE, "no tet mesh set");
+  if (n == 0) return XDGCU_OK;
+  if (!start || !org || !dir) return set_err(XDGCU_ERR_INVALID_ARG, "null inputs");
+  if (walk && (!dist || !seg_elem || !seg_len || !seg_count || max_segs <= 0))
+    return set_err(XDGCU_ERR_INVALID_ARG, "walk_elements: bad outputs or max_segs");
+  if (!walk && (!next_out || !dist_out))
+    return set_err(XDGCU_ERR_INVALID_ARG, "next_element: null outputs");
+  const int kind = classify({start, org, dir, dist, seg_elem, seg_len, seg_count, next_out,
+                             dist_out, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  WalkArgs a{};
+  a.xyz = c->d_xyz.p;
+  a.xyz32 = c->d_xyz32.p;
+  a.conn = c->d_conn.p;
+  a.adj = c->d_adj.p;
+  a.elem_ids = c->d_elem_ids.p;
+  a.n_tets = (int32_t)c->n_tet;
+  std::memcpy(a.face, c->face, sizeof(a.face));
+  a.n = n;
+  a.max_segs = max_segs;
+  cudaStream_t st = (cudaStream_t)stream;
+  auto launch = [&]() -> cudaError_t {
+    return walk ? launch_walk(precision == XDGCU_MIXED, c->face_order, a, st)
+                : launch_next_element(precision == XDGCU_MIXED, c->face_order, a, st);
+  };
+  if (kind == 1) {
+    a.start = start;
+    a.org = org;
+    a.dir = dir;
+    a.dist = dist;
+    a.seg_elem = seg_elem;
+    a.seg_len = seg_len;
+    a.seg_count = seg_count;
+    a.next_out = next_out;
+    a.dist_out = dist_out;
+    a.status = status;
+    int rc = begin_query(c, st, &a.counters);
+    if (rc) return rc;
+    API_CUDA(launch(), "walk launch");
+    return XDGCU_OK;
+  }
+  Slot* s = get_slot(c);
+  if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  if (!st) st = s->stream;
+  const size_t ns = walk ? (size_t)n * (size_t)max_segs : 0;
+  Arr A_s{start, nullptr, sizeof(int32_t) * n};
+  Arr A_o{org, nullptr, sizeof(double) * 3 * n}, A_d{dir, nullptr, sizeof(double) * 3 * n};
+  Arr A_l{dist, nullptr, walk ? sizeof(double) * n : 0};
+  Arr A_se{nullptr, seg_elem, sizeof(int32_t) * ns}, A_sl{nullptr, seg_len, sizeof(double) * ns};
+  Arr A_sc{nullptr, seg_count, walk ? sizeof(int32_t) * n : 0};
+  Arr A_no{nullptr, next_out, walk ? 0 : sizeof(int32_t) * n};
+  Arr A_do{nullptr, dist_out, walk ? 0 : sizeof(double) * n};
+  Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
+  std::vector<Arr*> all = {&A_s, &A_o, &A_d, &A_l, &A_se, &A_sl, &A_sc, &A_no, &A_do, &A_st};
+  int rc = stage_in(s, all, st);
+  if (rc) return rc;
+  a.start = (const int32_t*)A_s.dev;
+  a.org = (const double*)A_o.dev;
+  a.dir = (const double*)A_d.dev;
+  a.dist = (const double*)A_l.dev;
+  a.seg_elem = (int32_t*)A_se.dev;
+  a.seg_len = (double*)A_sl.dev;
+  a.seg_count = (int32_t*)A_sc.dev;
+  a.next_out = (int32_t*)A_no.dev;
+  a.dist_out = (double*)A_do.dev;
+  a.status = (int32_t*)A_st.dev;
+  rc = begin_query(c, st, &a.counters);
+  if (rc) return rc;
+  API_CUDA(launch(), "walk launch");
+  return stage_out(all, st);
+}
+
+int xdgcu_next_element(xdgcu_ctx* c, int64_t n, const int32_t* elem_index, const double* positions,
+                       const double* directions, int32_t* next_out, double* dist_out,
+                       int32_t* status, int32_t precision, void* stream) {
+  return walk_query(c, false, n, elem_index, positions, directions, nullptr, 0, nullptr, nullptr,
+                    nullptr, next_out, dist_out, status, precision, stream);
+}
+
+int xdgcu_walk_elements(xdgcu_ctx* c, int64_t n, const int32_t* start_index, const double* start,
+                        const double* u, const double* distance, int32_t max_segs,
+                        int32_t* seg_elem, double* seg_len, int32_t* seg_count, int32_t* status,
+                        int32_t precision, void* stream) {
+  return walk_query(c, true, n, start_index, start, u, distance, max_segs, seg_elem, seg_len,
+                    seg_count, nullptr, nullptr, status, precision, stream);
+}
+
+}  // extern "C"

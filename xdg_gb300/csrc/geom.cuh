@@ -1,0 +1,339 @@
+// geom.cuh -- device geometry kernels of the XDG ray-query engine.
+//
+// Two families live here:
+//
+//  * FP64 routines that reproduce the reference's double-precision arithmetic
+//    operation for operation (the translation unit is compiled with
+//    -fmad=false, so no multiply-add is fused and every product and sum
+//    rounds exactly as in the reference's C++):
+//      plucker64      include/xdg/geometry/plucker.h:35-161
+//      tet_contains64 src/tetrahedron_contain.cpp:11-43
+//      closest64      src/geometry/closest.cpp:6-183
+//      normalize64    include/xdg/vec3da.h:61-66
+//
+//  * an FP32 pre-filter for the Plucker test that returns a certified answer
+//    ("this FP64 test would certainly reject") or "unknown", in which case the
+//    caller escalates to plucker64.  The filter only ever skips candidates
+//    that the FP64 test rejects, so results stay bit-identical.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+namespace xdgcu {
+
+// constants.h:15, 30 / dp_math.h:36
+constexpr double INFTY = 1.7976931348623157e+308;
+constexpr double ZERO_TOL = 20.0 * DBL_EPSILON;
+// constants.h:90: float(FLT_MIN * 1e5); (double)FLT_MIN*1e5 rounded to float
+constexpr float MIN_RCP_INPUT = 1.17549435e-33f;
+constexpr double TINY_BIT = 1e-10;
+
+struct d3 {
+  double x, y, z;
+};
+
+__host__ __device__ __forceinline__ d3 mk3(double x, double y, double z) {
+  d3 r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  return r;
+}
+__host__ __device__ __forceinline__ d3 sub3(d3 a, d3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ d3 add3(d3 a, d3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ d3 scl3(double s, d3 a) { return mk3(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ __forceinline__ d3 neg3(d3 a) { return mk3(-a.x, -a.y, -a.z); }
+// vec3da.h:80-83: (x*x' + y*y') + z*z'
+__host__ __device__ __forceinline__ double dot3(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// vec3da.h:85-90
+__host__ __device__ __forceinline__ d3 cross3(d3 a, d3 b) {
+  return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__host__ __device__ __forceinline__ double comp3(d3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+
+// vec3da.h:61-66 (Vec3da::normalize with the min_rcp_input clamp)
+__host__ __device__ __forceinline__ d3 normalize64(d3 a) {
+  double len = sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  len = len < (double)MIN_RCP_INPUT ? (double)MIN_RCP_INPUT : len;
+  a.x /= len;
+  a.y /= len;
+  a.z /= len;
+  return a;
+}
+
+// mesh_manager_interface.cpp:216-220
+__host__ __device__ __forceinline__ d3 face_normal64(d3 v0, d3 v1, d3 v2) {
+  return normalize64(cross3(sub3(v1, v0), sub3(v2, v0)));
+}
+
+// plucker.h:35-43
+__host__ __device__ __forceinline__ bool first_lower(d3 a, d3 b) {
+  if (a.x < b.x) return true;
+  if (a.x > b.x) return false;
+  if (a.y < b.y) return true;
+  if (a.y > b.y) return false;
+  return a.z < b.z;
+}
+
+// plucker.h:45-62
+__host__ __device__ __forceinline__ double plucker_edge64(d3 va, d3 vb, d3 ray, d3 rn) {
+  double pip;
+  if (first_lower(va, vb)) {
+    const d3 e = sub3(vb, va);
+    const d3 en = cross3(e, va);
+    pip = dot3(ray, en) + dot3(rn, e);
+  } else {
+    const d3 e = sub3(va, vb);
+    const d3 en = cross3(e, vb);
+    pip = dot3(ray, en) + dot3(rn, e);
+    pip = -pip;
+  }
+  if (ZERO_TOL > fabs(pip)) pip = 0.0;
+  return pip;
+}
+
+// plucker.h:64-161.  `rn` is cross(direction, origin) (plucker.h:75), passed
+// in so callers testing many triangles against one ray compute it once; the
+// value is identical to recomputing it per call.
+__host__ __device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn,
+                                                   double t_max, double t_min, bool use_or,
+                                                   int orient, double* t_out) {
+  const double c0 = plucker_edge64(v0, v1, d, rn);
+  if (use_or && orient * c0 > 0) return false;
+  const double c1 = plucker_edge64(v1, v2, d, rn);
+  if (use_or) {
+    if (orient * c1 > 0) return false;
+  } else if ((0.0 < c0 && 0.0 > c1) || (0.0 > c0 && 0.0 < c1)) {
+    return false;
+  }
+  const double c2 = plucker_edge64(v2, v0, d, rn);
+  if (use_or) {
+    if (orient * c2 > 0) return false;
+  } else if ((0.0 < c1 && 0.0 > c2) || (0.0 > c1 && 0.0 < c2) || (0.0 < c0 && 0.0 > c2) ||
+             (0.0 > c0 && 0.0 < c2)) {
+    return false;
+  }
+  if (0.0 == c0 && 0.0 == c1 && 0.0 == c2) return false;
+  const double inv = 1.0 / (c0 + c1 + c2);
+  const d3 hit = add3(add3(scl3(c0 * inv, v2), scl3(c1 * inv, v0)), scl3(c2 * inv, v1));
+  int idx = 0;
+  double max_abs = 0;
+  for (int i = 0; i < 3; ++i) {
+    const double a = fabs(comp3(d, i));
+    if (a > max_abs) {
+      idx = i;
+      max_abs = a;
+    }
+  }
+  double dist = (comp3(hit, idx) - comp3(o, idx)) / comp3(d, idx);
+  const double u = c2 * inv;
+  const double v = c0 * inv;
+  if (u < 0.0 || v < 0.0 || (u + v) > 1.0) dist = -1.0;
+  if (dist < t_min || dist > t_max) return false;
+  *t_out = dist;
+  return true;
+}
+
+// tetrahedron_contain.cpp:11-43.  The reference solves T*lambda = p - v0 with
+// T's columns e0 = v1-v0, e1 = v2-v0, e2 = v3-v0 through its linalg
+// dependency: inverse = adjugate / determinant, then mul(inverse, rhs) summed
+// over columns.  The same formula and order are used here.
+__host__ __device__ __forceinline__ bool tet_contains64(d3 p, d3 v0, d3 v1, d3 v2, d3 v3) {
+  const d3 X = sub3(v1, v0), Y = sub3(v2, v0), Z = sub3(v3, v0);
+  const d3 ax = mk3(Y.y * Z.z - Z.y * Y.z, Z.y * X.z - X.y * Z.z, X.y * Y.z - Y.y * X.z);
+  const d3 ay = mk3(Y.z * Z.x - Z.z * Y.x, Z.z * X.x - X.z * Z.x, X.z * Y.x - Y.z * X.x);
+  const d3 az = mk3(Y.x * Z.y - Z.x * Y.y, Z.x * X.y - X.x * Z.y, X.x * Y.y - Y.x * X.y);
+  const double det = X.x * (Y.y * Z.z - Z.y * Y.z) + X.y * (Y.z * Z.x - Z.z * Y.x) +
+                     X.z * (Y.x * Z.y - Z.x * Y.y);
+  const d3 ix = mk3(ax.x / det, ax.y / det, ax.z / det);
+  const d3 iy = mk3(ay.x / det, ay.y / det, ay.z / det);
+  const d3 iz = mk3(az.x / det, az.y / det, az.z / det);
+  const d3 rhs = sub3(p, v0);
+  const d3 l = add3(add3(scl3(rhs.x, ix), scl3(rhs.y, iy)), scl3(rhs.z, iz));
+  const double l0 = 1.0 - (l.x + l.y + l.z);
+  const double hi = 1.0 + ZERO_TOL;
+  if (l0 < -ZERO_TOL || l0 > hi) return false;
+  if (l.x < -ZERO_TOL || l.x > hi) return false;
+  if (l.y < -ZERO_TOL || l.y > hi) return false;
+  if (l.z < -ZERO_TOL || l.z > hi) return false;
+  return true;
+}
+
+// closest.cpp:54-183 (Eberly's seven-region closest point, MOAB variant)
+__host__ __device__ __forceinline__ d3 closest64(d3 v0, d3 v1, d3 v2, d3 p) {
+  const d3 sv = sub3(v1, v0);
+  const d3 tv = sub3(v2, v0);
+  const d3 pv = sub3(v0, p);
+  const double ss = dot3(sv, sv);
+  const double st = dot3(sv, tv);
+  const double tt = dot3(tv, tv);
+  const double sp = dot3(sv, pv);
+  const double tp = dot3(tv, pv);
+  const double det = ss * tt - st * st;
+  double s = st * tp - tt * sp;
+  double t = st * sp - ss * tp;
+  int region;  // closest.cpp:6-28
+  if (s + t < det) {
+    region = (s < 0) ? (t < 0 ? 4 : 3) : (t < 0 ? 5 : 0);
+  } else {
+    region = (s < 0) ? 2 : (t < 0 ? 6 : 1);
+  }
+  switch (region) {
+    case 0: {
+      const double inv_det = 1.0 / det;
+      s *= inv_det;
+      t *= inv_det;
+      return add3(add3(v0, scl3(s, sv)), scl3(t, tv));
+    }
+    case 1: {
+      const double num = tt + tp - st - sp;
+      if (num <= 0) return v2;
+      const double den = ss - 2 * st + tt;
+      if (num >= den) return v1;
+      const double q = num / den;
+      return add3(scl3(q, v1), scl3(1 - q, v2));
+    }
+    case 2: {
+      s = st + sp;
+      t = tt + tp;
+      if (t > s) {
+        const double num = t - s;
+        const double den = ss - 2 * st + tt;
+        if (num > den) return v1;
+        const double q = num / den;
+        return add3(scl3(q, v1), scl3(1 - q, v2));
+      } else if (t <= 0) {
+        return v2;
+      } else if (tp >= 0) {
+        return v0;
+      }
+      return sub3(v0, scl3(tp / tt, tv));
+    }
+    case 3:
+      if (tp >= 0) return v0;
+      if (-tp >= tt) return v2;
+      return sub3(v0, scl3(tp / tt, tv));
+    case 4:
+      if (sp < 0) {
+        if (-sp > ss) return v1;
+        return sub3(v0, scl3(sp / ss, sv));
+      } else if (tp < 0) {
+        if (-tp > tt) return v2;
+        return sub3(v0, scl3(tp / tt, tv));
+      }
+      return v0;
+    case 5:
+      if (sp >= 0.0) return v0;
+      if (-sp >= ss) return v1;
+      return sub3(v0, scl3(sp / ss, sv));
+    default: {
+      t = st + tp;
+      s = ss + sp;
+      if (s > t) {
+        const double num = t - s;
+        const double den = tt - 2 * st + ss;
+        if (num > den) return v2;
+        t = num / den;
+        s = 1 - t;
+        return add3(scl3(s, v1), scl3(t, v2));
+      } else if (s <= 0) {
+        return v1;
+      } else if (sp >= 0) {
+        return v0;
+      }
+      return sub3(v0, scl3(sp / ss, sv));
+    }
+  }
+}
+
+// length of (a - p) as Vec3da::length (vec3da.h:58-59)
+__host__ __device__ __forceinline__ double dist64(d3 a, d3 p) {
+  const d3 w = sub3(a, p);
+  return sqrt(w.x * w.x + w.y * w.y + w.z * w.z);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 pre-filter
+// ---------------------------------------------------------------------------
+//
+// The exact Plucker coordinate of edge va->vb for the ray (o, d) is the triple
+// product  pip = d . ((vb - va) x (va - o))  (expand plucker.h:45-62:
+// d.(e x va) + (d x o).e = d.(e x va) - d.(e x o)).  The filter evaluates it
+// in FP32 from
+//    v0 = fl32(v0),  e1 = fl32(v1 - v0),  e2 = fl32(v2 - v0)   (stored per prim)
+//    w0 = v0 - o32,  w1 = w0 + e1,  w2 = w0 + e2
+//    pip01 = d.(e1 x w0), pip12 = d.((e2-e1) x w1), pip20 = d.((-e2) x w2)
+// and bounds its distance to the exact value by standard rounding analysis
+// (u = 2^-24; every stored/rounded input contributes u|x|, each 6-term triple
+// product is evaluated with at most 5 roundings per term, gamma_5 ~ 5u):
+//    |pip32 - pip| <= u * D * E * (68 W0 + 76 E + 7 A)
+// with D = |d|_inf, E = max edge |.|_inf, W0 = |w0|_inf, A = |v0|_inf + |o|_inf.
+// The FP64 evaluation in plucker64 is within 2^-46 * D * E * (A + 2E) of the
+// exact value, and values with |pip64| < 20*DBL_EPSILON are snapped to zero.
+// Hence if |pip32| exceeds the sum of the three terms, pip64 is non-zero and
+// has pip32's sign.  Inputs that overflow FP32 give inf/NaN, which never pass
+// the comparison and therefore escalate.
+struct Ray32 {
+  float ox, oy, oz;     // fl32(o)
+  float dx, dy, dz;     // fl32(d)
+  float du;             // u * |d|_inf * (1 + 2^-20)
+  float oabs;           // |fl32(o)|_inf
+};
+
+__device__ __forceinline__ Ray32 make_ray32(d3 o, d3 d) {
+  Ray32 r;
+  r.ox = __double2float_rn(o.x);
+  r.oy = __double2float_rn(o.y);
+  r.oz = __double2float_rn(o.z);
+  r.dx = __double2float_rn(d.x);
+  r.dy = __double2float_rn(d.y);
+  r.dz = __double2float_rn(d.z);
+  const float dmax = fmaxf(fabsf(r.dx), fmaxf(fabsf(r.dy), fabsf(r.dz)));
+  r.du = dmax * (5.9604645e-08f * 1.000001f);
+  r.oabs = fmaxf(fabsf(r.ox), fmaxf(fabsf(r.oy), fabsf(r.oz)));
+  return r;
+}
+
+// Returns a 3-bit sign code per coordinate: for coordinate k, bit pos[k] set
+// means "certainly > 0" and bit neg[k] "certainly < 0".  v0/e1/e2 as above;
+// emax = max |edge|_inf (stored per prim, rounded up); v0abs = |v0|_inf.
+struct SignCert {
+  unsigned pos, neg;
+};
+
+__device__ __forceinline__ float triple32(float dx, float dy, float dz, float ex, float ey,
+                                          float ez, float wx, float wy, float wz) {
+  const float cx = ey * wz - ez * wy;
+  const float cy = ez * wx - ex * wz;
+  const float cz = ex * wy - ey * wx;
+  return dx * cx + dy * cy + dz * cz;
+}
+
+__device__ __forceinline__ SignCert plucker_filter32(const Ray32& r, float v0x, float v0y,
+                                                     float v0z, float e1x, float e1y, float e1z,
+                                                     float e2x, float e2y, float e2z, float emax,
+                                                     float v0abs) {
+  const float w0x = v0x - r.ox, w0y = v0y - r.oy, w0z = v0z - r.oz;
+  const float w1x = w0x + e1x, w1y = w0y + e1y, w1z = w0z + e1z;
+  const float w2x = w0x + e2x, w2y = w0y + e2y, w2z = w0z + e2z;
+  const float p01 = triple32(r.dx, r.dy, r.dz, e1x, e1y, e1z, w0x, w0y, w0z);
+  const float p12 = triple32(r.dx, r.dy, r.dz, e2x - e1x, e2y - e1y, e2z - e1z, w1x, w1y, w1z);
+  const float p20 = triple32(r.dx, r.dy, r.dz, -e2x, -e2y, -e2z, w2x, w2y, w2z);
+  const float w0a = fmaxf(fabsf(w0x), fmaxf(fabsf(w0y), fabsf(w0z)));
+  const float A = v0abs + r.oabs;
+  // u*D*E*(68 W0 + 76 E + 7 A) + 2^-46 D E (A + 2E) + 20 DBL_EPSILON, rounded up
+  const float de = r.du * emax;
+  const float thr = de * (68.0f * w0a + 76.0f * emax + 7.0001f * A) * 1.0001f + 4.5e-15f;
+  SignCert c;
+  c.pos = (p01 > thr ? 1u : 0u) | (p12 > thr ? 2u : 0u) | (p20 > thr ? 4u : 0u);
+  c.neg = (p01 < -thr ? 1u : 0u) | (p12 < -thr ? 2u : 0u) | (p20 < -thr ? 4u : 0u);
+  return c;
+}
+
+// Non-oriented test (ray_fire, point_in_volume, occluded): the FP64 test
+// rejects whenever two coordinates have strictly opposite signs
+// (plucker.h:99-121), so a certified opposite pair is a certified miss.
+__device__ __forceinline__ bool certified_miss(SignCert c) { return c.pos != 0u && c.neg != 0u; }
+
+}  // namespace xdgcu

@@ -1,0 +1,61 @@
+// queries.h -- launch interface of the tree-query kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "internal.cuh"
+
+namespace xdgcu {
+
+enum QueryMode : int { MODE_RAY_FIRE = 0, MODE_PIV = 1, MODE_OCCLUDED = 2 };
+
+struct SurfArgs {
+  const TreeDev* trees;  // indexed by tree id - 1
+  int32_t n_trees;
+  int32_t tree;
+  const int32_t* ray_trees;
+  int64_t n;
+  const double* org;
+  const double* dir;
+  const double* tmax;
+  int32_t orientation;
+  const int32_t* excl_off;
+  const int32_t* excl_ids;
+  // geometry tables (global triangle / surface index)
+  const int32_t* tri_face;
+  const int32_t* tri_surf;
+  const int32_t* surf_id;
+  const int32_t* surf_rev_tree;
+  // outputs (any may be null where the mode does not write them)
+  double* t_out;
+  int32_t* surf_out;
+  int32_t* face_out;
+  int32_t* flag_out;   // PIV inside / occluded flag
+  double* dist_out;    // occluded distance
+  int32_t* status;
+  unsigned long long* counters;
+};
+
+struct PointArgs {
+  const TreeDev* trees;
+  int32_t n_trees;
+  int32_t tree;
+  const int32_t* ray_trees;
+  int64_t n;
+  const double* pts;
+  const int32_t* tri_face;   // closest: face ids
+  const int32_t* elem_ids;   // find_element: element mesh ids
+  double* dist_out;
+  int32_t* id_out;
+  int32_t* index_out;
+  int32_t* status;
+  unsigned long long* counters;
+};
+
+cudaError_t launch_surface_query(int mode, bool mixed, const SurfArgs& a, cudaStream_t st);
+cudaError_t launch_closest(bool mixed, const PointArgs& a, cudaStream_t st);
+cudaError_t launch_find_element(bool mixed, const PointArgs& a, cudaStream_t st);
+
+}  // namespace xdgcu

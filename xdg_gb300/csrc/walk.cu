@@ -1,0 +1,286 @@
+// walk.cu -- face-adjacency tet walk (MeshManager::next_element /
+// walk_elements, mesh_manager_interface.cpp:106-200) on the GPU.
+//
+// One thread walks one track.  Each step tests the four faces of the current
+// tet for an exiting Plucker hit (orientation +1, plucker.h:64-161), takes
+// the nearest (strict <, lowest face index on ties, :186-196), emits
+// (element id, min(exit, remaining)) -- zero-length segments included -- and
+// moves r += len * u in FP64, exactly like :117-133.
+//
+// The FP64 variant evaluates all four faces with plucker64.  The mixed
+// variant first evaluates the six edge coordinates of the tet once in FP32
+// (each face uses three of them, with a sign flip when it runs an edge
+// backwards -- the exact coordinates of opposite directions are exact
+// negatives) and skips a face only when some coordinate is certainly
+// positive, which makes the FP64 test exit early (plucker.h:83-113).  The
+// remaining faces -- normally just the exit face -- are evaluated with
+// plucker64, so lengths and element sequences are bit-identical.
+//
+// FP32 bound for a tet (u = 2^-24, D = |u|_inf, W = max |v_k - r|_inf,
+// Av = max |v_k|_inf, A = Av + |r|_inf; vertices and r rounded to FP32
+// individually, edges e = v_b - v_a so |e| <= 2W):
+//    |pip32 - pip| <= u D W (97 W + 13 Av + 13 A)
+// (gamma_5 rounding of the triple product plus the input perturbations; the
+// FP64 evaluation error and the 20*DBL_EPSILON snap are added as in geom.cuh).
+#include "walk.h"
+
+#include "internal.cuh"
+
+namespace xdgcu {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr float kU32 = 5.9604645e-08f;
+
+// MOAB canonical face order (moab/direct_access.h:181-183)
+__device__ __forceinline__ constexpr int moab_face(int f, int j) {
+  return (f == 0) ? (j == 0 ? 0 : (j == 1 ? 1 : 3))
+         : (f == 1) ? (j == 0 ? 1 : (j == 1 ? 2 : 3))
+         : (f == 2) ? (j == 0 ? 2 : (j == 1 ? 0 : 3))
+                    : (j == 0 ? 0 : (j == 1 ? 2 : 1));
+}
+
+template <int FO>
+__device__ __forceinline__ int face_local(const WalkArgs& a, int f, int j) {
+  if (FO == 0) return moab_face(f, j);
+  return a.face[3 * f + j];
+}
+
+template <typename T>
+__device__ __forceinline__ T sel4(const T* v, int k) {
+  return k == 0 ? v[0] : (k == 1 ? v[1] : (k == 2 ? v[2] : v[3]));
+}
+
+__device__ __forceinline__ float sel6(const float* v, int k) {
+  return k == 0 ? v[0]
+                : (k == 1 ? v[1] : (k == 2 ? v[2] : (k == 3 ? v[3] : (k == 4 ? v[4] : v[5]))));
+}
+
+__device__ __forceinline__ float triple32(float dx, float dy, float dz, float ex, float ey,
+                                          float ez, float wx, float wy, float wz) {
+  const float cx = ey * wz - ez * wy;
+  const float cy = ez * wx - ex * wz;
+  const float cz = ex * wy - ey * wx;
+  return dx * cx + dy * cy + dz * cz;
+}
+
+// index of the unordered vertex pair (i, j), i != j, in
+// (0,1),(0,2),(0,3),(1,2),(1,3),(2,3)
+__device__ __forceinline__ int pair_index(int i, int j) {
+  const int a = i < j ? i : j, b = i < j ? j : i;
+  return a == 0 ? b - 1 : (a == 1 ? b + 1 : 5);
+}
+
+struct StepCnt {
+  unsigned long long steps, esc;
+};
+
+// MeshManager::next_element for tet `elem` at r along u.  Returns the face
+// index (or -1) and writes the exit distance.
+template <int FO, bool MIXED>
+__device__ __forceinline__ int next_face(const WalkArgs& a, int32_t elem, d3 r, d3 u,
+                                         double* exit_dist, StepCnt& cnt) {
+  const int4 c = __ldg(&a.conn[elem]);
+  const int32_t ci[4] = {c.x, c.y, c.z, c.w};
+  const d3 rn = cross3(u, r);  // plucker.h:75
+  double dists[4];
+  if (!MIXED) {
+    d3 V[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) V[k] = load3(a.xyz, ci[k]);
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const d3 f0 = sel4(V, face_local<FO>(a, f, 0));
+      const d3 f1 = sel4(V, face_local<FO>(a, f, 1));
+      const d3 f2 = sel4(V, face_local<FO>(a, f, 2));
+      double t;
+      const bool hit = plucker64(f0, f1, f2, r, u, rn, INFTY, 0.0, true, 1, &t);
+      dists[f] = hit ? ((0.0 < t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
+    }
+    cnt.esc += 4;
+  } else {
+    float4 P[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) P[k] = __ldg(&a.xyz32[ci[k]]);
+    const float rx = __double2float_rn(r.x), ry = __double2float_rn(r.y),
+                rz = __double2float_rn(r.z);
+    const float ux = __double2float_rn(u.x), uy = __double2float_rn(u.y),
+                uz = __double2float_rn(u.z);
+    float wx[4], wy[4], wz[4];
+    float W = 0.0f, Av = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      wx[k] = P[k].x - rx;
+      wy[k] = P[k].y - ry;
+      wz[k] = P[k].z - rz;
+      W = fmaxf(W, fmaxf(fabsf(wx[k]), fmaxf(fabsf(wy[k]), fabsf(wz[k]))));
+      Av = fmaxf(Av, P[k].w);
+    }
+    const float D = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz)));
+    const float A = Av + fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz)));
+    const float thr =
+        kU32 * 1.000001f * D * W * (97.0f * W + 13.0f * Av + 13.0f * A) * 1.0001f + 4.5e-15f;
+    // pip(i -> j) = u . ((v_j - v_i) x (v_i - r)) for the six pairs i < j
+    float pe[6];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = i + 1; j < 4; ++j)
+        pe[pair_index(i, j)] = triple32(ux, uy, uz, P[j].x - P[i].x, P[j].y - P[i].y,
+                                        P[j].z - P[i].z, wx[i], wy[i], wz[i]);
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const int l0 = face_local<FO>(a, f, 0), l1 = face_local<FO>(a, f, 1),
+                l2 = face_local<FO>(a, f, 2);
+      const int e0 = pair_index(l0, l1), e1 = pair_index(l1, l2), e2 = pair_index(l2, l0);
+      const float p0 = l0 < l1 ? sel6(pe, e0) : -sel6(pe, e0);
+      const float p1 = l1 < l2 ? sel6(pe, e1) : -sel6(pe, e1);
+      const float p2 = l2 < l0 ? sel6(pe, e2) : -sel6(pe, e2);
+      dists[f] = INFTY;
+      if (p0 > thr || p1 > thr || p2 > thr) continue;  // certified early exit
+      cnt.esc++;
+      const d3 f0 = load3(a.xyz, ci[l0]);
+      const d3 f1 = load3(a.xyz, ci[l1]);
+      const d3 f2 = load3(a.xyz, ci[l2]);
+      double t;
+      const bool hit = plucker64(f0, f1, f2, r, u, rn, INFTY, 0.0, true, 1, &t);
+      dists[f] = hit ? ((0.0 < t) ? t : 0.0) : INFTY;
+    }
+  }
+  int idx = -1;
+  double best = INFTY;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    if (dists[f] < best) {
+      best = dists[f];
+      idx = f;
+    }
+  }
+  *exit_dist = best;
+  return idx;
+}
+
+__device__ __forceinline__ void flush(unsigned long long* g, const StepCnt& c, unsigned long long rays) {
+  unsigned long long v[3] = {c.steps, c.esc, rays};
+  for (int k = 0; k < 3; ++k) {
+    unsigned long long x = v[k];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(__activemask(), x, off);
+    v[k] = x;
+  }
+  if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
+    atomicAdd(&g[CNT_STEPS], v[0]);
+    atomicAdd(&g[CNT_ESCALATE], v[1]);
+    atomicAdd(&g[CNT_RAYS], v[2]);
+  }
+}
+
+template <int FO, bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  StepCnt cnt = {0, 0};
+  if (i < a.n) {
+    d3 r = load3(a.org, i);
+    const d3 u = load3(a.dir, i);
+    double dist = a.dist[i];
+    int32_t elem = a.start[i];
+    int32_t k = 0;
+    int32_t st = RAY_OK;
+    int32_t* oe = a.seg_elem + i * (int64_t)a.max_segs;
+    double* ol = a.seg_len + i * (int64_t)a.max_segs;
+    if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u) || isnan(dist)) {
+      st = RAY_INVALID;
+    } else {
+      while (dist > 0) {  // mesh_manager_interface.cpp:117
+        if (k >= a.max_segs) {
+          st = RAY_WALK_LIMIT;
+          break;
+        }
+        cnt.steps++;
+        double ex;
+        const int f = next_face<FO, MIXED>(a, elem, r, u, &ex, cnt);
+        int32_t nxt = -1;
+        if (f < 0) {
+          st = RAY_NO_EXIT_FACE;  // the reference would index adjacency with -1
+        } else {
+          const int4 ad = __ldg(&a.adj[elem]);
+          nxt = f == 0 ? ad.x : (f == 1 ? ad.y : (f == 2 ? ad.z : ad.w));
+        }
+        ex = (dist < ex) ? dist : ex;  // std::min(exit, distance)
+        dist -= ex;
+        oe[k] = __ldg(&a.elem_ids[elem]);
+        ol[k] = ex;
+        ++k;
+        r = add3(r, scl3(ex, u));  // r += exit.second * u
+        if (nxt < -1 || nxt >= a.n_tets) {
+          st = RAY_INVALID;  // corrupt adjacency: stop instead of reading out of range
+          break;
+        }
+        elem = nxt;
+        if (elem == -1) break;
+      }
+    }
+    a.seg_count[i] = k;
+    if (a.status) a.status[i] = st;
+  }
+  if (a.counters) flush(a.counters, cnt, i < a.n ? 1ull : 0ull);
+}
+
+template <int FO, bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_next(WalkArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  StepCnt cnt = {0, 0};
+  if (i < a.n) {
+    const d3 r = load3(a.org, i);
+    const d3 u = load3(a.dir, i);
+    const int32_t elem = a.start[i];
+    int32_t st = RAY_OK, nxt = -1;
+    double ex = INFTY;
+    if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u)) {
+      st = RAY_INVALID;
+    } else {
+      cnt.steps++;
+      const int f = next_face<FO, MIXED>(a, elem, r, u, &ex, cnt);
+      if (f < 0) {
+        st = RAY_NO_EXIT_FACE;
+      } else {
+        const int4 ad = __ldg(&a.adj[elem]);
+        nxt = f == 0 ? ad.x : (f == 1 ? ad.y : (f == 2 ? ad.z : ad.w));
+      }
+    }
+    a.next_out[i] = nxt;
+    a.dist_out[i] = ex;
+    if (a.status) a.status[i] = st;
+  }
+  if (a.counters) flush(a.counters, cnt, i < a.n ? 1ull : 0ull);
+}
+
+}  // namespace
+
+cudaError_t launch_walk(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)((a.n + kBlock - 1) / kBlock);
+  const int sel = (face_order == 0 ? 0 : 2) + (mixed ? 1 : 0);
+  switch (sel) {
+    case 0: k_walk<0, false><<<g, kBlock, 0, st>>>(a); break;
+    case 1: k_walk<0, true><<<g, kBlock, 0, st>>>(a); break;
+    case 2: k_walk<1, false><<<g, kBlock, 0, st>>>(a); break;
+    default: k_walk<1, true><<<g, kBlock, 0, st>>>(a); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_next_element(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  const unsigned g = (unsigned)((a.n + kBlock - 1) / kBlock);
+  const int sel = (face_order == 0 ? 0 : 2) + (mixed ? 1 : 0);
+  switch (sel) {
+    case 0: k_next<0, false><<<g, kBlock, 0, st>>>(a); break;
+    case 1: k_next<0, true><<<g, kBlock, 0, st>>>(a); break;
+    case 2: k_next<1, false><<<g, kBlock, 0, st>>>(a); break;
+    default: k_next<1, true><<<g, kBlock, 0, st>>>(a); break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace xdgcu

@@ -1,0 +1,38 @@
+// walk.h -- launch interface of the tet-walk kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace xdgcu {
+
+struct WalkArgs {
+  const double* xyz;     // 3 doubles per vertex
+  const float4* xyz32;   // fl32 vertex, w = |v|_inf
+  const int4* conn;      // 4 vertex indices per tet
+  const int4* adj;       // 4 neighbour tets per tet (-1 boundary), face order
+  const int32_t* elem_ids;
+  int32_t n_tets;
+  int32_t face[12];      // local face table
+  int64_t n;
+  const int32_t* start;  // tet index per track
+  const double* org;
+  const double* dir;
+  const double* dist;    // walk: track lengths
+  int32_t max_segs;
+  int32_t* seg_elem;
+  double* seg_len;
+  int32_t* seg_count;
+  int32_t* status;
+  int32_t* next_out;     // next_element mode
+  double* dist_out;
+  unsigned long long* counters;
+};
+
+// face_order: 0 = the MOAB table {0,1,3},{1,2,3},{2,0,3},{0,2,1} (compiled in),
+// 1 = any other table (read from WalkArgs::face).
+cudaError_t launch_walk(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st);
+cudaError_t launch_next_element(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st);
+
+}  // namespace xdgcu

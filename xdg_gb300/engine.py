@@ -1,0 +1,491 @@
+"""Host-side mirror of XDG's RayTracer plugin API and XDG facade over the
+CUDA engine (C ABI in include/xdgcu.h).
+
+``CudaRayTracer`` follows xdg::RayTracer (include/xdg/ray_tracing_interface.h:
+16-147): register_volume / create_*_tree / ray_fire / point_in_volume /
+occluded / closest / find_element, tree ids counted from 1 per kind.  ``XDG``
+follows the facade in src/xdg.cpp (prepare_raytracer, per-volume dispatch,
+find_volume, segments).  Every query is batched: arrays of n rays in, arrays
+out.  NumPy inputs run through the host-staging path of the C ABI; torch CUDA
+tensors run on the device without copies, on torch's current stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import ANY, ENTERING, EXITING, FP64, MIXED, check  # noqa: F401
+
+INFTY = np.finfo(np.float64).max
+TINY_BIT = 1e-10  # constants.h:32
+ID_NONE = -1
+TREE_NONE = -1
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _addr(x):
+    """Device/host address of an array argument (None stays None)."""
+    if x is None:
+        return None
+    if _is_torch(x):
+        return ctypes.c_void_p(x.data_ptr())
+    return x.ctypes.data_as(ctypes.c_void_p)
+
+
+def _host(a, dtype, shape=None):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a.reshape(shape) if shape is not None else a
+
+
+class _Out:
+    """Allocates outputs of the same kind (numpy / torch cuda) as the inputs."""
+
+    def __init__(self, like):
+        self.torch = _is_torch(like)
+        if self.torch:
+            import torch
+            self._torch = torch
+            self.device = like.device
+
+    def f64(self, *shape):
+        if self.torch:
+            return self._torch.empty(shape, dtype=self._torch.float64, device=self.device)
+        return np.empty(shape, dtype=np.float64)
+
+    def i32(self, *shape):
+        if self.torch:
+            return self._torch.empty(shape, dtype=self._torch.int32, device=self.device)
+        return np.empty(shape, dtype=np.int32)
+
+    def stream(self):
+        if self.torch:
+            return ctypes.c_void_p(self._torch.cuda.current_stream(self.device).cuda_stream)
+        return None
+
+
+def _prep(x, dtype, cols=None):
+    if x is None:
+        return None
+    if _is_torch(x):
+        return x.contiguous()
+    return _host(x, dtype, (-1, cols) if cols else (-1,))
+
+
+def _csr(exclude, n, torch_like=None):
+    if exclude is None:
+        return None, None
+    off = np.zeros(n + 1, dtype=np.int32)
+    off[1:] = np.cumsum([len(e) for e in exclude])
+    ids = (np.concatenate([np.asarray(e, dtype=np.int32) for e in exclude]) if off[-1]
+           else np.zeros(1, dtype=np.int32))
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    if torch_like is not None and _is_torch(torch_like):
+        import torch
+        return (torch.from_numpy(off).to(torch_like.device),
+                torch.from_numpy(ids).to(torch_like.device))
+    return off, ids
+
+
+def volume_bounding_box(model, volume):
+    """MeshManager::volume_bounding_box (mesh_manager_interface.cpp:236-267).
+
+    Its BoundingBox starts at all zeros (bbox.h:17-25) and is then grown, so
+    the box always contains the origin; that quirk is kept.
+    """
+    lo = np.zeros(3)
+    hi = np.zeros(3)
+    for s, _ in model.volume_surfaces(volume):
+        x = s.vertices[s.triangles.reshape(-1)]
+        lo = np.minimum(lo, x.min(0))
+        hi = np.maximum(hi, x.max(0))
+    return lo, hi
+
+
+def bounding_box_bump(model, volume, numerical_precision=1e-3):
+    """RayTracer::bounding_box_bump (ray_tracing_interface.cpp:20-24)."""
+    lo, hi = volume_bounding_box(model, volume)
+    w = hi - lo
+    chord = np.sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2])
+    return max(chord * 1e-6, numerical_precision)
+
+
+class CudaRayTracer:
+    """The CUDA backend behind XDG's RayTracer interface."""
+
+    def __init__(self, device: int = 0):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.L.xdgcu_create(ctypes.byref(h), device)
+        check(rc, None, "xdgcu_create")
+        self.ctx = h
+        self.device = device
+        self._registered = set()
+        self._tets_set = False
+        self.global_surface_tree = TREE_NONE
+        self.global_element_tree = TREE_NONE
+        self.surface_trees = []
+        self.element_trees = []
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.xdgcu_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        check(rc, self.ctx, what)
+
+    def library(self):
+        return "CUDA"
+
+    # ---- registration -------------------------------------------------
+
+    def register_surface(self, surface):
+        """First-visit registration of a surface (embree/ray_tracer.cpp:107-147)."""
+        if surface.surface_id in self._registered:
+            return
+        xyz = surface.tri_xyz()
+        fid = _host(surface.face_ids, np.int32)
+        self._check(self.L.xdgcu_register_surface(self.ctx, int(surface.surface_id), len(fid),
+                                                   _addr(xyz), _addr(fid)),
+                    "register_surface")
+        self._registered.add(surface.surface_id)
+
+    def create_surface_tree(self, model, volume):
+        """RayTracer::create_surface_tree (embree/ray_tracer.cpp:49-105)."""
+        pairs = model.volume_surfaces(volume)
+        for s, _ in pairs:
+            self.register_surface(s)
+        ids = np.array([s.surface_id for s, _ in pairs], dtype=np.int32)
+        sense = np.array([sn for _, sn in pairs], dtype=np.int32)
+        bump = bounding_box_bump(model, volume)
+        tree = ctypes.c_int32(-1)
+        self._check(self.L.xdgcu_create_surface_tree(self.ctx, _addr(ids), _addr(sense), len(ids),
+                                                      float(bump), ctypes.byref(tree)),
+                    "create_surface_tree")
+        self.surface_trees.append(tree.value)
+        return tree.value
+
+    def set_tet_mesh(self, tets):
+        if self._tets_set:
+            return
+        v = _host(tets.vertices, np.float64, (-1, 3))
+        c = _host(tets.conn, np.int32, (-1, 4))
+        a = _host(tets.adj, np.int32, (-1, 4))
+        ids = _host(tets.elem_ids, np.int32)
+        ft = _host(tets.face_table, np.int32, (12,))
+        self._check(self.L.xdgcu_set_tet_mesh(self.ctx, len(v), _addr(v), len(c), _addr(c), _addr(a),
+                                               _addr(ids), _addr(ft)), "set_tet_mesh")
+        self._tets_set = True
+
+    def create_element_tree(self, model, volume):
+        """RayTracer::create_element_tree (embree/ray_tracer.cpp:149-188)."""
+        elems = model.volume_elements(volume)
+        if elems is None or len(elems) == 0:
+            return TREE_NONE
+        self.set_tet_mesh(model.tets)
+        e = _host(elems, np.int32)
+        tree = ctypes.c_int32(-1)
+        self._check(self.L.xdgcu_create_element_tree(self.ctx, _addr(e), len(e), ctypes.byref(tree)),
+                    "create_element_tree")
+        self.element_trees.append(tree.value)
+        return tree.value
+
+    def register_volume(self, model, volume):
+        """RayTracer::register_volume (embree/ray_tracer.cpp:38-47)."""
+        return self.create_surface_tree(model, volume), self.create_element_tree(model, volume)
+
+    def create_global_surface_tree(self):
+        tree = ctypes.c_int32(-1)
+        self._check(self.L.xdgcu_create_global_surface_tree(self.ctx, ctypes.byref(tree)),
+                    "create_global_surface_tree")
+        self.surface_trees.append(tree.value)
+        self.global_surface_tree = tree.value
+        return tree.value
+
+    def create_global_element_tree(self):
+        tree = ctypes.c_int32(-1)
+        self._check(self.L.xdgcu_create_global_element_tree(self.ctx, ctypes.byref(tree)),
+                    "create_global_element_tree")
+        self.element_trees.append(tree.value)
+        self.global_element_tree = tree.value
+        return tree.value
+
+    def init(self):
+        pass
+
+    def num_registered_trees(self):
+        return self.num_registered_surface_trees() + self.num_registered_element_trees()
+
+    def num_registered_surface_trees(self):
+        return int(self.L.xdgcu_num_surface_trees(self.ctx))
+
+    def num_registered_element_trees(self):
+        return int(self.L.xdgcu_num_element_trees(self.ctx))
+
+    def tree_info(self, tree, element=False):
+        out = (ctypes.c_int64 * 8)()
+        fn = self.L.xdgcu_element_tree_info if element else self.L.xdgcu_surface_tree_info
+        self._check(fn(self.ctx, int(tree), out), "tree_info")
+        return dict(nodes=out[0], prims=out[1], depth=out[2], bytes32=out[3], bytes64=out[4])
+
+    def set_counting(self, on: bool):
+        self._check(self.L.xdgcu_set_counting(self.ctx, 1 if on else 0), "set_counting")
+
+    def counters(self):
+        out = (ctypes.c_int64 * 8)()
+        self._check(self.L.xdgcu_get_counters(self.ctx, out), "get_counters")
+        return dict(box=out[0], node=out[1], prim=out[2], escalate=out[3], rays=out[4],
+                    steps=out[5])
+
+    # ---- queries ------------------------------------------------------
+
+    def ray_fire(self, tree, origins, dirs, dist_limit=None, orientation=EXITING, exclude=None,
+                 precision=MIXED, ray_trees=None, status=False, stream=None):
+        """Batched RayTracer::ray_fire.  Returns (t, surface, face[, status]).
+
+        ``exclude`` is a list of per-ray face-id lists (the reference's
+        exclude_primitives); the reference appends the hit face to it, which
+        the caller can do with the returned face ids."""
+        o = _prep(origins, np.float64, 3)
+        d = _prep(dirs, np.float64, 3)
+        n = o.shape[0]
+        dl = None
+        if dist_limit is not None:
+            dl = dist_limit if _is_torch(dist_limit) else _host(np.broadcast_to(dist_limit, (n,)),
+                                                                 np.float64)
+        rt = _prep(ray_trees, np.int32)
+        eo, ei = _csr(exclude, n, o)
+        out = _Out(o)
+        t, s, f, st = out.f64(n), out.i32(n), out.i32(n), out.i32(n)
+        self._check(self.L.xdgcu_ray_fire(self.ctx, int(tree or 0), _addr(rt), n, _addr(o), _addr(d),
+                                          _addr(dl), int(orientation), _addr(eo), _addr(ei),
+                                          _addr(t), _addr(s), _addr(f), _addr(st), int(precision),
+                                          stream if stream is not None else out.stream()),
+                    "ray_fire")
+        return (t, s, f, st) if status else (t, s, f)
+
+    def point_in_volume(self, tree, points, dirs=None, exclude=None, precision=MIXED,
+                        ray_trees=None, stream=None):
+        p = _prep(points, np.float64, 3)
+        d = _prep(dirs, np.float64, 3)
+        n = p.shape[0]
+        rt = _prep(ray_trees, np.int32)
+        eo, ei = _csr(exclude, n, p)
+        out = _Out(p)
+        r = out.i32(n)
+        self._check(self.L.xdgcu_point_in_volume(self.ctx, int(tree or 0), _addr(rt), n, _addr(p),
+                                                 _addr(d), _addr(eo), _addr(ei), _addr(r), None,
+                                                 int(precision),
+                                                 stream if stream is not None else out.stream()),
+                    "point_in_volume")
+        return r
+
+    def occluded(self, tree, origins, dirs, precision=MIXED, ray_trees=None, stream=None):
+        o = _prep(origins, np.float64, 3)
+        d = _prep(dirs, np.float64, 3)
+        n = o.shape[0]
+        rt = _prep(ray_trees, np.int32)
+        out = _Out(o)
+        occ, dist = out.i32(n), out.f64(n)
+        self._check(self.L.xdgcu_occluded(self.ctx, int(tree or 0), _addr(rt), n, _addr(o), _addr(d),
+                                          _addr(occ), _addr(dist), None, int(precision),
+                                          stream if stream is not None else out.stream()),
+                    "occluded")
+        return occ, dist
+
+    def closest(self, tree, points, precision=MIXED, ray_trees=None, stream=None):
+        p = _prep(points, np.float64, 3)
+        n = p.shape[0]
+        rt = _prep(ray_trees, np.int32)
+        out = _Out(p)
+        dist, face = out.f64(n), out.i32(n)
+        self._check(self.L.xdgcu_closest(self.ctx, int(tree or 0), _addr(rt), n, _addr(p),
+                                         _addr(dist), _addr(face), None, int(precision),
+                                         stream if stream is not None else out.stream()),
+                    "closest")
+        return dist, face
+
+    def find_element(self, tree, points, precision=MIXED, ray_trees=None, stream=None):
+        """Returns (element mesh id, tet index); tree None -> global tree."""
+        if tree is None:
+            tree = self.global_element_tree
+        p = _prep(points, np.float64, 3)
+        n = p.shape[0]
+        rt = _prep(ray_trees, np.int32)
+        out = _Out(p)
+        eid, eidx = out.i32(n), out.i32(n)
+        self._check(self.L.xdgcu_find_element(self.ctx, int(tree or 0), _addr(rt), n, _addr(p),
+                                              _addr(eid), _addr(eidx), None, int(precision),
+                                              stream if stream is not None else out.stream()),
+                    "find_element")
+        return eid, eidx
+
+    def next_element(self, elem_index, positions, dirs, precision=MIXED, stream=None):
+        e = _prep(elem_index, np.int32)
+        r = _prep(positions, np.float64, 3)
+        u = _prep(dirs, np.float64, 3)
+        n = r.shape[0]
+        out = _Out(r)
+        nxt, dist, st = out.i32(n), out.f64(n), out.i32(n)
+        self._check(self.L.xdgcu_next_element(self.ctx, n, _addr(e), _addr(r), _addr(u), _addr(nxt),
+                                              _addr(dist), _addr(st), int(precision),
+                                              stream if stream is not None else out.stream()),
+                    "next_element")
+        return nxt, dist, st
+
+    def walk_elements(self, start_index, start, u, distance, max_segs=256, precision=MIXED,
+                      stream=None):
+        """Returns (seg_elem [n, max_segs], seg_len, seg_count, status)."""
+        e = _prep(start_index, np.int32)
+        r = _prep(start, np.float64, 3)
+        uu = _prep(u, np.float64, 3)
+        n = r.shape[0]
+        dist = distance if _is_torch(distance) else _host(np.broadcast_to(distance, (n,)),
+                                                           np.float64)
+        out = _Out(r)
+        se, sl, sc, st = out.i32(n, max_segs), out.f64(n, max_segs), out.i32(n), out.i32(n)
+        self._check(self.L.xdgcu_walk_elements(self.ctx, n, _addr(e), _addr(r), _addr(uu),
+                                               _addr(dist), int(max_segs), _addr(se), _addr(sl),
+                                               _addr(sc), _addr(st), int(precision),
+                                               stream if stream is not None else out.stream()),
+                    "walk_elements")
+        return se, sl, sc, st
+
+
+class XDG:
+    """The XDG facade (src/xdg.cpp) over a model and the CUDA ray tracer."""
+
+    def __init__(self, model, device: int = 0, ray_tracer: CudaRayTracer | None = None):
+        self.model = model
+        self.rti = ray_tracer or CudaRayTracer(device)
+        self.volume_to_surface_tree = {}
+        self.volume_to_point_location_tree = {}
+
+    def ray_tracing_interface(self):
+        return self.rti
+
+    def prepare_volume_for_raytracing(self, volume):
+        st, et = self.rti.register_volume(self.model, volume)
+        self.volume_to_surface_tree[volume] = st
+        self.volume_to_point_location_tree[volume] = et
+
+    def prepare_raytracer(self):
+        """xdg.cpp:37-47."""
+        for v in self.model.volumes:
+            self.prepare_volume_for_raytracing(v)
+        self.rti.create_global_element_tree()
+        self.rti.create_global_surface_tree()
+        self.rti.init()
+
+    def _trees(self, volumes):
+        v = np.asarray(volumes)
+        return np.array([self.volume_to_surface_tree[int(x)] for x in v.reshape(-1)],
+                        dtype=np.int32)
+
+    def ray_fire(self, volume, origins, dirs, dist_limit=None, orientation=EXITING, exclude=None,
+                 precision=MIXED):
+        """xdg.cpp:237-247 (volume may be one id or one per ray)."""
+        if np.ndim(volume) == 0:
+            return self.rti.ray_fire(self.volume_to_surface_tree[int(volume)], origins, dirs,
+                                     dist_limit, orientation, exclude, precision)
+        return self.rti.ray_fire(0, origins, dirs, dist_limit, orientation, exclude, precision,
+                                 ray_trees=self._trees(volume))
+
+    def point_in_volume(self, volume, points, dirs=None, exclude=None, precision=MIXED):
+        """xdg.cpp:104-111."""
+        if np.ndim(volume) == 0:
+            return self.rti.point_in_volume(self.volume_to_surface_tree[int(volume)], points, dirs,
+                                            exclude, precision)
+        return self.rti.point_in_volume(0, points, dirs, exclude, precision,
+                                        ray_trees=self._trees(volume))
+
+    def find_volume(self, points, dirs, precision=MIXED):
+        """xdg.cpp:113-128: first non-implicit-complement volume whose
+        point_in_volume is true, else the implicit complement.  Volumes are
+        tried in ascending id order."""
+        p = _host(points, np.float64, (-1, 3))
+        d = _host(dirs, np.float64, (-1, 3))
+        ipc = self.model.implicit_complement
+        out = np.full(len(p), ipc, dtype=np.int32)
+        todo = np.arange(len(p))
+        for v in sorted(self.volume_to_surface_tree):
+            if v == ipc or len(todo) == 0:
+                continue
+            inside = self.point_in_volume(v, p[todo], d[todo], precision=precision).astype(bool)
+            out[todo[inside]] = v
+            todo = todo[~inside]
+        return out
+
+    def find_element(self, points, volume=None, precision=MIXED):
+        """xdg.cpp:130-140 (global tree when volume is None)."""
+        tree = None if volume is None else self.volume_to_point_location_tree[int(volume)]
+        return self.rti.find_element(tree, points, precision)
+
+    def closest(self, volume, points, precision=MIXED):
+        """xdg.cpp:249-254."""
+        return self.rti.closest(self.volume_to_surface_tree[int(volume)], points, precision)
+
+    def occluded(self, volume, origins, dirs, precision=MIXED):
+        """xdg.cpp:263-270."""
+        return self.rti.occluded(self.volume_to_surface_tree[int(volume)], origins, dirs, precision)
+
+    def next_element(self, elem_index, r, u, precision=MIXED):
+        return self.rti.next_element(elem_index, r, u, precision)
+
+    def segments(self, volume, starts, ends, max_segs=1024, precision=MIXED):
+        """XDG::segments(volume, start, end) (xdg.cpp:200-227) for n tracks.
+
+        Returns a list of (element ids, lengths) per track."""
+        s = _host(starts, np.float64, (-1, 3))
+        e = _host(ends, np.float64, (-1, 3))
+        n = len(s)
+        tree = self.volume_to_point_location_tree[int(volume)]
+        u = _normalize_rows(e - s)
+        start_copy = s.copy()
+        eid, eidx = self.rti.find_element(tree, s, precision)
+        eidx = eidx.copy()
+        miss = np.nonzero(eidx < 0)[0]
+        valid = np.ones(n, dtype=bool)
+        if len(miss):
+            t, surf, _ = self.ray_fire(volume, s[miss], u[miss], None, ENTERING,
+                                       precision=precision)
+            hit = surf != ID_NONE
+            valid[miss[~hit]] = False
+            m = miss[hit]
+            th = t[hit]
+            nudged = s[m] + u[m] * (th + TINY_BIT)[:, None]
+            _, idx2 = self.rti.find_element(tree, nudged, precision)
+            valid[m[idx2 < 0]] = False
+            eidx[m] = idx2
+            start_copy[m] = s[m] + u[m] * th[:, None]
+        # walk_elements(start, end) overload (mesh_manager_interface.cpp:138-147)
+        w = e - start_copy
+        dist = np.sqrt(w[:, 0] * w[:, 0] + w[:, 1] * w[:, 1] + w[:, 2] * w[:, 2])
+        uw = _normalize_rows(w)
+        idx = np.nonzero(valid)[0]
+        out = [(np.zeros(0, dtype=np.int32), np.zeros(0)) for _ in range(n)]
+        if len(idx):
+            se, sl, sc, st = self.rti.walk_elements(eidx[idx], start_copy[idx], uw[idx], dist[idx],
+                                                    max_segs, precision)
+            for k, i in enumerate(idx):
+                out[i] = (se[k, :sc[k]].copy(), sl[k, :sc[k]].copy())
+        return out
+
+
+def _normalize_rows(v):
+    """Vec3da::normalize (vec3da.h:61-66), row-wise."""
+    min_rcp = float(np.float32(np.float64(np.finfo(np.float32).tiny) * 1e5))
+    ln = np.sqrt(v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2])
+    ln = np.where(ln < min_rcp, min_rcp, ln)
+    return v / ln[:, None]
