@@ -1,0 +1,540 @@
+"""Benchmark of the XDG ray-query hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+Headline workload (one JSON line on rank 0): 8 nested, radially jittered
+level-6 icospheres (radii 1..8, 9 volumes) and 1e7 rays from uniform points
+in [-9,9]^3 with isotropic directions, each fired (EXITING) in the volume
+point_in_volume/find_volume assigns it.  One step = one batched ray_fire of
+all 1e7 rays, inputs resident in HBM; `value` is mixed-precision Mrays/s.
+Beside it the line reports the all-FP64 path on the same rays, the 1e7
+point_in_volume queries, and the tet-walk workload (50^3 hexes x 6 jittered
+Kuhn tets = 750,000 tets, 1e6 tracks: find_element + walk_elements) in
+Msegs/s for both precisions, plus id/distance agreement between the two
+precisions and against the CPU oracle on a sample.
+
+All inputs are seeded synthetic data (the reference's model files are not
+available).  The streamed inputs (1e7 rays x 52 B = 520 MB) exceed the
+129 MB L2, so no explicit L2 flush is done between steps; the BVHs (the
+model) stay cache resident, as they would in production.
+
+--impl reference times the reference algorithm on the host cores instead:
+the C restatement of the reference's FP64 path (oracle/, BVH mode, OpenMP on
+every core), on a bounded sample of the same rays per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from xdg_gb300 import dist, synth  # noqa: E402
+
+METRIC = "ray_fire Mrays/s, tet-walk Msegs/s on 1 GB300: mixed vs FP64, 0 ID mismatches"
+N_RAYS = 10_000_000
+N_TRACKS = 1_000_000
+MAX_SEGS = 512
+WORKLOAD = "nested_spheres_8x_icosphere_L6_jitter1e-3_1e7_rays"
+WALK_WORKLOAD = "tet_cube_50^3x6_kuhn_jitter0.2_1e6_tracks_exp5"
+CPU_SAMPLE = 4_000_000      # rays of the same workload timed on the host cores
+REF_STEP_SAMPLE = 1_000_000  # rays per step of --impl reference
+BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
+BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
+BYTES_TRI64 = 76            # 72 B FP64 triangle + 4 B id (escalations)
+BYTES_IO = 68               # 48 B origin/dir + 4 B tree id in, 8 B t + 4 B surface + 4 B face out
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# --------------------------------------------------------------------------
+# workloads
+# --------------------------------------------------------------------------
+
+def c2_rays(n, seed):
+    rng = np.random.default_rng(seed)
+    p = rng.uniform(-9.0, 9.0, (n, 3))
+    d = synth.isotropic_dirs(rng, n)
+    return np.ascontiguousarray(p), np.ascontiguousarray(d)
+
+
+def c5_tracks(n, seed):
+    rng = np.random.default_rng(seed)
+    s = rng.uniform(0.0, 10.0, (n, 3))
+    u = synth.isotropic_dirs(rng, n)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t1 = (0.0 - s) / u
+        t2 = (10.0 - s) / u
+    ex = np.where(u > 0, t2, np.where(u < 0, t1, np.inf)).min(axis=1)
+    length = np.minimum(rng.exponential(5.0, n), ex)
+    return np.ascontiguousarray(s), np.ascontiguousarray(u), np.ascontiguousarray(length)
+
+
+# --------------------------------------------------------------------------
+# clocks
+# --------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-ray DRAM bytes of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ray_fire_mixed_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+# --------------------------------------------------------------------------
+# reference arm (host cores)
+# --------------------------------------------------------------------------
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from oracle import oracle as xo
+    xo.build()
+    cores = os.cpu_count() or 1
+    model = synth.nested_spheres(8, 6, 1e-3, 7)
+    trees = {v: xo.volume_tree(model, v) for v in model.volumes}
+    p, d = c2_rays(REF_STEP_SAMPLE, dist.rank_seed(1234, 0))
+    vols = oracle_find_volume(trees, model, p, d, cores)
+
+    def step():
+        for v in model.volumes:
+            sel = np.nonzero(vols == v)[0]
+            if len(sel):
+                trees[v].ray_fire(p[sel], d[sel], threads=cores)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / args.steps
+    value = REF_STEP_SAMPLE / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "rays_per_step": REF_STEP_SAMPLE},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": f"{REF_STEP_SAMPLE} rays of the workload per step"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def oracle_find_volume(trees, model, p, d, cores):
+    vols = np.full(len(p), model.implicit_complement, dtype=np.int32)
+    todo = np.arange(len(p))
+    for v in sorted(model.volumes):
+        if v == model.implicit_complement or len(todo) == 0:
+            continue
+        ins = trees[v].point_in_volume(p[todo], d[todo], threads=cores).astype(bool)
+        vols[todo[ins]] = v
+        todo = todo[~ins]
+    return vols
+
+
+# --------------------------------------------------------------------------
+# engine arm
+# --------------------------------------------------------------------------
+
+def timed(torch, fn, steps, warmup, world, stream):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    dist.barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier(world)
+    ms = e0.elapsed_time(e1) / steps
+    return dist.max_over_ranks(ms, world)
+
+
+def run_engine(args, rank, world, local):
+    import torch
+
+    from xdg_gb300 import _lib
+    from xdg_gb300.engine import FP64, MIXED, XDG
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    L = _lib.load()
+
+    # ---- C2: nested spheres -------------------------------------------
+    t0 = time.perf_counter()
+    model = synth.nested_spheres(8, 6, 1e-3, 7)
+    x = XDG(model, device=local)
+    x.prepare_raytracer()
+    rti = x.rti
+    p_h, d_h = c2_rays(N_RAYS, dist.rank_seed(1234, rank))
+    vols_h = x.find_volume(p_h, d_h, precision=MIXED)  # volume of each ray origin
+    lut = np.zeros(max(model.volumes) + 1, dtype=np.int32)
+    for v, t in x.volume_to_surface_tree.items():
+        lut[v] = t
+    trees_h = lut[vols_h]
+    p = torch.from_numpy(p_h).to(dev)
+    d = torch.from_numpy(d_h).to(dev)
+    trees = torch.from_numpy(trees_h).to(dev)
+    t_out = torch.empty(N_RAYS, dtype=torch.float64, device=dev)
+    s_out = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+    f_out = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+    log(f"[bench] C2 setup {time.perf_counter() - t0:.1f}s, "
+        f"{sum(len(s.face_ids) for s in model.surfaces)} triangles")
+
+    def rf(prec, t=t_out, s=s_out, f=f_out):
+        def go():
+            rc = L.xdgcu_ray_fire(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), N_RAYS,
+                                  ctypes.c_void_p(p.data_ptr()), ctypes.c_void_p(d.data_ptr()), None,
+                                  0, None, None, ctypes.c_void_p(t.data_ptr()),
+                                  ctypes.c_void_p(s.data_ptr()), ctypes.c_void_p(f.data_ptr()),
+                                  None, prec, sptr)
+            _lib.check(rc, rti.ctx, "ray_fire")
+        return go
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_mixed = timed(torch, rf(MIXED), args.steps, args.warmup, world, stream)
+    clk = clocks.stop()
+    t_mixed, s_mixed, f_mixed = t_out.clone(), s_out.clone(), f_out.clone()
+    ms_fp64 = timed(torch, rf(FP64), max(3, args.steps // 4), max(1, args.warmup // 2), world,
+                    stream)
+    id_mism = int((s_out != s_mixed).sum().item()) + int((f_out != f_mixed).sum().item())
+    t_mism = int((t_out != t_mixed).sum().item())
+    hit_frac = float((s_mixed >= 0).float().mean().item())
+
+    # point_in_volume of the same points in their own volume (all must be inside)
+    piv_out = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+
+    def piv(prec):
+        def go():
+            rc = L.xdgcu_point_in_volume(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), N_RAYS,
+                                         ctypes.c_void_p(p.data_ptr()), ctypes.c_void_p(d.data_ptr()),
+                                         None, None, ctypes.c_void_p(piv_out.data_ptr()), None,
+                                         prec, sptr)
+            _lib.check(rc, rti.ctx, "point_in_volume")
+        return go
+
+    ms_piv = timed(torch, piv(MIXED), max(3, args.steps // 2), 2, world, stream)
+    ipc = model.implicit_complement
+    not_ipc = torch.from_numpy(vols_h != ipc).to(dev)
+    piv_inside_frac = float(piv_out[not_ipc].float().mean().item()) if not_ipc.any() else 1.0
+    ms_piv64 = timed(torch, piv(FP64), 3, 1, world, stream)
+
+    # algorithmic work counters (untimed run)
+    rti.set_counting(True)
+    rf(MIXED)()
+    torch.cuda.synchronize()
+    cnt = rti.counters()
+    rti.set_counting(False)
+    rays = max(1, cnt["rays"])
+    per_ray = {k: cnt[k] / rays for k in ("node", "prim", "escalate")}
+    bytes_per_ray = (BYTES_IO + BYTES_NODE * per_ray["node"] + BYTES_TRI32 * per_ray["prim"]
+                     + BYTES_TRI64 * per_ray["escalate"])
+
+    # oracle agreement on a sample (rank 0)
+    oracle_mism = None
+    cpu_baseline = None
+    if rank == 0 and not args.no_oracle:
+        from oracle import oracle as xo
+        xo.build()
+        cores = os.cpu_count() or 1
+        t1 = time.perf_counter()
+        otrees = {v: xo.volume_tree(model, v) for v in model.volumes}
+        sample = np.arange(0, N_RAYS, N_RAYS // 100_000)
+        th, sh = t_mixed.cpu().numpy(), s_mixed.cpu().numpy()
+        mism = 0
+        for v in model.volumes:
+            sel = sample[vols_h[sample] == v]
+            if len(sel):
+                ot, os_, of = otrees[v].ray_fire(p_h[sel], d_h[sel], threads=cores)
+                mism += int((ot != th[sel]).sum() + (os_ != sh[sel]).sum())
+        oracle_mism = {"rays": int(len(sample)), "mismatches": mism}
+        # CPU baseline: the oracle (C restatement of the FP64 path) on the host cores
+        cs = min(CPU_SAMPLE, N_RAYS)
+        tc = time.perf_counter()
+        for v in model.volumes:
+            sel = np.nonzero(vols_h[:cs] == v)[0]
+            if len(sel):
+                otrees[v].ray_fire(p_h[sel], d_h[sel], threads=cores)
+        dtc = time.perf_counter() - tc
+        cpu_baseline = {"value": cs / dtc / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                        "sample": f"first {cs} rays of the workload, FP64, BVH, OpenMP"}
+        log(f"[bench] oracle check + cpu baseline {time.perf_counter() - t1:.1f}s")
+
+    # ---- e2e through the C ABI with pinned host buffers ------------------
+    org_h = torch.empty((N_RAYS, 3), dtype=torch.float64, pin_memory=True)
+    dir_h = torch.empty((N_RAYS, 3), dtype=torch.float64, pin_memory=True)
+    tr_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
+    org_h.copy_(torch.from_numpy(p_h))
+    dir_h.copy_(torch.from_numpy(d_h))
+    tr_h.copy_(torch.from_numpy(trees_h))
+    to_h = torch.empty(N_RAYS, dtype=torch.float64, pin_memory=True)
+    so_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
+    fo_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
+
+    def e2e_call():
+        rc = L.xdgcu_ray_fire(rti.ctx, 0, ctypes.c_void_p(tr_h.data_ptr()), N_RAYS,
+                              ctypes.c_void_p(org_h.data_ptr()), ctypes.c_void_p(dir_h.data_ptr()),
+                              None, 0, None, None, ctypes.c_void_p(to_h.data_ptr()),
+                              ctypes.c_void_p(so_h.data_ptr()), ctypes.c_void_p(fo_h.data_ptr()),
+                              None, MIXED, None)
+        _lib.check(rc, rti.ctx, "ray_fire (host buffers)")
+
+    for _ in range(2):
+        e2e_call()
+    torch.cuda.synchronize()
+    dist.barrier(world)
+    te = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_call()
+    torch.cuda.synchronize()
+    ms_e2e = dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world)
+    e2e_ok = bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    del org_h, dir_h, tr_h, to_h, so_h, fo_h
+
+    # ---- C5: tet walk ------------------------------------------------------
+    t0 = time.perf_counter()
+    tm = synth.tet_cube(50, 10.0, 0.2, 11)
+    wm = synth.Model(volumes=[1], tets=tm, elements={1: np.arange(len(tm.conn), dtype=np.int32)})
+    wr = XDG(wm, device=local)
+    wr.prepare_raytracer()
+    s_h, u_h, len_h = c5_tracks(N_TRACKS, dist.rank_seed(4321, rank))
+    ws = torch.from_numpy(s_h).to(dev)
+    wu = torch.from_numpy(u_h).to(dev)
+    wl = torch.from_numpy(len_h).to(dev)
+    we_idx = torch.empty(N_TRACKS, dtype=torch.int32, device=dev)
+    we_id = torch.empty(N_TRACKS, dtype=torch.int32, device=dev)
+    seg_e = torch.empty((N_TRACKS, MAX_SEGS), dtype=torch.int32, device=dev)
+    seg_l = torch.empty((N_TRACKS, MAX_SEGS), dtype=torch.float64, device=dev)
+    seg_c = torch.empty(N_TRACKS, dtype=torch.int32, device=dev)
+    wst = torch.empty(N_TRACKS, dtype=torch.int32, device=dev)
+    et = wr.volume_to_point_location_tree[1]
+    log(f"[bench] C5 setup {time.perf_counter() - t0:.1f}s")
+
+    def walk(prec, e=seg_e, ln=seg_l, c=seg_c):
+        def go():
+            rc = L.xdgcu_find_element(wr.rti.ctx, et, None, N_TRACKS, ctypes.c_void_p(ws.data_ptr()),
+                                      ctypes.c_void_p(we_id.data_ptr()),
+                                      ctypes.c_void_p(we_idx.data_ptr()), None, prec, sptr)
+            _lib.check(rc, wr.rti.ctx, "find_element")
+            rc = L.xdgcu_walk_elements(wr.rti.ctx, N_TRACKS, ctypes.c_void_p(we_idx.data_ptr()),
+                                       ctypes.c_void_p(ws.data_ptr()), ctypes.c_void_p(wu.data_ptr()),
+                                       ctypes.c_void_p(wl.data_ptr()), MAX_SEGS,
+                                       ctypes.c_void_p(e.data_ptr()), ctypes.c_void_p(ln.data_ptr()),
+                                       ctypes.c_void_p(c.data_ptr()), ctypes.c_void_p(wst.data_ptr()),
+                                       prec, sptr)
+            _lib.check(rc, wr.rti.ctx, "walk_elements")
+        return go
+
+    ms_walk = timed(torch, walk(MIXED), args.steps, args.warmup, world, stream)
+    n_segs = int(seg_c.sum().item())
+    walk_status_bad = int((wst != 0).sum().item())
+    c_mixed = seg_c.clone()
+    # FP64 path into separate buffers for the sequence comparison
+    seg_e64 = torch.empty_like(seg_e)
+    seg_l64 = torch.empty_like(seg_l)
+    seg_c64 = torch.empty_like(seg_c)
+    ms_walk64 = timed(torch, walk(FP64, seg_e64, seg_l64, seg_c64), max(3, args.steps // 4), 1,
+                      world, stream)
+    cols = torch.arange(MAX_SEGS, device=dev)[None, :]
+    valid = cols < c_mixed[:, None]
+    walk_elem_mism = int((seg_c64 != c_mixed).sum().item()) + int(
+        ((seg_e64 != seg_e) & valid).sum().item())
+    walk_len_mism = int(((seg_l64 != seg_l) & valid).sum().item())
+    del seg_e64, seg_l64
+
+    # ---- report -------------------------------------------------------------
+    total_rays = dist.sum_over_ranks(N_RAYS, world)
+    total_segs = dist.sum_over_ranks(n_segs, world)
+    value = total_rays / (ms_mixed / 1e3) / 1e6
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_per_ray * N_RAYS / (ms_mixed / 1e3) / 1e9
+    prof = profile_traffic()
+    traffic = None
+    if prof and prof.get("dram_bytes_per_ray"):
+        traffic = prof["dram_bytes_per_ray"] * N_RAYS
+    h2d = N_RAYS * (24 + 24 + 4)
+    d2h = N_RAYS * (8 + 4 + 4)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "Mrays/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mixed,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD,
+            "rays_per_gpu": N_RAYS,
+            "triangles": int(sum(len(s.face_ids) for s in model.surfaces)),
+            "volumes": len(model.volumes),
+            "precision": "mixed (FP32 boxes + certified FP32 Plucker filter, FP64 escalation)",
+            "l2": "streamed inputs 520 MB > 129 MB L2 per step; no flush",
+            "parallelism": f"replicas{world} (rays sharded by rank, geometry replicated)",
+        },
+        "fp64": {"value": total_rays / (ms_fp64 / 1e3) / 1e6, "unit": "Mrays/s",
+                 "ms_per_step": ms_fp64},
+        "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "id_mismatches_mixed_vs_fp64": id_mism,
+        "t_mismatches_mixed_vs_fp64": t_mism,
+        "hit_fraction": hit_frac,
+        "oracle_check": oracle_mism,
+        "escalations_per_ray": per_ray["escalate"],
+        "nodes_per_ray": per_ray["node"],
+        "prims_per_ray": per_ray["prim"],
+        "point_in_volume": {
+            "value": total_rays / (ms_piv / 1e3) / 1e6, "unit": "Mpoints/s",
+            "fp64_value": total_rays / (ms_piv64 / 1e3) / 1e6,
+            "inside_fraction_own_volume": piv_inside_frac,
+        },
+        "walk": {
+            "workload": WALK_WORKLOAD,
+            "value": total_segs / (ms_walk / 1e3) / 1e6, "unit": "Msegs/s",
+            "fp64_value": total_segs / (ms_walk64 / 1e3) / 1e6,
+            "ms_per_step": ms_walk, "fp64_ms_per_step": ms_walk64,
+            "segments": n_segs, "tracks": N_TRACKS,
+            "speedup_mixed_vs_fp64": ms_walk64 / ms_walk,
+            "element_mismatches_mixed_vs_fp64": walk_elem_mism,
+            "length_mismatches_mixed_vs_fp64": walk_len_mism,
+            "tracks_with_status": walk_status_bad,
+            "step": "find_element + walk_elements",
+        },
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": traffic,
+            "peak_kind": f"{peak_kind} HBM copy bandwidth",
+            "kernel": "k_surface<RAY_FIRE, mixed>",
+            "algorithmic_bytes_per_ray": bytes_per_ray,
+        },
+        "cpu_baseline": cpu_baseline,
+        "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "matches_device_path": e2e_ok},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-oracle", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local = dist.env_rank()
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        if args.impl == "engine":
+            torch.cuda.set_device(local)
+            tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            tdist.init_process_group("gloo")
+    try:
+        if args.impl == "reference":
+            return run_reference(args, rank, world)
+        return run_engine(args, rank, world, local)
+    finally:
+        if world > 1:
+            import torch.distributed as tdist
+            tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,453 @@
+// trace.cu -- warp-synchronous BVH traversal for ray_fire, point_in_volume
+// and occluded.
+//
+// GB300 issues FP64 at 1/64 of the FP32 rate, and an FP64 instruction costs
+// its full issue slot however few lanes of the warp are active.  So the
+// kernel keeps all per-lane work in FP32 and routes every FP64 evaluation
+// through a per-warp queue that the whole warp drains together:
+//
+//   * each lane owns one ray at a time and advances it by one step per loop
+//     iteration: either one 4-child node test or one triangle test;
+//   * a triangle test runs the certified FP32 Plucker filter (geom.cuh); a
+//     candidate it cannot reject is appended to the warp's queue;
+//   * when 32 candidates are queued (or lanes are waiting on the queue), all
+//     32 lanes evaluate one queued candidate each with the FP64 Plucker test
+//     and the hit bookkeeping of triangle_intersect.cpp:52-109, then each ray
+//     merges its own results (lowest (t, face id) wins, the fixed tie rule);
+//   * a lane whose ray is finished and has nothing queued writes its result
+//     and refills from the warp's contiguous chunk of rays (no global atomics),
+//     so long rays do not hold a whole warp idle.
+//
+// Merging candidates evaluated against an older best distance gives the same
+// answer as evaluating them one by one: the Plucker test's tMax only rejects
+// t > tMax (plucker.h:158) and every other cull is independent of the best
+// hit, so the result is the minimum over all accepted candidates.
+//
+// The all-FP64 variant (MIXED = false) uses the same loop with FP64 node
+// boxes and queues every candidate triangle.
+//
+// Why the FP32 box test never loses a hit: every primitive box is dilated by
+// `bump` (>= 1e-3 for surface trees, ray_tracing_interface.cpp:20-24), so the
+// exact slab interval of a ray around any hit point has slack bump/|d|_inf on
+// both sides, while the FP32 evaluation errs by at most ~5u(|box| + |o|).  A
+// ray for which 8u(max|coordinate| + |o|_inf) is not below the bump tests FP64
+// boxes instead (checked per ray, `use64`).
+//
+// Stack: 64 entries per lane in shared memory, [entry][thread] so that lanes
+// hit distinct banks; each entry keeps its near distance so entries beyond a
+// closer hit found meanwhile are discarded without fetching the node.
+#include "traverse.cuh"
+
+namespace xdgcu {
+
+namespace {
+
+constexpr int kTBlock = 128;
+constexpr int kTWarps = kTBlock / 32;
+constexpr int kTStack = 64;
+constexpr int kQ = 64;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct WarpQueue {
+  int32_t prim[kQ];
+  int32_t owner[kQ];
+  double rt[32];
+  int32_t rface[32];
+  int32_t rsurf[32];
+  int32_t rflags[32];  // bit 0: accepted, bit 1: dot(d, n) > 0
+  int32_t count;
+  int32_t pad[3];
+};
+
+struct TraceShared {
+  int32_t sref[kTStack][kTBlock];
+  float stn[kTStack][kTBlock];
+  WarpQueue q[kTWarps];
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+template <int MODE, bool MIXED>
+__global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TraceShared& S = *reinterpret_cast<TraceShared*>(smem_raw);
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int tx = threadIdx.x;
+  WarpQueue& Q = S.q[wib];
+  const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t cursor = gwarp * chunk;
+  const int64_t end = min(a.n, cursor + chunk);
+  if (lane == 0) Q.count = 0;
+  __syncwarp();
+
+  Counters cnt = {0, 0, 0, 0};
+  unsigned long long rays_done = 0;
+
+  // ---- lane state ----
+  bool has_ray = false, trav = false, use64 = false;
+  int64_t ray = 0;
+  int32_t tid = 0, status = RAY_OK, npend = 0;
+  d3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
+  const Node32* n32 = nullptr;
+  const Node64* n64 = nullptr;
+  const float4* prim32 = nullptr;
+  const double* prim64 = nullptr;
+  const int32_t* prim_ref = nullptr;
+  int32_t cur = CHILD_EMPTY, leaf_p = 0, leaf_end = 0;
+  int sp = 0;
+  double bt = INFTY;
+  float bt32 = INFINITY;
+  int32_t bface = -1, bsurf = -1;
+  bool bhas = false, bdot = false;
+  const int32_t* excl = nullptr;
+  int32_t nexcl = 0;
+  BoxRay32 br32;
+  Ray32 r32;
+  BoxRay64 br64;
+
+  auto pop = [&]() {
+    cur = CHILD_EMPTY;
+    while (sp > 0) {
+      --sp;
+      const int32_t r = S.sref[sp][tx];
+      const float t = S.stn[sp][tx];
+      if (t <= bt32) {
+        if (ref_is_leaf(r)) {
+          leaf_p = leaf_first(r);
+          leaf_end = leaf_p + leaf_count(r);
+        } else {
+          cur = r;
+        }
+        return;
+      }
+    }
+    trav = false;
+  };
+
+  while (true) {
+    // ---- finalize finished rays ----
+    if (has_ray && !trav && npend == 0) {
+      if (MODE == MODE_RAY_FIRE) {
+        a.t_out[ray] = bhas ? bt : INFTY;
+        a.surf_out[ray] = bhas ? bsurf : -1;
+        if (a.face_out) a.face_out[ray] = bhas ? bface : -1;
+      } else if (MODE == MODE_PIV) {
+        a.flag_out[ray] = (bhas && bdot) ? 1 : 0;  // embree/ray_tracer.cpp:282-286
+      } else {
+        a.flag_out[ray] = bhas ? 1 : 0;
+        if (a.dist_out) a.dist_out[ray] = bhas ? -INFTY : INFTY;  // :368-369
+      }
+      if (a.status) a.status[ray] = status;
+      has_ray = false;
+      rays_done++;
+    }
+    // ---- refill from the warp's chunk ----
+    const unsigned need = __ballot_sync(kFull, !has_ray);
+    if (need != 0u && cursor < end) {
+      if (!has_ray) {
+        const int64_t idx = cursor + __popc(need & lanemask_lt());
+        if (idx < end) {
+          ray = idx;
+          has_ray = true;
+          status = RAY_OK;
+          npend = 0;
+          sp = 0;
+          bhas = false;
+          bdot = false;
+          bface = -1;
+          bsurf = -1;
+          leaf_p = leaf_end = 0;
+          tid = a.ray_trees ? a.ray_trees[idx] : a.tree;
+          o = load3(a.org, idx);
+          if (MODE == MODE_PIV && a.dir == nullptr)
+            d = mk3(1. / sqrt(2.0), 1 / sqrt(2.0), 0.0);  // embree/ray_tracer.cpp:268
+          else
+            d = load3(a.dir, idx);
+          bt = (MODE == MODE_RAY_FIRE && a.tmax) ? a.tmax[idx] : INFTY;
+          excl = nullptr;
+          nexcl = 0;
+          if (MODE != MODE_OCCLUDED && a.excl_off) {
+            const int32_t e0 = a.excl_off[idx];
+            excl = a.excl_ids + e0;
+            nexcl = a.excl_off[idx + 1] - e0;
+          }
+          trav = true;
+          if (tid < 1 || tid > a.n_trees || !finite3(o) || !finite3(d) || isnan(bt)) {
+            status = RAY_INVALID;
+            trav = false;
+          } else {
+            const TreeDev* T = a.trees + (tid - 1);
+            n32 = T->n32;
+            n64 = T->n64;
+            prim32 = T->prim32;
+            prim64 = T->prim64;
+            prim_ref = T->prim_ref;
+            const int32_t root = T->root;
+            bt32 = (MODE == MODE_OCCLUDED) ? INFINITY : __double2float_ru(bt);
+            if (MIXED) {
+              br32 = make_boxray32(o, d);
+              r32 = make_ray32(o, d);
+              // FP32 box-test safety (see the file comment)
+              use64 = !(8.0f * kU32 * (T->max_abs + r32.oabs) < T->bump);
+            }
+            if (!MIXED || use64) br64 = make_boxray64(o, d);
+            if (root == CHILD_EMPTY) {
+              trav = false;
+            } else if (ref_is_leaf(root)) {
+              cur = CHILD_EMPTY;
+              leaf_p = leaf_first(root);
+              leaf_end = leaf_p + leaf_count(root);
+            } else {
+              cur = root;
+            }
+          }
+        }
+      }
+      cursor += __popc(need);
+    }
+    if (__ballot_sync(kFull, has_ray) == 0u) break;
+
+    // ---- one traversal step per active lane ----
+    const unsigned act = __ballot_sync(kFull, trav);
+    if (trav) {
+      bool esc = false;
+      int32_t esc_prim = 0;
+      if (leaf_p < leaf_end) {
+        const int32_t p = leaf_p++;
+        cnt.prim++;
+        if (MIXED) {
+          const float4 A = __ldg(&prim32[3 * (int64_t)p]);
+          const float4 B = __ldg(&prim32[3 * (int64_t)p + 1]);
+          const float4 C = __ldg(&prim32[3 * (int64_t)p + 2]);
+          const SignCert c = plucker_filter32(r32, A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y, C.z,
+                                              B.w, A.w);
+          esc = !certified_miss(c);
+        } else {
+          esc = true;
+        }
+        esc_prim = p;
+        if (leaf_p >= leaf_end && cur == CHILD_EMPTY) pop();
+      } else {
+        // inner node
+        cnt.node++;
+        cnt.box += 4;
+        int32_t cr[4];
+        float key[4];
+        if (MIXED && !use64) {
+          node_test32(n32 + cur, br32, bt32, key, cr);
+        } else {
+          double tn[4];
+          node_test64(n64 + cur, br64, (MODE == MODE_OCCLUDED) ? INFTY : bt, tn, cr);
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            key[k] = tn[k] < INFINITY ? __double2float_rd(tn[k]) : INFINITY;
+        }
+        sort4(key, cr);
+        int nhit = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) nhit += key[k] < INFINITY ? 1 : 0;
+        if (nhit == 0) {
+          pop();
+        } else if (sp + nhit - 1 > kTStack) {
+          status = RAY_STACK_OVERFLOW;
+          trav = false;
+        } else {
+          for (int k = nhit - 1; k >= 1; --k) {
+            S.sref[sp][tx] = cr[k];
+            S.stn[sp][tx] = key[k];
+            ++sp;
+          }
+          if (ref_is_leaf(cr[0])) {
+            cur = CHILD_EMPTY;
+            leaf_p = leaf_first(cr[0]);
+            leaf_end = leaf_p + leaf_count(cr[0]);
+          } else {
+            cur = cr[0];
+          }
+        }
+      }
+      // enqueue escalations (all lanes of `act` reach this point)
+      const unsigned m = __ballot_sync(act, esc);
+      if (m != 0u) {
+        const int base = Q.count;
+        __syncwarp(act);
+        if (esc) {
+          const int pos = base + __popc(m & lanemask_lt());
+          Q.prim[pos] = esc_prim;
+          Q.owner[pos] = lane;
+          npend++;
+          cnt.esc++;
+        }
+        if (lane == __ffs(m) - 1) Q.count = base + __popc(m);
+      }
+    }
+    __syncwarp();
+
+    // ---- drain the FP64 queue with the whole warp ----
+    const int qn = Q.count;
+    const unsigned act2 = __ballot_sync(kFull, trav);
+    const unsigned waiting = __ballot_sync(kFull, has_ray && !trav && npend > 0);
+    if (qn >= 32 || (qn > 0 && (act2 == 0u || __popc(waiting) >= 8))) {
+      const int nq = min(qn, 32);
+      const bool mine = lane < nq;
+      const int owner = mine ? Q.owner[lane] : lane;
+      const int32_t prim = mine ? Q.prim[lane] : 0;
+      // the owner's ray, tree and current best
+      d3 oo, od;
+      oo.x = __shfl_sync(kFull, o.x, owner);
+      oo.y = __shfl_sync(kFull, o.y, owner);
+      oo.z = __shfl_sync(kFull, o.z, owner);
+      od.x = __shfl_sync(kFull, d.x, owner);
+      od.y = __shfl_sync(kFull, d.y, owner);
+      od.z = __shfl_sync(kFull, d.z, owner);
+      const double obt = __shfl_sync(kFull, bt, owner);
+      const int32_t obface = __shfl_sync(kFull, bface, owner);
+      const bool obhas = __shfl_sync(kFull, bhas ? 1 : 0, owner) != 0;
+      const int32_t otid = __shfl_sync(kFull, tid, owner);
+      const double* op64 = reinterpret_cast<const double*>(
+          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(prim64), owner));
+      const int32_t* opref = reinterpret_cast<const int32_t*>(
+          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(prim_ref), owner));
+      const int32_t* oexcl = reinterpret_cast<const int32_t*>(
+          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(excl), owner));
+      const int32_t onexcl = __shfl_sync(kFull, nexcl, owner);
+      int32_t flags = 0;
+      double rt = 0.0;
+      int32_t rface = -1, rsurf = -1;
+      if (mine) {
+        d3 v0, v1, v2;
+        load_tri64(op64 + kPrim64Stride * (int64_t)prim, v0, v1, v2);
+        const d3 rn = cross3(od, oo);  // plucker.h:75
+        double t;
+        const double tmax = (MODE == MODE_OCCLUDED) ? INFTY : obt;
+        if (plucker64(v0, v1, v2, oo, od, rn, tmax, 0.0, false, 0, &t)) {
+          if (MODE == MODE_OCCLUDED) {
+            flags = 1;
+          } else if (!(t > obt)) {  // triangle_intersect.cpp:78
+            const int32_t gtri = __ldg(&opref[prim]);
+            const int32_t fid = __ldg(&a.tri_face[gtri]);
+            if (!(obhas && t == obt && fid >= obface)) {
+              d3 nrm = face_normal64(v0, v1, v2);  // :80
+              const int32_t sidx = __ldg(&a.tri_surf[gtri]);
+              if (__ldg(&a.surf_rev_tree[sidx]) == otid) nrm = neg3(nrm);  // :84-87
+              const double dp = dot3(od, nrm);
+              bool keep = true;
+              if (MODE == MODE_RAY_FIRE) {  // orientation_cull, :12-24
+                if (a.orientation == 0 && dp < 0.0) keep = false;
+                if (a.orientation == 1 && dp >= 0.0) keep = false;
+              }
+              for (int32_t k = 0; keep && k < onexcl; ++k)  // primitive_mask_cull, :26-34
+                if (__ldg(&oexcl[k]) == fid) keep = false;
+              if (keep) {
+                flags = 1 | (dp > 0.0 ? 2 : 0);
+                rt = t;
+                rface = fid;
+                rsurf = __ldg(&a.surf_id[sidx]);
+              }
+            }
+          }
+        }
+      }
+      Q.rflags[lane] = flags;
+      Q.rt[lane] = rt;
+      Q.rface[lane] = rface;
+      Q.rsurf[lane] = rsurf;
+      __syncwarp();
+      // each ray merges its own results in queue order
+      bool changed = false;
+      for (int j = 0; j < nq; ++j) {
+        if (Q.owner[j] != lane) continue;
+        npend--;
+        const int32_t fl = Q.rflags[j];
+        if (!(fl & 1)) continue;
+        if (MODE == MODE_OCCLUDED) {
+          bhas = true;
+          trav = false;
+          continue;
+        }
+        const double t = Q.rt[j];
+        const int32_t f = Q.rface[j];
+        if (!bhas || t < bt || (t == bt && f < bface)) {
+          bhas = true;
+          bt = t;
+          bface = f;
+          bsurf = Q.rsurf[j];
+          bdot = (fl & 2) != 0;
+          changed = true;
+        }
+      }
+      if (changed) bt32 = __double2float_ru(bt);
+      // keep the entries beyond the first 32
+      const int rest = qn - nq;
+      int32_t keep_prim = 0, keep_owner = 0;
+      if (lane < rest) {
+        keep_prim = Q.prim[nq + lane];
+        keep_owner = Q.owner[nq + lane];
+      }
+      __syncwarp();
+      if (lane < rest) {
+        Q.prim[lane] = keep_prim;
+        Q.owner[lane] = keep_owner;
+      }
+      if (lane == 0) Q.count = rest;
+      __syncwarp();
+    }
+  }
+  if (a.counters) {
+    // rays_done is per lane; flush_counters sums lanes
+    flush_counters(a.counters, cnt, rays_done);
+  }
+}
+
+int g_num_sms = 0;
+int g_blocks_per_sm[6] = {0, 0, 0, 0, 0, 0};
+
+template <int MODE, bool MIXED>
+cudaError_t launch_one(const SurfArgs& a, cudaStream_t st, int slot) {
+  const size_t smem = sizeof(TraceShared);
+  auto kern = k_trace<MODE, MIXED>;
+  if (g_blocks_per_sm[slot] == 0) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    int b = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kTBlock, smem);
+    if (e != cudaSuccess) return e;
+    g_blocks_per_sm[slot] = b > 0 ? b : 1;
+  }
+  const int64_t warps_needed = (a.n + 31) / 32;
+  int64_t blocks = (int64_t)g_num_sms * g_blocks_per_sm[slot];
+  const int64_t max_blocks = (warps_needed + kTWarps - 1) / kTWarps;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks < 1) blocks = 1;
+  const int64_t warps = blocks * kTWarps;
+  const int64_t chunk = (a.n + warps - 1) / warps;
+  kern<<<(unsigned)blocks, kTBlock, smem, st>>>(a, chunk);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_surface_query(int mode, bool mixed, const SurfArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  switch (mode * 2 + (mixed ? 1 : 0)) {
+    case 0: return launch_one<MODE_RAY_FIRE, false>(a, st, 0);
+    case 1: return launch_one<MODE_RAY_FIRE, true>(a, st, 1);
+    case 2: return launch_one<MODE_PIV, false>(a, st, 2);
+    case 3: return launch_one<MODE_PIV, true>(a, st, 3);
+    case 4: return launch_one<MODE_OCCLUDED, false>(a, st, 4);
+    case 5: return launch_one<MODE_OCCLUDED, true>(a, st, 5);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace xdgcu

@@ -129,6 +129,8 @@ __device__ __forceinline__ int next_face(const WalkArgs& a, int32_t elem, d3 r, 
       for (int j = i + 1; j < 4; ++j)
         pe[pair_index(i, j)] = triple32(ux, uy, uz, P[j].x - P[i].x, P[j].y - P[i].y,
                                         P[j].z - P[i].z, wx[i], wy[i], wz[i]);
+    // faces whose FP32 coordinates do not certify an early exit
+    unsigned escm = 0u;
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
       const int l0 = face_local<FO>(a, f, 0), l1 = face_local<FO>(a, f, 1),
@@ -137,16 +139,33 @@ __device__ __forceinline__ int next_face(const WalkArgs& a, int32_t elem, d3 r, 
       const float p0 = l0 < l1 ? sel6(pe, e0) : -sel6(pe, e0);
       const float p1 = l1 < l2 ? sel6(pe, e1) : -sel6(pe, e1);
       const float p2 = l2 < l0 ? sel6(pe, e2) : -sel6(pe, e2);
-      dists[f] = INFTY;
-      if (p0 > thr || p1 > thr || p2 > thr) continue;  // certified early exit
+      if (!(p0 > thr || p1 > thr || p2 > thr)) escm |= 1u << f;
+    }
+    // FP64 for the remaining faces, in increasing face order (the strict-<
+    // argmin below is then the reference's, :191-196).  Every lane runs its
+    // first escalated face in the same iteration, so the FP64 work of a warp
+    // is issued once for all lanes.
+    int idx = -1;
+    double best = INFTY;
+    while (escm) {
+      const int f = __ffs(escm) - 1;
+      escm &= escm - 1u;
       cnt.esc++;
-      const d3 f0 = load3(a.xyz, ci[l0]);
-      const d3 f1 = load3(a.xyz, ci[l1]);
-      const d3 f2 = load3(a.xyz, ci[l2]);
+      const int l0 = face_local<FO>(a, f, 0), l1 = face_local<FO>(a, f, 1),
+                l2 = face_local<FO>(a, f, 2);
+      const d3 f0 = load3(a.xyz, sel4(ci, l0));
+      const d3 f1 = load3(a.xyz, sel4(ci, l1));
+      const d3 f2 = load3(a.xyz, sel4(ci, l2));
       double t;
       const bool hit = plucker64(f0, f1, f2, r, u, rn, INFTY, 0.0, true, 1, &t);
-      dists[f] = hit ? ((0.0 < t) ? t : 0.0) : INFTY;
+      const double df = hit ? ((0.0 < t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
+      if (df < best) {
+        best = df;
+        idx = f;
+      }
     }
+    *exit_dist = best;
+    return idx;
   }
   int idx = -1;
   double best = INFTY;
@@ -175,27 +194,60 @@ __device__ __forceinline__ void flush(unsigned long long* g, const StepCnt& c, u
   }
 }
 
+// Persistent walk: each warp owns a contiguous chunk of tracks; a lane whose
+// track has ended takes the next track of the chunk, so a warp keeps all 32
+// lanes stepping until its chunk is exhausted (track lengths are
+// exponentially distributed, so one-track-per-lane would leave most lanes
+// idle behind the longest track of the warp).
 template <int FO, bool MIXED>
-__global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t cursor = gwarp * chunk;
+  const int64_t end = min(a.n, cursor + chunk);
   StepCnt cnt = {0, 0};
-  if (i < a.n) {
-    d3 r = load3(a.org, i);
-    const d3 u = load3(a.dir, i);
-    double dist = a.dist[i];
-    int32_t elem = a.start[i];
-    int32_t k = 0;
-    int32_t st = RAY_OK;
-    int32_t* oe = a.seg_elem + i * (int64_t)a.max_segs;
-    double* ol = a.seg_len + i * (int64_t)a.max_segs;
-    if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u) || isnan(dist)) {
-      st = RAY_INVALID;
-    } else {
-      while (dist > 0) {  // mesh_manager_interface.cpp:117
-        if (k >= a.max_segs) {
-          st = RAY_WALK_LIMIT;
-          break;
+  unsigned long long tracks = 0;
+  bool has = false;
+  int64_t i = 0;
+  d3 r = mk3(0, 0, 0), u = mk3(0, 0, 0);
+  double dist = 0.0;
+  int32_t elem = -1, k = 0, st = RAY_OK;
+  int32_t* oe = nullptr;
+  double* ol = nullptr;
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, !has);
+    if (need != 0u && cursor < end) {
+      if (!has) {
+        unsigned lt;
+        asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+        const int64_t idx = cursor + __popc(need & lt);
+        if (idx < end) {
+          i = idx;
+          has = true;
+          r = load3(a.org, i);
+          u = load3(a.dir, i);
+          dist = a.dist[i];
+          elem = a.start[i];
+          k = 0;
+          st = RAY_OK;
+          oe = a.seg_elem + i * (int64_t)a.max_segs;
+          ol = a.seg_len + i * (int64_t)a.max_segs;
+          if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u) || isnan(dist)) {
+            st = RAY_INVALID;
+            dist = 0.0;  // finishes below without a step
+          }
         }
+      }
+      cursor += __popc(need);
+    }
+    if (__ballot_sync(0xffffffffu, has) == 0u) break;
+    if (has) {
+      bool done = !(dist > 0);  // mesh_manager_interface.cpp:117
+      if (!done && k >= a.max_segs) {
+        st = RAY_WALK_LIMIT;
+        done = true;
+      }
+      if (!done) {
         cnt.steps++;
         double ex;
         const int f = next_face<FO, MIXED>(a, elem, r, u, &ex, cnt);
@@ -214,16 +266,21 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a) {
         r = add3(r, scl3(ex, u));  // r += exit.second * u
         if (nxt < -1 || nxt >= a.n_tets) {
           st = RAY_INVALID;  // corrupt adjacency: stop instead of reading out of range
-          break;
+          done = true;
+        } else {
+          elem = nxt;
+          if (elem == -1) done = true;
         }
-        elem = nxt;
-        if (elem == -1) break;
+      }
+      if (done) {
+        a.seg_count[i] = k;
+        if (a.status) a.status[i] = st;
+        has = false;
+        tracks++;
       }
     }
-    a.seg_count[i] = k;
-    if (a.status) a.status[i] = st;
   }
-  if (a.counters) flush(a.counters, cnt, i < a.n ? 1ull : 0ull);
+  if (a.counters) flush(a.counters, cnt, tracks);
 }
 
 template <int FO, bool MIXED>
@@ -255,19 +312,40 @@ __global__ void __launch_bounds__(kBlock) k_next(WalkArgs a) {
   if (a.counters) flush(a.counters, cnt, i < a.n ? 1ull : 0ull);
 }
 
+template <int FO, bool MIXED>
+cudaError_t launch_walk_t(const WalkArgs& a, cudaStream_t st) {
+  static int num_sms = 0, per_sm = 0;
+  auto kern = k_walk<FO, MIXED>;
+  if (per_sm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaError_t e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+  }
+  int64_t blocks = (int64_t)num_sms * per_sm;
+  const int64_t max_blocks = (a.n + kBlock - 1) / kBlock;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks < 1) blocks = 1;
+  const int64_t warps = blocks * (kBlock / 32);
+  const int64_t chunk = (a.n + warps - 1) / warps;
+  kern<<<(unsigned)blocks, kBlock, 0, st>>>(a, chunk);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 cudaError_t launch_walk(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
-  const unsigned g = (unsigned)((a.n + kBlock - 1) / kBlock);
   const int sel = (face_order == 0 ? 0 : 2) + (mixed ? 1 : 0);
   switch (sel) {
-    case 0: k_walk<0, false><<<g, kBlock, 0, st>>>(a); break;
-    case 1: k_walk<0, true><<<g, kBlock, 0, st>>>(a); break;
-    case 2: k_walk<1, false><<<g, kBlock, 0, st>>>(a); break;
-    default: k_walk<1, true><<<g, kBlock, 0, st>>>(a); break;
+    case 0: return launch_walk_t<0, false>(a, st);
+    case 1: return launch_walk_t<0, true>(a, st);
+    case 2: return launch_walk_t<1, false>(a, st);
+    default: return launch_walk_t<1, true>(a, st);
   }
-  return cudaGetLastError();
 }
 
 cudaError_t launch_next_element(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st) {
