@@ -213,6 +213,14 @@ int xdgcu_walk_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
 int xdgcu_set_counting(xdgcu_ctx* ctx, int32_t enable);
 int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
 
+/* Launch and build parameters picked by an autotuner (no counterpart in the
+ * reference, whose Embree backend has no tunables).  Keys:
+ *   "trace_occupancy"  resident blocks per SM the ray-traversal kernel is
+ *                      compiled for (2, 3 or 4; more blocks = fewer registers)
+ *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4) */
+int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
+int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);
+
 /* Tree statistics: out[0] = nodes, [1] = primitives, [2] = depth,
  * [3] = bytes of FP32 nodes, [4] = bytes of FP64 nodes. */
 int xdgcu_surface_tree_info(const xdgcu_ctx* ctx, int32_t tree, int64_t out[8]);

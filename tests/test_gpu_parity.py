@@ -235,3 +235,23 @@ def test_invalid_inputs(cuda, sphere_box):
     t, s, f, st = x.rti.ray_fire(0, o, d, ray_trees=np.array([1, 1, 77], dtype=np.int32),
                                  status=True)
     assert st[2] == RAY_INVALID
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_walk_against_reference_vectors(cuda, prec):
+    """The engine's walk against the segments the reference's own
+    MeshManager::walk_elements produced (tests/golden/make_golden.py)."""
+    import os
+    from conftest import ROOT
+    g = np.load(os.path.join(ROOT, "tests", "golden", "reference_vectors.npz"))
+    tm = synth.TetMesh(vertices=g["tw_xyz"], conn=g["tw_conn"], adj=g["tw_adj"],
+                       face_table=g["tw_faces"], elem_ids=np.arange(len(g["tw_conn"]), dtype=np.int32))
+    rti = CudaRayTracer()
+    rti.set_tet_mesh(tm)
+    se, sl, sc, st = rti.walk_elements(g["tw_start"], g["tw_s"], g["tw_u"], g["tw_len"], 128, prec)
+    assert np.array_equal(sc, g["tw_count"])
+    assert (st == 0).all()
+    for k in range(len(sc)):
+        c = sc[k]
+        assert np.array_equal(se[k, :c], g["tw_elem"][k, :c])
+        assert np.array_equal(sl[k, :c], g["tw_seglen"][k, :c])

@@ -49,6 +49,8 @@ SIGNATURES = {
     "xdgcu_next_element": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_walk_elements": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _VP, _VP, _VP, _VP,
                                    _i32, _VP]),
+    "xdgcu_set_tuning": (_int, [_VP, ctypes.c_char_p, _i64]),
+    "xdgcu_get_tuning": (_int, [_VP, ctypes.c_char_p, _I64]),
     "xdgcu_set_counting": (_int, [_VP, _i32]),
     "xdgcu_get_counters": (_int, [_VP, _I64]),
     "xdgcu_surface_tree_info": (_int, [_VP, _i32, _I64]),

@@ -85,7 +85,6 @@ int cuda_err(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_err(e_, what); \
   } while (0)
 
-constexpr int32_t kLeafMax = 4;
 const int32_t kMoabFaces[12] = {0, 1, 3, 1, 2, 3, 2, 0, 3, 0, 2, 1};
 
 // ---------------------------------------------------------------------------
@@ -225,6 +224,9 @@ struct xdgcu_ctx {
   std::vector<std::unique_ptr<TreeHost>> surf_trees, elem_trees;
   DevMem<TreeDev> d_surf_trees, d_elem_trees;
   bool surf_trees_dirty = true, elem_trees_dirty = true;
+  // tuning (xdgcu_set_tuning)
+  int32_t trace_occupancy = 3;
+  int32_t leaf_max = 4;
   // diagnostics
   bool counting = false;
   DevMem<unsigned long long> d_counters;
@@ -339,7 +341,7 @@ int build_surface_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tri
     API_CUDA(cudaGetLastError(), "triangle boxes");
   }
   BuiltTree b;
-  API_CUDA(build_wide_bvh(d_box.p, n, kLeafMax, st, &b), "bvh build");
+  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, st, &b), "bvh build");
   API_CUDA(t.prim32.alloc(3 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim64.alloc(kPrim64Stride * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
@@ -369,7 +371,7 @@ int build_element_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tet
     API_CUDA(cudaGetLastError(), "tet boxes");
   }
   BuiltTree b;
-  API_CUDA(build_wide_bvh(d_box.p, n, kLeafMax, st, &b), "bvh build");
+  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, st, &b), "bvh build");
   API_CUDA(t.prim64.alloc(12 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
   if (n > 0) {
@@ -711,6 +713,30 @@ int xdgcu_element_tree_info(const xdgcu_ctx* c, int32_t tree, int64_t out[8]) {
   return tree_info(c->elem_trees, tree, out);
 }
 
+int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
+  if (!c || !key) return set_err(XDGCU_ERR_INVALID_ARG, "null argument");
+  const std::string k(key);
+  if (k == "trace_occupancy") {
+    if (value < 2 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "trace_occupancy must be 2..4");
+    c->trace_occupancy = (int32_t)value;
+  } else if (k == "leaf_max") {
+    if (value < 1 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "leaf_max must be 1..4");
+    c->leaf_max = (int32_t)value;
+  } else {
+    return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
+  }
+  return XDGCU_OK;
+}
+
+int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
+  if (!c || !key || !value) return set_err(XDGCU_ERR_INVALID_ARG, "null argument");
+  const std::string k(key);
+  if (k == "trace_occupancy") *value = c->trace_occupancy;
+  else if (k == "leaf_max") *value = c->leaf_max;
+  else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
+  return XDGCU_OK;
+}
+
 int xdgcu_set_counting(xdgcu_ctx* c, int32_t enable) {
   if (!c) return set_err(XDGCU_ERR_INVALID_ARG, "null context");
   c->counting = enable != 0;
@@ -775,6 +801,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.tri_surf = c->d_tri_surf.p;
   a.surf_id = c->d_surf_id.p;
   a.surf_rev_tree = c->d_surf_rev.p;
+  a.occupancy = c->trace_occupancy;
   cudaStream_t st = (cudaStream_t)stream;
   if (kind == 1) {
     a.ray_trees = ray_trees;

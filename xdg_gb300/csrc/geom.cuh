@@ -265,30 +265,65 @@ __host__ __device__ __forceinline__ double dist64(d3 a, d3 p) {
 //    w0 = v0 - o32,  w1 = w0 + e1,  w2 = w0 + e2
 //    pip01 = d.(e1 x w0), pip12 = d.((e2-e1) x w1), pip20 = d.((-e2) x w2)
 // and bounds its distance to the exact value by standard rounding analysis
-// (u = 2^-24; every stored/rounded input contributes u|x|, each 6-term triple
-// product is evaluated with at most 5 roundings per term, gamma_5 ~ 5u):
-//    |pip32 - pip| <= u * D * E * (68 W0 + 76 E + 7 A)
+// (u = 2^-24; the stored vertex/edges are rounded to nearest (u|x|), the ray
+// origin/direction are truncated (2u|x|), and each 6-term triple product is
+// evaluated with at most 5 roundings per term, gamma_5 ~ 5u):
+//    |pip32 - pip| <= u * D * E * (74 W0 + 77 E + 13 A)
 // with D = |d|_inf, E = max edge |.|_inf, W0 = |w0|_inf, A = |v0|_inf + |o|_inf.
 // The FP64 evaluation in plucker64 is within 2^-46 * D * E * (A + 2E) of the
 // exact value, and values with |pip64| < 20*DBL_EPSILON are snapped to zero.
 // Hence if |pip32| exceeds the sum of the three terms, pip64 is non-zero and
 // has pip32's sign.  Inputs that overflow FP32 give inf/NaN, which never pass
 // the comparison and therefore escalate.
+// Double -> float conversions done with integer operations, so per-ray setup
+// costs no FP64-pipe issue slots.  f32_trunc rounds toward zero (relative
+// error < 2u = 2^-23), flushes magnitudes below FLT_MIN to zero (absolute
+// error < 2^-126) and keeps inf/NaN (which then escalate or are rejected).
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  const unsigned m23 = (unsigned)((b >> 29) & 0x7fffffull);
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m23 ? 0x400000u : 0u));
+  const int fe = e - 1023 + 127;
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  if (fe <= 0) return __uint_as_float(sign);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | m23);
+}
+
+// An FP32 value >= x for finite x >= 0 (the next float above the truncation),
+// used for the culling distance; +inf for DBL_MAX or inf.
+__device__ __forceinline__ float f32_up(double x) {
+  const float t = f32_trunc(x);
+  if (!(x > 0.0)) return t;
+  const unsigned tb = __float_as_uint(t);
+  return (tb >= 0x7f800000u) ? __uint_as_float(0x7f800000u) : __uint_as_float(tb + 1u);
+}
+
+__device__ __forceinline__ bool nan_bits(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu) != 0x7ffu;
+}
+
 struct Ray32 {
-  float ox, oy, oz;     // fl32(o)
-  float dx, dy, dz;     // fl32(d)
+  float ox, oy, oz;     // f32_trunc(o)
+  float dx, dy, dz;     // f32_trunc(d)
   float du;             // u * |d|_inf * (1 + 2^-20)
-  float oabs;           // |fl32(o)|_inf
+  float oabs;           // |o32|_inf
 };
 
 __device__ __forceinline__ Ray32 make_ray32(d3 o, d3 d) {
   Ray32 r;
-  r.ox = __double2float_rn(o.x);
-  r.oy = __double2float_rn(o.y);
-  r.oz = __double2float_rn(o.z);
-  r.dx = __double2float_rn(d.x);
-  r.dy = __double2float_rn(d.y);
-  r.dz = __double2float_rn(d.z);
+  r.ox = f32_trunc(o.x);
+  r.oy = f32_trunc(o.y);
+  r.oz = f32_trunc(o.z);
+  r.dx = f32_trunc(d.x);
+  r.dy = f32_trunc(d.y);
+  r.dz = f32_trunc(d.z);
   const float dmax = fmaxf(fabsf(r.dx), fmaxf(fabsf(r.dy), fabsf(r.dz)));
   r.du = dmax * (5.9604645e-08f * 1.000001f);
   r.oabs = fmaxf(fabsf(r.ox), fmaxf(fabsf(r.oy), fabsf(r.oz)));
@@ -322,9 +357,9 @@ __device__ __forceinline__ SignCert plucker_filter32(const Ray32& r, float v0x, 
   const float p20 = triple32(r.dx, r.dy, r.dz, -e2x, -e2y, -e2z, w2x, w2y, w2z);
   const float w0a = fmaxf(fabsf(w0x), fmaxf(fabsf(w0y), fabsf(w0z)));
   const float A = v0abs + r.oabs;
-  // u*D*E*(68 W0 + 76 E + 7 A) + 2^-46 D E (A + 2E) + 20 DBL_EPSILON, rounded up
+  // u*D*E*(74 W0 + 77 E + 13 A) + 2^-46 D E (A + 2E) + 20 DBL_EPSILON, rounded up
   const float de = r.du * emax;
-  const float thr = de * (68.0f * w0a + 76.0f * emax + 7.0001f * A) * 1.0001f + 4.5e-15f;
+  const float thr = de * (74.0f * w0a + 77.0f * emax + 13.0f * A) * 1.0001f + 4.5e-15f;
   SignCert c;
   c.pos = (p01 > thr ? 1u : 0u) | (p12 > thr ? 2u : 0u) | (p20 > thr ? 4u : 0u);
   c.neg = (p01 < -thr ? 1u : 0u) | (p12 < -thr ? 2u : 0u) | (p20 < -thr ? 4u : 0u);

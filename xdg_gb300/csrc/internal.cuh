@@ -97,7 +97,7 @@ enum : int {
 };
 
 __device__ __forceinline__ bool finite3(d3 a) {
-  return isfinite(a.x) && isfinite(a.y) && isfinite(a.z);
+  return finite_bits(a.x) && finite_bits(a.y) && finite_bits(a.z);
 }
 
 __device__ __forceinline__ d3 load3(const double* p, int64_t i) {

@@ -36,6 +36,7 @@ struct SurfArgs {
   double* dist_out;    // occluded distance
   int32_t* status;
   unsigned long long* counters;
+  int32_t occupancy;   // traversal kernel variant: minimum resident blocks per SM (2..4)
 };
 
 struct PointArgs {

@@ -44,19 +44,20 @@ namespace {
 
 constexpr int kTBlock = 128;
 constexpr int kTWarps = kTBlock / 32;
-constexpr int kTStack = 64;
-constexpr int kQ = 64;
+constexpr int kTStack = 48;
+constexpr int kQ = 256;  // ring buffer, power of two; at most 31 + 4*32 entries live
 constexpr unsigned kFull = 0xffffffffu;
 
+// Queue entries pack (owner lane << 27) | leaf-order primitive index (trees
+// hold < 2^27 primitives).
 struct WarpQueue {
-  int32_t prim[kQ];
-  int32_t owner[kQ];
+  uint32_t ent[kQ];
   double rt[32];
   int32_t rface[32];
   int32_t rsurf[32];
   int32_t rflags[32];  // bit 0: accepted, bit 1: dot(d, n) > 0
-  int32_t count;
-  int32_t pad[3];
+  uint32_t head, tail;
+  int32_t pad[2];
 };
 
 struct TraceShared {
@@ -71,8 +72,8 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
-template <int MODE, bool MIXED>
-__global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
+template <int MODE, bool MIXED, int MINB>
+__global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chunk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TraceShared& S = *reinterpret_cast<TraceShared*>(smem_raw);
   const int lane = threadIdx.x & 31;
@@ -82,7 +83,10 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
   const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t cursor = gwarp * chunk;
   const int64_t end = min(a.n, cursor + chunk);
-  if (lane == 0) Q.count = 0;
+  if (lane == 0) {
+    Q.head = 0u;
+    Q.tail = 0u;
+  }
   __syncwarp();
 
   Counters cnt = {0, 0, 0, 0};
@@ -94,10 +98,8 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
   int32_t tid = 0, status = RAY_OK, npend = 0;
   d3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
   const Node32* n32 = nullptr;
-  const Node64* n64 = nullptr;
   const float4* prim32 = nullptr;
-  const double* prim64 = nullptr;
-  const int32_t* prim_ref = nullptr;
+  const TreeDev* tree = nullptr;
   int32_t cur = CHILD_EMPTY, leaf_p = 0, leaf_end = 0;
   int sp = 0;
   double bt = INFTY;
@@ -177,25 +179,23 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
             nexcl = a.excl_off[idx + 1] - e0;
           }
           trav = true;
-          if (tid < 1 || tid > a.n_trees || !finite3(o) || !finite3(d) || isnan(bt)) {
+          if (tid < 1 || tid > a.n_trees || !finite3(o) || !finite3(d) || nan_bits(bt)) {
             status = RAY_INVALID;
             trav = false;
           } else {
             const TreeDev* T = a.trees + (tid - 1);
+            tree = T;
             n32 = T->n32;
-            n64 = T->n64;
             prim32 = T->prim32;
-            prim64 = T->prim64;
-            prim_ref = T->prim_ref;
             const int32_t root = T->root;
-            bt32 = (MODE == MODE_OCCLUDED) ? INFINITY : __double2float_ru(bt);
+            bt32 = (MODE == MODE_OCCLUDED) ? INFINITY : f32_up(bt);
             if (MIXED) {
               br32 = make_boxray32(o, d);
               r32 = make_ray32(o, d);
               // FP32 box-test safety (see the file comment)
               use64 = !(8.0f * kU32 * (T->max_abs + r32.oabs) < T->bump);
             }
-            if (!MIXED || use64) br64 = make_boxray64(o, d);
+            if (!MIXED) br64 = make_boxray64(o, d);
             if (root == CHILD_EMPTY) {
               trav = false;
             } else if (ref_is_leaf(root)) {
@@ -214,24 +214,33 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
 
     // ---- one traversal step per active lane ----
     const unsigned act = __ballot_sync(kFull, trav);
+    unsigned escm = 0u;   // escalated primitives of this step (bit k -> esc_p0 + k)
+    int32_t esc_p0 = 0;
     if (trav) {
-      bool esc = false;
-      int32_t esc_prim = 0;
       if (leaf_p < leaf_end) {
-        const int32_t p = leaf_p++;
-        cnt.prim++;
-        if (MIXED) {
-          const float4 A = __ldg(&prim32[3 * (int64_t)p]);
-          const float4 B = __ldg(&prim32[3 * (int64_t)p + 1]);
-          const float4 C = __ldg(&prim32[3 * (int64_t)p + 2]);
-          const SignCert c = plucker_filter32(r32, A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y, C.z,
-                                              B.w, A.w);
-          esc = !certified_miss(c);
-        } else {
-          esc = true;
+        // the whole leaf (<= 4 primitives) in one step: its loads overlap
+        const int32_t p0 = leaf_p;
+        const int np = leaf_end - leaf_p;
+        leaf_p = leaf_end;
+        esc_p0 = p0;
+        cnt.prim += np;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (k < np) {
+            if (MIXED) {
+              const int64_t q = 3 * (int64_t)(p0 + k);
+              const float4 A = __ldg(&prim32[q]);
+              const float4 B = __ldg(&prim32[q + 1]);
+              const float4 C = __ldg(&prim32[q + 2]);
+              const SignCert c = plucker_filter32(r32, A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
+                                                  C.z, B.w, A.w);
+              if (!certified_miss(c)) escm |= 1u << k;
+            } else {
+              escm |= 1u << k;
+            }
+          }
         }
-        esc_prim = p;
-        if (leaf_p >= leaf_end && cur == CHILD_EMPTY) pop();
+        if (cur == CHILD_EMPTY) pop();
       } else {
         // inner node
         cnt.node++;
@@ -242,7 +251,8 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
           node_test32(n32 + cur, br32, bt32, key, cr);
         } else {
           double tn[4];
-          node_test64(n64 + cur, br64, (MODE == MODE_OCCLUDED) ? INFTY : bt, tn, cr);
+          if (MIXED) br64 = make_boxray64(o, d);  // rare: rays failing the FP32 safety test
+          node_test64(tree->n64 + cur, br64, (MODE == MODE_OCCLUDED) ? INFTY : bt, tn, cr);
 #pragma unroll
           for (int k = 0; k < 4; ++k)
             key[k] = tn[k] < INFINITY ? __double2float_rd(tn[k]) : INFINITY;
@@ -271,32 +281,48 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
           }
         }
       }
-      // enqueue escalations (all lanes of `act` reach this point)
-      const unsigned m = __ballot_sync(act, esc);
-      if (m != 0u) {
-        const int base = Q.count;
-        __syncwarp(act);
-        if (esc) {
-          const int pos = base + __popc(m & lanemask_lt());
-          Q.prim[pos] = esc_prim;
-          Q.owner[pos] = lane;
-          npend++;
-          cnt.esc++;
+    }
+    (void)act;
+    // ---- enqueue this step's escalations (warp-wide exclusive scan) ----
+    {
+      const int c = __popc(escm);
+      int incl = c;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += y;
+      }
+      const int total = __shfl_sync(kFull, incl, 31);
+      if (total > 0) {
+        const uint32_t tail = Q.tail;
+        __syncwarp();
+        uint32_t pos = tail + (uint32_t)(incl - c);
+        unsigned m = escm;
+        while (m) {
+          const int k = __ffs(m) - 1;
+          m &= m - 1u;
+          Q.ent[pos & (kQ - 1)] = ((uint32_t)lane << 27) | (uint32_t)(esc_p0 + k);
+          ++pos;
         }
-        if (lane == __ffs(m) - 1) Q.count = base + __popc(m);
+        npend += c;
+        cnt.esc += c;
+        if (lane == 0) Q.tail = tail + (uint32_t)total;
       }
     }
     __syncwarp();
 
     // ---- drain the FP64 queue with the whole warp ----
-    const int qn = Q.count;
-    const unsigned act2 = __ballot_sync(kFull, trav);
-    const unsigned waiting = __ballot_sync(kFull, has_ray && !trav && npend > 0);
-    if (qn >= 32 || (qn > 0 && (act2 == 0u || __popc(waiting) >= 8))) {
+    while (true) {
+      const uint32_t head = Q.head;
+      const int qn = (int)(Q.tail - head);
+      const unsigned act2 = __ballot_sync(kFull, trav);
+      const unsigned waiting = __ballot_sync(kFull, has_ray && !trav && npend > 0);
+      if (!(qn >= 32 || (qn > 0 && (act2 == 0u || __popc(waiting) >= 8)))) break;
       const int nq = min(qn, 32);
       const bool mine = lane < nq;
-      const int owner = mine ? Q.owner[lane] : lane;
-      const int32_t prim = mine ? Q.prim[lane] : 0;
+      const uint32_t ent = mine ? Q.ent[(head + lane) & (kQ - 1)] : ((uint32_t)lane << 27);
+      const int owner = (int)(ent >> 27);
+      const int32_t prim = (int32_t)(ent & 0x7ffffffu);
       // the owner's ray, tree and current best
       d3 oo, od;
       oo.x = __shfl_sync(kFull, o.x, owner);
@@ -309,10 +335,8 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
       const int32_t obface = __shfl_sync(kFull, bface, owner);
       const bool obhas = __shfl_sync(kFull, bhas ? 1 : 0, owner) != 0;
       const int32_t otid = __shfl_sync(kFull, tid, owner);
-      const double* op64 = reinterpret_cast<const double*>(
-          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(prim64), owner));
-      const int32_t* opref = reinterpret_cast<const int32_t*>(
-          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(prim_ref), owner));
+      const TreeDev* otree = reinterpret_cast<const TreeDev*>(
+          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(tree), owner));
       const int32_t* oexcl = reinterpret_cast<const int32_t*>(
           __shfl_sync(kFull, reinterpret_cast<unsigned long long>(excl), owner));
       const int32_t onexcl = __shfl_sync(kFull, nexcl, owner);
@@ -320,6 +344,8 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
       double rt = 0.0;
       int32_t rface = -1, rsurf = -1;
       if (mine) {
+        const double* op64 = otree->prim64;
+        const int32_t* opref = otree->prim_ref;
         d3 v0, v1, v2;
         load_tri64(op64 + kPrim64Stride * (int64_t)prim, v0, v1, v2);
         const d3 rn = cross3(od, oo);  // plucker.h:75
@@ -357,11 +383,12 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
       Q.rt[lane] = rt;
       Q.rface[lane] = rface;
       Q.rsurf[lane] = rsurf;
+      const int my_owner = owner;
       __syncwarp();
       // each ray merges its own results in queue order
       bool changed = false;
       for (int j = 0; j < nq; ++j) {
-        if (Q.owner[j] != lane) continue;
+        if (__shfl_sync(kFull, my_owner, j) != lane) continue;
         npend--;
         const int32_t fl = Q.rflags[j];
         if (!(fl & 1)) continue;
@@ -381,20 +408,9 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
           changed = true;
         }
       }
-      if (changed) bt32 = __double2float_ru(bt);
-      // keep the entries beyond the first 32
-      const int rest = qn - nq;
-      int32_t keep_prim = 0, keep_owner = 0;
-      if (lane < rest) {
-        keep_prim = Q.prim[nq + lane];
-        keep_owner = Q.owner[nq + lane];
-      }
+      if (changed) bt32 = f32_up(bt);
       __syncwarp();
-      if (lane < rest) {
-        Q.prim[lane] = keep_prim;
-        Q.owner[lane] = keep_owner;
-      }
-      if (lane == 0) Q.count = rest;
+      if (lane == 0) Q.head = head + (uint32_t)nq;
       __syncwarp();
     }
   }
@@ -405,13 +421,14 @@ __global__ void __launch_bounds__(kTBlock) k_trace(SurfArgs a, int64_t chunk) {
 }
 
 int g_num_sms = 0;
-int g_blocks_per_sm[6] = {0, 0, 0, 0, 0, 0};
+int g_blocks_per_sm[6][3] = {};
 
-template <int MODE, bool MIXED>
-cudaError_t launch_one(const SurfArgs& a, cudaStream_t st, int slot) {
+template <int MODE, bool MIXED, int MINB>
+cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
   const size_t smem = sizeof(TraceShared);
-  auto kern = k_trace<MODE, MIXED>;
-  if (g_blocks_per_sm[slot] == 0) {
+  auto kern = k_trace<MODE, MIXED, MINB>;
+  int* cache = &g_blocks_per_sm[slot][MINB - 2];
+  if (*cache == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
@@ -422,10 +439,10 @@ cudaError_t launch_one(const SurfArgs& a, cudaStream_t st, int slot) {
     int b = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kTBlock, smem);
     if (e != cudaSuccess) return e;
-    g_blocks_per_sm[slot] = b > 0 ? b : 1;
+    *cache = b > 0 ? b : 1;
   }
   const int64_t warps_needed = (a.n + 31) / 32;
-  int64_t blocks = (int64_t)g_num_sms * g_blocks_per_sm[slot];
+  int64_t blocks = (int64_t)g_num_sms * (*cache);
   const int64_t max_blocks = (warps_needed + kTWarps - 1) / kTWarps;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks < 1) blocks = 1;
@@ -433,6 +450,15 @@ cudaError_t launch_one(const SurfArgs& a, cudaStream_t st, int slot) {
   const int64_t chunk = (a.n + warps - 1) / warps;
   kern<<<(unsigned)blocks, kTBlock, smem, st>>>(a, chunk);
   return cudaGetLastError();
+}
+
+template <int MODE, bool MIXED>
+cudaError_t launch_one(const SurfArgs& a, cudaStream_t st, int slot) {
+  switch (a.occupancy) {
+    case 2: return launch_minb<MODE, MIXED, 2>(a, st, slot);
+    case 4: return launch_minb<MODE, MIXED, 4>(a, st, slot);
+    default: return launch_minb<MODE, MIXED, 3>(a, st, slot);
+  }
 }
 
 }  // namespace

@@ -80,8 +80,8 @@ __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 
 // FP32 ray data for the box test
 struct BoxRay32 {
-  float ix, iy, iz;     // 1 / fl32(d) (tiny components replaced by +-1e-20)
-  float ox, oy, oz;     // fl32(o) * inv
+  float ix, iy, iz;     // 1 / f32(d) (tiny components replaced by +-1e-20)
+  float ox, oy, oz;     // f32(o) * inv
   int nx, ny, nz;       // index of the near plane vector (0 = lo, 1 = hi) per axis
 };
 
@@ -94,12 +94,12 @@ __device__ __forceinline__ double safe_d(double x) {
 
 __device__ __forceinline__ BoxRay32 make_boxray32(d3 o, d3 d) {
   BoxRay32 r;
-  r.ix = 1.0f / safe_f(__double2float_rn(d.x));
-  r.iy = 1.0f / safe_f(__double2float_rn(d.y));
-  r.iz = 1.0f / safe_f(__double2float_rn(d.z));
-  r.ox = __double2float_rn(o.x) * r.ix;
-  r.oy = __double2float_rn(o.y) * r.iy;
-  r.oz = __double2float_rn(o.z) * r.iz;
+  r.ix = 1.0f / safe_f(f32_trunc(d.x));
+  r.iy = 1.0f / safe_f(f32_trunc(d.y));
+  r.iz = 1.0f / safe_f(f32_trunc(d.z));
+  r.ox = f32_trunc(o.x) * r.ix;
+  r.oy = f32_trunc(o.y) * r.iy;
+  r.oz = f32_trunc(o.z) * r.iz;
   r.nx = signbit(r.ix) ? 1 : 0;
   r.ny = signbit(r.iy) ? 1 : 0;
   r.nz = signbit(r.iz) ? 1 : 0;

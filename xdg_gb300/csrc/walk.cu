@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
           st = RAY_OK;
           oe = a.seg_elem + i * (int64_t)a.max_segs;
           ol = a.seg_len + i * (int64_t)a.max_segs;
-          if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u) || isnan(dist)) {
+          if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u) || nan_bits(dist)) {
             st = RAY_INVALID;
             dist = 0.0;  // finishes below without a step
           }

@@ -239,6 +239,14 @@ class CudaRayTracer:
         self._check(fn(self.ctx, int(tree), out), "tree_info")
         return dict(nodes=out[0], prims=out[1], depth=out[2], bytes32=out[3], bytes64=out[4])
 
+    def set_tuning(self, key: str, value: int):
+        self._check(self.L.xdgcu_set_tuning(self.ctx, key.encode(), int(value)), "set_tuning")
+
+    def get_tuning(self, key: str) -> int:
+        v = ctypes.c_int64()
+        self._check(self.L.xdgcu_get_tuning(self.ctx, key.encode(), ctypes.byref(v)), "get_tuning")
+        return int(v.value)
+
     def set_counting(self, on: bool):
         self._check(self.L.xdgcu_set_counting(self.ctx, 1 if on else 0), "set_counting")
 
