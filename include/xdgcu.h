@@ -12,7 +12,9 @@
  *   - surface and element tree ids are separate counters starting at 1
  *     (ray_tracing_interface.cpp:10-18);
  *   - a miss is {t = INFTY (DBL_MAX), surface = ID_NONE} (embree/ray_tracer.cpp:320-321);
- *   - positions/directions are n x 3 doubles (AoS), as Position/Direction.
+ *   - positions/directions are n x 3 doubles (AoS), as Position/Direction;
+ *   - coordinates must be finite with magnitude below 2^300 (so no product of
+ *     three of them overflows); rays outside that range get XDGCU_RAY_INVALID.
  *
  * Batched queries take `n` rays and either one tree (`tree` > 0,
  * `ray_trees` = NULL) or one tree per ray (`ray_trees` != NULL, `tree`
@@ -217,6 +219,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  * reference, whose Embree backend has no tunables).  Keys:
  *   "trace_occupancy"  resident blocks per SM the ray-traversal kernel is
  *                      compiled for (2, 3 or 4; more blocks = fewer registers)
+ *   "trace_node_iters" inner-node steps a lane takes between two leaf phases
+ *                      of the warp-synchronous traversal, mixed precision (1..64)
+ *   "trace_node_iters_fp64"  the same for the all-FP64 path
  *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4) */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);

@@ -208,3 +208,31 @@ def test_tracks_mock(cuda, oracle, prec):
     segs = x2.segments(0, [start], [c], precision=prec)
     exp = c[0] - synth.MOCK_BOX_LO[0]
     assert abs(segs[0][1].sum() - exp) <= 1e-5 * exp
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_degenerate_lattice_rays(cuda, oracle, prec):
+    """Origins on an integer lattice covering faces, edges and corners of the
+    mock box, the 26 lattice directions with +0/-0 components, unnormalised
+    and normalised: every query agrees with the oracle bit for bit."""
+    m = synth.mock_cube(False)
+    rti = CudaRayTracer()
+    vt, _ = rti.register_volume(m, 0)
+    ot = oracle.volume_tree(m, 0)
+    g = np.arange(-3.0, 7.0)
+    O = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    dirs = np.array([(i, j, k) for i in (-1.0, 0.0, 1.0) for j in (-1.0, 0.0, 1.0)
+                     for k in (-1.0, 0.0, 1.0) if (i, j, k) != (0.0, 0.0, 0.0)])
+    negz = np.where(dirs == 0.0, -0.0, dirs)  # the same directions with -0.0 components
+    D = np.concatenate([dirs, negz, synth.normalize_rows(dirs), 2.5 * dirs])
+    oo = np.repeat(O, len(D), axis=0)
+    dd = np.tile(D, (len(O), 1))
+    oo = np.where(oo == 0.0, np.where(np.arange(len(oo))[:, None] % 2 == 0, -0.0, 0.0), oo)
+    for orient in (EXITING, ENTERING, -1):
+        t, s, f = rti.ray_fire(vt, oo, dd, None, orient, precision=prec)
+        t2, s2, f2 = ot.ray_fire(oo, dd, None, orient)
+        assert np.array_equal(s, s2) and np.array_equal(f, f2) and np.array_equal(t, t2), orient
+    assert np.array_equal(rti.point_in_volume(vt, oo, dd, precision=prec), ot.point_in_volume(oo, dd))
+    occ, dist = rti.occluded(vt, oo, dd, prec)
+    oocc, odist = ot.occluded(oo, dd)
+    assert np.array_equal(occ, oocc) and np.array_equal(dist, odist)

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -164,18 +165,81 @@ __global__ void k_tet_boxes(const double* __restrict__ xyz, const int4* __restri
   }
 }
 
+// Leaf-ordered tet data.  prim64: the 4 vertices (12 doubles).  prim32: the
+// data of the FP32 containment pre-filter (geom.cuh, tet_filter32):
+//   float4 (v0.xyz, m)  (M row 0, |v0|_inf)  (M row 1, e64)  (M row 2, 0)
+// with M = T^{-1} (T's columns v1-v0, v2-v0, v3-v0) rounded to FP32,
+// m >= max row |.|_1 of M, and e64 a bound on the error of the reference's
+// FP64 barycentric coordinates for any point in the tet's box (+inf for
+// degenerate or badly conditioned tets, which then always take the FP64 test).
 __global__ void k_tet_gather(const double* __restrict__ xyz, const int4* __restrict__ conn,
                              const int32_t* __restrict__ tets, const int32_t* __restrict__ order,
-                             int32_t n, double* __restrict__ prim64, int32_t* __restrict__ prim_ref) {
+                             int32_t n, double* __restrict__ prim64, float4* __restrict__ prim32,
+                             int32_t* __restrict__ prim_ref) {
   int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const int32_t t = tets[order[j]];
   const int4 c = conn[t];
   const int32_t ci[4] = {c.x, c.y, c.z, c.w};
+  double v[4][3];
   double* o = prim64 + 12 * (int64_t)j;
   for (int k = 0; k < 4; ++k)
-    for (int a = 0; a < 3; ++a) o[3 * k + a] = xyz[3 * (int64_t)ci[k] + a];
+    for (int a = 0; a < 3; ++a) {
+      v[k][a] = xyz[3 * (int64_t)ci[k] + a];
+      o[3 * k + a] = v[k][a];
+    }
   prim_ref[j] = t;
+  // T[r][col]: column col = v_{col+1} - v0
+  double T[3][3], Tmax = 0.0, lo[3], hi[3];
+  for (int r = 0; r < 3; ++r) {
+    lo[r] = fmin(fmin(v[0][r], v[1][r]), fmin(v[2][r], v[3][r]));
+    hi[r] = fmax(fmax(v[0][r], v[1][r]), fmax(v[2][r], v[3][r]));
+    for (int col = 0; col < 3; ++col) {
+      T[r][col] = v[col + 1][r] - v[0][r];
+      Tmax = fmax(Tmax, fabs(T[r][col]));
+    }
+  }
+  const double det = T[0][0] * (T[1][1] * T[2][2] - T[1][2] * T[2][1]) -
+                     T[0][1] * (T[1][0] * T[2][2] - T[1][2] * T[2][0]) +
+                     T[0][2] * (T[1][0] * T[2][1] - T[1][1] * T[2][0]);
+  double M[3][3];
+  M[0][0] = (T[1][1] * T[2][2] - T[1][2] * T[2][1]) / det;
+  M[0][1] = (T[0][2] * T[2][1] - T[0][1] * T[2][2]) / det;
+  M[0][2] = (T[0][1] * T[1][2] - T[0][2] * T[1][1]) / det;
+  M[1][0] = (T[1][2] * T[2][0] - T[1][0] * T[2][2]) / det;
+  M[1][1] = (T[0][0] * T[2][2] - T[0][2] * T[2][0]) / det;
+  M[1][2] = (T[0][2] * T[1][0] - T[0][0] * T[1][2]) / det;
+  M[2][0] = (T[1][0] * T[2][1] - T[1][1] * T[2][0]) / det;
+  M[2][1] = (T[0][1] * T[2][0] - T[0][0] * T[2][1]) / det;
+  M[2][2] = (T[0][0] * T[1][1] - T[0][1] * T[1][0]) / det;
+  double m = 0.0;
+  for (int r = 0; r < 3; ++r) m = fmax(m, fabs(M[r][0]) + fabs(M[r][1]) + fabs(M[r][2]));
+  // largest |p - v0|_inf for p in the (dilated) box
+  double rmax = 0.0;
+  for (int r = 0; r < 3; ++r) rmax = fmax(rmax, fmax(fabs(hi[r] - v[0][r]), fabs(v[0][r] - lo[r])));
+  const double w = sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                        (hi[2] - lo[2]) * (hi[2] - lo[2]));
+  rmax += 2.0 * w * 1e-6 + 1e-300;
+  const double krel = Tmax * Tmax * Tmax / fabs(det);
+  const double eps = DBL_EPSILON;
+  // error of adjugate/determinant barycentrics, see tet_filter32
+  double e64 = 3.0 * eps * rmax * (18.0 * krel / Tmax + 47.0 * krel * m) +
+               3.0 * eps * (1.0 + 3.0 * m * rmax);
+  e64 *= 2.0;
+  const bool ok = det > 0.0 && isfinite(det) && m < 1e20 && krel < 1e6 && isfinite(e64);
+  const float mf = ok ? __double2float_ru(m * (1.0 + 1e-6)) : INFINITY;
+  const float ef = ok ? __double2float_ru(e64) : INFINITY;
+  const float v0x = __double2float_rn(v[0][0]), v0y = __double2float_rn(v[0][1]),
+              v0z = __double2float_rn(v[0][2]);
+  const float v0abs = fmaxf(fabsf(v0x), fmaxf(fabsf(v0y), fabsf(v0z)));
+  float4* q = prim32 + 4 * (int64_t)j;
+  q[0] = make_float4(v0x, v0y, v0z, mf);
+  q[1] = make_float4(__double2float_rn(M[0][0]), __double2float_rn(M[0][1]),
+                     __double2float_rn(M[0][2]), v0abs);
+  q[2] = make_float4(__double2float_rn(M[1][0]), __double2float_rn(M[1][1]),
+                     __double2float_rn(M[1][2]), ef);
+  q[3] = make_float4(__double2float_rn(M[2][0]), __double2float_rn(M[2][1]),
+                     __double2float_rn(M[2][2]), 0.0f);
 }
 
 __global__ void k_vert32(const double* __restrict__ xyz, int64_t n, float4* __restrict__ out) {
@@ -226,6 +290,8 @@ struct xdgcu_ctx {
   bool surf_trees_dirty = true, elem_trees_dirty = true;
   // tuning (xdgcu_set_tuning)
   int32_t trace_occupancy = 3;
+  int32_t trace_node_iters = 4;       // mixed precision
+  int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
   int32_t leaf_max = 4;
   // diagnostics
   bool counting = false;
@@ -373,10 +439,11 @@ int build_element_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tet
   BuiltTree b;
   API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, st, &b), "bvh build");
   API_CUDA(t.prim64.alloc(12 * (int64_t)std::max(1, n)), "alloc prims");
+  API_CUDA(t.prim32.alloc(4 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
   if (n > 0) {
     k_tet_gather<<<grid(n), 256, 0, st>>>(c->d_xyz.p, c->d_conn.p, d_tets.p, b.order, n,
-                                          t.prim64.p, t.prim_ref.p);
+                                          t.prim64.p, t.prim32.p, t.prim_ref.p);
     API_CUDA(cudaGetLastError(), "gather");
   }
   API_CUDA(cudaStreamSynchronize(st), "build sync");
@@ -515,6 +582,10 @@ int xdgcu_register_surface(xdgcu_ctx* c, int32_t surface_id, int64_t n_faces, co
     return set_err(XDGCU_ERR_STATE, "register_surface: surface already registered");
   if ((int64_t)c->h_tri_face.size() + n_faces > (int64_t)(1 << 27))
     return set_err(XDGCU_ERR_INVALID_ARG, "register_surface: more than 2^27 triangles");
+  for (int64_t i = 0; i < 9 * n_faces; ++i)
+    if (!(std::fabs(tri_xyz[i]) < 0x1p300))
+      return set_err(XDGCU_ERR_INVALID_ARG,
+                     "register_surface: coordinates must be finite and below 2^300 in magnitude");
   SurfaceRec r;
   r.id = surface_id;
   r.first = (int64_t)c->h_tri_face.size();
@@ -610,6 +681,10 @@ int xdgcu_set_tet_mesh(xdgcu_ctx* c, int64_t n_vertices, const double* xyz, int6
   for (int k = 0; k < 12; ++k)
     if (face_table[k] < 0 || face_table[k] > 3)
       return set_err(XDGCU_ERR_INVALID_ARG, "set_tet_mesh: face table entries must be 0..3");
+  for (int64_t i = 0; i < 3 * n_vertices; ++i)
+    if (!(std::fabs(xyz[i]) < 0x1p300))
+      return set_err(XDGCU_ERR_INVALID_ARG,
+                     "set_tet_mesh: coordinates must be finite and below 2^300 in magnitude");
   for (int64_t i = 0; i < 4 * n_tets; ++i) {
     if (conn[i] < 0 || conn[i] >= n_vertices)
       return set_err(XDGCU_ERR_INVALID_ARG, "set_tet_mesh: connectivity out of range");
@@ -719,6 +794,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   if (k == "trace_occupancy") {
     if (value < 2 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "trace_occupancy must be 2..4");
     c->trace_occupancy = (int32_t)value;
+  } else if (k == "trace_node_iters" || k == "trace_node_iters_fp64") {
+    if (value < 1 || value > 64) return set_err(XDGCU_ERR_INVALID_ARG, k + " must be 1..64");
+    (k == "trace_node_iters" ? c->trace_node_iters : c->trace_node_iters_fp64) = (int32_t)value;
   } else if (k == "leaf_max") {
     if (value < 1 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "leaf_max must be 1..4");
     c->leaf_max = (int32_t)value;
@@ -732,6 +810,8 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   if (!c || !key || !value) return set_err(XDGCU_ERR_INVALID_ARG, "null argument");
   const std::string k(key);
   if (k == "trace_occupancy") *value = c->trace_occupancy;
+  else if (k == "trace_node_iters") *value = c->trace_node_iters;
+  else if (k == "trace_node_iters_fp64") *value = c->trace_node_iters_fp64;
   else if (k == "leaf_max") *value = c->leaf_max;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   return XDGCU_OK;
@@ -802,6 +882,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.surf_id = c->d_surf_id.p;
   a.surf_rev_tree = c->d_surf_rev.p;
   a.occupancy = c->trace_occupancy;
+  a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   cudaStream_t st = (cudaStream_t)stream;
   if (kind == 1) {
     a.ray_trees = ray_trees;

@@ -67,17 +67,43 @@ __host__ __device__ __forceinline__ d3 face_normal64(d3 v0, d3 v1, d3 v2) {
   return normalize64(cross3(sub3(v1, v0), sub3(v2, v0)));
 }
 
+// ---------------------------------------------------------------------------
+// Exact comparisons of doubles on the integer ALU.
+//
+// GB300 issues FP64 instructions (comparisons included) at 1/64 of the FP32
+// rate.  For non-NaN doubles the map okey() below is strictly monotone and
+// sends -0.0 and +0.0 to the same key, so every comparison of the reference's
+// code can be evaluated on integer keys with identical outcome.  The engine
+// rejects non-finite and huge (|x| >= 2^400) inputs at the C ABI, so no NaN
+// can arise inside these routines.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ long long okey(double x) {
+  long long b = dbits(x);
+  b = (b == (long long)0x8000000000000000ull) ? 0ll : b;
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ bool gt0(double x) { return dbits(x) > 0; }
+__device__ __forceinline__ bool lt0(double x) { return okey(x) < 0; }
+__device__ __forceinline__ bool is0(double x) { return (dbits(x) << 1) == 0; }
+__device__ __forceinline__ unsigned long long absbits(double x) {
+  return (unsigned long long)dbits(x) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return okey(a) < okey(b); }
+
 // plucker.h:35-43
-__host__ __device__ __forceinline__ bool first_lower(d3 a, d3 b) {
-  if (a.x < b.x) return true;
-  if (a.x > b.x) return false;
-  if (a.y < b.y) return true;
-  if (a.y > b.y) return false;
-  return a.z < b.z;
+__device__ __forceinline__ bool first_lower(d3 a, d3 b) {
+  const long long ax = okey(a.x), bx = okey(b.x);
+  if (ax < bx) return true;
+  if (ax > bx) return false;
+  const long long ay = okey(a.y), by = okey(b.y);
+  if (ay < by) return true;
+  if (ay > by) return false;
+  return okey(a.z) < okey(b.z);
 }
 
 // plucker.h:45-62
-__host__ __device__ __forceinline__ double plucker_edge64(d3 va, d3 vb, d3 ray, d3 rn) {
+__device__ __forceinline__ double plucker_edge64(d3 va, d3 vb, d3 ray, d3 rn) {
   double pip;
   if (first_lower(va, vb)) {
     const d3 e = sub3(vb, va);
@@ -89,48 +115,50 @@ __host__ __device__ __forceinline__ double plucker_edge64(d3 va, d3 vb, d3 ray, 
     pip = dot3(ray, en) + dot3(rn, e);
     pip = -pip;
   }
-  if (ZERO_TOL > fabs(pip)) pip = 0.0;
+  // ZERO_TOL > fabs(pip)
+  if (absbits(pip) < absbits(ZERO_TOL)) pip = 0.0;
   return pip;
 }
 
 // plucker.h:64-161.  `rn` is cross(direction, origin) (plucker.h:75), passed
 // in so callers testing many triangles against one ray compute it once; the
-// value is identical to recomputing it per call.
-__host__ __device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn,
-                                                   double t_max, double t_min, bool use_or,
-                                                   int orient, double* t_out) {
+// value is identical to recomputing it per call.  `orient` is +1 or -1 when
+// use_or is set.
+__device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn, double t_max,
+                                          double t_min, bool use_or, int orient, double* t_out) {
+  // orientation * c > 0
+  auto exits = [&](double c) { return orient > 0 ? gt0(c) : lt0(c); };
   const double c0 = plucker_edge64(v0, v1, d, rn);
-  if (use_or && orient * c0 > 0) return false;
+  if (use_or && exits(c0)) return false;
   const double c1 = plucker_edge64(v1, v2, d, rn);
+  const bool p0 = gt0(c0), n0 = lt0(c0), p1 = gt0(c1), n1 = lt0(c1);
   if (use_or) {
-    if (orient * c1 > 0) return false;
-  } else if ((0.0 < c0 && 0.0 > c1) || (0.0 > c0 && 0.0 < c1)) {
+    if (exits(c1)) return false;
+  } else if ((p0 && n1) || (n0 && p1)) {
     return false;
   }
   const double c2 = plucker_edge64(v2, v0, d, rn);
+  const bool p2 = gt0(c2), n2 = lt0(c2);
   if (use_or) {
-    if (orient * c2 > 0) return false;
-  } else if ((0.0 < c1 && 0.0 > c2) || (0.0 > c1 && 0.0 < c2) || (0.0 < c0 && 0.0 > c2) ||
-             (0.0 > c0 && 0.0 < c2)) {
+    if (exits(c2)) return false;
+  } else if ((p1 && n2) || (n1 && p2) || (p0 && n2) || (n0 && p2)) {
     return false;
   }
-  if (0.0 == c0 && 0.0 == c1 && 0.0 == c2) return false;
+  if (is0(c0) && is0(c1) && is0(c2)) return false;
   const double inv = 1.0 / (c0 + c1 + c2);
   const d3 hit = add3(add3(scl3(c0 * inv, v2), scl3(c1 * inv, v0)), scl3(c2 * inv, v1));
+  // index of the largest |d| component, first maximum wins
+  const unsigned long long ax = absbits(d.x), ay = absbits(d.y), az = absbits(d.z);
   int idx = 0;
-  double max_abs = 0;
-  for (int i = 0; i < 3; ++i) {
-    const double a = fabs(comp3(d, i));
-    if (a > max_abs) {
-      idx = i;
-      max_abs = a;
-    }
-  }
+  unsigned long long mx = 0ull;
+  if (ax > mx) { idx = 0; mx = ax; }
+  if (ay > mx) { idx = 1; mx = ay; }
+  if (az > mx) { idx = 2; mx = az; }
   double dist = (comp3(hit, idx) - comp3(o, idx)) / comp3(d, idx);
   const double u = c2 * inv;
   const double v = c0 * inv;
-  if (u < 0.0 || v < 0.0 || (u + v) > 1.0) dist = -1.0;
-  if (dist < t_min || dist > t_max) return false;
+  if (lt0(u) || lt0(v) || dlt(1.0, u + v)) dist = -1.0;
+  if (dlt(dist, t_min) || dlt(t_max, dist)) return false;
   *t_out = dist;
   return true;
 }
@@ -139,7 +167,7 @@ __host__ __device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3
 // T's columns e0 = v1-v0, e1 = v2-v0, e2 = v3-v0 through its linalg
 // dependency: inverse = adjugate / determinant, then mul(inverse, rhs) summed
 // over columns.  The same formula and order are used here.
-__host__ __device__ __forceinline__ bool tet_contains64(d3 p, d3 v0, d3 v1, d3 v2, d3 v3) {
+__device__ __forceinline__ bool tet_contains64(d3 p, d3 v0, d3 v1, d3 v2, d3 v3) {
   const d3 X = sub3(v1, v0), Y = sub3(v2, v0), Z = sub3(v3, v0);
   const d3 ax = mk3(Y.y * Z.z - Z.y * Y.z, Z.y * X.z - X.y * Z.z, X.y * Y.z - Y.y * X.z);
   const d3 ay = mk3(Y.z * Z.x - Z.z * Y.x, Z.z * X.x - X.z * Z.x, X.z * Y.x - Y.z * X.x);
@@ -152,11 +180,13 @@ __host__ __device__ __forceinline__ bool tet_contains64(d3 p, d3 v0, d3 v1, d3 v
   const d3 rhs = sub3(p, v0);
   const d3 l = add3(add3(scl3(rhs.x, ix), scl3(rhs.y, iy)), scl3(rhs.z, iz));
   const double l0 = 1.0 - (l.x + l.y + l.z);
-  const double hi = 1.0 + ZERO_TOL;
-  if (l0 < -ZERO_TOL || l0 > hi) return false;
-  if (l.x < -ZERO_TOL || l.x > hi) return false;
-  if (l.y < -ZERO_TOL || l.y > hi) return false;
-  if (l.z < -ZERO_TOL || l.z > hi) return false;
+  // bary < -PLUCKER_ZERO_TOL || bary > 1.0f + PLUCKER_ZERO_TOL, on integer keys
+  const long long lo = okey(-ZERO_TOL), hi = okey(1.0 + ZERO_TOL);
+  const long long k0 = okey(l0), k1 = okey(l.x), k2 = okey(l.y), k3 = okey(l.z);
+  if (k0 < lo || k0 > hi) return false;
+  if (k1 < lo || k1 > hi) return false;
+  if (k2 < lo || k2 > hi) return false;
+  if (k3 < lo || k3 > hi) return false;
   return true;
 }
 
@@ -305,6 +335,11 @@ __device__ __forceinline__ bool nan_bits(double x) {
   return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
 }
 
+// finite and |x| < 2^300, so no product of three inputs can overflow
+__device__ __forceinline__ bool sane_bits(double x) {
+  return ((unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu) < 1023u + 300u;
+}
+
 __device__ __forceinline__ bool finite_bits(double x) {
   return ((unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu) != 0x7ffu;
 }
@@ -364,6 +399,40 @@ __device__ __forceinline__ SignCert plucker_filter32(const Ray32& r, float v0x, 
   c.pos = (p01 > thr ? 1u : 0u) | (p12 > thr ? 2u : 0u) | (p20 > thr ? 4u : 0u);
   c.neg = (p01 < -thr ? 1u : 0u) | (p12 < -thr ? 2u : 0u) | (p20 < -thr ? 4u : 0u);
   return c;
+}
+
+// FP32 pre-filter of tet containment (tetrahedron_contain.cpp:11-43).
+// Returns +1 when the FP64 test certainly accepts, -1 when it certainly
+// rejects, 0 when only the FP64 test can tell.
+//
+// With the per-tet data of k_tet_gather (M = T^{-1} rounded to FP32, m >= the
+// max row 1-norm of M, e64 >= the error of the reference's FP64 barycentric
+// coordinates anywhere in the tet's box), the FP32 coordinates
+//    l = M32 (p32 - v0_32),  l0 = 1 - (l1 + l2 + l3)
+// are within E32 = u (16 m (R + |p| + |v0|) + 4 (1 + sum |l|)) of the exact
+// barycentric coordinates (R = |p32 - v0_32|_inf; p, v0 and M rounded to
+// nearest (u; the bound allows 2u for p), 3-term dot products gamma_3), and the FP64 coordinates are
+// within e64 of them.  The reference accepts iff every coordinate lies in
+// [-20 eps, 1 + 20 eps]; so l_k < -(E32 + e64 + 20 eps) for some k certifies a
+// rejection, and E32 + e64 <= l_k <= 1 - (E32 + e64) for all k an acceptance.
+__device__ __forceinline__ int tet_filter32(float px, float py, float pz, float pabs, float4 f0,
+                                            float4 f1, float4 f2, float4 f3) {
+  const float m = f0.w;
+  if (!(m < INFINITY)) return 0;
+  const float rx = px - f0.x, ry = py - f0.y, rz = pz - f0.z;
+  const float R = fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz)));
+  const float l1 = f1.x * rx + f1.y * ry + f1.z * rz;
+  const float l2 = f2.x * rx + f2.y * ry + f2.z * rz;
+  const float l3 = f3.x * rx + f3.y * ry + f3.z * rz;
+  const float l0 = 1.0f - (l1 + l2 + l3);
+  const float sl = fabsf(l1) + fabsf(l2) + fabsf(l3);
+  const float E = (5.9604645e-08f * (16.0f * m * (R + pabs + f1.w) + 4.0f * (1.0f + sl))) * 1.0001f +
+                  f2.w + 4.5e-15f;
+  const float lmin = fminf(fminf(l0, l1), fminf(l2, l3));
+  const float lmax = fmaxf(fmaxf(l0, l1), fmaxf(l2, l3));
+  if (lmin < -E || lmax > 1.0f + E) return -1;
+  if (lmin >= E && lmax <= 1.0f - E) return 1;
+  return 0;
 }
 
 // Non-oriented test (ray_fire, point_in_volume, occluded): the FP64 test

@@ -96,8 +96,9 @@ enum : int {
   CNT_N = 8,
 };
 
+// inputs the engine accepts: finite, |x| < 2^300 (see geom.cuh)
 __device__ __forceinline__ bool finite3(d3 a) {
-  return finite_bits(a.x) && finite_bits(a.y) && finite_bits(a.z);
+  return sane_bits(a.x) && sane_bits(a.y) && sane_bits(a.z);
 }
 
 __device__ __forceinline__ d3 load3(const double* p, int64_t i) {

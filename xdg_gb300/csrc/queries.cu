@@ -164,6 +164,7 @@ __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
       // conservative
       const float px = __double2float_rn(p.x), py = __double2float_rn(p.y),
                   pz = __double2float_rn(p.z);
+      const float pabs = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
       int32_t stack[kStackSize];
       int sp = 0;
       int32_t ref = T.root;
@@ -211,6 +212,22 @@ __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
           const int32_t first = leaf_first(ref), count = leaf_count(ref);
           for (int32_t q = first; q < first + count; ++q) {
             cnt.prim++;
+            if (MIXED) {
+              const float4* f = T.prim32 + 4 * (int64_t)q;
+              const int c = tet_filter32(px, py, pz, pabs, __ldg(f), __ldg(f + 1), __ldg(f + 2),
+                                         __ldg(f + 3));
+              if (c < 0) continue;
+              if (c > 0) {
+                const int32_t idx = __ldg(&T.prim_ref[q]);
+                const int32_t id = __ldg(&a.elem_ids[idx]);
+                if (best_idx < 0 || id < best_id) {
+                  best_id = id;
+                  best_idx = idx;
+                }
+                continue;
+              }
+              cnt.esc++;
+            }
             const double* v = T.prim64 + 12 * (int64_t)q;
             const d3 v0 = mk3(__ldg(v + 0), __ldg(v + 1), __ldg(v + 2));
             const d3 v1 = mk3(__ldg(v + 3), __ldg(v + 4), __ldg(v + 5));

@@ -37,6 +37,7 @@ struct SurfArgs {
   int32_t* status;
   unsigned long long* counters;
   int32_t occupancy;   // traversal kernel variant: minimum resident blocks per SM (2..4)
+  int32_t node_iters;  // inner-node steps per lane between leaf phases (1..64)
 };
 
 struct PointArgs {

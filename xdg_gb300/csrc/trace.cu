@@ -213,36 +213,14 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
     if (__ballot_sync(kFull, has_ray) == 0u) break;
 
     // ---- one traversal step per active lane ----
-    const unsigned act = __ballot_sync(kFull, trav);
     unsigned escm = 0u;   // escalated primitives of this step (bit k -> esc_p0 + k)
     int32_t esc_p0 = 0;
-    if (trav) {
-      if (leaf_p < leaf_end) {
-        // the whole leaf (<= 4 primitives) in one step: its loads overlap
-        const int32_t p0 = leaf_p;
-        const int np = leaf_end - leaf_p;
-        leaf_p = leaf_end;
-        esc_p0 = p0;
-        cnt.prim += np;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          if (k < np) {
-            if (MIXED) {
-              const int64_t q = 3 * (int64_t)(p0 + k);
-              const float4 A = __ldg(&prim32[q]);
-              const float4 B = __ldg(&prim32[q + 1]);
-              const float4 C = __ldg(&prim32[q + 2]);
-              const SignCert c = plucker_filter32(r32, A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
-                                                  C.z, B.w, A.w);
-              if (!certified_miss(c)) escm |= 1u << k;
-            } else {
-              escm |= 1u << k;
-            }
-          }
-        }
-        if (cur == CHILD_EMPTY) pop();
-      } else {
-        // inner node
+    // node phase: lanes without a pending leaf descend through inner nodes
+    // (up to node_iters steps) until they hold a leaf or run out of work
+    for (int it = 0; it < a.node_iters; ++it) {
+      const bool want = trav && leaf_p >= leaf_end;
+      if (__ballot_sync(kFull, want) == 0u) break;
+      if (want) {
         cnt.node++;
         cnt.box += 4;
         int32_t cr[4];
@@ -282,7 +260,31 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
         }
       }
     }
-    (void)act;
+    // leaf phase: the whole leaf (<= 4 primitives) at once, so its loads overlap
+    if (trav && leaf_p < leaf_end) {
+      const int32_t p0 = leaf_p;
+      const int np = leaf_end - leaf_p;
+      leaf_p = leaf_end;
+      esc_p0 = p0;
+      cnt.prim += np;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k < np) {
+          if (MIXED) {
+            const int64_t q = 3 * (int64_t)(p0 + k);
+            const float4 A = __ldg(&prim32[q]);
+            const float4 B = __ldg(&prim32[q + 1]);
+            const float4 C = __ldg(&prim32[q + 2]);
+            const SignCert c = plucker_filter32(r32, A.x, A.y, A.z, B.x, B.y, B.z, C.x, C.y,
+                                                C.z, B.w, A.w);
+            if (!certified_miss(c)) escm |= 1u << k;
+          } else {
+            escm |= 1u << k;
+          }
+        }
+      }
+      if (cur == CHILD_EMPTY) pop();
+    }
     // ---- enqueue this step's escalations (warp-wide exclusive scan) ----
     {
       const int c = __popc(escm);
@@ -354,23 +356,23 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
         if (plucker64(v0, v1, v2, oo, od, rn, tmax, 0.0, false, 0, &t)) {
           if (MODE == MODE_OCCLUDED) {
             flags = 1;
-          } else if (!(t > obt)) {  // triangle_intersect.cpp:78
+          } else if (!dlt(obt, t)) {  // triangle_intersect.cpp:78: t > dtfar rejects
             const int32_t gtri = __ldg(&opref[prim]);
             const int32_t fid = __ldg(&a.tri_face[gtri]);
-            if (!(obhas && t == obt && fid >= obface)) {
+            if (!(obhas && okey(t) == okey(obt) && fid >= obface)) {
               d3 nrm = face_normal64(v0, v1, v2);  // :80
               const int32_t sidx = __ldg(&a.tri_surf[gtri]);
               if (__ldg(&a.surf_rev_tree[sidx]) == otid) nrm = neg3(nrm);  // :84-87
               const double dp = dot3(od, nrm);
               bool keep = true;
               if (MODE == MODE_RAY_FIRE) {  // orientation_cull, :12-24
-                if (a.orientation == 0 && dp < 0.0) keep = false;
-                if (a.orientation == 1 && dp >= 0.0) keep = false;
+                if (a.orientation == 0 && lt0(dp)) keep = false;   // dot < 0
+                if (a.orientation == 1 && !lt0(dp)) keep = false;  // dot >= 0
               }
               for (int32_t k = 0; keep && k < onexcl; ++k)  // primitive_mask_cull, :26-34
                 if (__ldg(&oexcl[k]) == fid) keep = false;
               if (keep) {
-                flags = 1 | (dp > 0.0 ? 2 : 0);
+                flags = 1 | (gt0(dp) ? 2 : 0);
                 rt = t;
                 rface = fid;
                 rsurf = __ldg(&a.surf_id[sidx]);
@@ -399,7 +401,8 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
         }
         const double t = Q.rt[j];
         const int32_t f = Q.rface[j];
-        if (!bhas || t < bt || (t == bt && f < bface)) {
+        const long long kt = okey(t), kb = okey(bt);
+        if (!bhas || kt < kb || (kt == kb && f < bface)) {
           bhas = true;
           bt = t;
           bface = f;

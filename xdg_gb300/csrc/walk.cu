@@ -96,7 +96,7 @@ __device__ __forceinline__ int next_face(const WalkArgs& a, int32_t elem, d3 r, 
       const d3 f2 = sel4(V, face_local<FO>(a, f, 2));
       double t;
       const bool hit = plucker64(f0, f1, f2, r, u, rn, INFTY, 0.0, true, 1, &t);
-      dists[f] = hit ? ((0.0 < t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
+      dists[f] = hit ? (gt0(t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
     }
     cnt.esc += 4;
   } else {
@@ -158,8 +158,8 @@ __device__ __forceinline__ int next_face(const WalkArgs& a, int32_t elem, d3 r, 
       const d3 f2 = load3(a.xyz, sel4(ci, l2));
       double t;
       const bool hit = plucker64(f0, f1, f2, r, u, rn, INFTY, 0.0, true, 1, &t);
-      const double df = hit ? ((0.0 < t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
-      if (df < best) {
+      const double df = hit ? (gt0(t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
+      if (dlt(df, best)) {
         best = df;
         idx = f;
       }
@@ -171,7 +171,7 @@ __device__ __forceinline__ int next_face(const WalkArgs& a, int32_t elem, d3 r, 
   double best = INFTY;
 #pragma unroll
   for (int f = 0; f < 4; ++f) {
-    if (dists[f] < best) {
+    if (dlt(dists[f], best)) {
       best = dists[f];
       idx = f;
     }
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
     }
     if (__ballot_sync(0xffffffffu, has) == 0u) break;
     if (has) {
-      bool done = !(dist > 0);  // mesh_manager_interface.cpp:117
+      bool done = !gt0(dist);  // while (distance > 0), mesh_manager_interface.cpp:117
       if (!done && k >= a.max_segs) {
         st = RAY_WALK_LIMIT;
         done = true;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
           const int4 ad = __ldg(&a.adj[elem]);
           nxt = f == 0 ? ad.x : (f == 1 ? ad.y : (f == 2 ? ad.z : ad.w));
         }
-        ex = (dist < ex) ? dist : ex;  // std::min(exit, distance)
+        ex = dlt(dist, ex) ? dist : ex;  // std::min(exit, distance)
         dist -= ex;
         oe[k] = __ldg(&a.elem_ids[elem]);
         ol[k] = ex;
