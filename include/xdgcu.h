@@ -60,7 +60,8 @@ enum {
   XDGCU_RAY_INVALID = 1,        /* NaN/inf origin or direction, or bad tree id */
   XDGCU_RAY_STACK_OVERFLOW = 2, /* traversal stack exhausted (result incomplete) */
   XDGCU_RAY_WALK_LIMIT = 4,     /* walk stopped at max_segs (output truncated) */
-  XDGCU_RAY_NO_EXIT_FACE = 5    /* next_element found no exiting face */
+  XDGCU_RAY_NO_EXIT_FACE = 5,   /* next_element found no exiting face */
+  XDGCU_RAY_OUTPUT_FULL = 6     /* packed walk output capacity exceeded */
 };
 
 /* shared_enums.h:11-15 */
@@ -203,6 +204,23 @@ int xdgcu_walk_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
                         int32_t max_segs, int32_t* seg_elem, double* seg_len,
                         int32_t* seg_count, int32_t* status, int32_t precision, void* stream);
 
+/* MeshManager::walk_elements for n tracks with packed, variable-length
+ * output -- the form of the reference's per-track
+ * std::vector<std::pair<MeshID, double>> (mesh_manager_interface.cpp:106-136).
+ * Track i's segments are seg_elem/seg_len[offsets[i] .. offsets[i+1]-1]
+ * (element MESH ids, lengths, zero-length segments included); offsets has
+ * n+1 entries and offsets[n] is the total.  Arrays hold `capacity` entries:
+ * a track whose segments do not fit is not written and gets
+ * XDGCU_RAY_OUTPUT_FULL (call again with capacity >= offsets[n]).  max_segs
+ * caps the segments of one track (XDGCU_RAY_WALK_LIMIT).  The tracks are
+ * walked twice (count, then emit at the scanned offsets); the scan's scratch
+ * is allocated on `stream` with cudaMallocAsync. */
+int xdgcu_walk_elements_packed(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
+                               const double* start, const double* u, const double* distance,
+                               int32_t max_segs, int64_t capacity, int32_t* seg_elem,
+                               double* seg_len, int64_t* offsets, int32_t* status,
+                               int32_t precision, void* stream);
+
 /* ------------------------------------------------------------------------
  * Diagnostics
  * ------------------------------------------------------------------------ */
@@ -222,6 +240,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *   "trace_node_iters" inner-node steps a lane takes between two leaf phases
  *                      of the warp-synchronous traversal, mixed precision (1..64)
  *   "trace_node_iters_fp64"  the same for the all-FP64 path
+ *   "trace_flush_wait" number of lanes (1..32) whose rays wait only on queued
+ *                      FP64 candidate tests before the warp drains a partly
+ *                      filled queue
  *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4) */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);

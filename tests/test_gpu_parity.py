@@ -255,3 +255,51 @@ def test_walk_against_reference_vectors(cuda, prec):
         c = sc[k]
         assert np.array_equal(se[k, :c], g["tw_elem"][k, :c])
         assert np.array_equal(sl[k, :c], g["tw_seglen"][k, :c])
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_packed_walk_matches_strided(cuda, tet_model, prec):
+    """xdgcu_walk_elements_packed: same segments as the strided walk, packed by
+    the scanned offsets; tracks that do not fit are flagged, not written."""
+    torch = cuda
+    from xdg_gb300._lib import RAY_OUTPUT_FULL
+    tm = tet_model
+    rti = CudaRayTracer()
+    rti.set_tet_mesh(tm)
+    m = synth.Model(volumes=[1], tets=tm, elements={1: np.arange(len(tm.conn), dtype=np.int32)})
+    et = rti.create_element_tree(m, 1)
+    rng = np.random.default_rng(31)
+    n = 5000
+    start = rng.uniform(0, 10, (n, 3))
+    u = synth.isotropic_dirs(rng, n)
+    length = np.minimum(rng.exponential(5.0, n), _exit_distance(start, u, 0.0, 10.0))
+    _, idx = rti.find_element(et, start, prec)
+    se, sl, sc, st = rti.walk_elements(idx, start, u, length, 512, prec)
+    total = int(sc.sum())
+    # host pointers
+    pe, pl, off, pst = rti.walk_elements_packed(idx, start, u, length, total, 512, prec)
+    assert off[0] == 0 and off[-1] == total and np.array_equal(np.diff(off), sc)
+    assert np.array_equal(pst, st)
+    for k in range(n):
+        assert np.array_equal(pe[off[k]:off[k + 1]], se[k, :sc[k]])
+        assert np.array_equal(pl[off[k]:off[k + 1]], sl[k, :sc[k]])
+    # device pointers, same result
+    dev = torch.device("cuda")
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    de, dl, doff, dst = rti.walk_elements_packed(T(idx), T(start), T(u), T(length), total, 512, prec)
+    torch.cuda.synchronize()
+    assert np.array_equal(doff.cpu().numpy(), off)
+    assert np.array_equal(de.cpu().numpy()[:total], pe[:total])
+    assert np.array_equal(dl.cpu().numpy()[:total], pl[:total])
+    # too small: offsets still complete, overflowing tracks flagged and unwritten
+    cap = total // 2
+    pe2, pl2, off2, pst2 = rti.walk_elements_packed(idx, start, u, length, cap, 512, prec)
+    assert np.array_equal(off2, off)
+    full = off[1:] > cap
+    assert (pst2[full & (sc > 0)] == RAY_OUTPUT_FULL).all()
+    fit = ~full
+    for k in np.nonzero(fit)[0][:200]:
+        assert np.array_equal(pe2[off[k]:off[k + 1]], se[k, :sc[k]])
+    # empty batch
+    e0, l0, off0, s0 = rti.walk_elements_packed(idx[:0], start[:0], u[:0], length[:0], 0, 512, prec)
+    assert len(off0) == 1 and off0[0] == 0

@@ -22,6 +22,7 @@ _dbl = ctypes.c_double
 # status / enums (xdgcu.h)
 OK = 0
 RAY_OK, RAY_INVALID, RAY_STACK_OVERFLOW, RAY_WALK_LIMIT, RAY_NO_EXIT_FACE = 0, 1, 2, 4, 5
+RAY_OUTPUT_FULL = 6
 ANY, EXITING, ENTERING = -1, 0, 1
 FP64, MIXED = 0, 1
 
@@ -49,6 +50,8 @@ SIGNATURES = {
     "xdgcu_next_element": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_walk_elements": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _VP, _VP, _VP, _VP,
                                    _i32, _VP]),
+    "xdgcu_walk_elements_packed": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _i64, _VP, _VP,
+                                          _VP, _VP, _i32, _VP]),
     "xdgcu_set_tuning": (_int, [_VP, ctypes.c_char_p, _i64]),
     "xdgcu_get_tuning": (_int, [_VP, ctypes.c_char_p, _I64]),
     "xdgcu_set_counting": (_int, [_VP, _i32]),

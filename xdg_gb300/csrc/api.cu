@@ -292,6 +292,7 @@ struct xdgcu_ctx {
   int32_t trace_occupancy = 3;
   int32_t trace_node_iters = 4;       // mixed precision
   int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
+  int32_t trace_flush_wait = 8;
   int32_t leaf_max = 4;
   // diagnostics
   bool counting = false;
@@ -797,6 +798,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "trace_node_iters" || k == "trace_node_iters_fp64") {
     if (value < 1 || value > 64) return set_err(XDGCU_ERR_INVALID_ARG, k + " must be 1..64");
     (k == "trace_node_iters" ? c->trace_node_iters : c->trace_node_iters_fp64) = (int32_t)value;
+  } else if (k == "trace_flush_wait") {
+    if (value < 1 || value > 32) return set_err(XDGCU_ERR_INVALID_ARG, "trace_flush_wait must be 1..32");
+    c->trace_flush_wait = (int32_t)value;
   } else if (k == "leaf_max") {
     if (value < 1 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "leaf_max must be 1..4");
     c->leaf_max = (int32_t)value;
@@ -812,6 +816,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   if (k == "trace_occupancy") *value = c->trace_occupancy;
   else if (k == "trace_node_iters") *value = c->trace_node_iters;
   else if (k == "trace_node_iters_fp64") *value = c->trace_node_iters_fp64;
+  else if (k == "trace_flush_wait") *value = c->trace_flush_wait;
   else if (k == "leaf_max") *value = c->leaf_max;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   return XDGCU_OK;
@@ -883,6 +888,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.surf_rev_tree = c->d_surf_rev.p;
   a.occupancy = c->trace_occupancy;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
+  a.flush_wait = c->trace_flush_wait;
   cudaStream_t st = (cudaStream_t)stream;
   if (kind == 1) {
     a.ray_trees = ray_trees;
@@ -1142,6 +1148,102 @@ static int walk_query(xdgcu_ctx* c, bool walk, int64_t n, const int32_t* start, 
   if (rc) return rc;
   API_CUDA(launch(), "walk launch");
   return stage_out(all, st);
+}
+
+int xdgcu_walk_elements_packed(xdgcu_ctx* c, int64_t n, const int32_t* start_index,
+                               const double* start, const double* u, const double* distance,
+                               int32_t max_segs, int64_t capacity, int32_t* seg_elem,
+                               double* seg_len, int64_t* offsets, int32_t* status,
+                               int32_t precision, void* stream) {
+  CHECK_CTX(c);
+  if (n < 0 || capacity < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative size");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (!c->has_tets) return set_err(XDGCU_ERR_STATE, "no tet mesh set");
+  if (!offsets) return set_err(XDGCU_ERR_INVALID_ARG, "walk_elements_packed: offsets required");
+  if (n > 0 && (!start_index || !start || !u || !distance || max_segs <= 0))
+    return set_err(XDGCU_ERR_INVALID_ARG, "walk_elements_packed: bad inputs");
+  if (capacity > 0 && (!seg_elem || !seg_len))
+    return set_err(XDGCU_ERR_INVALID_ARG, "walk_elements_packed: null segment arrays");
+  const int kind = classify({start_index, start, u, distance, seg_elem, seg_len, offsets, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  WalkArgs a{};
+  a.xyz = c->d_xyz.p;
+  a.xyz32 = c->d_xyz32.p;
+  a.conn = c->d_conn.p;
+  a.adj = c->d_adj.p;
+  a.elem_ids = c->d_elem_ids.p;
+  a.n_tets = (int32_t)c->n_tet;
+  std::memcpy(a.face, c->face, sizeof(a.face));
+  a.n = n;
+  a.max_segs = max_segs;
+  a.capacity = capacity;
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool mixed = precision == XDGCU_MIXED;
+  auto run = [&](cudaStream_t s) -> int {
+    a.out_mode = WALK_COUNT;
+    API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (count)");
+    int64_t* sums = nullptr;
+    API_CUDA(cudaMallocAsync(&sums, sizeof(int64_t) * scan_scratch_entries(n), s), "scan scratch");
+    cudaError_t e = scan_offsets(a.offsets, n, sums, s);
+    cudaFreeAsync(sums, s);
+    API_CUDA(e, "scan");
+    a.out_mode = WALK_PACKED;
+    API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (emit)");
+    return XDGCU_OK;
+  };
+  if (kind == 1) {
+    a.start = start_index;
+    a.org = start;
+    a.dir = u;
+    a.dist = distance;
+    a.seg_elem = seg_elem;
+    a.seg_len = seg_len;
+    a.offsets = offsets;
+    a.status = status;
+    return n > 0 ? run(st) : (cudaMemsetAsync(offsets, 0, sizeof(int64_t), st) == cudaSuccess
+                                  ? XDGCU_OK
+                                  : set_err(XDGCU_ERR_CUDA, "memset"));
+  }
+  if (n == 0) {
+    offsets[0] = 0;
+    return XDGCU_OK;
+  }
+  Slot* s = get_slot(c);
+  if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  if (!st) st = s->stream;
+  Arr A_s{start_index, nullptr, sizeof(int32_t) * n};
+  Arr A_o{start, nullptr, sizeof(double) * 3 * n}, A_d{u, nullptr, sizeof(double) * 3 * n};
+  Arr A_l{distance, nullptr, sizeof(double) * n};
+  Arr A_off{nullptr, nullptr, sizeof(int64_t) * (n + 1)};
+  Arr A_se{nullptr, nullptr, sizeof(int32_t) * capacity}, A_sl{nullptr, nullptr, sizeof(double) * capacity};
+  Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
+  std::vector<Arr*> all = {&A_s, &A_o, &A_d, &A_l, &A_off, &A_se, &A_sl, &A_st};
+  int rc = stage_in(s, all, st);
+  if (rc) return rc;
+  a.start = (const int32_t*)A_s.dev;
+  a.org = (const double*)A_o.dev;
+  a.dir = (const double*)A_d.dev;
+  a.dist = (const double*)A_l.dev;
+  a.offsets = (int64_t*)A_off.dev;
+  a.seg_elem = (int32_t*)A_se.dev;
+  a.seg_len = (double*)A_sl.dev;
+  a.status = (int32_t*)A_st.dev;
+  rc = run(st);
+  if (rc) return rc;
+  API_CUDA(cudaMemcpyAsync(offsets, A_off.dev, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st),
+           "D2H");
+  rc = stage_out({&A_st}, st);
+  if (rc) return rc;
+  const int64_t used = std::min(offsets[n], capacity);
+  if (used > 0) {
+    API_CUDA(cudaMemcpyAsync(seg_elem, A_se.dev, sizeof(int32_t) * used, cudaMemcpyDeviceToHost, st),
+             "D2H");
+    API_CUDA(cudaMemcpyAsync(seg_len, A_sl.dev, sizeof(double) * used, cudaMemcpyDeviceToHost, st),
+             "D2H");
+    API_CUDA(cudaStreamSynchronize(st), "sync");
+  }
+  return XDGCU_OK;
 }
 
 int xdgcu_next_element(xdgcu_ctx* c, int64_t n, const int32_t* elem_index, const double* positions,

@@ -67,6 +67,7 @@ __host__ __device__ __forceinline__ d3 face_normal64(d3 v0, d3 v1, d3 v2) {
   return normalize64(cross3(sub3(v1, v0), sub3(v2, v0)));
 }
 
+
 // ---------------------------------------------------------------------------
 // Exact comparisons of doubles on the integer ALU.
 //
@@ -146,7 +147,6 @@ __device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn
   }
   if (is0(c0) && is0(c1) && is0(c2)) return false;
   const double inv = 1.0 / (c0 + c1 + c2);
-  const d3 hit = add3(add3(scl3(c0 * inv, v2), scl3(c1 * inv, v0)), scl3(c2 * inv, v1));
   // index of the largest |d| component, first maximum wins
   const unsigned long long ax = absbits(d.x), ay = absbits(d.y), az = absbits(d.z);
   int idx = 0;
@@ -154,13 +154,36 @@ __device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn
   if (ax > mx) { idx = 0; mx = ax; }
   if (ay > mx) { idx = 1; mx = ay; }
   if (az > mx) { idx = 2; mx = az; }
-  double dist = (comp3(hit, idx) - comp3(o, idx)) / comp3(d, idx);
-  const double u = c2 * inv;
-  const double v = c0 * inv;
+  // only component idx of the intersection point (plucker.h:132-134) is used;
+  // it is computed alone, with the same operations and order
+  const double w0 = c0 * inv, w1 = c1 * inv, w2 = c2 * inv;
+  const double hit_i = (w0 * comp3(v2, idx) + w1 * comp3(v0, idx)) + w2 * comp3(v1, idx);
+  double dist = (hit_i - comp3(o, idx)) / comp3(d, idx);
+  const double u = w2;
+  const double v = w0;
   if (lt0(u) || lt0(v) || dlt(1.0, u + v)) dist = -1.0;
   if (dlt(dist, t_min) || dlt(t_max, dist)) return false;
   *t_out = dist;
   return true;
+}
+
+// Sign of dot(d, face_normal64(v0, v1, v2)) as the reference computes it
+// (-1, 0, +1), without the square root and divisions of the normalisation
+// when the rounding bound allows.  With c = (v1-v0) x (v2-v0) rounded as the
+// reference rounds it, the reference's value is dot(d, c / len) evaluated
+// with <= 4 roundings per term, so len * dot = sum d_i c_i (1 + th_i) with
+// |th_i| <= gamma_4; the FP64 sum s = fl(sum d_i c_i) is within gamma_3
+// sum |d_i c_i| of the exact sum.  If |s| > 8 eps sum |d_i c_i|, both have the
+// sign of s and neither is zero; otherwise the exact normalised value decides.
+__device__ __forceinline__ int normal_dot_sign(d3 d, d3 v0, d3 v1, d3 v2) {
+  const d3 c = cross3(sub3(v1, v0), sub3(v2, v0));
+  const double p0 = d.x * c.x, p1 = d.y * c.y, p2 = d.z * c.z;
+  const double s = p0 + p1 + p2;
+  const double bound = (fabs(p0) + fabs(p1) + fabs(p2)) * (8.0 * DBL_EPSILON);
+  // (the second test keeps the reference's value away from underflow)
+  if (absbits(s) > absbits(bound) && absbits(s) > 0x0100000000000000ull) return gt0(s) ? 1 : -1;
+  const double dp = dot3(d, normalize64(c));
+  return gt0(dp) ? 1 : (lt0(dp) ? -1 : 0);
 }
 
 // tetrahedron_contain.cpp:11-43.  The reference solves T*lambda = p - v0 with

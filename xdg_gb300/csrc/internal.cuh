@@ -83,6 +83,7 @@ enum : int32_t {
   RAY_STACK_OVERFLOW = 2,
   RAY_WALK_LIMIT = 4,
   RAY_NO_EXIT_FACE = 5,
+  RAY_OUTPUT_FULL = 6,
 };
 
 // work counters (xdgcu_get_counters)

@@ -38,6 +38,7 @@ struct SurfArgs {
   unsigned long long* counters;
   int32_t occupancy;   // traversal kernel variant: minimum resident blocks per SM (2..4)
   int32_t node_iters;  // inner-node steps per lane between leaf phases (1..64)
+  int32_t flush_wait;  // lanes waiting on the FP64 queue that force a partial drain (1..32)
 };
 
 struct PointArgs {

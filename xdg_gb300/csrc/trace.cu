@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
       const int qn = (int)(Q.tail - head);
       const unsigned act2 = __ballot_sync(kFull, trav);
       const unsigned waiting = __ballot_sync(kFull, has_ray && !trav && npend > 0);
-      if (!(qn >= 32 || (qn > 0 && (act2 == 0u || __popc(waiting) >= 8)))) break;
+      if (!(qn >= 32 || (qn > 0 && (act2 == 0u || __popc(waiting) >= a.flush_wait)))) break;
       const int nq = min(qn, 32);
       const bool mine = lane < nq;
       const uint32_t ent = mine ? Q.ent[(head + lane) & (kQ - 1)] : ((uint32_t)lane << 27);
@@ -360,19 +360,20 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
             const int32_t gtri = __ldg(&opref[prim]);
             const int32_t fid = __ldg(&a.tri_face[gtri]);
             if (!(obhas && okey(t) == okey(obt) && fid >= obface)) {
-              d3 nrm = face_normal64(v0, v1, v2);  // :80
+              // sign of dot(d, normal), normal flipped in the surface's
+              // reverse-sense tree (:80, :84-87)
               const int32_t sidx = __ldg(&a.tri_surf[gtri]);
-              if (__ldg(&a.surf_rev_tree[sidx]) == otid) nrm = neg3(nrm);  // :84-87
-              const double dp = dot3(od, nrm);
+              int sg = normal_dot_sign(od, v0, v1, v2);
+              if (__ldg(&a.surf_rev_tree[sidx]) == otid) sg = -sg;
               bool keep = true;
               if (MODE == MODE_RAY_FIRE) {  // orientation_cull, :12-24
-                if (a.orientation == 0 && lt0(dp)) keep = false;   // dot < 0
-                if (a.orientation == 1 && !lt0(dp)) keep = false;  // dot >= 0
+                if (a.orientation == 0 && sg < 0) keep = false;   // dot < 0
+                if (a.orientation == 1 && sg >= 0) keep = false;  // dot >= 0
               }
               for (int32_t k = 0; keep && k < onexcl; ++k)  // primitive_mask_cull, :26-34
                 if (__ldg(&oexcl[k]) == fid) keep = false;
               if (keep) {
-                flags = 1 | (gt0(dp) ? 2 : 0);
+                flags = 1 | (sg > 0 ? 2 : 0);
                 rt = t;
                 rface = fid;
                 rsurf = __ldg(&a.surf_id[sidx]);

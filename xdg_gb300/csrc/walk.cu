@@ -230,8 +230,23 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
           elem = a.start[i];
           k = 0;
           st = RAY_OK;
-          oe = a.seg_elem + i * (int64_t)a.max_segs;
-          ol = a.seg_len + i * (int64_t)a.max_segs;
+          if (a.out_mode == WALK_STRIDED) {
+            oe = a.seg_elem + i * (int64_t)a.max_segs;
+            ol = a.seg_len + i * (int64_t)a.max_segs;
+          } else if (a.out_mode == WALK_PACKED) {
+            const int64_t off = a.offsets[i];
+            const int64_t cnt_i = a.offsets[i + 1] - off;
+            if (off + cnt_i <= a.capacity) {
+              oe = a.seg_elem + off;
+              ol = a.seg_len + off;
+            } else {
+              oe = nullptr;  // does not fit: the track is walked, nothing is written
+              ol = nullptr;
+            }
+          } else {
+            oe = nullptr;
+            ol = nullptr;
+          }
           if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u) || nan_bits(dist)) {
             st = RAY_INVALID;
             dist = 0.0;  // finishes below without a step
@@ -260,8 +275,10 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
         }
         ex = dlt(dist, ex) ? dist : ex;  // std::min(exit, distance)
         dist -= ex;
-        oe[k] = __ldg(&a.elem_ids[elem]);
-        ol[k] = ex;
+        if (oe) {
+          oe[k] = __ldg(&a.elem_ids[elem]);
+          ol[k] = ex;
+        }
         ++k;
         r = add3(r, scl3(ex, u));  // r += exit.second * u
         if (nxt < -1 || nxt >= a.n_tets) {
@@ -273,7 +290,12 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
         }
       }
       if (done) {
-        a.seg_count[i] = k;
+        if (a.out_mode == WALK_COUNT) {
+          a.offsets[i] = k;
+        } else {
+          if (a.seg_count) a.seg_count[i] = k;
+          if (a.out_mode == WALK_PACKED && !oe && k > 0 && st == RAY_OK) st = RAY_OUTPUT_FULL;
+        }
         if (a.status) a.status[i] = st;
         has = false;
         tracks++;
@@ -312,6 +334,88 @@ __global__ void __launch_bounds__(kBlock) k_next(WalkArgs a) {
   if (a.counters) flush(a.counters, cnt, i < a.n ? 1ull : 0ull);
 }
 
+constexpr int kScanBlock = 1024;
+
+// sum of each block of kScanBlock counts
+__global__ void __launch_bounds__(kScanBlock) k_block_sums(const int64_t* __restrict__ v, int64_t n,
+                                                           int64_t* __restrict__ sums) {
+  __shared__ int64_t ws[kScanBlock / 32];
+  const int64_t i = blockIdx.x * (int64_t)kScanBlock + threadIdx.x;
+  int64_t x = i < n ? v[i] : 0;
+  for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int64_t y = ws[threadIdx.x];
+    for (int off = 16; off > 0; off >>= 1) y += __shfl_xor_sync(0xffffffffu, y, off);
+    if (threadIdx.x == 0) sums[blockIdx.x] = y;
+  }
+}
+
+// exclusive scan of the block sums by one block; sums[nb] = total
+__global__ void __launch_bounds__(kScanBlock) k_scan_sums(int64_t* __restrict__ sums, int64_t nb) {
+  __shared__ int64_t ws[kScanBlock / 32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < nb; base += kScanBlock) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t x = i < nb ? sums[i] : 0;
+    int64_t incl = x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int off = 1; off < 32; off <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += y;
+    }
+    if (lane == 31) ws[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+      int64_t s = ws[lane];
+      for (int off = 1; off < 32; off <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, s, off);
+        if (lane >= off) s += y;
+      }
+      ws[lane] = s;
+    }
+    __syncthreads();
+    const int64_t before = carry + (w > 0 ? ws[w - 1] : 0) + incl - x;
+    if (i < nb) sums[i] = before;
+    __syncthreads();
+    if (threadIdx.x == kScanBlock - 1) carry = before + x;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+// in-place exclusive scan of each block plus its block offset
+__global__ void __launch_bounds__(kScanBlock) k_scan_apply(int64_t* __restrict__ v, int64_t n,
+                                                           const int64_t* __restrict__ sums,
+                                                           int64_t nb) {
+  __shared__ int64_t ws[kScanBlock / 32];
+  const int64_t i = blockIdx.x * (int64_t)kScanBlock + threadIdx.x;
+  const int64_t x = i < n ? v[i] : 0;
+  int64_t incl = x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int off = 1; off < 32; off <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += y;
+  }
+  if (lane == 31) ws[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int64_t s = ws[lane];
+    for (int off = 1; off < 32; off <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, s, off);
+      if (lane >= off) s += y;
+    }
+    ws[lane] = s;
+  }
+  __syncthreads();
+  const int64_t excl = sums[blockIdx.x] + (w > 0 ? ws[w - 1] : 0) + incl - x;
+  if (i < n) v[i] = excl;
+  if (blockIdx.x == 0 && threadIdx.x == 0) v[n] = sums[nb];
+}
+
 template <int FO, bool MIXED>
 cudaError_t launch_walk_t(const WalkArgs& a, cudaStream_t st) {
   static int num_sms = 0, per_sm = 0;
@@ -346,6 +450,17 @@ cudaError_t launch_walk(bool mixed, int face_order, const WalkArgs& a, cudaStrea
     case 2: return launch_walk_t<1, false>(a, st);
     default: return launch_walk_t<1, true>(a, st);
   }
+}
+
+int64_t scan_scratch_entries(int64_t n) { return (n + kScanBlock - 1) / kScanBlock + 1; }
+
+cudaError_t scan_offsets(int64_t* offsets, int64_t n, int64_t* block_sums, cudaStream_t st) {
+  if (n <= 0) return cudaMemsetAsync(offsets, 0, sizeof(int64_t), st);
+  const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+  k_block_sums<<<(unsigned)nb, kScanBlock, 0, st>>>(offsets, n, block_sums);
+  k_scan_sums<<<1, kScanBlock, 0, st>>>(block_sums, nb);
+  k_scan_apply<<<(unsigned)nb, kScanBlock, 0, st>>>(offsets, n, block_sums, nb);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_next_element(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st) {

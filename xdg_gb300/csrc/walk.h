@@ -28,7 +28,20 @@ struct WalkArgs {
   int32_t* next_out;     // next_element mode
   double* dist_out;
   unsigned long long* counters;
+  // output layout: 0 = track-major with stride max_segs; 1 = count only
+  // (offsets[i] = number of segments of track i); 2 = packed, track i's
+  // segments at offsets[i] .. offsets[i+1]-1 of arrays of `capacity` entries
+  int32_t out_mode;
+  int64_t* offsets;
+  int64_t capacity;
 };
+
+enum : int32_t { WALK_STRIDED = 0, WALK_COUNT = 1, WALK_PACKED = 2 };
+
+// In-place exclusive scan of offsets[0..n) with offsets[n] = total.
+// block_sums needs scan_scratch_entries(n) int64 entries.
+int64_t scan_scratch_entries(int64_t n);
+cudaError_t scan_offsets(int64_t* offsets, int64_t n, int64_t* block_sums, cudaStream_t st);
 
 // face_order: 0 = the MOAB table {0,1,3},{1,2,3},{2,0,3},{0,2,1} (compiled in),
 // 1 = any other table (read from WalkArgs::face).

@@ -371,6 +371,30 @@ class CudaRayTracer:
         return se, sl, sc, st
 
 
+    def walk_elements_packed(self, start_index, start, u, distance, capacity, max_segs=4096,
+                             precision=MIXED, stream=None):
+        """Packed walk: returns (seg_elem [capacity], seg_len, offsets [n+1], status)."""
+        e = _prep(start_index, np.int32)
+        r = _prep(start, np.float64, 3)
+        uu = _prep(u, np.float64, 3)
+        n = r.shape[0]
+        dist = distance if _is_torch(distance) else _host(np.broadcast_to(distance, (n,)),
+                                                           np.float64)
+        out = _Out(r)
+        se, sl, st = out.i32(max(1, capacity)), out.f64(max(1, capacity)), out.i32(n)
+        if out.torch:
+            off = out._torch.empty(n + 1, dtype=out._torch.int64, device=out.device)
+        else:
+            off = np.empty(n + 1, dtype=np.int64)
+        self._check(self.L.xdgcu_walk_elements_packed(self.ctx, n, _addr(e), _addr(r), _addr(uu),
+                                                      _addr(dist), int(max_segs), int(capacity),
+                                                      _addr(se), _addr(sl), _addr(off), _addr(st),
+                                                      int(precision),
+                                                      stream if stream is not None else out.stream()),
+                    "walk_elements_packed")
+        return se, sl, off, st
+
+
 class XDG:
     """The XDG facade (src/xdg.cpp) over a model and the CUDA ray tracer."""
 
