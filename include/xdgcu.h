@@ -221,6 +221,32 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* ctx, int64_t n, const int32_t* start_i
                                double* seg_len, int64_t* offsets, int32_t* status,
                                int32_t precision, void* stream);
 
+/* Largest batch of xdgcu_walk_elements_packed_noalloc. */
+#define XDGCU_NOALLOC_MAX_TRACKS 4194304
+
+/* xdgcu_walk_elements_packed for callers that cannot let the library
+ * allocate device memory -- e.g. a transport code or framework whose own
+ * allocator owns the device memory (a caching pool that reserves the free
+ * memory at start-up, where a foreign cudaMalloc fails or fragments it), or a
+ * particle loop that must stay out of the allocator once set up.  This entry
+ * point has no counterpart in the reference.  Same arguments and results as
+ * xdgcu_walk_elements_packed, with these differences:
+ *   - it calls no cudaMalloc/cudaFree/cudaMallocAsync or other allocating
+ *     routine: the scan scratch is a static device array of 32 KiB in the
+ *     library, which every GPU that loads the library holds until exit;
+ *   - n must not exceed XDGCU_NOALLOC_MAX_TRACKS (else XDGCU_ERR_INVALID_ARG);
+ *   - all array arguments must be device (or managed) memory;
+ *   - the first call on a device looks up the static array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture;
+ *   - all calls share the static array, so calls whose work overlaps on the
+ *     GPU (other streams or host threads) race and must be serialised. */
+int xdgcu_walk_elements_packed_noalloc(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
+                                       const double* start, const double* u,
+                                       const double* distance, int32_t max_segs,
+                                       int64_t capacity, int32_t* seg_elem, double* seg_len,
+                                       int64_t* offsets, int32_t* status, int32_t precision,
+                                       void* stream);
+
 /* ------------------------------------------------------------------------
  * Diagnostics
  * ------------------------------------------------------------------------ */

@@ -52,6 +52,8 @@ SIGNATURES = {
                                    _i32, _VP]),
     "xdgcu_walk_elements_packed": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _i64, _VP, _VP,
                                           _VP, _VP, _i32, _VP]),
+    "xdgcu_walk_elements_packed_noalloc": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _i64,
+                                                  _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_set_tuning": (_int, [_VP, ctypes.c_char_p, _i64]),
     "xdgcu_get_tuning": (_int, [_VP, ctypes.c_char_p, _I64]),
     "xdgcu_set_counting": (_int, [_VP, _i32]),

@@ -536,6 +536,27 @@ int begin_query(xdgcu_ctx* c, cudaStream_t st, unsigned long long** counters) {
 
 }  // namespace
 
+// Helpers for the allocation-free walk entry point (noalloc.cu).
+namespace xdgcu {
+
+int set_last_error(int code, const char* msg) { return set_err(code, msg); }
+
+const char* walk_args_for(const xdgcu_ctx* c, WalkArgs* a, int* face_order, int* device) {
+  if (!c->has_tets) return "no tet mesh set";
+  a->xyz = c->d_xyz.p;
+  a->xyz32 = c->d_xyz32.p;
+  a->conn = c->d_conn.p;
+  a->adj = c->d_adj.p;
+  a->elem_ids = c->d_elem_ids.p;
+  a->n_tets = (int32_t)c->n_tet;
+  std::memcpy(a->face, c->face, sizeof(a->face));
+  *face_order = c->face_order;
+  *device = c->device;
+  return nullptr;
+}
+
+}  // namespace xdgcu
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
