@@ -55,6 +55,11 @@ BYTES_TRI64 = 76            # 72 B FP64 triangle + 4 B id (escalations)
 BYTES_IO = 68               # 48 B origin/dir + 4 B tree id in, 8 B t + 4 B surface + 4 B face out
 
 
+def set_sizes(rays, tracks):
+    global N_RAYS, N_TRACKS
+    N_RAYS, N_TRACKS = int(rays), int(tracks)
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -320,7 +325,7 @@ def run_engine(args, rank, world, local):
         cores = os.cpu_count() or 1
         t1 = time.perf_counter()
         otrees = {v: xo.volume_tree(model, v) for v in model.volumes}
-        sample = np.arange(0, N_RAYS, N_RAYS // 100_000)
+        sample = np.arange(0, N_RAYS, max(1, N_RAYS // 100_000))
         th, sh = t_mixed.cpu().numpy(), s_mixed.cpu().numpy()
         mism = 0
         for v in model.volumes:
@@ -450,7 +455,7 @@ def run_engine(args, rank, world, local):
         "dtype": "f32+f64",
         "data": "synthetic",
         "config": {
-            "workload": WORKLOAD,
+            "workload": WORKLOAD if N_RAYS == 10_000_000 else f"{WORKLOAD}_profile_case_{N_RAYS}",
             "rays_per_gpu": N_RAYS,
             "triangles": int(sum(len(s.face_ids) for s in model.surfaces)),
             "volumes": len(model.volumes),
@@ -493,7 +498,7 @@ def run_engine(args, rank, world, local):
             "frac": achieved / peak,
             "traffic": traffic,
             "peak_kind": f"{peak_kind} HBM copy bandwidth",
-            "kernel": "k_surface<RAY_FIRE, mixed>",
+            "kernel": "k_trace<RAY_FIRE, mixed, 3>",
             "algorithmic_bytes_per_ray": bytes_per_ray,
         },
         "cpu_baseline": cpu_baseline,
@@ -515,7 +520,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-oracle", action="store_true")
+    ap.add_argument("--rays", type=int, default=N_RAYS,
+                    help="rays per GPU (smaller values are profiling cases, not the workload)")
+    ap.add_argument("--tracks", type=int, default=N_TRACKS, help="walk tracks per GPU")
     args = ap.parse_args()
+    set_sizes(args.rays, args.tracks)
     args.warmup = max(3, args.warmup)
     rank, world, local = dist.env_rank()
     if world > 1:
