@@ -47,6 +47,8 @@ N_TRACKS = 1_000_000
 MAX_SEGS = 512
 WORKLOAD = "nested_spheres_8x_icosphere_L6_jitter1e-3_1e7_rays"
 WALK_WORKLOAD = "tet_cube_50^3x6_kuhn_jitter0.2_1e6_tracks_exp5"
+MANY_SURFACES = 256
+MANY_WORKLOAD = "256_surfaces_sphere_torus_tris_10^U(3,5.7)_rays_10^U(3,6)"
 CPU_SAMPLE = 4_000_000      # rays of the same workload timed on the host cores
 REF_STEP_SAMPLE = 1_000_000  # rays per step of --impl reference
 BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
@@ -231,6 +233,90 @@ def timed(torch, fn, steps, warmup, world, stream):
     dist.barrier(world)
     ms = e0.elapsed_time(e1) / steps
     return dist.max_over_ranks(ms, world)
+
+
+def bench_many_surfaces(torch, L, dev, stream, args, rank, world):
+    """256 closed surfaces (alternating icospheres and tori, each its own
+    volume), ~2.2e7 triangles, 10^U(3,6) rays per surface from interior
+    points: ray_fire of every ray in its own volume as (a) one launch with a
+    tree id per ray, (b) one launch per volume, (c) the launches of (b)
+    captured once in a CUDA graph and replayed."""
+    from xdg_gb300 import _lib
+    from xdg_gb300.engine import EXITING, MIXED, XDG
+
+    t0 = time.perf_counter()
+    model, shapes = synth.many_surfaces(MANY_SURFACES, seed=5)
+    rng = np.random.default_rng(dist.rank_seed(77, rank))
+    o_h, d_h, vol_h, off = synth.many_surface_rays(shapes, rng)
+    x = XDG(model, device=dev.index)
+    x.prepare_raytracer()
+    rti = x.rti
+    lut = np.zeros(max(model.volumes) + 1, dtype=np.int32)
+    for v, t in x.volume_to_surface_tree.items():
+        lut[v] = t
+    n = len(o_h)
+    o = torch.from_numpy(o_h).to(dev)
+    d = torch.from_numpy(d_h).to(dev)
+    trees = torch.from_numpy(lut[vol_h]).to(dev)
+    vol = torch.from_numpy(vol_h).to(dev)
+    del o_h, d_h
+    t_a = torch.empty(n, dtype=torch.float64, device=dev)
+    s_a = torch.empty(n, dtype=torch.int32, device=dev)
+    f_a = torch.empty(n, dtype=torch.int32, device=dev)
+    t_b, s_b, f_b = torch.empty_like(t_a), torch.empty_like(s_a), torch.empty_like(f_a)
+    log(f"[bench] many-surface setup {time.perf_counter() - t0:.1f}s, {n} rays")
+
+    def one_launch():
+        rc = L.xdgcu_ray_fire(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), n,
+                              ctypes.c_void_p(o.data_ptr()), ctypes.c_void_p(d.data_ptr()), None,
+                              EXITING, None, None, ctypes.c_void_p(t_a.data_ptr()),
+                              ctypes.c_void_p(s_a.data_ptr()), ctypes.c_void_p(f_a.data_ptr()),
+                              None, MIXED, ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+        _lib.check(rc, rti.ctx, "ray_fire")
+
+    def per_volume():
+        sp = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+        for k in range(len(off) - 1):
+            a, b = int(off[k]), int(off[k + 1])
+            rc = L.xdgcu_ray_fire(rti.ctx, int(lut[k + 1]), None, b - a,
+                                  ctypes.c_void_p(o.data_ptr() + 24 * a),
+                                  ctypes.c_void_p(d.data_ptr() + 24 * a), None, EXITING, None, None,
+                                  ctypes.c_void_p(t_b.data_ptr() + 8 * a),
+                                  ctypes.c_void_p(s_b.data_ptr() + 4 * a),
+                                  ctypes.c_void_p(f_b.data_ptr() + 4 * a), None, MIXED, sp)
+            _lib.check(rc, rti.ctx, "ray_fire")
+
+    steps = max(3, args.steps // 4)
+    ms_one = timed(torch, one_launch, steps, args.warmup, world, stream)
+    ms_per = timed(torch, per_volume, steps, args.warmup, world, stream)
+    same_per = bool(torch.equal(t_a, t_b) and torch.equal(s_a, s_b) and torch.equal(f_a, f_b))
+    s_b.fill_(-7)
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(stream)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+            per_volume()
+    torch.cuda.synchronize()
+    ms_graph = timed(torch, g.replay, steps, args.warmup, world, stream)
+    same_graph = bool(torch.equal(s_a, s_b) and torch.equal(t_a, t_b))
+    own = bool(torch.equal(s_a, vol))
+    total = dist.sum_over_ranks(n, world)
+    return {
+        "workload": MANY_WORKLOAD,
+        "surfaces": MANY_SURFACES,
+        "triangles": int(sum(len(s.face_ids) for s in model.surfaces)),
+        "rays": n,
+        "unit": "Mrays/s",
+        "one_launch": total / (ms_one / 1e3) / 1e6,
+        "per_volume_launches": total / (ms_per / 1e3) / 1e6,
+        "per_volume_graph": total / (ms_graph / 1e3) / 1e6,
+        "ms_one_launch": ms_one, "ms_per_volume": ms_per, "ms_graph": ms_graph,
+        "all_rays_exit_own_surface": own,
+        "per_volume_equals_one_launch": same_per,
+        "graph_equals_one_launch": same_graph,
+        "precision": "mixed",
+    }
 
 
 def run_engine(args, rank, world, local):
@@ -429,6 +515,9 @@ def run_engine(args, rank, world, local):
     walk_len_mism = int(((seg_l64 != seg_l) & valid).sum().item())
     del seg_e64, seg_l64
 
+    # ---- many surfaces: one launch vs one launch per volume vs CUDA graph -----
+    many = bench_many_surfaces(torch, L, dev, stream, args, rank, world) if args.many else None
+
     # ---- report -------------------------------------------------------------
     total_rays = dist.sum_over_ranks(N_RAYS, world)
     total_segs = dist.sum_over_ranks(n_segs, world)
@@ -505,6 +594,7 @@ def run_engine(args, rank, world, local):
         "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "matches_device_path": e2e_ok},
+        "many_surfaces": many,
         "gpu_launches": args.steps,
         "clocks": clk,
     }
@@ -523,6 +613,8 @@ def main():
     ap.add_argument("--rays", type=int, default=N_RAYS,
                     help="rays per GPU (smaller values are profiling cases, not the workload)")
     ap.add_argument("--tracks", type=int, default=N_TRACKS, help="walk tracks per GPU")
+    ap.add_argument("--no-many", dest="many", action="store_false",
+                    help="skip the 256-surface launch comparison")
     args = ap.parse_args()
     set_sizes(args.rays, args.tracks)
     args.warmup = max(3, args.warmup)

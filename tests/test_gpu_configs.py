@@ -1,0 +1,191 @@
+"""The benchmark's other configurations as parity cases, at their full sizes
+where the oracle finishes in seconds:
+
+* single sphere in a box (5,120 + 12 triangles, 1e5 rays; the ray-benchmark
+  tool's own sampler and the isotropic variant),
+* the degenerate-hit stress (level-6 icosphere, 1e6 rays aimed at vertices,
+  edge midpoints and centroids): zero lost hits, bit-exact against the
+  oracle, and the re-fire with the hit face excluded agrees as well,
+* many surfaces (scaled: 32 alternating spheres / tori, each its own
+  volume): one launch with per-ray trees, one launch per volume, and the
+  per-volume launches replayed from a CUDA graph all agree with the oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from xdg_gb300 import synth
+from xdg_gb300.engine import EXITING, FP64, ID_NONE, MIXED, XDG
+
+pytestmark = pytest.mark.gpu
+
+PRECISIONS = [FP64, MIXED]
+CORES = os.cpu_count() or 1
+
+
+def assert_same(a, b, what):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    bad = np.nonzero(a != b)[0]
+    assert len(bad) == 0, f"{what}: {len(bad)} mismatches, first at {bad[:5]}"
+
+
+@pytest.fixture(scope="module")
+def sphere_box():
+    m = synth.single_sphere_in_box(level=4, radius=10.0, half_width=20.0)
+    x = XDG(m)
+    x.prepare_raytracer()
+    return m, x
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("sampler", ["isotropic", "ray_benchmark"])
+def test_sphere_in_box_full_size(cuda, oracle, sphere_box, prec, sampler):
+    """1e5 rays from the ball r <= 9.9, seed 12345, ray_fire(volume 1, EXITING)."""
+    m, x = sphere_box
+    n = 100_000
+    if sampler == "isotropic":
+        o, d = synth.lcg_ball_rays(n, 9.9, seed=12345)
+    else:
+        o, d = synth.lcg_benchmark_rays(n, (0.0, 0.0, 0.0), 9.9, seed=12345)
+    t, s, f = x.ray_fire(1, o, d, orientation=EXITING, precision=prec)
+    ot, os_, of = oracle.volume_tree(m, 1).ray_fire(o, d, threads=CORES)
+    assert (s == 1).all()
+    assert_same(s, os_, "surface")
+    assert_same(f, of, "face")
+    assert_same(t, ot, "t")
+
+
+@pytest.fixture(scope="module")
+def stress_model():
+    v, tri = synth.icosphere(6, 5.0)
+    s = synth.Surface(1, v, tri, np.arange(len(tri), dtype=np.int32), 1, 2)
+    m = synth.Model(surfaces=[s], volumes=[1, 2], implicit_complement=2)
+    x = XDG(m)
+    x.prepare_raytracer()
+    # origins strictly inside the triangulation (its inscribed radius is
+    # 4.9997 for radius 5 at level 6)
+    o, d, kind = synth.watertight_rays(v, tri, 1_000_000, 4.99, seed=4)
+    return m, x, o, d, kind
+
+
+def test_degenerate_hits_full_size(cuda, oracle, stress_model):
+    m, x, o, d, kind = stress_model
+    res = {p: x.ray_fire(1, o, d, precision=p) for p in PRECISIONS}
+    for p in PRECISIONS:
+        t, s, f = res[p]
+        lost = np.nonzero(s != 1)[0]
+        assert len(lost) == 0, f"{len(lost)} lost hits (precision {p}), kinds {np.bincount(kind[lost])}"
+    assert_same(res[MIXED][0], res[FP64][0], "t mixed vs fp64")
+    assert_same(res[MIXED][2], res[FP64][2], "face mixed vs fp64")
+    ot, os_, of = oracle.volume_tree(m, 1).ray_fire(o, d, threads=CORES)
+    assert_same(res[MIXED][2], of, "face vs oracle")
+    assert_same(res[MIXED][0], ot, "t vs oracle")
+
+
+def test_degenerate_refire_with_exclusion(cuda, oracle, stress_model):
+    """Re-fire from the hit point with the hit face excluded (the reference's
+    surface-crossing step).  Near an edge or vertex the rounded hit point puts
+    the new line through a neighbouring face, which the reference's
+    semantics then report as a second hit at t ~ 0 (about 0.6 % of these
+    feature-aimed rays); the engine must report exactly what the oracle
+    reports, doubled hits included."""
+    m, x, o, d, kind = stress_model
+    n = 200_000
+    o, d = o[:n], d[:n]
+    t, s, f = x.ray_fire(1, o, d, precision=MIXED)
+    p = o + d * t[:, None]
+    excl = [[int(ff)] for ff in f]
+    ot = oracle.volume_tree(m, 1)
+    for prec in PRECISIONS:
+        t2, s2, f2 = x.ray_fire(1, p, d, exclude=excl, precision=prec)
+        ot2, os2, of2 = ot.ray_fire(p, d, excl=excl, threads=CORES)
+        assert_same(s2, os2, "surface")
+        assert_same(f2, of2, "face")
+        assert_same(t2, ot2, "t")
+    doubled = (s2 != ID_NONE) & (t2 < 1e-6)
+    odoubled = (os2 != ID_NONE) & (ot2 < 1e-6)
+    assert np.array_equal(doubled, odoubled)
+    # a doubled hit is on another face than the excluded one
+    assert (f2[doubled] != f[doubled]).all()
+
+
+@pytest.fixture(scope="module")
+def many():
+    m, shapes = synth.many_surfaces(32, seed=5, tri_range=(1e3, 3e4))
+    rng = np.random.default_rng(6)
+    o, d, vol, off = synth.many_surface_rays(shapes, rng, ray_range=(1e2, 1e4))
+    x = XDG(m)
+    x.prepare_raytracer()
+    return m, x, o, d, vol, off
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_many_surfaces_one_launch(cuda, oracle, many, prec):
+    m, x, o, d, vol, off = many
+    inside = x.point_in_volume(vol, o, precision=prec)
+    assert inside.all(), f"{(~inside.astype(bool)).sum()} origins outside their volume"
+    t, s, f = x.ray_fire(vol, o, d, precision=prec)
+    assert_same(s, vol, "every ray exits through its own surface")
+    for k in range(len(off) - 1):
+        sl = slice(off[k], off[k + 1])
+        ot, os_, of = oracle.volume_tree(m, k + 1).ray_fire(o[sl], d[sl], threads=CORES)
+        assert_same(s[sl], os_, f"surface vol {k + 1}")
+        assert_same(f[sl], of, f"face vol {k + 1}")
+        assert_same(t[sl], ot, f"t vol {k + 1}")
+
+
+def test_many_surfaces_per_volume_launches_and_graph(cuda, many):
+    """One launch per volume, eagerly and replayed from a CUDA graph, gives
+    the results of the single per-ray-tree launch."""
+    torch = cuda
+    m, x, o, d, vol, off = many
+    dev = torch.device("cuda", 0)
+    og = torch.from_numpy(o).to(dev)
+    dg = torch.from_numpy(d).to(dev)
+    vg = torch.from_numpy(vol).to(dev)
+    trees = torch.from_numpy(np.asarray([x.volume_to_surface_tree[int(v)] for v in vol],
+                                        dtype=np.int32)).to(dev)
+    rti = x.rti
+    t1, s1, f1 = rti.ray_fire(None, og, dg, ray_trees=trees)
+    n = og.shape[0]
+    t2 = torch.empty(n, dtype=torch.float64, device=dev)
+    s2 = torch.empty(n, dtype=torch.int32, device=dev)
+    f2 = torch.empty(n, dtype=torch.int32, device=dev)
+    import ctypes
+    from xdg_gb300 import _lib
+    L = _lib.load()
+
+    def per_volume(stream):
+        for k in range(len(off) - 1):
+            a, b = int(off[k]), int(off[k + 1])
+            tree = x.volume_to_surface_tree[k + 1]
+            rc = L.xdgcu_ray_fire(rti.ctx, tree, None, b - a,
+                                  ctypes.c_void_p(og[a:].data_ptr()),
+                                  ctypes.c_void_p(dg[a:].data_ptr()), None, EXITING, None, None,
+                                  ctypes.c_void_p(t2[a:].data_ptr()),
+                                  ctypes.c_void_p(s2[a:].data_ptr()),
+                                  ctypes.c_void_p(f2[a:].data_ptr()), None, MIXED,
+                                  ctypes.c_void_p(stream.cuda_stream))
+            _lib.check(rc, rti.ctx, "ray_fire")
+
+    per_volume(torch.cuda.current_stream(dev))
+    torch.cuda.synchronize()
+    for a, b, what in ((t1, t2, "t"), (s1, s2, "surface"), (f1, f2, "face")):
+        assert torch.equal(a, b), what
+    assert torch.equal(s1, vg)
+    # the same launches captured once and replayed
+    t2.zero_()
+    s2.fill_(-7)
+    f2.fill_(-7)
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+            per_volume(side)
+    g.replay()
+    torch.cuda.synchronize()
+    for a, b, what in ((t1, t2, "t"), (s1, s2, "surface"), (f1, f2, "face")):
+        assert torch.equal(a, b), f"graph replay: {what}"

@@ -421,9 +421,25 @@ class XDG:
         self.rti.init()
 
     def _trees(self, volumes):
-        v = np.asarray(volumes)
-        return np.array([self.volume_to_surface_tree[int(x)] for x in v.reshape(-1)],
-                        dtype=np.int32)
+        """Surface tree of each ray's volume (NumPy, or a torch tensor on the
+        volumes' device)."""
+        lut = np.full(max(self.volume_to_surface_tree) + 1, TREE_NONE, dtype=np.int32)
+        for v, t in self.volume_to_surface_tree.items():
+            lut[v] = t
+        if _is_torch(volumes):
+            import torch
+            vt = volumes.reshape(-1).long()
+            if len(vt) and (int(vt.min()) < 0 or int(vt.max()) >= len(lut)):
+                raise KeyError("volume without a surface tree")
+            out = torch.from_numpy(lut).to(volumes.device)[vt]
+        else:
+            v = np.asarray(volumes).reshape(-1)
+            if len(v) and (v.min() < 0 or v.max() >= len(lut)):
+                raise KeyError("volume without a surface tree")
+            out = lut[v]
+        if len(out) and int((out == TREE_NONE).sum()) > 0:
+            raise KeyError("volume without a surface tree")
+        return out
 
     def ray_fire(self, volume, origins, dirs, dist_limit=None, orientation=EXITING, exclude=None,
                  precision=MIXED):

@@ -429,3 +429,126 @@ def normalize_rows(v: np.ndarray) -> np.ndarray:
     ln = np.sqrt(v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2])
     ln = np.where(ln < min_rcp, min_rcp, ln)
     return np.ascontiguousarray(v / ln[:, None])
+
+
+# --------------------------------------------------------------------------
+# Degenerate-hit rays (watertightness stress) and many-surface models
+# --------------------------------------------------------------------------
+
+def watertight_rays(vertices: np.ndarray, triangles: np.ndarray, n: int, radius: float,
+                    seed: int = 4):
+    """Rays from origins uniform in a ball of ``radius`` aimed at triangle
+    features: 40 % at a random vertex, 40 % at a random edge midpoint, 20 % at
+    a centroid, each target moved by an isotropic jitter of length
+    10^U(-12, -6).  Returns (origins, unit directions, kind) with kind 0 =
+    vertex, 1 = edge, 2 = centroid."""
+    rng = np.random.default_rng(seed)
+    o = lcg_ball_rays(n, radius, seed=seed)[0]
+    u = rng.uniform(0.0, 1.0, n)
+    ti = rng.integers(0, len(triangles), n)
+    corners = vertices[triangles[ti]]
+    target = corners.mean(1)
+    kind = np.full(n, 2, dtype=np.int8)
+    vi = u < 0.4
+    kind[vi] = 0
+    target[vi] = corners[vi, rng.integers(0, 3, vi.sum())]
+    ei = (u >= 0.4) & (u < 0.8)
+    kind[ei] = 1
+    a = rng.integers(0, 3, ei.sum())
+    target[ei] = 0.5 * (corners[ei, a] + corners[ei, (a + 1) % 3])
+    jit = 10.0 ** rng.uniform(-12.0, -6.0, n)
+    target += isotropic_dirs(rng, n) * jit[:, None]
+    return np.ascontiguousarray(o), normalize_rows(target - o), kind
+
+
+@dataclass
+class Shape:
+    """Analytic description of a closed surface, for interior sampling."""
+    kind: str                 # "sphere" or "torus"
+    center: np.ndarray
+    inner: float              # sphere: inscribed radius; torus: inscribed tube radius
+    major: float = 0.0        # torus centre-line radius
+
+
+def _sphere_inscribed(v: np.ndarray, f: np.ndarray, center: np.ndarray) -> float:
+    p0, p1, p2 = v[f[:, 0]], v[f[:, 1]], v[f[:, 2]]
+    n = np.cross(p1 - p0, p2 - p0)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    return float(np.abs(((p0 - center) * n).sum(1)).min())
+
+
+def many_surfaces(n: int = 256, seed: int = 5, tri_range=(1e3, 5e5), spacing: float = 4.0):
+    """``n`` closed surfaces on a grid, alternating icosphere / torus, each the
+    forward boundary of its own volume (surface k+1 bounds volume k+1); volume
+    n+1 is the implicit complement around all of them.
+
+    Triangle counts are 10^U(log10 lo, log10 hi): spheres take the nearest
+    subdivision level (20*4^L triangles), tori an n_major x n_minor grid with
+    R/r ~ U[2, 5].  Returns (model, shapes) with one ``Shape`` per surface.
+    """
+    rng = np.random.default_rng(seed)
+    g = int(np.ceil(n ** (1.0 / 3.0) - 1e-9))
+    m = Model()
+    shapes = []
+    base = 0
+    lo, hi = np.log10(tri_range[0]), np.log10(tri_range[1])
+    for k in range(n):
+        cell = np.array([k % g, (k // g) % g, k // (g * g)], dtype=np.float64)
+        c = spacing * (cell + 0.5)
+        target = 10.0 ** rng.uniform(lo, hi)
+        if k % 2 == 0:
+            level = int(np.clip(np.round(np.log(target / 20.0) / np.log(4.0)), 1, 7))
+            v, f = icosphere(level, 0.4 * spacing, c)
+            shapes.append(Shape("sphere", c, _sphere_inscribed(v, f, c)))
+        else:
+            a = rng.uniform(2.0, 5.0)
+            minor = 0.45 * spacing / (a + 1.0)
+            major = a * minor
+            n_minor = max(6, int(round(np.sqrt(target / (2.0 * a)))))
+            n_major = max(12, int(round(a * n_minor)))
+            v, f = torus(major, minor, n_major, n_minor, c)
+            sag = ((major + minor) * (1.0 - np.cos(np.pi / n_major))
+                   + minor * (1.0 - np.cos(np.pi / n_minor)))
+            shapes.append(Shape("torus", c, minor - 1.5 * sag, major))
+        ids = np.arange(base, base + len(f), dtype=np.int32)
+        base += len(f)
+        m.surfaces.append(Surface(k + 1, v, f, ids, k + 1, n + 1))
+    m.volumes = list(range(1, n + 2))
+    m.implicit_complement = n + 1
+    return m, shapes
+
+
+def interior_points(shape: Shape, count: int, rng: np.random.Generator, margin: float = 0.98):
+    """``count`` points uniform inside the shape's inscribed solid, shrunk by
+    ``margin`` (so they are strictly inside the triangulated surface)."""
+    if shape.kind == "sphere":
+        r = margin * shape.inner * np.cbrt(rng.uniform(0.0, 1.0, count))
+        return shape.center + isotropic_dirs(rng, count) * r[:, None]
+    tube = margin * shape.inner
+    out = np.empty((0, 3))
+    while len(out) < count:
+        k = 2 * (count - len(out)) + 16
+        s = tube * np.sqrt(rng.uniform(0.0, 1.0, k))
+        ph = rng.uniform(0.0, 2.0 * np.pi, k)
+        th = rng.uniform(0.0, 2.0 * np.pi, k)
+        keep = rng.uniform(0.0, 1.0, k) * (shape.major + tube) < shape.major + s * np.cos(ph)
+        rad = shape.major + s * np.cos(ph)
+        p = np.stack([rad * np.cos(th), rad * np.sin(th), s * np.sin(ph)], 1)[keep]
+        out = np.concatenate([out, p])
+    return shape.center + out[:count]
+
+
+def many_surface_rays(shapes, rng: np.random.Generator, ray_range=(1e3, 1e6)):
+    """Per surface 10^U(log10 lo, log10 hi) rays from uniform interior origins
+    with isotropic directions, grouped by volume.  Returns (origins, dirs,
+    volume of each ray, offsets) with the rays of surface k at
+    offsets[k]:offsets[k+1] and volume k+1."""
+    lo, hi = np.log10(ray_range[0]), np.log10(ray_range[1])
+    counts = np.round(10.0 ** rng.uniform(lo, hi, len(shapes))).astype(np.int64)
+    offsets = np.concatenate([[0], np.cumsum(counts)])
+    o = np.empty((offsets[-1], 3))
+    for k, sh in enumerate(shapes):
+        o[offsets[k]:offsets[k + 1]] = interior_points(sh, int(counts[k]), rng)
+    d = isotropic_dirs(rng, int(offsets[-1]))
+    vol = np.repeat(np.arange(1, len(shapes) + 1, dtype=np.int32), counts)
+    return np.ascontiguousarray(o), d, vol, offsets
