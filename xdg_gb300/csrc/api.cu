@@ -63,11 +63,29 @@ struct TreeHost {
   }
 };
 
+// Per-host-thread staging state for calls with host arrays: a device
+// workspace, the compute stream, two copy streams and chunk events, so that
+// host->device copies, kernels and device->host copies of consecutive chunks
+// overlap.
 struct Slot {
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;    // compute
+  cudaStream_t copy_in = nullptr;
+  cudaStream_t copy_out = nullptr;
+  std::vector<cudaEvent_t> ev;
   DevMem<char> buf;
   ~Slot() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
+    if (copy_in) cudaStreamDestroy(copy_in);
+    if (copy_out) cudaStreamDestroy(copy_out);
+  }
+  bool events(size_t k) {
+    while (ev.size() < k) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+      ev.push_back(e);
+    }
+    return true;
   }
 };
 
@@ -482,7 +500,9 @@ Slot* get_slot(xdgcu_ctx* c) {
   auto& s = c->slots[std::this_thread::get_id()];
   if (!s) {
     s.reset(new Slot());
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->copy_out, cudaStreamNonBlocking) != cudaSuccess) {
       s.reset();
       return nullptr;
     }
@@ -505,6 +525,87 @@ int stage_in(Slot* s, std::vector<Arr*> arrs, cudaStream_t st) {
     if (a->host_in)
       API_CUDA(cudaMemcpyAsync(a->dev, a->host_in, a->bytes, cudaMemcpyHostToDevice, st), "H2D");
   }
+  return XDGCU_OK;
+}
+
+// A per-ray array of a host call: `per_ray` bytes for each of the n rays.
+struct RayArr {
+  const void* host_in = nullptr;
+  void* host_out = nullptr;
+  size_t per_ray = 0;
+  char* dev = nullptr;
+};
+
+constexpr int64_t kChunkRays = 1 << 20;
+constexpr int64_t kMaxChunks = 16;
+
+// Runs a per-ray query over host arrays in chunks: the inputs of chunk k+1
+// are copied in while chunk k computes and chunk k-1 is copied out.  `whole`
+// arrays (exclusion lists) are copied once before the first chunk.
+// launch(first, count, stream) enqueues the kernel for rays [first,
+// first+count) with the device pointers of the RayArr entries offset by
+// `first`.  Returns when all results are in host memory.
+int begin_query(xdgcu_ctx* c, cudaStream_t st, unsigned long long** counters);
+
+template <typename Launch>
+int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<Arr*> whole,
+               std::vector<RayArr*> rays, unsigned long long** counters, Launch launch) {
+  size_t total = 0;
+  for (Arr* a : whole) total += (a->bytes + 255) & ~(size_t)255;
+  for (RayArr* r : rays) total += (r->per_ray * (size_t)n + 255) & ~(size_t)255;
+  if ((int64_t)total > s->buf.n)
+    API_CUDA(s->buf.alloc((int64_t)std::max<size_t>(total, 1 << 20)), "workspace");
+  size_t off = 0;
+  for (Arr* a : whole) {
+    if (a->bytes == 0) continue;
+    a->dev = s->buf.p + off;
+    off += (a->bytes + 255) & ~(size_t)255;
+  }
+  for (RayArr* r : rays) {
+    if (r->per_ray == 0) continue;
+    r->dev = s->buf.p + off;
+    off += (r->per_ray * (size_t)n + 255) & ~(size_t)255;
+  }
+  const int64_t chunks =
+      n <= 2 * kChunkRays ? 1 : std::min<int64_t>(kMaxChunks, (n + kChunkRays - 1) / kChunkRays);
+  const int64_t per = (n + chunks - 1) / chunks;
+  if (!s->events((size_t)(2 * chunks + 1))) return set_err(XDGCU_ERR_CUDA, "event creation");
+  // order after the caller's stream (if any)
+  if (user) {
+    API_CUDA(cudaEventRecord(s->ev[2 * chunks], user), "event");
+    API_CUDA(cudaStreamWaitEvent(s->copy_in, s->ev[2 * chunks], 0), "event wait");
+  }
+  for (Arr* a : whole)
+    if (a->host_in && a->bytes)
+      API_CUDA(cudaMemcpyAsync(a->dev, a->host_in, a->bytes, cudaMemcpyHostToDevice, s->copy_in),
+               "H2D");
+  int rc = begin_query(c, s->stream, counters);
+  if (rc) return rc;
+  for (int64_t k = 0; k < chunks; ++k) {
+    const int64_t first = k * per;
+    const int64_t cnt = std::min<int64_t>(per, n - first);
+    if (cnt <= 0) break;
+    for (RayArr* r : rays)
+      if (r->host_in && r->per_ray)
+        API_CUDA(cudaMemcpyAsync(r->dev + r->per_ray * first,
+                                 (const char*)r->host_in + r->per_ray * first, r->per_ray * cnt,
+                                 cudaMemcpyHostToDevice, s->copy_in),
+                 "H2D");
+    API_CUDA(cudaEventRecord(s->ev[2 * k], s->copy_in), "event");
+    API_CUDA(cudaStreamWaitEvent(s->stream, s->ev[2 * k], 0), "event wait");
+    API_CUDA(launch(first, cnt, s->stream), "query launch");
+    API_CUDA(cudaEventRecord(s->ev[2 * k + 1], s->stream), "event");
+    API_CUDA(cudaStreamWaitEvent(s->copy_out, s->ev[2 * k + 1], 0), "event wait");
+    for (RayArr* r : rays)
+      if (r->host_out && r->per_ray)
+        API_CUDA(cudaMemcpyAsync((char*)r->host_out + r->per_ray * first,
+                                 r->dev + r->per_ray * first, r->per_ray * cnt,
+                                 cudaMemcpyDeviceToHost, s->copy_out),
+                 "D2H");
+  }
+  API_CUDA(cudaStreamSynchronize(s->copy_out), "sync");
+  API_CUDA(cudaStreamSynchronize(s->stream), "sync");
+  API_CUDA(cudaStreamSynchronize(s->copy_in), "sync");
   return XDGCU_OK;
 }
 
@@ -931,43 +1032,44 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   }
   Slot* s = get_slot(c);
   if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
-  if (!st) st = s->stream;
-  const size_t n3 = sizeof(double) * 3 * (size_t)n;
   int64_t n_excl = 0;
   if (excl_off) n_excl = excl_off[n];
   if (n_excl < 0) return set_err(XDGCU_ERR_INVALID_ARG, "bad exclusion offsets");
-  Arr A_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) * n : 0};
-  Arr A_org{org, nullptr, n3}, A_dir{dir, nullptr, dir ? n3 : 0};
-  Arr A_tmax{tmax, nullptr, tmax ? sizeof(double) * n : 0};
   Arr A_eo{excl_off, nullptr, excl_off ? sizeof(int32_t) * (n + 1) : 0};
   Arr A_ei{excl_ids, nullptr, excl_ids ? sizeof(int32_t) * std::max<int64_t>(1, n_excl) : 0};
-  Arr A_t{nullptr, t_out, t_out ? sizeof(double) * n : 0};
-  Arr A_s{nullptr, surf_out, surf_out ? sizeof(int32_t) * n : 0};
-  Arr A_f{nullptr, face_out, face_out ? sizeof(int32_t) * n : 0};
-  Arr A_fl{nullptr, flag_out, flag_out ? sizeof(int32_t) * n : 0};
-  Arr A_d{nullptr, dist_out, dist_out ? sizeof(double) * n : 0};
-  Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
   if (excl_off && n_excl == 0) A_ei.host_in = nullptr;
-  std::vector<Arr*> all = {&A_trees, &A_org, &A_dir, &A_tmax, &A_eo, &A_ei,
-                           &A_t, &A_s, &A_f, &A_fl, &A_d, &A_st};
-  int rc = stage_in(s, all, st);
-  if (rc) return rc;
-  a.ray_trees = (const int32_t*)A_trees.dev;
-  a.org = (const double*)A_org.dev;
-  a.dir = (const double*)A_dir.dev;
-  a.tmax = (const double*)A_tmax.dev;
-  a.excl_off = (const int32_t*)A_eo.dev;
-  a.excl_ids = (const int32_t*)A_ei.dev;
-  a.t_out = (double*)A_t.dev;
-  a.surf_out = (int32_t*)A_s.dev;
-  a.face_out = (int32_t*)A_f.dev;
-  a.flag_out = (int32_t*)A_fl.dev;
-  a.dist_out = (double*)A_d.dev;
-  a.status = (int32_t*)A_st.dev;
-  rc = begin_query(c, st, &a.counters);
-  if (rc) return rc;
-  API_CUDA(launch_surface_query(mode, precision == XDGCU_MIXED, a, st), "query launch");
-  return stage_out(all, st);
+  RayArr R_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) : 0};
+  RayArr R_org{org, nullptr, sizeof(double) * 3}, R_dir{dir, nullptr, dir ? sizeof(double) * 3 : 0};
+  RayArr R_tmax{tmax, nullptr, tmax ? sizeof(double) : 0};
+  RayArr R_t{nullptr, t_out, t_out ? sizeof(double) : 0};
+  RayArr R_s{nullptr, surf_out, surf_out ? sizeof(int32_t) : 0};
+  RayArr R_f{nullptr, face_out, face_out ? sizeof(int32_t) : 0};
+  RayArr R_fl{nullptr, flag_out, flag_out ? sizeof(int32_t) : 0};
+  RayArr R_d{nullptr, dist_out, dist_out ? sizeof(double) : 0};
+  RayArr R_st{nullptr, status, status ? sizeof(int32_t) : 0};
+  auto at = [](const RayArr& r, int64_t first) -> char* {
+    return r.dev ? r.dev + r.per_ray * first : nullptr;
+  };
+  return run_staged(
+      c, s, st, n, {&A_eo, &A_ei},
+      {&R_trees, &R_org, &R_dir, &R_tmax, &R_t, &R_s, &R_f, &R_fl, &R_d, &R_st}, &a.counters,
+      [&](int64_t first, int64_t cnt, cudaStream_t cs) {
+        SurfArgs b = a;
+        b.n = cnt;
+        b.ray_trees = (const int32_t*)at(R_trees, first);
+        b.org = (const double*)at(R_org, first);
+        b.dir = (const double*)at(R_dir, first);
+        b.tmax = (const double*)at(R_tmax, first);
+        b.excl_off = A_eo.dev ? (const int32_t*)A_eo.dev + first : nullptr;
+        b.excl_ids = (const int32_t*)A_ei.dev;
+        b.t_out = (double*)at(R_t, first);
+        b.surf_out = (int32_t*)at(R_s, first);
+        b.face_out = (int32_t*)at(R_f, first);
+        b.flag_out = (int32_t*)at(R_fl, first);
+        b.dist_out = (double*)at(R_d, first);
+        b.status = (int32_t*)at(R_st, first);
+        return launch_surface_query(mode, precision == XDGCU_MIXED, b, cs);
+      });
 }
 
 int xdgcu_ray_fire(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,
@@ -1051,26 +1153,28 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
   }
   Slot* s = get_slot(c);
   if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
-  if (!st) st = s->stream;
-  Arr A_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) * n : 0};
-  Arr A_p{pts, nullptr, sizeof(double) * 3 * n};
-  Arr A_d{nullptr, dist_out, dist_out ? sizeof(double) * n : 0};
-  Arr A_i{nullptr, id_out, id_out ? sizeof(int32_t) * n : 0};
-  Arr A_x{nullptr, index_out, index_out ? sizeof(int32_t) * n : 0};
-  Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
-  std::vector<Arr*> all = {&A_trees, &A_p, &A_d, &A_i, &A_x, &A_st};
-  int rc = stage_in(s, all, st);
-  if (rc) return rc;
-  a.ray_trees = (const int32_t*)A_trees.dev;
-  a.pts = (const double*)A_p.dev;
-  a.dist_out = (double*)A_d.dev;
-  a.id_out = (int32_t*)A_i.dev;
-  a.index_out = (int32_t*)A_x.dev;
-  a.status = (int32_t*)A_st.dev;
-  rc = begin_query(c, st, &a.counters);
-  if (rc) return rc;
-  API_CUDA(launch(), "query launch");
-  return stage_out(all, st);
+  RayArr R_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) : 0};
+  RayArr R_p{pts, nullptr, sizeof(double) * 3};
+  RayArr R_d{nullptr, dist_out, dist_out ? sizeof(double) : 0};
+  RayArr R_i{nullptr, id_out, id_out ? sizeof(int32_t) : 0};
+  RayArr R_x{nullptr, index_out, index_out ? sizeof(int32_t) : 0};
+  RayArr R_st{nullptr, status, status ? sizeof(int32_t) : 0};
+  auto at = [](const RayArr& r, int64_t first) -> char* {
+    return r.dev ? r.dev + r.per_ray * first : nullptr;
+  };
+  return run_staged(c, s, st, n, {}, {&R_trees, &R_p, &R_d, &R_i, &R_x, &R_st}, &a.counters,
+                    [&](int64_t first, int64_t cnt, cudaStream_t cs) {
+                      PointArgs b = a;
+                      b.n = cnt;
+                      b.ray_trees = (const int32_t*)at(R_trees, first);
+                      b.pts = (const double*)at(R_p, first);
+                      b.dist_out = (double*)at(R_d, first);
+                      b.id_out = (int32_t*)at(R_i, first);
+                      b.index_out = (int32_t*)at(R_x, first);
+                      b.status = (int32_t*)at(R_st, first);
+                      return closest ? launch_closest(precision == XDGCU_MIXED, b, cs)
+                                     : launch_find_element(precision == XDGCU_MIXED, b, cs);
+                    });
 }
 
 int xdgcu_closest(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,
