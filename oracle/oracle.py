@@ -391,3 +391,65 @@ def volume_tree(model, vol, use_bvh=True, bumps=None):
         bump = max(bump, bumps[s.surface_id])
     return TriTree(np.concatenate(xs), np.concatenate(fs), np.concatenate(ss),
                    np.concatenate(fl), bump, use_bvh)
+
+
+# --------------------------------------------------------------------------
+# XDG::segments(start, end) (xdg.cpp:142-198), one track at a time
+# --------------------------------------------------------------------------
+
+TINY_BIT = 1e-10  # constants.h:32
+
+
+class GlobalTracker:
+    """The global track loop of xdg.cpp:142-198 over oracle trees: find the
+    element at r in the global element tree (ignoring the element just left),
+    else fire an EXITING ray in the implicit complement from r + u*TINY_BIT,
+    step to the hit plus TINY_BIT and re-enter through
+    get_boundary_face_element of the hit face; walk; repeat while distance
+    remains."""
+
+    def __init__(self, model):
+        tm = model.tets
+        self.model = model
+        self.elem_ids = np.asarray(tm.elem_ids, dtype=np.int32)
+        self.tets = TetTree(tm.tet_xyz(), tm.elem_ids)
+        self.walker = TetWalker(tm.vertices, tm.conn, tm.adj, tm.face_table)
+        self.ipc = volume_tree(model, model.implicit_complement)
+        self.bfe = model.boundary_face_element
+
+    def segments(self, start, end, max_segs=4096, max_rounds=10_000):
+        r = np.array(start, dtype=np.float64)
+        e = np.array(end, dtype=np.float64)
+        u = e - r
+        dist = float(np.sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]))
+        u = u / dist
+        out_e, out_l = [], []
+        rounds = 0
+        while dist > 0 and rounds < max_rounds:
+            rounds += 1
+            eid, eidx = self.tets.find_element(r[None, :], threads=1)
+            cur = int(eidx[0])
+            if out_e and int(eid[0]) == out_e[-1]:
+                cur = -1
+            if cur < 0:
+                o = r + u * TINY_BIT
+                t, s, f = self.ipc.ray_fire(o[None, :], u[None, :], None, EXITING, [[]], threads=1)
+                if s[0] == -1 or t[0] > dist:
+                    break
+                hd = t[0] + TINY_BIT
+                r = r + u * hd
+                dist = dist - hd
+                cur = int(self.bfe[f[0]]) if self.bfe is not None else -1
+                if cur < 0:
+                    break
+            el, ln, cnt, st = self.walker.walk(np.array([cur], dtype=np.int32), r[None, :],
+                                               u[None, :], np.array([dist]), max_segs, threads=1)
+            k = int(cnt[0])
+            ssum = 0.0
+            for j in range(k):
+                out_e.append(int(self.elem_ids[el[0, j]]))
+                out_l.append(float(ln[0, j]))
+                ssum = ssum + float(ln[0, j])
+            r = r + u * ssum
+            dist = dist - ssum
+        return np.array(out_e, dtype=np.int32), np.array(out_l)

@@ -51,6 +51,9 @@ class Model:
     implicit_complement: int = -1
     tets: "TetMesh | None" = None
     elements: dict = field(default_factory=dict)  # volume -> tet indices
+    # MeshManager::get_boundary_face_element: tet index adjacent to each
+    # surface face id (-1 for a face with no element), or None
+    boundary_face_element: "np.ndarray | None" = None
 
     def volume_elements(self, vol):
         """MeshManager::get_volume_elements: tet indices of ``vol`` (or None)."""
@@ -552,3 +555,78 @@ def many_surface_rays(shapes, rng: np.random.Generator, ray_range=(1e3, 1e6)):
     d = isotropic_dirs(rng, int(offsets[-1]))
     vol = np.repeat(np.arange(1, len(shapes) + 1, dtype=np.int32), counts)
     return np.ascontiguousarray(o), d, vol, offsets
+
+
+# --------------------------------------------------------------------------
+# Meshed volumes bounded by their own boundary faces
+# --------------------------------------------------------------------------
+
+def model_from_tets(tm: TetMesh, tet_volume: np.ndarray) -> Model:
+    """A model whose volumes are sets of tets: volume v (ids from
+    ``tet_volume``) is bounded by one surface (id v) made of the boundary
+    faces of its tets -- the faces without a neighbour -- with the outward
+    orientation of the tet face (MOAB faces of a positive tet point out).
+    The implicit complement (id max+1) holds every surface in reverse.
+    ``boundary_face_element`` maps each face id to its tet, as
+    MeshManager::get_boundary_face_element does (moab/direct_access.h:250-281).
+    """
+    tet_volume = np.asarray(tet_volume, dtype=np.int32)
+    vols = sorted(int(v) for v in np.unique(tet_volume))
+    ipc = vols[-1] + 1
+    t_idx, f_idx = np.nonzero(tm.adj < 0)
+    tris = tm.conn[t_idx[:, None], tm.face_table[f_idx]]
+    # keep the outward orientation explicit (normal away from the tet centroid)
+    v = tm.vertices
+    n = np.cross(v[tris[:, 1]] - v[tris[:, 0]], v[tris[:, 2]] - v[tris[:, 0]])
+    out = v[tris].mean(1) - v[tm.conn[t_idx]].mean(1)
+    flip = (n * out).sum(1) < 0
+    tris[flip] = tris[flip][:, [0, 2, 1]]
+    m = Model()
+    bfe = []
+    base = 0
+    for vol in vols:
+        sel = np.nonzero(tet_volume[t_idx] == vol)[0]
+        ids = np.arange(base, base + len(sel), dtype=np.int32)
+        base += len(sel)
+        m.surfaces.append(Surface(vol, v, tris[sel].astype(np.int32), ids, vol, ipc))
+        bfe.append(t_idx[sel])
+    m.volumes = vols + [ipc]
+    m.implicit_complement = ipc
+    m.tets = tm
+    m.elements = {vol: np.nonzero(tet_volume == vol)[0].astype(np.int32) for vol in vols}
+    m.boundary_face_element = np.concatenate(bfe).astype(np.int32)
+    return m
+
+
+def tet_blocks(blocks, jitter=0.2, seed=11) -> Model:
+    """Separate meshed boxes, each its own volume (1, 2, ...), with gaps of
+    implicit complement between them.  ``blocks`` is a list of (origin, n,
+    size): an n^3 x 6 Kuhn-tet cube of edge ``size`` at ``origin``."""
+    verts, conns, vol = [], [], []
+    nv = 0
+    for b, (origin, n, size) in enumerate(blocks):
+        tm = tet_cube(n, size, jitter, seed + b, origin)
+        verts.append(tm.vertices)
+        conns.append(tm.conn + nv)
+        vol.append(np.full(len(tm.conn), b + 1, dtype=np.int32))
+        nv += len(tm.vertices)
+    conn = np.concatenate(conns).astype(np.int32)
+    tm = TetMesh(vertices=np.concatenate(verts), conn=conn,
+                 adj=face_adjacency(conn, MOAB_TET_FACES), face_table=MOAB_TET_FACES.copy(),
+                 elem_ids=np.arange(len(conn), dtype=np.int32))
+    return model_from_tets(tm, np.concatenate(vol))
+
+
+def single_tet(vertices=None) -> Model:
+    """One positively oriented tet as volume 1 (one surface of its four faces);
+    volume 2 is the implicit complement."""
+    v = np.asarray(vertices if vertices is not None else
+                   [[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]],
+                   dtype=np.float64)
+    conn = np.array([[0, 1, 2, 3]], dtype=np.int32)
+    a, b, c, d = v
+    if np.dot(np.cross(b - a, c - a), d - a) < 0:
+        conn = conn[:, [0, 2, 1, 3]]
+    tm = TetMesh(vertices=v, conn=conn, adj=np.full((1, 4), -1, dtype=np.int32),
+                 face_table=MOAB_TET_FACES.copy(), elem_ids=np.zeros(1, dtype=np.int32))
+    return model_from_tets(tm, np.ones(1, dtype=np.int32))
