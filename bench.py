@@ -391,6 +391,34 @@ def run_engine(args, rank, world, local):
     piv_inside_frac = float(piv_out[not_ipc].float().mean().item()) if not_ipc.any() else 1.0
     ms_piv64 = timed(torch, piv(FP64), 3, 1, world, stream)
 
+    # find_volume of the same points: one fused launch vs one launch per volume
+    fv = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+    fv_vols = [v for v in sorted(x.volume_to_surface_tree) if v != ipc]
+
+    def fv_fused():
+        rc = L.xdgcu_find_volume(rti.ctx, N_RAYS, ctypes.c_void_p(p.data_ptr()),
+                                 ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(fv.data_ptr()),
+                                 None, MIXED, sptr)
+        _lib.check(rc, rti.ctx, "find_volume")
+
+    fv_loop = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+
+    def fv_per_volume():
+        fv_loop.fill_(ipc)
+        todo = torch.arange(N_RAYS, device=dev)
+        for v in fv_vols:
+            if todo.numel() == 0:
+                break
+            pin = rti.point_in_volume(x.volume_to_surface_tree[v], p[todo], d[todo],
+                                      precision=MIXED).bool()
+            fv_loop[todo[pin]] = v
+            todo = todo[~pin]
+
+    ms_fv = timed(torch, fv_fused, max(3, args.steps // 4), 2, world, stream)
+    ms_fv_loop = timed(torch, fv_per_volume, 3, 1, world, stream)
+    fv_same = bool(torch.equal(fv, fv_loop))
+    fv_host_same = bool(np.array_equal(fv.cpu().numpy(), vols_h))
+
     # algorithmic work counters (untimed run)
     rti.set_counting(True)
     rf(MIXED)()
@@ -566,6 +594,13 @@ def run_engine(args, rank, world, local):
             "value": total_rays / (ms_piv / 1e3) / 1e6, "unit": "Mpoints/s",
             "fp64_value": total_rays / (ms_piv64 / 1e3) / 1e6,
             "inside_fraction_own_volume": piv_inside_frac,
+        },
+        "find_volume": {
+            "value": total_rays / (ms_fv / 1e3) / 1e6, "unit": "Mpoints/s",
+            "per_volume_launches_value": total_rays / (ms_fv_loop / 1e3) / 1e6,
+            "ms_fused": ms_fv, "ms_per_volume": ms_fv_loop,
+            "fused_equals_per_volume": fv_same, "device_equals_host_path": fv_host_same,
+            "volumes_tried_in_order": len(fv_vols),
         },
         "walk": {
             "workload": WALK_WORKLOAD,

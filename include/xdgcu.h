@@ -165,6 +165,24 @@ int xdgcu_point_in_volume(xdgcu_ctx* ctx, int32_t tree, const int32_t* ray_trees
                           const int32_t* excl_offsets, const int32_t* excl_ids,
                           int32_t* inside_out, int32_t* status, int32_t precision, void* stream);
 
+/* Sets the volumes XDG::find_volume tries, in order, with their surface
+ * trees (XDG::volume_to_surface_tree_map_, xdg.h:125, filled by
+ * prepare_raytracer, xdg.cpp:37-47).  Entries equal to implicit_complement
+ * are skipped, as find_volume skips that volume (xdg.cpp:119).  The
+ * reference iterates an unordered_map; the order given here is the order
+ * tried (for volumes that do not overlap, every order gives the same
+ * answer).  Must not be called while queries of this context are running. */
+int xdgcu_set_volume_map(xdgcu_ctx* ctx, int32_t n_volumes, const int32_t* volume_ids,
+                         const int32_t* surface_trees, int32_t implicit_complement);
+
+/* XDG::find_volume (xdg.cpp:113-128) for n points in one launch: for each
+ * point, point_in_volume in the trees of the volume map in order until one
+ * holds the point (each lane restarts its traversal in the next tree);
+ * volume_out = that volume's id, else the implicit complement.  directions
+ * may be NULL (the point_in_volume default direction). */
+int xdgcu_find_volume(xdgcu_ctx* ctx, int64_t n, const double* points, const double* directions,
+                      int32_t* volume_out, int32_t* status, int32_t precision, void* stream);
+
 /* RayTracer::occluded (ray_tracing_interface.h:112-115; embree/ray_tracer.cpp:
  * 347-370).  occluded_out: 1/0; dist_out (may be NULL): -INFTY when occluded,
  * INFTY otherwise, the value the reference writes through its `dist`. */

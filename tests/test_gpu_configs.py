@@ -189,3 +189,43 @@ def test_many_surfaces_per_volume_launches_and_graph(cuda, many):
     torch.cuda.synchronize()
     for a, b, what in ((t1, t2, "t"), (s1, s2, "surface"), (f1, f2, "face")):
         assert torch.equal(a, b), f"graph replay: {what}"
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_find_volume_fused_matches_per_volume(cuda, oracle, prec):
+    """The fused find_volume launch equals one point_in_volume launch per
+    volume on the points still unplaced, and the oracle's composition."""
+    m = synth.nested_spheres(n=8, level=3, jitter=1e-3, seed=7)
+    x = XDG(m)
+    x.prepare_raytracer()
+    rng = np.random.default_rng(12)
+    n = 50_000
+    p = rng.uniform(-9, 9, (n, 3))
+    d = synth.isotropic_dirs(rng, n)
+    fused = x.find_volume(p, d, precision=prec)
+    assert_same(fused, x.find_volume_per_volume(p, d, precision=prec), "fused vs per volume")
+    # default direction (NULL directions)
+    fused0 = x.rti.find_volume(p, None, prec)
+    ovol = np.full(n, m.implicit_complement, dtype=np.int32)
+    todo = np.arange(n)
+    for v in sorted(m.volumes):
+        if v == m.implicit_complement:
+            continue
+        ins = oracle.volume_tree(m, v).point_in_volume(p[todo], threads=CORES).astype(bool)
+        ovol[todo[ins]] = v
+        todo = todo[~ins]
+    assert_same(fused0, ovol, "fused, default direction, vs oracle")
+    # device arrays
+    import torch
+    pd = torch.from_numpy(p).cuda()
+    dd = torch.from_numpy(d).cuda()
+    assert_same(x.rti.find_volume(pd, dd, prec).cpu().numpy(), fused, "device path")
+
+
+def test_find_volume_many_surfaces(cuda, many):
+    m, x, o, d, vol, off = many
+    assert_same(x.find_volume(o, d), vol, "interior origins are found in their own volume")
+    rng = np.random.default_rng(3)
+    q = rng.uniform(-1.0, 17.0, (20000, 3))
+    qd = synth.isotropic_dirs(rng, 20000)
+    assert_same(x.find_volume(q, qd), x.find_volume_per_volume(q, qd), "fused vs per volume")

@@ -45,6 +45,8 @@ SIGNATURES = {
     "xdgcu_point_in_volume": (_int, [_VP, _i32, _VP, _i64, _VP, _VP, _VP, _VP, _VP, _VP, _i32,
                                      _VP]),
     "xdgcu_occluded": (_int, [_VP, _i32, _VP, _i64, _VP, _VP, _VP, _VP, _VP, _i32, _VP]),
+    "xdgcu_set_volume_map": (_int, [_VP, _i32, _VP, _VP, _i32]),
+    "xdgcu_find_volume": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_closest": (_int, [_VP, _i32, _VP, _i64, _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_find_element": (_int, [_VP, _i32, _VP, _i64, _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_next_element": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _VP, _VP, _i32, _VP]),

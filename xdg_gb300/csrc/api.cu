@@ -306,6 +306,11 @@ struct xdgcu_ctx {
   std::vector<std::unique_ptr<TreeHost>> surf_trees, elem_trees;
   DevMem<TreeDev> d_surf_trees, d_elem_trees;
   bool surf_trees_dirty = true, elem_trees_dirty = true;
+  // volume -> surface tree map for find_volume (xdgcu_set_volume_map)
+  DevMem<int32_t> d_vol_ids, d_vol_trees;
+  int32_t n_vols = 0;
+  int32_t ipc_volume = -1;
+  bool has_volume_map = false;
   // tuning (xdgcu_set_tuning)
   int32_t trace_occupancy = 3;
   int32_t trace_node_iters = 4;       // mixed precision
@@ -976,7 +981,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
     return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
   if (n == 0) return XDGCU_OK;
-  if (!org || (!dir && mode != MODE_PIV))
+  if (!org || (!dir && mode != MODE_PIV && mode != MODE_FIND_VOLUME))
     return set_err(XDGCU_ERR_INVALID_ARG, "null origins/directions");
   if (mode == MODE_RAY_FIRE && (!t_out || !surf_out))
     return set_err(XDGCU_ERR_INVALID_ARG, "ray_fire: t_out and surface_out are required");
@@ -986,8 +991,10 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   if (mode == MODE_RAY_FIRE && orientation != XDGCU_ANY && orientation != XDGCU_EXITING &&
       orientation != XDGCU_ENTERING)
     return set_err(XDGCU_ERR_INVALID_ARG, "bad orientation");
-  if (!ray_trees && (tree < 1 || tree > (int32_t)c->surf_trees.size()))
+  if (mode != MODE_FIND_VOLUME && !ray_trees && (tree < 1 || tree > (int32_t)c->surf_trees.size()))
     return set_err(XDGCU_ERR_NOT_FOUND, "no such surface tree");
+  if (mode == MODE_FIND_VOLUME && !c->has_volume_map)
+    return set_err(XDGCU_ERR_STATE, "find_volume: no volume map (xdgcu_set_volume_map)");
   {
     std::lock_guard<std::mutex> g(c->mu);
     int rc = sync_surfaces(c);
@@ -1011,6 +1018,10 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.occupancy = c->trace_occupancy;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
+  a.vol_ids = c->d_vol_ids.p;
+  a.vol_trees = c->d_vol_trees.p;
+  a.n_vols = c->n_vols;
+  a.ipc_volume = c->ipc_volume;
   cudaStream_t st = (cudaStream_t)stream;
   if (kind == 1) {
     a.ray_trees = ray_trees;
@@ -1089,6 +1100,42 @@ int xdgcu_point_in_volume(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, 
   return surface_query(c, MODE_PIV, tree, ray_trees, n, points, directions, nullptr, XDGCU_ANY,
                        excl_offsets, excl_ids, nullptr, nullptr, nullptr, inside_out, nullptr,
                        status, precision, stream);
+}
+
+int xdgcu_set_volume_map(xdgcu_ctx* c, int32_t n_volumes, const int32_t* volume_ids,
+                         const int32_t* surface_trees, int32_t implicit_complement) {
+  CHECK_CTX(c);
+  if (n_volumes < 0 || (n_volumes > 0 && (!volume_ids || !surface_trees)))
+    return set_err(XDGCU_ERR_INVALID_ARG, "set_volume_map: bad arguments");
+  std::vector<int32_t> ids, trees;
+  for (int32_t k = 0; k < n_volumes; ++k) {
+    if (volume_ids[k] == implicit_complement) continue;  // xdg.cpp:119
+    if (surface_trees[k] < 1 || surface_trees[k] > (int32_t)c->surf_trees.size())
+      return set_err(XDGCU_ERR_NOT_FOUND, "set_volume_map: no such surface tree");
+    ids.push_back(volume_ids[k]);
+    trees.push_back(surface_trees[k]);
+  }
+  std::lock_guard<std::mutex> g(c->mu);
+  const int64_t m = std::max<size_t>(1, ids.size());
+  API_CUDA(c->d_vol_ids.alloc(m), "alloc volume map");
+  API_CUDA(c->d_vol_trees.alloc(m), "alloc volume map");
+  if (!ids.empty()) {
+    API_CUDA(cudaMemcpy(c->d_vol_ids.p, ids.data(), sizeof(int32_t) * ids.size(),
+                        cudaMemcpyHostToDevice), "upload volume map");
+    API_CUDA(cudaMemcpy(c->d_vol_trees.p, trees.data(), sizeof(int32_t) * trees.size(),
+                        cudaMemcpyHostToDevice), "upload volume map");
+  }
+  c->n_vols = (int32_t)ids.size();
+  c->ipc_volume = implicit_complement;
+  c->has_volume_map = true;
+  return XDGCU_OK;
+}
+
+int xdgcu_find_volume(xdgcu_ctx* c, int64_t n, const double* points, const double* directions,
+                      int32_t* volume_out, int32_t* status, int32_t precision, void* stream) {
+  return surface_query(c, MODE_FIND_VOLUME, 0, nullptr, n, points, directions, nullptr, XDGCU_ANY,
+                       nullptr, nullptr, nullptr, nullptr, nullptr, volume_out, nullptr, status,
+                       precision, stream);
 }
 
 int xdgcu_occluded(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t n,

@@ -9,7 +9,7 @@
 
 namespace xdgcu {
 
-enum QueryMode : int { MODE_RAY_FIRE = 0, MODE_PIV = 1, MODE_OCCLUDED = 2 };
+enum QueryMode : int { MODE_RAY_FIRE = 0, MODE_PIV = 1, MODE_OCCLUDED = 2, MODE_FIND_VOLUME = 3 };
 
 struct SurfArgs {
   const TreeDev* trees;  // indexed by tree id - 1
@@ -39,6 +39,12 @@ struct SurfArgs {
   int32_t occupancy;   // traversal kernel variant: minimum resident blocks per SM (2..4)
   int32_t node_iters;  // inner-node steps per lane between leaf phases (1..64)
   int32_t flush_wait;  // lanes waiting on the FP64 queue that force a partial drain (1..32)
+  // MODE_FIND_VOLUME: the volumes tried in order (their surface trees) and
+  // the id written when none contains the point; the id goes to flag_out
+  const int32_t* vol_ids;
+  const int32_t* vol_trees;
+  int32_t n_vols;
+  int32_t ipc_volume;
 };
 
 struct PointArgs {

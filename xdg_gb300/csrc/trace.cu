@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
   // ---- lane state ----
   bool has_ray = false, trav = false, use64 = false;
   int64_t ray = 0;
-  int32_t tid = 0, status = RAY_OK, npend = 0;
+  int32_t tid = 0, status = RAY_OK, npend = 0, vk = 0;
   d3 o = mk3(0, 0, 0), d = mk3(0, 0, 0);
   const Node32* n32 = nullptr;
   const float4* prim32 = nullptr;
@@ -131,22 +131,77 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
     trav = false;
   };
 
+  // starts the traversal of the lane's ray in tree `tid` (status RAY_INVALID
+  // for an unknown tree)
+  auto begin_tree = [&]() {
+    if (tid < 1 || tid > a.n_trees) {
+      status = RAY_INVALID;
+      trav = false;
+      return;
+    }
+    trav = true;
+    const TreeDev* T = a.trees + (tid - 1);
+    tree = T;
+    n32 = T->n32;
+    prim32 = T->prim32;
+    const int32_t root = T->root;
+    bt32 = (MODE == MODE_OCCLUDED) ? INFINITY : f32_up(bt);
+    if (MIXED) {
+      br32 = make_boxray32(o, d);
+      r32 = make_ray32(o, d);
+      // FP32 box-test safety (see the file comment)
+      use64 = !(8.0f * kU32 * (T->max_abs + r32.oabs) < T->bump);
+    }
+    if (!MIXED) br64 = make_boxray64(o, d);
+    if (root == CHILD_EMPTY) {
+      trav = false;
+    } else if (ref_is_leaf(root)) {
+      cur = CHILD_EMPTY;
+      leaf_p = leaf_first(root);
+      leaf_end = leaf_p + leaf_count(root);
+    } else {
+      cur = root;
+    }
+  };
+
   while (true) {
     // ---- finalize finished rays ----
     if (has_ray && !trav && npend == 0) {
+      bool done = true;
       if (MODE == MODE_RAY_FIRE) {
         a.t_out[ray] = bhas ? bt : INFTY;
         a.surf_out[ray] = bhas ? bsurf : -1;
         if (a.face_out) a.face_out[ray] = bhas ? bface : -1;
       } else if (MODE == MODE_PIV) {
         a.flag_out[ray] = (bhas && bdot) ? 1 : 0;  // embree/ray_tracer.cpp:282-286
+      } else if (MODE == MODE_FIND_VOLUME) {
+        // xdg.cpp:113-128: the first volume whose point_in_volume is true;
+        // otherwise the lane restarts the same point in the next volume
+        const bool inside = bhas && bdot;
+        if (!inside && status == RAY_OK && vk + 1 < a.n_vols) {
+          ++vk;
+          tid = a.vol_trees[vk];
+          bt = INFTY;
+          bhas = false;
+          bdot = false;
+          bface = -1;
+          bsurf = -1;
+          sp = 0;
+          leaf_p = leaf_end = 0;
+          begin_tree();
+          done = false;
+        } else {
+          a.flag_out[ray] = inside ? a.vol_ids[vk] : a.ipc_volume;
+        }
       } else {
         a.flag_out[ray] = bhas ? 1 : 0;
         if (a.dist_out) a.dist_out[ray] = bhas ? -INFTY : INFTY;  // :368-369
       }
-      if (a.status) a.status[ray] = status;
-      has_ray = false;
-      rays_done++;
+      if (done) {
+        if (a.status) a.status[ray] = status;
+        has_ray = false;
+        rays_done++;
+      }
     }
     // ---- refill from the warp's chunk ----
     const unsigned need = __ballot_sync(kFull, !has_ray);
@@ -164,47 +219,29 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
           bface = -1;
           bsurf = -1;
           leaf_p = leaf_end = 0;
-          tid = a.ray_trees ? a.ray_trees[idx] : a.tree;
+          vk = 0;
+          tid = (MODE == MODE_FIND_VOLUME) ? (a.n_vols > 0 ? a.vol_trees[0] : 0)
+                                           : (a.ray_trees ? a.ray_trees[idx] : a.tree);
           o = load3(a.org, idx);
-          if (MODE == MODE_PIV && a.dir == nullptr)
+          if ((MODE == MODE_PIV || MODE == MODE_FIND_VOLUME) && a.dir == nullptr)
             d = mk3(1. / sqrt(2.0), 1 / sqrt(2.0), 0.0);  // embree/ray_tracer.cpp:268
           else
             d = load3(a.dir, idx);
           bt = (MODE == MODE_RAY_FIRE && a.tmax) ? a.tmax[idx] : INFTY;
           excl = nullptr;
           nexcl = 0;
-          if (MODE != MODE_OCCLUDED && a.excl_off) {
+          if (MODE != MODE_OCCLUDED && MODE != MODE_FIND_VOLUME && a.excl_off) {
             const int32_t e0 = a.excl_off[idx];
             excl = a.excl_ids + e0;
             nexcl = a.excl_off[idx + 1] - e0;
           }
-          trav = true;
-          if (tid < 1 || tid > a.n_trees || !finite3(o) || !finite3(d) || nan_bits(bt)) {
+          if (!finite3(o) || !finite3(d) || nan_bits(bt)) {
             status = RAY_INVALID;
             trav = false;
+          } else if (MODE == MODE_FIND_VOLUME && a.n_vols == 0) {
+            trav = false;  // no volume to try: the implicit complement
           } else {
-            const TreeDev* T = a.trees + (tid - 1);
-            tree = T;
-            n32 = T->n32;
-            prim32 = T->prim32;
-            const int32_t root = T->root;
-            bt32 = (MODE == MODE_OCCLUDED) ? INFINITY : f32_up(bt);
-            if (MIXED) {
-              br32 = make_boxray32(o, d);
-              r32 = make_ray32(o, d);
-              // FP32 box-test safety (see the file comment)
-              use64 = !(8.0f * kU32 * (T->max_abs + r32.oabs) < T->bump);
-            }
-            if (!MIXED) br64 = make_boxray64(o, d);
-            if (root == CHILD_EMPTY) {
-              trav = false;
-            } else if (ref_is_leaf(root)) {
-              cur = CHILD_EMPTY;
-              leaf_p = leaf_first(root);
-              leaf_end = leaf_p + leaf_count(root);
-            } else {
-              cur = root;
-            }
+            begin_tree();
           }
         }
       }
@@ -425,7 +462,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
 }
 
 int g_num_sms = 0;
-int g_blocks_per_sm[6][3] = {};
+int g_blocks_per_sm[8][3] = {};
 
 template <int MODE, bool MIXED, int MINB>
 cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
@@ -476,6 +513,8 @@ cudaError_t launch_surface_query(int mode, bool mixed, const SurfArgs& a, cudaSt
     case 3: return launch_one<MODE_PIV, true>(a, st, 3);
     case 4: return launch_one<MODE_OCCLUDED, false>(a, st, 4);
     case 5: return launch_one<MODE_OCCLUDED, true>(a, st, 5);
+    case 6: return launch_one<MODE_FIND_VOLUME, false>(a, st, 6);
+    case 7: return launch_one<MODE_FIND_VOLUME, true>(a, st, 7);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -299,6 +299,26 @@ class CudaRayTracer:
                     "point_in_volume")
         return r
 
+    def set_volume_map(self, volume_ids, surface_trees, implicit_complement):
+        """The volumes find_volume tries, in order, and their surface trees."""
+        ids = _host(volume_ids, np.int32)
+        trees = _host(surface_trees, np.int32)
+        self._check(self.L.xdgcu_set_volume_map(self.ctx, len(ids), _addr(ids), _addr(trees),
+                                                 int(implicit_complement)), "set_volume_map")
+
+    def find_volume(self, points, dirs=None, precision=MIXED, status=False, stream=None):
+        """XDG::find_volume for n points in one launch (volume map order)."""
+        p = _prep(points, np.float64, 3)
+        d = _prep(dirs, np.float64, 3)
+        n = p.shape[0]
+        out = _Out(p)
+        vol, st = out.i32(n), out.i32(n)
+        self._check(self.L.xdgcu_find_volume(self.ctx, n, _addr(p), _addr(d), _addr(vol), _addr(st),
+                                             int(precision),
+                                             stream if stream is not None else out.stream()),
+                    "find_volume")
+        return (vol, st) if status else vol
+
     def occluded(self, tree, origins, dirs, precision=MIXED, ray_trees=None, stream=None):
         o = _prep(origins, np.float64, 3)
         d = _prep(dirs, np.float64, 3)
@@ -403,11 +423,13 @@ class XDG:
         self.rti = ray_tracer or CudaRayTracer(device)
         self.volume_to_surface_tree = {}
         self.volume_to_point_location_tree = {}
+        self._volume_map_set = False
 
     def ray_tracing_interface(self):
         return self.rti
 
     def prepare_volume_for_raytracing(self, volume):
+        self._volume_map_set = False
         st, et = self.rti.register_volume(self.model, volume)
         self.volume_to_surface_tree[volume] = st
         self.volume_to_point_location_tree[volume] = et
@@ -461,7 +483,17 @@ class XDG:
     def find_volume(self, points, dirs, precision=MIXED):
         """xdg.cpp:113-128: first non-implicit-complement volume whose
         point_in_volume is true, else the implicit complement.  Volumes are
-        tried in ascending id order."""
+        tried in ascending id order, all of them in one fused launch."""
+        if not self._volume_map_set:
+            vols = sorted(self.volume_to_surface_tree)
+            self.rti.set_volume_map(vols, [self.volume_to_surface_tree[v] for v in vols],
+                                    self.model.implicit_complement)
+            self._volume_map_set = True
+        return self.rti.find_volume(points, dirs, precision)
+
+    def find_volume_per_volume(self, points, dirs, precision=MIXED):
+        """find_volume as one point_in_volume launch per volume on the points
+        not yet placed (the unfused form, for comparison)."""
         p = _host(points, np.float64, (-1, 3))
         d = _host(dirs, np.float64, (-1, 3))
         ipc = self.model.implicit_complement
