@@ -287,7 +287,12 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *   "trace_flush_wait" number of lanes (1..32) whose rays wait only on queued
  *                      FP64 candidate tests before the warp drains a partly
  *                      filled queue
- *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4) */
+ *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4)
+ *   "walk_queue"       mixed-precision walk: 1 (default) runs the FP64 face
+ *                      tests of a warp's tracks 32 at a time from a per-warp
+ *                      queue, 0 lets each lane evaluate its own faces
+ *   "walk_flush_wait"  number of tracks (1..32) waiting only on queued FP64
+ *                      face tests before the warp runs a partly filled round */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);
 

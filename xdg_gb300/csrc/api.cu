@@ -317,6 +317,8 @@ struct xdgcu_ctx {
   int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
   int32_t trace_flush_wait = 8;
   int32_t leaf_max = 4;
+  int32_t walk_queue = 1;
+  int32_t walk_flush_wait = 8;
   // diagnostics
   bool counting = false;
   DevMem<unsigned long long> d_counters;
@@ -656,6 +658,8 @@ const char* walk_args_for(const xdgcu_ctx* c, WalkArgs* a, int* face_order, int*
   a->elem_ids = c->d_elem_ids.p;
   a->n_tets = (int32_t)c->n_tet;
   std::memcpy(a->face, c->face, sizeof(a->face));
+  a->walk_queue = c->walk_queue;
+  a->flush_wait = c->walk_flush_wait;
   *face_order = c->face_order;
   *device = c->device;
   return nullptr;
@@ -931,6 +935,12 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "leaf_max") {
     if (value < 1 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "leaf_max must be 1..4");
     c->leaf_max = (int32_t)value;
+  } else if (k == "walk_queue") {
+    if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "walk_queue must be 0 or 1");
+    c->walk_queue = (int32_t)value;
+  } else if (k == "walk_flush_wait") {
+    if (value < 1 || value > 32) return set_err(XDGCU_ERR_INVALID_ARG, "walk_flush_wait must be 1..32");
+    c->walk_flush_wait = (int32_t)value;
   } else {
     return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   }
@@ -945,6 +955,8 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "trace_node_iters_fp64") *value = c->trace_node_iters_fp64;
   else if (k == "trace_flush_wait") *value = c->trace_flush_wait;
   else if (k == "leaf_max") *value = c->leaf_max;
+  else if (k == "walk_queue") *value = c->walk_queue;
+  else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   return XDGCU_OK;
 }
@@ -1268,6 +1280,8 @@ static int walk_query(xdgcu_ctx* c, bool walk, int64_t n, const int32_t* start, 
   a.elem_ids = c->d_elem_ids.p;
   a.n_tets = (int32_t)c->n_tet;
   std::memcpy(a.face, c->face, sizeof(a.face));
+  a.walk_queue = c->walk_queue;
+  a.flush_wait = c->walk_flush_wait;
   a.n = n;
   a.max_segs = max_segs;
   cudaStream_t st = (cudaStream_t)stream;
@@ -1347,6 +1361,8 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* c, int64_t n, const int32_t* start_ind
   a.elem_ids = c->d_elem_ids.p;
   a.n_tets = (int32_t)c->n_tet;
   std::memcpy(a.face, c->face, sizeof(a.face));
+  a.walk_queue = c->walk_queue;
+  a.flush_wait = c->walk_flush_wait;
   a.n = n;
   a.max_segs = max_segs;
   a.capacity = capacity;

@@ -103,19 +103,19 @@ __device__ __forceinline__ bool first_lower(d3 a, d3 b) {
   return okey(a.z) < okey(b.z);
 }
 
-// plucker.h:45-62
+// plucker.h:45-62.  The reference branches on the lexicographic order of the
+// two vertices and evaluates the same formula with the operands swapped, then
+// negates.  Here the operands are selected first and the sign is flipped on
+// the integer bits, so the FP64 instructions are identical for every lane and
+// a warp never runs both arms (the values are bit-identical to the branch).
 __device__ __forceinline__ double plucker_edge64(d3 va, d3 vb, d3 ray, d3 rn) {
-  double pip;
-  if (first_lower(va, vb)) {
-    const d3 e = sub3(vb, va);
-    const d3 en = cross3(e, va);
-    pip = dot3(ray, en) + dot3(rn, e);
-  } else {
-    const d3 e = sub3(va, vb);
-    const d3 en = cross3(e, vb);
-    pip = dot3(ray, en) + dot3(rn, e);
-    pip = -pip;
-  }
+  const bool f = first_lower(va, vb);
+  const d3 lo = f ? va : vb;
+  const d3 hi = f ? vb : va;
+  const d3 e = sub3(hi, lo);
+  const d3 en = cross3(e, lo);
+  double pip = dot3(ray, en) + dot3(rn, e);
+  pip = __longlong_as_double(__double_as_longlong(pip) ^ (f ? 0ll : (long long)0x8000000000000000ull));
   // ZERO_TOL > fabs(pip)
   if (absbits(pip) < absbits(ZERO_TOL)) pip = 0.0;
   return pip;
@@ -127,25 +127,23 @@ __device__ __forceinline__ double plucker_edge64(d3 va, d3 vb, d3 ray, d3 rn) {
 // use_or is set.
 __device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn, double t_max,
                                           double t_min, bool use_or, int orient, double* t_out) {
+  // The three coordinates are evaluated unconditionally (the reference
+  // returns after the first one that fails, :83-113); the decisions below use
+  // the same values, so the outcome is the same, and lanes of a warp do not
+  // diverge in the FP64 part.
+  const double c0 = plucker_edge64(v0, v1, d, rn);
+  const double c1 = plucker_edge64(v1, v2, d, rn);
+  const double c2 = plucker_edge64(v2, v0, d, rn);
   // orientation * c > 0
   auto exits = [&](double c) { return orient > 0 ? gt0(c) : lt0(c); };
-  const double c0 = plucker_edge64(v0, v1, d, rn);
-  if (use_or && exits(c0)) return false;
-  const double c1 = plucker_edge64(v1, v2, d, rn);
-  const bool p0 = gt0(c0), n0 = lt0(c0), p1 = gt0(c1), n1 = lt0(c1);
+  const bool p0 = gt0(c0), n0 = lt0(c0), p1 = gt0(c1), n1 = lt0(c1), p2 = gt0(c2), n2 = lt0(c2);
+  bool rej;
   if (use_or) {
-    if (exits(c1)) return false;
-  } else if ((p0 && n1) || (n0 && p1)) {
-    return false;
+    rej = exits(c0) || exits(c1) || exits(c2);
+  } else {
+    rej = (p0 && n1) || (n0 && p1) || (p1 && n2) || (n1 && p2) || (p0 && n2) || (n0 && p2);
   }
-  const double c2 = plucker_edge64(v2, v0, d, rn);
-  const bool p2 = gt0(c2), n2 = lt0(c2);
-  if (use_or) {
-    if (exits(c2)) return false;
-  } else if ((p1 && n2) || (n1 && p2) || (p0 && n2) || (n0 && p2)) {
-    return false;
-  }
-  if (is0(c0) && is0(c1) && is0(c2)) return false;
+  if (rej || (is0(c0) && is0(c1) && is0(c2))) return false;
   const double inv = 1.0 / (c0 + c1 + c2);
   // index of the largest |d| component, first maximum wins
   const unsigned long long ax = absbits(d.x), ay = absbits(d.y), az = absbits(d.z);

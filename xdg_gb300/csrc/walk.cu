@@ -334,6 +334,323 @@ __global__ void __launch_bounds__(kBlock) k_next(WalkArgs a) {
   if (a.counters) flush(a.counters, cnt, i < a.n ? 1ull : 0ull);
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-precision walk with a per-warp FP64 queue.
+//
+// Each step of a track runs the FP32 edge filter for its tet (six edge
+// coordinates, truncated FP32 inputs, bound below) and queues every face the
+// filter cannot reject as a (lane, face) task.  When 32 tasks are queued, or
+// lanes wait on the queue, the whole warp runs 32 tasks at once -- each lane
+// evaluates one face of some lane's tet with the FP64 Plucker test -- and each
+// owner keeps the smallest (distance, face index) of its results, which is
+// the reference's strict-< scan over faces 0..3 (:186-196) in any order.  A
+// lane whose tasks are all done completes its step (segment, r += len * u)
+// and starts the next one, so FP64 instructions run with (nearly) all 32
+// lanes busy however many faces each step escalates.
+//
+// FP32 bound with truncated inputs (u = 2^-24; r and the direction truncated,
+// relative error 2u; stored vertices rounded, u; W = max |v_k - r|_inf over
+// the FP32 differences; Wb = W (1 + 2^-20) + 1.01 u (Av + 2 R) bounds the
+// exact |v_k - r|_inf; edges |e| <= 2 Wb; D = |u|_inf, Av = max |v_k|_inf,
+// R = |r|_inf):
+//   rounding of the triple product (gamma_5, six terms)   <= 60 u D Wb^2
+//   input perturbation (direction 2u, edges, differences) <= u D Wb (48 Wb + 24 Av + 24 R)
+// so |pip32 - pip| <= u D Wb (108 Wb + 24 Av + 24 R); the threshold uses
+// 110 / 26 / 26 and a factor 1.01 for second-order terms, the FP64
+// evaluation error and the rounding of the threshold itself, plus the
+// 20*DBL_EPSILON snap.
+// ---------------------------------------------------------------------------
+
+constexpr int kWQ = 256;  // ring entries per warp: < 32 left over + 4 per lane
+
+struct WalkQueue {
+  uint32_t ent[kWQ];  // (owner lane << 2) | face
+  double rd[32];
+  int32_t rf[32];
+  uint32_t head, tail;
+};
+
+template <int FO>
+__device__ __forceinline__ unsigned walk_filter32(const WalkArgs& a, const int32_t ci[4], float rx,
+                                                  float ry, float rz, float ux, float uy, float uz,
+                                                  float D, float R) {
+  float4 P[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) P[k] = __ldg(&a.xyz32[ci[k]]);
+  float wx[4], wy[4], wz[4];
+  float W = 0.0f, Av = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    wx[k] = P[k].x - rx;
+    wy[k] = P[k].y - ry;
+    wz[k] = P[k].z - rz;
+    W = fmaxf(W, fmaxf(fabsf(wx[k]), fmaxf(fabsf(wy[k]), fabsf(wz[k]))));
+    Av = fmaxf(Av, P[k].w);
+  }
+  const float Wb = W * 1.000001f + kU32 * 1.01f * (Av + 2.0f * R);
+  const float thr = kU32 * D * Wb * (110.0f * Wb + 26.0f * Av + 26.0f * R) * 1.01f + 4.5e-15f;
+  float pe[6];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = i + 1; j < 4; ++j)
+      pe[pair_index(i, j)] = triple32(ux, uy, uz, P[j].x - P[i].x, P[j].y - P[i].y,
+                                      P[j].z - P[i].z, wx[i], wy[i], wz[i]);
+  unsigned escm = 0u;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const int l0 = face_local<FO>(a, f, 0), l1 = face_local<FO>(a, f, 1),
+              l2 = face_local<FO>(a, f, 2);
+    const int e0 = pair_index(l0, l1), e1 = pair_index(l1, l2), e2 = pair_index(l2, l0);
+    const float p0 = l0 < l1 ? sel6(pe, e0) : -sel6(pe, e0);
+    const float p1 = l1 < l2 ? sel6(pe, e1) : -sel6(pe, e1);
+    const float p2 = l2 < l0 ? sel6(pe, e2) : -sel6(pe, e2);
+    if (!(p0 > thr || p1 > thr || p2 > thr)) escm |= 1u << f;
+  }
+  return escm;
+}
+
+template <int FO>
+__global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
+  __shared__ WalkQueue qs[kBlock / 32];
+  WalkQueue& Q = qs[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t cursor = gwarp * chunk;
+  const int64_t end = min(a.n, cursor + chunk);
+  if (lane == 0) {
+    Q.head = 0u;
+    Q.tail = 0u;
+  }
+  __syncwarp();
+  StepCnt cnt = {0, 0};
+  unsigned long long tracks = 0;
+  // track state
+  bool has = false;
+  int64_t i = 0;
+  d3 r = mk3(0, 0, 0), u = mk3(0, 0, 0);
+  double dist = 0.0;
+  int32_t elem = -1, k = 0, st = RAY_OK;
+  int32_t* oe = nullptr;
+  double* ol = nullptr;
+  float ux = 0.f, uy = 0.f, uz = 0.f, D = 0.f;
+  // step state
+  bool in_step = false;
+  int npend = 0;
+  double bd = INFTY;
+  int32_t bf = -1;
+  d3 rn = mk3(0, 0, 0);
+  int32_t ci[4] = {0, 0, 0, 0};
+
+  while (true) {
+    // ---- refill lanes without a track from the warp's chunk ----
+    const unsigned need = __ballot_sync(0xffffffffu, !has);
+    if (need != 0u && cursor < end) {
+      if (!has) {
+        unsigned lt;
+        asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+        const int64_t idx = cursor + __popc(need & lt);
+        if (idx < end) {
+          i = idx;
+          has = true;
+          in_step = false;
+          r = load3(a.org, i);
+          u = load3(a.dir, i);
+          dist = a.dist[i];
+          elem = a.start[i];
+          k = 0;
+          st = RAY_OK;
+          ux = f32_trunc(u.x);
+          uy = f32_trunc(u.y);
+          uz = f32_trunc(u.z);
+          D = fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz))) * 1.0000002f;
+          if (a.out_mode == WALK_STRIDED) {
+            oe = a.seg_elem + i * (int64_t)a.max_segs;
+            ol = a.seg_len + i * (int64_t)a.max_segs;
+          } else if (a.out_mode == WALK_PACKED) {
+            const int64_t off = a.offsets[i];
+            const int64_t cnt_i = a.offsets[i + 1] - off;
+            if (off + cnt_i <= a.capacity) {
+              oe = a.seg_elem + off;
+              ol = a.seg_len + off;
+            } else {
+              oe = nullptr;  // does not fit: the track is walked, nothing is written
+              ol = nullptr;
+            }
+          } else {
+            oe = nullptr;
+            ol = nullptr;
+          }
+          if (elem < 0 || elem >= a.n_tets || !finite3(r) || !finite3(u) || nan_bits(dist)) {
+            st = RAY_INVALID;
+            dist = 0.0;  // finishes below without a step
+          }
+        }
+      }
+      cursor += __popc(need);
+    }
+    if (__ballot_sync(0xffffffffu, has) == 0u) break;
+
+    // ---- start a step: FP32 filter, queue the faces it cannot reject ----
+    unsigned escm = 0u;
+    if (has && !in_step) {
+      bool done = !gt0(dist);  // while (distance > 0), mesh_manager_interface.cpp:117
+      if (!done && k >= a.max_segs) {
+        st = RAY_WALK_LIMIT;
+        done = true;
+      }
+      if (done) {
+        if (a.out_mode == WALK_COUNT) {
+          a.offsets[i] = k;
+        } else {
+          if (a.seg_count) a.seg_count[i] = k;
+          if (a.out_mode == WALK_PACKED && !oe && k > 0 && st == RAY_OK) st = RAY_OUTPUT_FULL;
+        }
+        if (a.status) a.status[i] = st;
+        has = false;
+        tracks++;
+      } else {
+        cnt.steps++;
+        in_step = true;
+        const int4 c = __ldg(&a.conn[elem]);
+        ci[0] = c.x;
+        ci[1] = c.y;
+        ci[2] = c.z;
+        ci[3] = c.w;
+        const float rx = f32_trunc(r.x), ry = f32_trunc(r.y), rz = f32_trunc(r.z);
+        const float R = fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz))) * 1.0000002f;
+        escm = walk_filter32<FO>(a, ci, rx, ry, rz, ux, uy, uz, D, R);
+        rn = cross3(u, r);  // plucker.h:75
+        bd = INFTY;
+        bf = -1;
+        npend = __popc(escm);
+        cnt.esc += npend;
+      }
+    }
+    {
+      const int c = __popc(escm);
+      int incl = c;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += y;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      if (total > 0) {
+        const uint32_t tail = Q.tail;
+        __syncwarp();
+        uint32_t pos = tail + (uint32_t)(incl - c);
+        unsigned m = escm;
+        while (m) {
+          const int f = __ffs(m) - 1;
+          m &= m - 1u;
+          Q.ent[pos & (kWQ - 1)] = ((uint32_t)lane << 2) | (uint32_t)f;
+          ++pos;
+        }
+        __syncwarp();
+        if (lane == 0) Q.tail = tail + (uint32_t)total;
+      }
+      __syncwarp();
+    }
+
+    // ---- run queued FP64 face tests with the whole warp ----
+    while (true) {
+      const uint32_t head = Q.head;
+      const int qn = (int)(Q.tail - head);
+      const unsigned waiting = __ballot_sync(0xffffffffu, in_step && npend > 0);
+      const unsigned progress = __ballot_sync(0xffffffffu, has && !(in_step && npend > 0));
+      if (!(qn >= 32 || (qn > 0 && (progress == 0u || __popc(waiting) >= a.flush_wait)))) break;
+      const int nq = min(qn, 32);
+      const bool mine = lane < nq;
+      const uint32_t ent = mine ? Q.ent[(head + lane) & (kWQ - 1)] : ((uint32_t)lane << 2);
+      const int owner = (int)(ent >> 2);
+      const int f = (int)(ent & 3u);
+      d3 orr, ou, orn;
+      orr.x = __shfl_sync(0xffffffffu, r.x, owner);
+      orr.y = __shfl_sync(0xffffffffu, r.y, owner);
+      orr.z = __shfl_sync(0xffffffffu, r.z, owner);
+      ou.x = __shfl_sync(0xffffffffu, u.x, owner);
+      ou.y = __shfl_sync(0xffffffffu, u.y, owner);
+      ou.z = __shfl_sync(0xffffffffu, u.z, owner);
+      orn.x = __shfl_sync(0xffffffffu, rn.x, owner);
+      orn.y = __shfl_sync(0xffffffffu, rn.y, owner);
+      orn.z = __shfl_sync(0xffffffffu, rn.z, owner);
+      int32_t oc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) oc[q] = __shfl_sync(0xffffffffu, ci[q], owner);
+      double df = INFTY;
+      if (mine) {
+        const int l0 = face_local<FO>(a, f, 0), l1 = face_local<FO>(a, f, 1),
+                  l2 = face_local<FO>(a, f, 2);
+        const d3 f0 = load3(a.xyz, sel4(oc, l0));
+        const d3 f1 = load3(a.xyz, sel4(oc, l1));
+        const d3 f2 = load3(a.xyz, sel4(oc, l2));
+        double t;
+        const bool hit = plucker64(f0, f1, f2, orr, ou, orn, INFTY, 0.0, true, 1, &t);
+        df = hit ? (gt0(t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
+      }
+      Q.rd[lane] = df;
+      Q.rf[lane] = f;
+      __syncwarp();
+      for (int j = 0; j < nq; ++j) {
+        if (__shfl_sync(0xffffffffu, owner, j) != lane) continue;
+        npend--;
+        const double dj = Q.rd[j];
+        const int32_t fj = Q.rf[j];
+        // first minimum over faces 0..3 with strict < (:186-196)
+        if (dlt(dj, bd) || (bf >= 0 && okey(dj) == okey(bd) && fj < bf)) {
+          bd = dj;
+          bf = fj;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) Q.head = head + (uint32_t)nq;
+      __syncwarp();
+    }
+
+    // ---- complete the steps whose faces are all evaluated ----
+    if (has && in_step && npend == 0) {
+      in_step = false;
+      int32_t nxt = -1;
+      double ex = bd;
+      if (bf < 0) {
+        st = RAY_NO_EXIT_FACE;  // the reference would index adjacency with -1
+      } else {
+        const int4 ad = __ldg(&a.adj[elem]);
+        nxt = bf == 0 ? ad.x : (bf == 1 ? ad.y : (bf == 2 ? ad.z : ad.w));
+      }
+      ex = dlt(dist, ex) ? dist : ex;  // std::min(exit, distance)
+      dist -= ex;
+      if (oe) {
+        oe[k] = __ldg(&a.elem_ids[elem]);
+        ol[k] = ex;
+      }
+      ++k;
+      r = add3(r, scl3(ex, u));  // r += exit.second * u
+      bool done = false;
+      if (nxt < -1 || nxt >= a.n_tets) {
+        st = RAY_INVALID;  // corrupt adjacency: stop instead of reading out of range
+        done = true;
+      } else {
+        elem = nxt;
+        if (elem == -1) done = true;
+      }
+      if (done) {
+        if (a.out_mode == WALK_COUNT) {
+          a.offsets[i] = k;
+        } else {
+          if (a.seg_count) a.seg_count[i] = k;
+          if (a.out_mode == WALK_PACKED && !oe && k > 0 && st == RAY_OK) st = RAY_OUTPUT_FULL;
+        }
+        if (a.status) a.status[i] = st;
+        has = false;
+        tracks++;
+      }
+    }
+  }
+  if (a.counters) flush(a.counters, cnt, tracks);
+}
+
 constexpr int kScanBlock = 1024;
 
 // sum of each block of kScanBlock counts
@@ -416,10 +733,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(int64_t* __restrict__
   if (blockIdx.x == 0 && threadIdx.x == 0) v[n] = sums[nb];
 }
 
-template <int FO, bool MIXED>
+template <int FO, bool MIXED, bool QUEUE>
 cudaError_t launch_walk_t(const WalkArgs& a, cudaStream_t st) {
   static int num_sms = 0, per_sm = 0;
-  auto kern = k_walk<FO, MIXED>;
+  auto kern = QUEUE ? k_walk_q<FO> : k_walk<FO, MIXED>;
   if (per_sm == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -444,11 +761,12 @@ cudaError_t launch_walk_t(const WalkArgs& a, cudaStream_t st) {
 cudaError_t launch_walk(bool mixed, int face_order, const WalkArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
   const int sel = (face_order == 0 ? 0 : 2) + (mixed ? 1 : 0);
+  const bool q = mixed && a.walk_queue;
   switch (sel) {
-    case 0: return launch_walk_t<0, false>(a, st);
-    case 1: return launch_walk_t<0, true>(a, st);
-    case 2: return launch_walk_t<1, false>(a, st);
-    default: return launch_walk_t<1, true>(a, st);
+    case 0: return launch_walk_t<0, false, false>(a, st);
+    case 1: return q ? launch_walk_t<0, true, true>(a, st) : launch_walk_t<0, true, false>(a, st);
+    case 2: return launch_walk_t<1, false, false>(a, st);
+    default: return q ? launch_walk_t<1, true, true>(a, st) : launch_walk_t<1, true, false>(a, st);
   }
 }
 

@@ -34,6 +34,9 @@ struct WalkArgs {
   int32_t out_mode;
   int64_t* offsets;
   int64_t capacity;
+  // mixed walk: 1 = per-warp FP64 queue (k_walk_q), 0 = per-lane escalation
+  int32_t walk_queue;
+  int32_t flush_wait;  // queue: lanes waiting that force a partial FP64 round
 };
 
 enum : int32_t { WALK_STRIDED = 0, WALK_COUNT = 1, WALK_PACKED = 2 };
