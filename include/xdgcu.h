@@ -292,7 +292,12 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      tests of a warp's tracks 32 at a time from a per-warp
  *                      queue, 0 lets each lane evaluate its own faces
  *   "walk_flush_wait"  number of tracks (1..32) waiting only on queued FP64
- *                      face tests before the warp runs a partly filled round */
+ *                      face tests before the warp runs a partly filled round
+ *   "walk_sort_min"    batches of at least this many tracks (default 16384;
+ *                      0 = never) are walked longest first: the tracks are
+ *                      sorted by length on the device and dealt round-robin
+ *                      to warps, so warps end on short tracks.  Results do not
+ *                      depend on it. */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);
 

@@ -319,6 +319,7 @@ struct xdgcu_ctx {
   int32_t leaf_max = 4;
   int32_t walk_queue = 1;
   int32_t walk_flush_wait = 8;
+  int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
   bool counting = false;
   DevMem<unsigned long long> d_counters;
@@ -635,6 +636,27 @@ int begin_query(xdgcu_ctx* c, cudaStream_t st, unsigned long long** counters) {
   return XDGCU_OK;
 }
 
+// Runs `body` with a.order set to the tracks sorted by decreasing length when
+// the batch is large enough (scratch allocated on the stream), else without.
+template <typename Body>
+int with_length_order(xdgcu_ctx* c, WalkArgs& a, cudaStream_t s, Body body) {
+  if (c->walk_sort_min <= 0 || a.n < c->walk_sort_min || a.n >= ((int64_t)1 << 31)) return body();
+  const size_t ord_bytes = ((sizeof(int32_t) * (size_t)a.n + 255) & ~(size_t)255);
+  const size_t scr = walk_order_scratch_bytes(a.n);
+  char* buf = nullptr;
+  API_CUDA(cudaMallocAsync((void**)&buf, ord_bytes + scr, s), "walk order scratch");
+  cudaError_t e = walk_order(a.dist, a.n, (int32_t*)buf, buf + ord_bytes, scr, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(buf, s);
+    return cuda_err(e, "walk order");
+  }
+  a.order = (const int32_t*)buf;
+  const int rc = body();
+  a.order = nullptr;
+  cudaFreeAsync(buf, s);
+  return rc;
+}
+
 #define CHECK_CTX(c)                                                            \
   do {                                                                          \
     if (!(c)) return set_err(XDGCU_ERR_INVALID_ARG, "null context");            \
@@ -941,6 +963,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "walk_flush_wait") {
     if (value < 1 || value > 32) return set_err(XDGCU_ERR_INVALID_ARG, "walk_flush_wait must be 1..32");
     c->walk_flush_wait = (int32_t)value;
+  } else if (k == "walk_sort_min") {
+    if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "walk_sort_min must be >= 0");
+    c->walk_sort_min = value;
   } else {
     return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   }
@@ -957,6 +982,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "leaf_max") *value = c->leaf_max;
   else if (k == "walk_queue") *value = c->walk_queue;
   else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
+  else if (k == "walk_sort_min") *value = c->walk_sort_min;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   return XDGCU_OK;
 }
@@ -1302,8 +1328,14 @@ static int walk_query(xdgcu_ctx* c, bool walk, int64_t n, const int32_t* start, 
     a.status = status;
     int rc = begin_query(c, st, &a.counters);
     if (rc) return rc;
-    API_CUDA(launch(), "walk launch");
-    return XDGCU_OK;
+    if (!walk) {
+      API_CUDA(launch(), "walk launch");
+      return XDGCU_OK;
+    }
+    return with_length_order(c, a, st, [&]() -> int {
+      API_CUDA(launch(), "walk launch");
+      return XDGCU_OK;
+    });
   }
   Slot* s = get_slot(c);
   if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
@@ -1332,7 +1364,15 @@ static int walk_query(xdgcu_ctx* c, bool walk, int64_t n, const int32_t* start, 
   a.status = (int32_t*)A_st.dev;
   rc = begin_query(c, st, &a.counters);
   if (rc) return rc;
-  API_CUDA(launch(), "walk launch");
+  if (walk) {
+    rc = with_length_order(c, a, st, [&]() -> int {
+      API_CUDA(launch(), "walk launch");
+      return XDGCU_OK;
+    });
+    if (rc) return rc;
+  } else {
+    API_CUDA(launch(), "walk launch");
+  }
   return stage_out(all, st);
 }
 
@@ -1369,16 +1409,18 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* c, int64_t n, const int32_t* start_ind
   cudaStream_t st = (cudaStream_t)stream;
   const bool mixed = precision == XDGCU_MIXED;
   auto run = [&](cudaStream_t s) -> int {
-    a.out_mode = WALK_COUNT;
-    API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (count)");
-    int64_t* sums = nullptr;
-    API_CUDA(cudaMallocAsync(&sums, sizeof(int64_t) * scan_scratch_entries(n), s), "scan scratch");
-    cudaError_t e = scan_offsets(a.offsets, n, sums, s);
-    cudaFreeAsync(sums, s);
-    API_CUDA(e, "scan");
-    a.out_mode = WALK_PACKED;
-    API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (emit)");
-    return XDGCU_OK;
+    return with_length_order(c, a, s, [&]() -> int {
+      a.out_mode = WALK_COUNT;
+      API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (count)");
+      int64_t* sums = nullptr;
+      API_CUDA(cudaMallocAsync(&sums, sizeof(int64_t) * scan_scratch_entries(n), s), "scan scratch");
+      cudaError_t e = scan_offsets(a.offsets, n, sums, s);
+      cudaFreeAsync(sums, s);
+      API_CUDA(e, "scan");
+      a.out_mode = WALK_PACKED;
+      API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (emit)");
+      return XDGCU_OK;
+    });
   };
   if (kind == 1) {
     a.start = start_index;

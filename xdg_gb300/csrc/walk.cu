@@ -24,6 +24,8 @@
 // FP64 evaluation error and the 20*DBL_EPSILON snap are added as in geom.cuh).
 #include "walk.h"
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "internal.cuh"
 
 namespace xdgcu {
@@ -203,8 +205,15 @@ template <int FO, bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
   const int lane = threadIdx.x & 31;
   const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int64_t cursor = gwarp * chunk;
-  const int64_t end = min(a.n, cursor + chunk);
+  // the warp's tracks: positions first + k * stride, k < count (a contiguous
+  // chunk, or with a length order every W-th track of it, longest first)
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t first = a.order ? gwarp : gwarp * chunk;
+  const int64_t stride = a.order ? nwarps : 1;
+  const int64_t count = a.order ? (gwarp < a.n ? (a.n - gwarp + nwarps - 1) / nwarps : 0)
+                                : max((int64_t)0, min(a.n, first + chunk) - first);
+  int64_t cursor = 0;
+  const int64_t end = count;
   StepCnt cnt = {0, 0};
   unsigned long long tracks = 0;
   bool has = false;
@@ -220,9 +229,10 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
       if (!has) {
         unsigned lt;
         asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-        const int64_t idx = cursor + __popc(need & lt);
-        if (idx < end) {
-          i = idx;
+        const int64_t kk = cursor + __popc(need & lt);
+        if (kk < end) {
+          const int64_t pos = first + kk * stride;
+          i = a.order ? (int64_t)__ldg(&a.order[pos]) : pos;
           has = true;
           r = load3(a.org, i);
           u = load3(a.dir, i);
@@ -416,8 +426,15 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
   WalkQueue& Q = qs[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int64_t cursor = gwarp * chunk;
-  const int64_t end = min(a.n, cursor + chunk);
+  // the warp's tracks: positions first + k * stride, k < count (a contiguous
+  // chunk, or with a length order every W-th track of it, longest first)
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t first = a.order ? gwarp : gwarp * chunk;
+  const int64_t stride = a.order ? nwarps : 1;
+  const int64_t count = a.order ? (gwarp < a.n ? (a.n - gwarp + nwarps - 1) / nwarps : 0)
+                                : max((int64_t)0, min(a.n, first + chunk) - first);
+  int64_t cursor = 0;
+  const int64_t end = count;
   if (lane == 0) {
     Q.head = 0u;
     Q.tail = 0u;
@@ -449,9 +466,10 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
       if (!has) {
         unsigned lt;
         asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
-        const int64_t idx = cursor + __popc(need & lt);
-        if (idx < end) {
-          i = idx;
+        const int64_t kk = cursor + __popc(need & lt);
+        if (kk < end) {
+          const int64_t pos = first + kk * stride;
+          i = a.order ? (int64_t)__ldg(&a.order[pos]) : pos;
           has = true;
           in_step = false;
           r = load3(a.org, i);
@@ -771,6 +789,39 @@ cudaError_t launch_walk(bool mixed, int face_order, const WalkArgs& a, cudaStrea
 }
 
 int64_t scan_scratch_entries(int64_t n) { return (n + kScanBlock - 1) / kScanBlock + 1; }
+
+namespace {
+__global__ void k_iota(int32_t* v, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (int32_t)i;
+}
+}  // namespace
+
+size_t walk_order_scratch_bytes(int64_t n) {
+  size_t tmp = 0;
+  cub::DeviceRadixSort::SortPairsDescending(nullptr, tmp, (const double*)nullptr, (double*)nullptr,
+                                            (const int32_t*)nullptr, (int32_t*)nullptr, (int)n);
+  return ((tmp + 255) & ~(size_t)255) + ((sizeof(double) * n + 255) & ~(size_t)255) +
+         ((sizeof(int32_t) * n + 255) & ~(size_t)255);
+}
+
+cudaError_t walk_order(const double* dist, int64_t n, int32_t* order, void* scratch,
+                       size_t scratch_bytes, cudaStream_t st) {
+  size_t tmp = 0;
+  cudaError_t e = cub::DeviceRadixSort::SortPairsDescending(
+      nullptr, tmp, (const double*)nullptr, (double*)nullptr, (const int32_t*)nullptr,
+      (int32_t*)nullptr, (int)n, 0, 64, st);
+  if (e != cudaSuccess) return e;
+  char* p = (char*)scratch;
+  const size_t tmp_al = (tmp + 255) & ~(size_t)255;
+  double* keys_out = (double*)(p + tmp_al);
+  int32_t* idx = (int32_t*)(p + tmp_al + ((sizeof(double) * n + 255) & ~(size_t)255));
+  if (tmp_al + ((sizeof(double) * n + 255) & ~(size_t)255) + sizeof(int32_t) * n > scratch_bytes)
+    return cudaErrorInvalidValue;
+  k_iota<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(idx, n);
+  return cub::DeviceRadixSort::SortPairsDescending(p, tmp, dist, keys_out, idx, order, (int)n, 0,
+                                                   64, st);
+}
 
 cudaError_t scan_offsets(int64_t* offsets, int64_t n, int64_t* block_sums, cudaStream_t st) {
   if (n <= 0) return cudaMemsetAsync(offsets, 0, sizeof(int64_t), st);

@@ -36,6 +36,9 @@ struct WalkArgs {
   int64_t capacity;
   // mixed walk: 1 = per-warp FP64 queue (k_walk_q), 0 = per-lane escalation
   int32_t walk_queue;
+  // optional: track indices by decreasing length; the kernels then deal them
+  // round-robin to warps, longest first, so warps finish on short tracks
+  const int32_t* order;
   int32_t flush_wait;  // queue: lanes waiting that force a partial FP64 round
 };
 
@@ -45,6 +48,12 @@ enum : int32_t { WALK_STRIDED = 0, WALK_COUNT = 1, WALK_PACKED = 2 };
 // block_sums needs scan_scratch_entries(n) int64 entries.
 int64_t scan_scratch_entries(int64_t n);
 cudaError_t scan_offsets(int64_t* offsets, int64_t n, int64_t* block_sums, cudaStream_t st);
+
+// Length order of n tracks (n < 2^31): order[k] = index of the k-th longest.
+// scratch holds walk_order_scratch_bytes(n) bytes.
+size_t walk_order_scratch_bytes(int64_t n);
+cudaError_t walk_order(const double* dist, int64_t n, int32_t* order, void* scratch,
+                       size_t scratch_bytes, cudaStream_t st);
 
 // face_order: 0 = the MOAB table {0,1,3},{1,2,3},{2,0,3},{0,2,1} (compiled in),
 // 1 = any other table (read from WalkArgs::face).
