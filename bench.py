@@ -49,6 +49,11 @@ WORKLOAD = "nested_spheres_8x_icosphere_L6_jitter1e-3_1e7_rays"
 WALK_WORKLOAD = "tet_cube_50^3x6_kuhn_jitter0.2_1e6_tracks_exp5"
 MANY_SURFACES = 256
 MANY_WORKLOAD = "256_surfaces_sphere_torus_tris_10^U(3,5.7)_rays_10^U(3,6)"
+TUNE_RAYS = 1_000_000       # autotuner sample (same distribution, its own seed)
+TUNE_TRACKS = 1_000_000     # the walk's length order pays off only on large batches
+TRACE_KEYS = ("trace_occupancy", "trace_stack", "trace_node_iters", "trace_node_iters_fp64",
+              "trace_flush_wait", "trace_grab", "trace_sort_min")
+WALK_KEYS = ("walk_queue", "walk_flush_wait", "walk_sort_min")
 CPU_SAMPLE = 4_000_000      # rays of the same workload timed on the host cores
 REF_STEP_SAMPLE = 1_000_000  # rays per step of --impl reference
 BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
@@ -265,6 +270,16 @@ def bench_many_surfaces(torch, L, dev, stream, args, rank, world):
     f_a = torch.empty(n, dtype=torch.int32, device=dev)
     t_b, s_b, f_b = torch.empty_like(t_a), torch.empty_like(s_a), torch.empty_like(f_a)
     log(f"[bench] many-surface setup {time.perf_counter() - t0:.1f}s, {n} rays")
+    tuned = None
+    if args.autotune:
+        from xdg_gb300.engine import QUERY_RAY_FIRE
+        sel = torch.arange(0, n, max(1, n // TUNE_RAYS), device=dev)
+        t1 = time.perf_counter()
+        _, tv = rti.autotune_trace(QUERY_RAY_FIRE, 0, o[sel], d[sel], precision=MIXED,
+                                   ray_trees=trees[sel], reps=3)
+        tuned = {"sample_rays": int(sel.numel()), "seconds": time.perf_counter() - t1,
+                 "trace": {k: tv[k] for k in TRACE_KEYS}}
+        log(f"[bench] many-surface autotune {tuned['seconds']:.1f}s: {tuned['trace']}")
 
     def one_launch():
         rc = L.xdgcu_ray_fire(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), n,
@@ -316,6 +331,7 @@ def bench_many_surfaces(torch, L, dev, stream, args, rank, world):
         "per_volume_equals_one_launch": same_per,
         "graph_equals_one_launch": same_graph,
         "precision": "mixed",
+        "tuning": tuned,
     }
 
 
@@ -352,6 +368,22 @@ def run_engine(args, rank, world, local):
     log(f"[bench] C2 setup {time.perf_counter() - t0:.1f}s, "
         f"{sum(len(s.face_ids) for s in model.surfaces)} triangles")
 
+    # ---- autotuner: launch settings picked on a separate sample ----------
+    tuning = {"autotuned": False}
+    if args.autotune:
+        from xdg_gb300.engine import QUERY_RAY_FIRE
+        ps_h, ds_h = c2_rays(min(TUNE_RAYS, N_RAYS), dist.rank_seed(999, rank))
+        ts = torch.from_numpy(lut[x.find_volume(ps_h, ds_h, precision=MIXED)]).to(dev)
+        ps, ds = torch.from_numpy(ps_h).to(dev), torch.from_numpy(ds_h).to(dev)
+        t1 = time.perf_counter()
+        ms_s, tuned = rti.autotune_trace(QUERY_RAY_FIRE, 0, ps, ds, precision=MIXED, ray_trees=ts,
+                                         reps=3)
+        tuning = {"autotuned": True, "trace_sample_rays": len(ps_h),
+                  "trace_seconds": time.perf_counter() - t1, "trace_sample_ms": ms_s,
+                  "trace": {k: tuned[k] for k in TRACE_KEYS}}
+        del ps, ds, ts
+        log(f"[bench] autotune trace {tuning['trace_seconds']:.1f}s: {tuning['trace']}")
+
     def rf(prec, t=t_out, s=s_out, f=f_out):
         def go():
             rc = L.xdgcu_ray_fire(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), N_RAYS,
@@ -365,6 +397,10 @@ def run_engine(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     ms_mixed = timed(torch, rf(MIXED), args.steps, args.warmup, world, stream)
+    # kernels of one timed step: the traversal, plus the order's key kernel and
+    # radix-sort passes when the coherent order is on (it is off unless tuned on)
+    launches_per_step = 1 if rti.get_tuning("trace_sort_min") in (0,) or \
+        N_RAYS < rti.get_tuning("trace_sort_min") else 6
     clk = clocks.stop()
     t_mixed, s_mixed, f_mixed = t_out.clone(), s_out.clone(), f_out.clone()
     ms_fp64 = timed(torch, rf(FP64), max(3, args.steps // 4), max(1, args.warmup // 2), world,
@@ -510,6 +546,16 @@ def run_engine(args, rank, world, local):
     wst = torch.empty(N_TRACKS, dtype=torch.int32, device=dev)
     et = wr.volume_to_point_location_tree[1]
     log(f"[bench] C5 setup {time.perf_counter() - t0:.1f}s")
+    if args.autotune:
+        ss_h, su_h, sl_h = c5_tracks(min(TUNE_TRACKS, N_TRACKS), dist.rank_seed(998, rank))
+        _, sidx = wr.find_element(ss_h, precision=MIXED)
+        sdev = [torch.from_numpy(a).to(dev) for a in (sidx.astype(np.int32), ss_h, su_h, sl_h)]
+        t1 = time.perf_counter()
+        ms_w, wt = wr.rti.autotune_walk(*sdev, max_segs=MAX_SEGS, precision=MIXED, reps=3)
+        tuning.update({"walk_sample_tracks": len(ss_h), "walk_seconds": time.perf_counter() - t1,
+                       "walk_sample_ms": ms_w, "walk": {k: wt[k] for k in WALK_KEYS}})
+        del sdev
+        log(f"[bench] autotune walk {tuning['walk_seconds']:.1f}s: {tuning['walk']}")
 
     def walk(prec, e=seg_e, ln=seg_l, c=seg_c):
         def go():
@@ -622,7 +668,7 @@ def run_engine(args, rank, world, local):
             "frac": achieved / peak,
             "traffic": traffic,
             "peak_kind": f"{peak_kind} HBM copy bandwidth",
-            "kernel": "k_trace<RAY_FIRE, mixed, 3>",
+            "kernel": f"k_trace<RAY_FIRE, mixed, {rti.get_tuning('trace_occupancy')}>",
             "algorithmic_bytes_per_ray": bytes_per_ray,
         },
         "cpu_baseline": cpu_baseline,
@@ -630,7 +676,8 @@ def run_engine(args, rank, world, local):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "matches_device_path": e2e_ok},
         "many_surfaces": many,
-        "gpu_launches": args.steps,
+        "tuning": tuning,
+        "gpu_launches": args.steps * launches_per_step,
         "clocks": clk,
     }
     if rank == 0:
@@ -650,6 +697,8 @@ def main():
     ap.add_argument("--tracks", type=int, default=N_TRACKS, help="walk tracks per GPU")
     ap.add_argument("--no-many", dest="many", action="store_false",
                     help="skip the 256-surface launch comparison")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default launch settings instead of autotuning them")
     args = ap.parse_args()
     set_sizes(args.rays, args.tracks)
     args.warmup = max(3, args.warmup)

@@ -287,6 +287,19 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *   "trace_flush_wait" number of lanes (1..32) whose rays wait only on queued
  *                      FP64 candidate tests before the warp drains a partly
  *                      filled queue
+ *   "trace_stack"      shared-memory traversal stack entries per ray (16..64,
+ *                      steps of 8; default 48).  Deeper stacks take shared
+ *                      memory and so resident blocks; a ray whose traversal
+ *                      needs more gets XDGCU_RAY_STACK_OVERFLOW
+ *   "trace_grab"       0 (default): each warp walks one contiguous slice of
+ *                      the batch fixed at launch; > 0 (a multiple of 32): warps
+ *                      take this many rays at a time from a device work queue,
+ *                      which balances batches of very uneven per-ray cost
+ *   "trace_sort_min"   batches of at least this many rays (default 0 = never)
+ *                      are traversed in a coherent order: sorted on the device
+ *                      by tree, direction octant and the Morton code of the
+ *                      origin.  Results are written at the callers' indices
+ *                      and do not depend on it
  *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4)
  *   "walk_queue"       mixed-precision walk: 1 (default) runs the FP64 face
  *                      tests of a warp's tracks 32 at a time from a per-warp
@@ -300,6 +313,41 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      depend on it. */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);
+
+/* Queries the traversal autotuner can tune for. */
+enum {
+  XDGCU_QUERY_RAY_FIRE = 0,
+  XDGCU_QUERY_POINT_IN_VOLUME = 1,
+  XDGCU_QUERY_OCCLUDED = 2,
+  XDGCU_QUERY_FIND_VOLUME = 3
+};
+
+/* Autotuner of the traversal launch parameters (no counterpart in the
+ * reference).  Runs the sample batch (device arrays; arguments as for the
+ * query, EXITING orientation for ray_fire, no exclusions) under settings of
+ * trace_occupancy, trace_stack, trace_node_iters (or trace_node_iters_fp64
+ * for XDGCU_FP64), trace_flush_wait, trace_grab and, for samples of at least
+ * 65,536 rays, trace_sort_min, one key at a time, and leaves the context set
+ * to the fastest combination found.  Each setting is timed as the median of
+ * `reps` launches after one untimed launch.  Every setting must reproduce
+ * the first run's outputs byte for byte (XDGCU_ERR_STATE otherwise); settings
+ * whose smaller stack overflows are skipped.  When the coherent order wins,
+ * trace_sort_min is set to max(65536, n/4).  best_ms (may be NULL) receives
+ * the sample's time under the chosen settings.  Synchronous; do not run
+ * queries of this context meanwhile. */
+int xdgcu_autotune_trace(xdgcu_ctx* ctx, int32_t query, int32_t tree, const int32_t* ray_trees,
+                         int64_t n, const double* origins, const double* directions,
+                         int32_t precision, int32_t reps, double* best_ms);
+
+/* Autotuner of the walk launch parameters (no counterpart in the reference):
+ * walk_queue (mixed precision only), walk_flush_wait and, for samples of at
+ * least 16,384 tracks, walk_sort_min, on a sample of xdgcu_walk_elements
+ * (device arrays, strided output of max_segs per track allocated by the
+ * tuner).  Same search, timing and result check as xdgcu_autotune_trace;
+ * when the length order wins, walk_sort_min is set to max(16384, n/4). */
+int xdgcu_autotune_walk(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
+                        const double* start, const double* u, const double* distance,
+                        int32_t max_segs, int32_t precision, int32_t reps, double* best_ms);
 
 /* Tree statistics: out[0] = nodes, [1] = primitives, [2] = depth,
  * [3] = bytes of FP32 nodes, [4] = bytes of FP64 nodes. */

@@ -1,0 +1,186 @@
+"""Launch parameters and the autotuner do not change results.
+
+The traversal's work distribution (contiguous slices or the device work
+queue), the coherent ray order, the stack depth, the occupancy variant and
+the node/flush schedule decide only which lane runs which ray when; ids and
+distances must stay bit-identical to the default settings and to the oracle.
+The autotuners must leave the context on settings that reproduce the same
+outputs, and report a positive sample time.
+"""
+import numpy as np
+import pytest
+
+from xdg_gb300 import synth
+from xdg_gb300.engine import (FP64, MIXED, QUERY_FIND_VOLUME, QUERY_POINT_IN_VOLUME,
+                              QUERY_RAY_FIRE, TUNING_KEYS, XDG)
+
+pytestmark = pytest.mark.gpu
+
+SETTINGS = [
+    {},
+    {"trace_grab": 32},
+    {"trace_grab": 256, "trace_sort_min": 1},
+    {"trace_sort_min": 1},
+    {"trace_stack": 64, "trace_occupancy": 2},
+    {"trace_stack": 32, "trace_occupancy": 4, "trace_node_iters": 1, "trace_node_iters_fp64": 4},
+    {"trace_grab": 4096, "trace_node_iters": 16, "trace_flush_wait": 32, "trace_stack": 40},
+    {"trace_flush_wait": 1, "trace_grab": 64},
+]
+
+
+def assert_same(a, b, what):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    bad = np.nonzero(a != b)[0]
+    assert len(bad) == 0, f"{what}: {len(bad)} mismatches, first at {bad[:5]}"
+
+
+@pytest.fixture(scope="module")
+def nested(cuda):
+    m = synth.nested_spheres(n=8, level=3, jitter=1e-3, seed=7)
+    x = XDG(m)
+    x.prepare_raytracer()
+    rng = np.random.default_rng(17)
+    n = 120_000
+    p = rng.uniform(-9, 9, (n, 3))
+    d = synth.isotropic_dirs(rng, n)
+    vols = x.find_volume(p, d)
+    return m, x, p, d, vols
+
+
+def _with(rti, settings):
+    old = rti.tuning()
+    for k, v in settings.items():
+        rti.set_tuning(k, v)
+    return old
+
+
+def _restore(rti, old):
+    for k, v in old.items():
+        rti.set_tuning(k, v)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_settings_do_not_change_results(nested, oracle, prec):
+    """ray_fire with per-ray trees, point_in_volume and find_volume under
+    every setting, host arrays (chunked staging) and device tensors."""
+    import torch
+    m, x, p, d, vols = nested
+    base_t, base_s, base_f = x.ray_fire(vols, p, d, precision=prec)
+    base_in = x.point_in_volume(3, p, precision=prec)
+    base_fv = x.find_volume(p, d, precision=prec)
+    # the default settings agree with the oracle (ascending volume order)
+    sub = slice(0, 20_000)
+    for v in np.unique(vols[sub]):
+        k = np.nonzero(vols[sub] == v)[0]
+        ot, os_, of = oracle.volume_tree(m, int(v)).ray_fire(p[k], d[k])
+        assert_same(base_t[k], ot, f"t vol {v}")
+        assert_same(base_f[k], of, f"face vol {v}")
+    pd, dd = torch.from_numpy(p).cuda(), torch.from_numpy(d).cuda()
+    td = torch.from_numpy(x._trees(vols)).cuda()
+    for st in SETTINGS[1:]:
+        old = _with(x.rti, st)
+        try:
+            t, s, f = x.ray_fire(vols, p, d, precision=prec)
+            assert_same(t, base_t, f"t {st}")
+            assert_same(s, base_s, f"surface {st}")
+            assert_same(f, base_f, f"face {st}")
+            assert_same(x.point_in_volume(3, p, precision=prec), base_in, f"piv {st}")
+            assert_same(x.find_volume(p, d, precision=prec), base_fv, f"find_volume {st}")
+            t2, s2, f2, status = x.rti.ray_fire(0, pd, dd, precision=prec, ray_trees=td,
+                                                status=True)
+            torch.cuda.synchronize()
+            assert int((status != 0).sum()) == 0
+            assert_same(t2.cpu().numpy(), base_t, f"device t {st}")
+            assert_same(f2.cpu().numpy(), base_f, f"device face {st}")
+        finally:
+            _restore(x.rti, old)
+
+
+def test_small_stack_overflow_is_reported(nested):
+    """A 16-entry stack may overflow on deep trees: such rays say so in their
+    status and every other ray keeps its result."""
+    import torch
+    m, x, p, d, vols = nested
+    pd, dd = torch.from_numpy(p).cuda(), torch.from_numpy(d).cuda()
+    td = torch.from_numpy(x._trees(vols)).cuda()
+    t0, s0, f0, st0 = x.rti.ray_fire(0, pd, dd, precision=MIXED, ray_trees=td, status=True)
+    old = _with(x.rti, {"trace_stack": 16})
+    try:
+        t1, s1, f1, st1 = x.rti.ray_fire(0, pd, dd, precision=MIXED, ray_trees=td, status=True)
+    finally:
+        _restore(x.rti, old)
+    st1 = st1.cpu().numpy()
+    assert set(np.unique(st1)) <= {0, 2}
+    ok = st1 == 0
+    assert_same(t1.cpu().numpy()[ok], t0.cpu().numpy()[ok], "t where no overflow")
+    assert_same(f1.cpu().numpy()[ok], f0.cpu().numpy()[ok], "face where no overflow")
+
+
+def test_bad_settings_rejected(nested):
+    _, x, _, _, _ = nested
+    for k, v in [("trace_stack", 12), ("trace_stack", 50), ("trace_stack", 72),
+                 ("trace_grab", 33), ("trace_grab", -32), ("trace_sort_min", -1)]:
+        with pytest.raises(Exception):
+            x.rti.set_tuning(k, v)
+    assert set(x.rti.tuning()) == set(TUNING_KEYS)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_autotune_trace(nested, prec):
+    import torch
+    m, x, p, d, vols = nested
+    pd, dd = torch.from_numpy(p).cuda(), torch.from_numpy(d).cuda()
+    td = torch.from_numpy(x._trees(vols)).cuda()
+    t0, s0, f0 = x.rti.ray_fire(0, pd, dd, precision=prec, ray_trees=td)
+    old = x.rti.tuning()
+    try:
+        ms, tuned = x.rti.autotune_trace(QUERY_RAY_FIRE, 0, pd, dd, precision=prec, ray_trees=td,
+                                         reps=3)
+        assert ms > 0
+        assert tuned["trace_occupancy"] in (2, 3, 4) and tuned["trace_stack"] in (32, 40, 48, 64)
+        t1, s1, f1 = x.rti.ray_fire(0, pd, dd, precision=prec, ray_trees=td)
+        torch.cuda.synchronize()
+        assert torch.equal(t0, t1) and torch.equal(s0, s1) and torch.equal(f0, f1)
+        ms2, _ = x.rti.autotune_trace(QUERY_POINT_IN_VOLUME, 3, pd, None, precision=prec, reps=2)
+        ms3, _ = x.rti.autotune_trace(QUERY_FIND_VOLUME, 0, pd, dd, precision=prec, reps=2)
+        assert ms2 > 0 and ms3 > 0
+    finally:
+        _restore(x.rti, old)
+
+
+def test_autotune_needs_device_sample(nested):
+    m, x, p, d, vols = nested
+    with pytest.raises(Exception, match="device memory"):
+        x.rti.autotune_trace(QUERY_RAY_FIRE, 1, p[:100], d[:100])
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_autotune_walk(cuda, prec):
+    import torch
+    tm = synth.tet_cube(n=16, size=10.0, jitter=0.2, seed=11)
+    m = synth.model_from_tets(tm, np.ones(len(tm.conn), dtype=np.int32))
+    x = XDG(m)
+    x.prepare_raytracer()
+    rng = np.random.default_rng(3)
+    n = 20_000
+    p = rng.uniform(0.01, 9.99, (n, 3))
+    u = synth.isotropic_dirs(rng, n)
+    dist = np.minimum(rng.exponential(5.0, n), 30.0)
+    eid, eidx = x.find_element(p)
+    assert (eidx >= 0).all()
+    dev = [torch.from_numpy(a).cuda() for a in (eidx.astype(np.int32), p, u, dist)]
+    e0, l0, c0, _ = x.rti.walk_elements(*dev, max_segs=256, precision=prec)
+    old = x.rti.tuning()
+    try:
+        ms, tuned = x.rti.autotune_walk(*dev, max_segs=256, precision=prec, reps=3)
+        assert ms > 0
+        e1, l1, c1, _ = x.rti.walk_elements(*dev, max_segs=256, precision=prec)
+        torch.cuda.synchronize()
+        assert torch.equal(c0, c1)
+        c = c0.cpu().numpy()
+        mask = np.arange(256)[None, :] < c[:, None]
+        assert_same(e1.cpu().numpy()[mask], e0.cpu().numpy()[mask], "elements")
+        assert_same(l1.cpu().numpy()[mask], l0.cpu().numpy()[mask], "lengths")
+    finally:
+        _restore(x.rti, old)

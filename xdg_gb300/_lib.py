@@ -25,6 +25,7 @@ RAY_OK, RAY_INVALID, RAY_STACK_OVERFLOW, RAY_WALK_LIMIT, RAY_NO_EXIT_FACE = 0, 1
 RAY_OUTPUT_FULL = 6
 ANY, EXITING, ENTERING = -1, 0, 1
 FP64, MIXED = 0, 1
+QUERY_RAY_FIRE, QUERY_POINT_IN_VOLUME, QUERY_OCCLUDED, QUERY_FIND_VOLUME = 0, 1, 2, 3
 
 # exported symbol -> (restype, argtypes)
 SIGNATURES = {
@@ -58,6 +59,8 @@ SIGNATURES = {
                                                   _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_set_tuning": (_int, [_VP, ctypes.c_char_p, _i64]),
     "xdgcu_get_tuning": (_int, [_VP, ctypes.c_char_p, _I64]),
+    "xdgcu_autotune_trace": (_int, [_VP, _i32, _i32, _VP, _i64, _VP, _VP, _i32, _i32, _D]),
+    "xdgcu_autotune_walk": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _i32, _i32, _D]),
     "xdgcu_set_counting": (_int, [_VP, _i32]),
     "xdgcu_get_counters": (_int, [_VP, _I64]),
     "xdgcu_surface_tree_info": (_int, [_VP, _i32, _I64]),

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libxdgcu.so")
-SOURCES = ["api.cu", "bvh.cu", "noalloc.cu", "queries.cu", "trace.cu", "walk.cu"]
+SOURCES = ["api.cu", "bvh.cu", "noalloc.cu", "order.cu", "queries.cu", "trace.cu", "tune.cu", "walk.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", os.path.join(HERE, "..", "include")]

@@ -316,6 +316,9 @@ struct xdgcu_ctx {
   int32_t trace_node_iters = 4;       // mixed precision
   int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
   int32_t trace_flush_wait = 8;
+  int32_t trace_stack = 48;      // shared-memory stack entries per lane
+  int32_t trace_grab = 0;        // 0: one contiguous chunk per warp; > 0: device work queue
+  int64_t trace_sort_min = 0;    // batches of at least this many rays run in coherent order (0 = never)
   int32_t leaf_max = 4;
   int32_t walk_queue = 1;
   int32_t walk_flush_wait = 8;
@@ -657,6 +660,39 @@ int with_length_order(xdgcu_ctx* c, WalkArgs& a, cudaStream_t s, Body body) {
   return rc;
 }
 
+// Enqueues one traversal launch with the context's work distribution: when
+// the device work queue is on (trace_grab > 0) a zeroed cursor, and when the
+// batch is large enough (trace_sort_min) a coherent ray order, both in one
+// stream-ordered scratch allocation freed after the launch.
+cudaError_t launch_trace(xdgcu_ctx* c, int mode, bool mixed, SurfArgs a, double extent,
+                         cudaStream_t s) {
+  if (a.n <= 0) return cudaSuccess;
+  const bool sort = c->trace_sort_min > 0 && a.n >= c->trace_sort_min && a.n < ((int64_t)1 << 31) &&
+                    extent > 0.0;
+  a.grab = c->trace_grab;
+  a.work = nullptr;
+  a.order = nullptr;
+  if (a.grab == 0 && !sort) return launch_surface_query(mode, mixed, a, s);
+  const size_t ord_bytes = sort ? ((sizeof(int32_t) * (size_t)a.n + 255) & ~(size_t)255) : 0;
+  const size_t scr = sort ? ray_order_scratch_bytes(a.n) : 0;
+  char* buf = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&buf, 256 + ord_bytes + scr, s);
+  if (e != cudaSuccess) return e;
+  if (a.grab > 0) {
+    a.work = (unsigned long long*)buf;
+    e = cudaMemsetAsync(buf, 0, sizeof(unsigned long long), s);
+  }
+  if (e == cudaSuccess && sort) {
+    a.order = (const int32_t*)(buf + 256);
+    const int32_t* trees = (mode == MODE_FIND_VOLUME) ? nullptr : a.ray_trees;
+    e = ray_order(a.org, a.dir, trees, a.n_trees, a.n, extent, (int32_t*)(buf + 256),
+                  buf + 256 + ord_bytes, scr, s);
+  }
+  if (e == cudaSuccess) e = launch_surface_query(mode, mixed, a, s);
+  const cudaError_t f = cudaFreeAsync(buf, s);
+  return e != cudaSuccess ? e : f;
+}
+
 #define CHECK_CTX(c)                                                            \
   do {                                                                          \
     if (!(c)) return set_err(XDGCU_ERR_INVALID_ARG, "null context");            \
@@ -954,6 +990,17 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "trace_flush_wait") {
     if (value < 1 || value > 32) return set_err(XDGCU_ERR_INVALID_ARG, "trace_flush_wait must be 1..32");
     c->trace_flush_wait = (int32_t)value;
+  } else if (k == "trace_stack") {
+    if (value < 16 || value > 64 || value % 8 != 0)
+      return set_err(XDGCU_ERR_INVALID_ARG, "trace_stack must be 16..64 in steps of 8");
+    c->trace_stack = (int32_t)value;
+  } else if (k == "trace_grab") {
+    if (value < 0 || value > (1 << 20) || value % 32 != 0)
+      return set_err(XDGCU_ERR_INVALID_ARG, "trace_grab must be 0 or a multiple of 32 up to 2^20");
+    c->trace_grab = (int32_t)value;
+  } else if (k == "trace_sort_min") {
+    if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "trace_sort_min must be >= 0");
+    c->trace_sort_min = value;
   } else if (k == "leaf_max") {
     if (value < 1 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "leaf_max must be 1..4");
     c->leaf_max = (int32_t)value;
@@ -979,6 +1026,9 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "trace_node_iters") *value = c->trace_node_iters;
   else if (k == "trace_node_iters_fp64") *value = c->trace_node_iters_fp64;
   else if (k == "trace_flush_wait") *value = c->trace_flush_wait;
+  else if (k == "trace_stack") *value = c->trace_stack;
+  else if (k == "trace_grab") *value = c->trace_grab;
+  else if (k == "trace_sort_min") *value = c->trace_sort_min;
   else if (k == "leaf_max") *value = c->leaf_max;
   else if (k == "walk_queue") *value = c->walk_queue;
   else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
@@ -1056,11 +1106,20 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.occupancy = c->trace_occupancy;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
+  a.stack = c->trace_stack;
   a.vol_ids = c->d_vol_ids.p;
   a.vol_trees = c->d_vol_trees.p;
   a.n_vols = c->n_vols;
   a.ipc_volume = c->ipc_volume;
   cudaStream_t st = (cudaStream_t)stream;
+  // origin extent for the coherent ray order: the bounds of the trees queried
+  double extent = 0.0;
+  if (mode == MODE_FIND_VOLUME || ray_trees) {
+    for (auto& t : c->surf_trees) extent = std::max(extent, (double)t->dev.max_abs);
+  } else {
+    extent = (double)c->surf_trees[tree - 1]->dev.max_abs;
+  }
+  const bool mixed = precision == XDGCU_MIXED;
   if (kind == 1) {
     a.ray_trees = ray_trees;
     a.org = org;
@@ -1076,7 +1135,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
     a.status = status;
     int rc = begin_query(c, st, &a.counters);
     if (rc) return rc;
-    API_CUDA(launch_surface_query(mode, precision == XDGCU_MIXED, a, st), "query launch");
+    API_CUDA(launch_trace(c, mode, mixed, a, extent, st), "query launch");
     return XDGCU_OK;
   }
   Slot* s = get_slot(c);
@@ -1117,7 +1176,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
         b.flag_out = (int32_t*)at(R_fl, first);
         b.dist_out = (double*)at(R_d, first);
         b.status = (int32_t*)at(R_st, first);
-        return launch_surface_query(mode, precision == XDGCU_MIXED, b, cs);
+        return launch_trace(c, mode, mixed, b, extent, cs);
       });
 }
 

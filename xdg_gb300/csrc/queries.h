@@ -39,6 +39,10 @@ struct SurfArgs {
   int32_t occupancy;   // traversal kernel variant: minimum resident blocks per SM (2..4)
   int32_t node_iters;  // inner-node steps per lane between leaf phases (1..64)
   int32_t flush_wait;  // lanes waiting on the FP64 queue that force a partial drain (1..32)
+  int32_t stack;       // shared-memory traversal stack entries per lane (16..64, multiple of 8)
+  int32_t grab;        // > 0: warps take rays from the device work queue `work`, `grab` at a time
+  unsigned long long* work;  // work-queue cursor (zero at launch), used when grab > 0
+  const int32_t* order;      // optional ray order (a permutation of 0..n-1), or null
   // MODE_FIND_VOLUME: the volumes tried in order (their surface trees) and
   // the id written when none contains the point; the id goes to flag_out
   const int32_t* vol_ids;
@@ -64,6 +68,14 @@ struct PointArgs {
 };
 
 cudaError_t launch_surface_query(int mode, bool mixed, const SurfArgs& a, cudaStream_t st);
+
+// Coherent ray order (order.cu): order = the ray indices sorted by
+// [tree | direction octant | Morton code of the origin in [-extent, extent]^3].
+// scratch holds ray_order_scratch_bytes(n) bytes; n < 2^31.
+size_t ray_order_scratch_bytes(int64_t n);
+cudaError_t ray_order(const double* org, const double* dir, const int32_t* ray_trees,
+                      int32_t n_trees, int64_t n, double extent, int32_t* order, void* scratch,
+                      size_t scratch_bytes, cudaStream_t st);
 cudaError_t launch_closest(bool mixed, const PointArgs& a, cudaStream_t st);
 cudaError_t launch_find_element(bool mixed, const PointArgs& a, cudaStream_t st);
 

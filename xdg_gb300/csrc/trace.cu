@@ -15,8 +15,14 @@
 //     and the hit bookkeeping of triangle_intersect.cpp:52-109, then each ray
 //     merges its own results (lowest (t, face id) wins, the fixed tie rule);
 //   * a lane whose ray is finished and has nothing queued writes its result
-//     and refills from the warp's contiguous chunk of rays (no global atomics),
-//     so long rays do not hold a whole warp idle.
+//     and refills from the warp's current chunk of rays, so long rays do not
+//     hold a whole warp idle.  Chunks are either one contiguous slice per warp
+//     fixed at launch (no global atomics) or, when `grab` > 0, taken `grab`
+//     rays at a time from a device work queue (one atomicAdd per chunk), which
+//     balances batches whose rays cost very different amounts (many
+//     geometries of uneven size in one launch).  An optional permutation
+//     `order` (rays sorted by tree, direction octant and origin) makes the
+//     rays of a warp coherent; results are written at the original index.
 //
 // Merging candidates evaluated against an older best distance gives the same
 // answer as evaluating them one by one: the Plucker test's tMax only rejects
@@ -33,9 +39,11 @@
 // ray for which 8u(max|coordinate| + |o|_inf) is not below the bump tests FP64
 // boxes instead (checked per ray, `use64`).
 //
-// Stack: 64 entries per lane in shared memory, [entry][thread] so that lanes
-// hit distinct banks; each entry keeps its near distance so entries beyond a
-// closer hit found meanwhile are discarded without fetching the node.
+// Stack: `stack` entries per lane (16..64, a launch parameter) in dynamic
+// shared memory, [entry][thread] so that lanes hit distinct banks; each entry
+// keeps its near distance so entries beyond a closer hit found meanwhile are
+// discarded without fetching the node.  A deeper stack costs shared memory
+// and so resident blocks; overflow ends the ray with RAY_STACK_OVERFLOW.
 #include "traverse.cuh"
 
 namespace xdgcu {
@@ -44,7 +52,7 @@ namespace {
 
 constexpr int kTBlock = 128;
 constexpr int kTWarps = kTBlock / 32;
-constexpr int kTStack = 48;
+constexpr int kTStackMin = 16, kTStackMax = 64;
 constexpr int kQ = 256;  // ring buffer, power of two; at most 31 + 4*32 entries live
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -60,11 +68,11 @@ struct WarpQueue {
   int32_t pad[2];
 };
 
-struct TraceShared {
-  int32_t sref[kTStack][kTBlock];
-  float stn[kTStack][kTBlock];
-  WarpQueue q[kTWarps];
-};
+// Dynamic shared memory: the warp queues, then the stack's references
+// [stack][kTBlock] and near distances [stack][kTBlock].
+__host__ __device__ constexpr size_t trace_smem_bytes(int stack) {
+  return sizeof(WarpQueue) * kTWarps + (size_t)stack * kTBlock * (sizeof(int32_t) + sizeof(float));
+}
 
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
@@ -75,14 +83,18 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 template <int MODE, bool MIXED, int MINB>
 __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chunk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TraceShared& S = *reinterpret_cast<TraceShared*>(smem_raw);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int tx = threadIdx.x;
-  WarpQueue& Q = S.q[wib];
+  WarpQueue& Q = reinterpret_cast<WarpQueue*>(smem_raw)[wib];
+  int32_t* const sref = reinterpret_cast<int32_t*>(smem_raw + sizeof(WarpQueue) * kTWarps);
+  float* const stn = reinterpret_cast<float*>(sref + (size_t)a.stack * kTBlock);
+  const int kstack = a.stack;
+  const bool dyn = a.grab > 0;
   const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int64_t cursor = gwarp * chunk;
-  const int64_t end = min(a.n, cursor + chunk);
+  int64_t cursor = dyn ? 0 : gwarp * chunk;
+  int64_t end = dyn ? 0 : min(a.n, cursor + chunk);
+  bool exhausted = false;  // work queue (grab > 0) has no rays left
   if (lane == 0) {
     Q.head = 0u;
     Q.tail = 0u;
@@ -116,8 +128,8 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
     cur = CHILD_EMPTY;
     while (sp > 0) {
       --sp;
-      const int32_t r = S.sref[sp][tx];
-      const float t = S.stn[sp][tx];
+      const int32_t r = sref[sp * kTBlock + tx];
+      const float t = stn[sp * kTBlock + tx];
       if (t <= bt32) {
         if (ref_is_leaf(r)) {
           leaf_p = leaf_first(r);
@@ -205,10 +217,23 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
     }
     // ---- refill from the warp's chunk ----
     const unsigned need = __ballot_sync(kFull, !has_ray);
+    if (need != 0u && dyn && cursor >= end && !exhausted) {
+      // cursor, end and exhausted are warp-uniform
+      unsigned long long base = 0ull;
+      if (lane == 0) base = atomicAdd(a.work, (unsigned long long)a.grab);
+      base = __shfl_sync(kFull, base, 0);
+      if ((int64_t)base >= a.n) {
+        exhausted = true;
+      } else {
+        cursor = (int64_t)base;
+        end = min(a.n, cursor + (int64_t)a.grab);
+      }
+    }
     if (need != 0u && cursor < end) {
       if (!has_ray) {
-        const int64_t idx = cursor + __popc(need & lanemask_lt());
-        if (idx < end) {
+        const int64_t pos = cursor + __popc(need & lanemask_lt());
+        if (pos < end) {
+          const int64_t idx = a.order ? (int64_t)__ldg(&a.order[pos]) : pos;
           ray = idx;
           has_ray = true;
           status = RAY_OK;
@@ -278,13 +303,13 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
         for (int k = 0; k < 4; ++k) nhit += key[k] < INFINITY ? 1 : 0;
         if (nhit == 0) {
           pop();
-        } else if (sp + nhit - 1 > kTStack) {
+        } else if (sp + nhit - 1 > kstack) {
           status = RAY_STACK_OVERFLOW;
           trav = false;
         } else {
           for (int k = nhit - 1; k >= 1; --k) {
-            S.sref[sp][tx] = cr[k];
-            S.stn[sp][tx] = key[k];
+            sref[sp * kTBlock + tx] = cr[k];
+            stn[sp * kTBlock + tx] = key[k];
             ++sp;
           }
           if (ref_is_leaf(cr[0])) {
@@ -462,17 +487,25 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
 }
 
 int g_num_sms = 0;
-int g_blocks_per_sm[8][3] = {};
+// resident blocks per SM, by kernel variant, MINB and stack depth (8..64 step 8)
+int g_blocks_per_sm[8][3][kTStackMax / 8 + 1] = {};
+bool g_smem_attr[8][3] = {};
 
 template <int MODE, bool MIXED, int MINB>
 cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
-  const size_t smem = sizeof(TraceShared);
+  if (a.stack < kTStackMin || a.stack > kTStackMax || a.stack % 8 != 0) return cudaErrorInvalidValue;
+  if (a.grab > 0 && (a.work == nullptr || a.grab % 32 != 0)) return cudaErrorInvalidValue;
+  const size_t smem = trace_smem_bytes(a.stack);
   auto kern = k_trace<MODE, MIXED, MINB>;
-  int* cache = &g_blocks_per_sm[slot][MINB - 2];
-  if (*cache == 0) {
+  if (!g_smem_attr[slot][MINB - 2]) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+                                         (int)trace_smem_bytes(kTStackMax));
     if (e != cudaSuccess) return e;
+    g_smem_attr[slot][MINB - 2] = true;
+  }
+  int* cache = &g_blocks_per_sm[slot][MINB - 2][a.stack / 8];
+  if (*cache == 0) {
+    cudaError_t e;
     int dev = 0;
     cudaGetDevice(&dev);
     e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -488,7 +521,7 @@ cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks < 1) blocks = 1;
   const int64_t warps = blocks * kTWarps;
-  const int64_t chunk = (a.n + warps - 1) / warps;
+  const int64_t chunk = a.grab > 0 ? 0 : (a.n + warps - 1) / warps;
   kern<<<(unsigned)blocks, kTBlock, smem, st>>>(a, chunk);
   return cudaGetLastError();
 }

@@ -17,6 +17,13 @@ import numpy as np
 
 from . import _lib
 from ._lib import ANY, ENTERING, EXITING, FP64, MIXED, check  # noqa: F401
+from ._lib import (QUERY_FIND_VOLUME, QUERY_OCCLUDED, QUERY_POINT_IN_VOLUME,  # noqa: F401
+                   QUERY_RAY_FIRE)
+
+# keys of xdgcu_set_tuning / xdgcu_get_tuning
+TUNING_KEYS = ("trace_occupancy", "trace_node_iters", "trace_node_iters_fp64",
+               "trace_flush_wait", "trace_stack", "trace_grab", "trace_sort_min", "leaf_max",
+               "walk_queue", "walk_flush_wait", "walk_sort_min")
 
 INFTY = np.finfo(np.float64).max
 TINY_BIT = 1e-10  # constants.h:32
@@ -246,6 +253,38 @@ class CudaRayTracer:
         v = ctypes.c_int64()
         self._check(self.L.xdgcu_get_tuning(self.ctx, key.encode(), ctypes.byref(v)), "get_tuning")
         return int(v.value)
+
+    def tuning(self) -> dict:
+        """Every tuning key with its current value."""
+        return {k: self.get_tuning(k) for k in TUNING_KEYS}
+
+    def autotune_trace(self, query, tree, origins, dirs=None, precision=MIXED, ray_trees=None,
+                       reps=5):
+        """xdgcu_autotune_trace on a sample batch (torch CUDA tensors).  Leaves
+        the context tuned; returns (sample ms under the chosen settings,
+        tuning dict)."""
+        o = _prep(origins, np.float64, 3)
+        d = _prep(dirs, np.float64, 3)
+        rt = _prep(ray_trees, np.int32)
+        ms = ctypes.c_double()
+        self._check(self.L.xdgcu_autotune_trace(self.ctx, int(query), int(tree or 0), _addr(rt),
+                                                o.shape[0], _addr(o), _addr(d), int(precision),
+                                                int(reps), ctypes.byref(ms)), "autotune_trace")
+        return ms.value, self.tuning()
+
+    def autotune_walk(self, start_index, start, u, distance, max_segs=256, precision=MIXED,
+                      reps=5):
+        """xdgcu_autotune_walk on a sample of tracks (torch CUDA tensors)."""
+        si = _prep(start_index, np.int32)
+        r = _prep(start, np.float64, 3)
+        uu = _prep(u, np.float64, 3)
+        dist = _prep(distance, np.float64)
+        ms = ctypes.c_double()
+        self._check(self.L.xdgcu_autotune_walk(self.ctx, si.shape[0], _addr(si), _addr(r),
+                                               _addr(uu), _addr(dist), int(max_segs),
+                                               int(precision), int(reps), ctypes.byref(ms)),
+                    "autotune_walk")
+        return ms.value, self.tuning()
 
     def set_counting(self, on: bool):
         self._check(self.L.xdgcu_set_counting(self.ctx, 1 if on else 0), "set_counting")
