@@ -55,6 +55,11 @@ TRACE_KEYS = ("trace_occupancy", "trace_stack", "trace_node_iters", "trace_node_
               "trace_flush_wait", "trace_grab", "trace_sort_min")
 WALK_KEYS = ("walk_queue", "walk_flush_wait", "walk_sort_min")
 CPU_SAMPLE = 4_000_000      # rays of the same workload timed on the host cores
+TRANSPORT_WORKLOAD = "tet_cube_50^3x6_kuhn_jitter0.2_1e6_particles_mfp1_walk_elements_tool"
+MFP = 1.0                   # tools/walk_elements.cpp: --mfp default
+MAX_EVENTS = 1_000_000
+TRANSPORT_CHECK = 2_000     # particles checked bit for bit against the oracle
+TRANSPORT_CPU_SAMPLE = 50_000
 REF_STEP_SAMPLE = 1_000_000  # rays per step of --impl reference
 BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
 BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
@@ -335,6 +340,83 @@ def bench_many_surfaces(torch, L, dev, stream, args, rank, world):
     }
 
 
+def bench_transport(torch, L, wr, dev, stream, sptr, ws, wu, we_idx, tm, args, rank, world):
+    """The walk_elements tool loop (tools/walk_elements.h:60-96) on the
+    750,000-tet cube: the walk's 1e6 track starts as particle sources,
+    isotropic directions, mean free path 1 (the tool's default), every event
+    of every particle until it leaves the mesh (a convex mesh: no re-entry)
+    in one xdgcu_transport_elements launch per step.  A step also resets the
+    particle state from the sources (device copies, ~60 MB)."""
+    from xdg_gb300 import _lib
+    from xdg_gb300.engine import FP64, MIXED
+    n = int(we_idx.numel())
+    seeds_h = wr.rti.seed_streams(dist.rank_seed(2024, rank), n)
+    s0 = torch.from_numpy(seeds_h.view(np.int64)).to(dev)
+    e = torch.empty_like(we_idx)
+    r = torch.empty_like(ws)
+    u = torch.empty_like(wu)
+    s = torch.empty_like(s0)
+    d = torch.empty(n, dtype=torch.float64, device=dev)
+    ev = torch.empty(n, dtype=torch.int32, device=dev)
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def step(prec):
+        def go():
+            e.copy_(we_idx)
+            r.copy_(ws)
+            u.copy_(wu)
+            s.copy_(s0)
+            d.zero_()
+            ev.zero_()
+            rc = L.xdgcu_transport_elements(
+                wr.rti.ctx, n, ctypes.c_void_p(e.data_ptr()), ctypes.c_void_p(r.data_ptr()),
+                ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(s.data_ptr()), MFP, MAX_EVENTS,
+                ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(ev.data_ptr()), None,
+                ctypes.c_void_p(st.data_ptr()), prec, sptr)
+            _lib.check(rc, wr.rti.ctx, "transport_elements")
+        return go
+
+    ms = timed(torch, step(MIXED), max(3, args.steps // 2), args.warmup, world, stream)
+    events = int(ev.sum().item())
+    bad = int((st != 0).sum().item())
+    mixed_state = [x.clone() for x in (e, r, u, s, d, ev)]
+    ms64 = timed(torch, step(FP64), 3, 1, world, stream)
+    mism = sum(int((a != b).reshape(n, -1).any(1).sum().item())
+               for a, b in zip(mixed_state, (e, r, u, s, d, ev)))
+    total = dist.sum_over_ranks(events, world)
+    out = {
+        "workload": TRANSPORT_WORKLOAD, "unit": "Mevents/s",
+        "value": total / (ms / 1e3) / 1e6, "fp64_value": total / (ms64 / 1e3) / 1e6,
+        "ms_per_step": ms, "fp64_ms_per_step": ms64, "particles": n, "events": events,
+        "events_per_particle": events / n, "speedup_mixed_vs_fp64": ms64 / ms,
+        "particles_differing_mixed_vs_fp64": mism, "particles_with_status": bad,
+        "step": "reset sources + one xdgcu_transport_elements launch (all events)",
+    }
+    if rank == 0 and not args.no_oracle:
+        from oracle import oracle as xo
+        walker = xo.TetWalker(tm.vertices, tm.conn, tm.adj, tm.face_table)
+        k = min(TRANSPORT_CHECK, n)
+        o = walker.transport(we_idx[:k].cpu().numpy(), ws[:k].cpu().numpy(),
+                             wu[:k].cpu().numpy(), seeds_h[:k], MFP, MAX_EVENTS)
+        got = [x[:k].cpu().numpy() for x in mixed_state]
+        got[3] = got[3].view(np.uint64)
+        out["oracle_check"] = {"particles": k, "mismatches": int(sum(
+            int((np.asarray(a) != np.asarray(b)).reshape(k, -1).any(1).sum())
+            for a, b in zip(got, o[:6])))}
+        # CPU baseline: the oracle's particle loop on every host core
+        kc = min(TRANSPORT_CPU_SAMPLE, n)
+        cores = os.cpu_count() or 1
+        tc = time.perf_counter()
+        oc = walker.transport(we_idx[:kc].cpu().numpy(), ws[:kc].cpu().numpy(),
+                              wu[:kc].cpu().numpy(), seeds_h[:kc], MFP, MAX_EVENTS,
+                              threads=cores)
+        dtc = time.perf_counter() - tc
+        out["cpu_baseline"] = {"value": float(oc[5].sum()) / dtc / 1e6, "unit": "Mevents/s",
+                               "cores": cores, "kind": "port",
+                               "sample": f"first {kc} particles, FP64 particle loop, OpenMP"}
+    return out
+
+
 def run_engine(args, rank, world, local):
     import torch
 
@@ -589,6 +671,10 @@ def run_engine(args, rank, world, local):
     walk_len_mism = int(((seg_l64 != seg_l) & valid).sum().item())
     del seg_e64, seg_l64
 
+    # ---- device particle loop (walk_elements tool) over the same mesh ------
+    transport = bench_transport(torch, L, wr, dev, stream, sptr, ws, wu, we_idx, tm, args, rank,
+                                world)
+
     # ---- many surfaces: one launch vs one launch per volume vs CUDA graph -----
     many = bench_many_surfaces(torch, L, dev, stream, args, rank, world) if args.many else None
 
@@ -675,6 +761,7 @@ def run_engine(args, rank, world, local):
         "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "matches_device_path": e2e_ok},
+        "transport": transport,
         "many_surfaces": many,
         "tuning": tuning,
         "gpu_launches": args.steps * launches_per_step,

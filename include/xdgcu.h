@@ -61,7 +61,9 @@ enum {
   XDGCU_RAY_STACK_OVERFLOW = 2, /* traversal stack exhausted (result incomplete) */
   XDGCU_RAY_WALK_LIMIT = 4,     /* walk stopped at max_segs (output truncated) */
   XDGCU_RAY_NO_EXIT_FACE = 5,   /* next_element found no exiting face */
-  XDGCU_RAY_OUTPUT_FULL = 6     /* packed walk output capacity exceeded */
+  XDGCU_RAY_OUTPUT_FULL = 6,    /* packed walk output capacity exceeded */
+  XDGCU_RAY_EVENT_LIMIT = 7,    /* particle stopped at max_events */
+  XDGCU_RAY_LOST = 8            /* particle found no surface ahead (particle_sim's "lost") */
 };
 
 /* shared_enums.h:11-15 */
@@ -238,6 +240,39 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* ctx, int64_t n, const int32_t* start_i
                                int32_t max_segs, int64_t capacity, int32_t* seg_elem,
                                double* seg_len, int64_t* offsets, int32_t* status,
                                int32_t precision, void* stream);
+
+/* Fills states[0..n) (host memory) with independent random stream states
+ * for the particle loops: SplitMix64's output function of
+ * seed + (i + 1) * 0x9E3779B97F4A7C15.  No counterpart in the reference,
+ * which draws from one drand48() stream. */
+int xdgcu_seed_streams(uint64_t seed, int64_t n, uint64_t* states);
+
+/* The particle loop of the walk_elements tool (tools/walk_elements.h:73-95)
+ * on the device, for particles inside the tet mesh: one call runs every
+ * event of every particle until it leaves the mesh or reaches max_events.
+ * Per event: (next, exit) = next_element(elem, r, u); a collision distance
+ * c = -log(1 - U) * mean_free_path; if c < exit the particle moves c and
+ * takes a new isotropic direction, else it moves to the exit face and into
+ * the next tet; events += 1.  The state is read and written back in place:
+ *   elem_index  tet index (-1 = outside the mesh: the particle is skipped);
+ *               on return -1 for particles that left the mesh
+ *   position, direction (n x 3), distance (path length so far), events;
+ *   rng_state   per-particle random stream state (SplitMix64; seed each
+ *               particle differently, e.g. with xdgcu_seed_streams).
+ * Random numbers come from each particle's own stream, not from the tool's
+ * shared drand48(), and directions are sampled by Marsaglia's method instead
+ * of rand_dir's acos/sin/cos (the same isotropic distribution), so every
+ * particle's history is reproducible.  elem_tally (may be NULL): n_tets
+ * doubles, each event adds its length to the tet it was made in (atomic
+ * additions, summation order not fixed).  status: XDGCU_RAY_OK (left the
+ * mesh, or was outside it), XDGCU_RAY_EVENT_LIMIT, XDGCU_RAY_INVALID.
+ * Re-entry after leaving the mesh (the tool's ray_fire in the implicit
+ * complement and find_element, :88-94) is the caller's: then call again. */
+int xdgcu_transport_elements(xdgcu_ctx* ctx, int64_t n, int32_t* elem_index, double* position,
+                             double* direction, uint64_t* rng_state, double mean_free_path,
+                             int32_t max_events, double* distance, int32_t* events,
+                             double* elem_tally, int32_t* status, int32_t precision,
+                             void* stream);
 
 /* Largest batch of xdgcu_walk_elements_packed_noalloc. */
 #define XDGCU_NOALLOC_MAX_TRACKS 4194304

@@ -83,6 +83,18 @@ def lib():
         L.xo_next_element.restype = _int
         L.xo_next_element.argtypes = [_VP, _i32, _D, _D, _I, _D]
         L.xo_walk_elements.argtypes = [_VP, _i64, _I, _D, _D, _D, _i32, _I, _D, _I, _I, _int]
+        _U64 = ctypes.POINTER(ctypes.c_uint64)
+        L.xo_uniform.restype = _dbl
+        L.xo_uniform.argtypes = [_U64]
+        L.xo_series_log.restype = _dbl
+        L.xo_series_log.argtypes = [_dbl]
+        L.xo_sample_collision.restype = _dbl
+        L.xo_sample_collision.argtypes = [_U64, _dbl]
+        L.xo_sample_direction.argtypes = [_U64, _D]
+        L.xo_transport_elements.argtypes = [_VP, _i64, _I, _D, _D, _U64, _dbl, _i32, _D, _I, _D,
+                                            _I, _int]
+        L.xo_walk_particles.argtypes = [_VP, _VP, _VP, _i64, _I, _D, _D, _U64, _dbl, _i32, _D,
+                                        _I, _I, _int]
         _lib = L
     return _lib
 
@@ -309,6 +321,59 @@ class TetWalker:
                                max_segs, _p(el, _I), _p(ln, _D), _p(cnt, _I), _p(st, _I),
                                threads or n_threads_default())
         return el, ln, cnt, st
+
+
+    def transport(self, elem, pos, dirs, rng, mfp, max_events, distance=None, events=None,
+                  n_tets=None, threads=1):
+        """xo_transport_elements on copies of the state; returns (elem, pos,
+        dir, rng, distance, events, status, tally)."""
+        U64 = ctypes.POINTER(ctypes.c_uint64)
+        e = _i32a(elem).copy()
+        n = len(e)
+        r, u = _f64(pos, (-1, 3)).copy(), _f64(dirs, (-1, 3)).copy()
+        s = np.ascontiguousarray(rng, dtype=np.uint64).copy()
+        d = np.zeros(n) if distance is None else _f64(distance).copy()
+        ev = np.zeros(n, dtype=np.int32) if events is None else _i32a(events).copy()
+        st = np.zeros(n, dtype=np.int32)
+        tally = np.zeros(int(n_tets if n_tets is not None else self._keep[1].shape[0]))
+        lib().xo_transport_elements(self.h, n, _p(e, _I), _p(r, _D), _p(u, _D), _p(s, U64),
+                                    float(mfp), int(max_events), _p(d, _D), _p(ev, _I),
+                                    _p(tally, _D), _p(st, _I), int(threads))
+        return e, r, u, s, d, ev, st, tally
+
+    def walk_particles(self, ipc_tree, elem_tree, elem, pos, dirs, rng, mfp, max_events,
+                       threads=None):
+        """xo_walk_particles (the whole walk_elements tool loop); returns
+        (elem, pos, dir, rng, distance, events, status)."""
+        U64 = ctypes.POINTER(ctypes.c_uint64)
+        e = _i32a(elem).copy()
+        n = len(e)
+        r, u = _f64(pos, (-1, 3)).copy(), _f64(dirs, (-1, 3)).copy()
+        s = np.ascontiguousarray(rng, dtype=np.uint64).copy()
+        d = np.zeros(n)
+        ev = np.zeros(n, dtype=np.int32)
+        st = np.zeros(n, dtype=np.int32)
+        lib().xo_walk_particles(self.h, ipc_tree.h, elem_tree.h, n, _p(e, _I), _p(r, _D),
+                                _p(u, _D), _p(s, U64), float(mfp), int(max_events), _p(d, _D),
+                                _p(ev, _I), _p(st, _I), threads or n_threads_default())
+        return e, r, u, s, d, ev, st
+
+
+def series_log(x):
+    return lib().xo_series_log(float(x))
+
+
+def sample_streams(states, draws):
+    """`draws` uniforms from each stream (for tests of the generator)."""
+    U64 = ctypes.POINTER(ctypes.c_uint64)
+    st = np.ascontiguousarray(states, dtype=np.uint64).copy()
+    out = np.zeros((len(st), draws))
+    one = np.zeros(1, dtype=np.uint64)
+    for i in range(len(st)):
+        one[0] = st[i]
+        for k in range(draws):
+            out[i, k] = lib().xo_uniform(_p(one, U64))
+    return out
 
 
 class RefWalker:

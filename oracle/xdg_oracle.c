@@ -905,4 +905,168 @@ void xo_walk_elements(const xo_tetmesh* m, int64_t n, const int32_t* start_elem,
   }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Particle loops                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* SplitMix64 (Steele, Lea & Flood, OOPSLA 2014): the per-particle stream */
+static inline uint64_t splitmix_next(uint64_t* s) {
+  *s += 0x9E3779B97F4A7C15ull;
+  uint64_t z = *s;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+double xo_uniform(uint64_t* s) { return (double)(splitmix_next(s) >> 11) * 1.1102230246251565e-16; }
+
+/* log x = e ln2 + 2 atanh(s), s = (m-1)/(m+1), m in [sqrt(1/2), sqrt(2)),
+ * atanh by its Taylor series to s^23 (x positive and normal) */
+double xo_series_log(double x) {
+  uint64_t b;
+  memcpy(&b, &x, sizeof b);
+  int e = (int)((b >> 52) & 0x7ff) - 1023;
+  uint64_t mb = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
+  double m;
+  memcpy(&m, &mb, sizeof m);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double z = s * s;
+  double p = 1.0 / 23.0;
+  p = p * z + 1.0 / 21.0;
+  p = p * z + 1.0 / 19.0;
+  p = p * z + 1.0 / 17.0;
+  p = p * z + 1.0 / 15.0;
+  p = p * z + 1.0 / 13.0;
+  p = p * z + 1.0 / 11.0;
+  p = p * z + 1.0 / 9.0;
+  p = p * z + 1.0 / 7.0;
+  p = p * z + 1.0 / 5.0;
+  p = p * z + 1.0 / 3.0;
+  const double l = (s + s * z * p) * 2.0;
+  const double hi = 0.6931471801362932, lo = 4.236521365809284e-10;
+  const double de = (double)e;
+  return de * hi + (de * lo + l);
+}
+
+/* tools/walk_elements.h:79: -std::log(1.0 - drand48()) * mean_free_path */
+double xo_sample_collision(uint64_t* s, double mfp) { return -xo_series_log(1.0 - xo_uniform(s)) * mfp; }
+
+/* Marsaglia (1972) in place of rand_dir (vec3da.h:170-176), then normalize */
+void xo_sample_direction(uint64_t* s, double out[3]) {
+  double x1 = 0.0, x2 = 0.0, q = 0.0;
+  int ok = 0;
+  for (int k = 0; k < 64 && !ok; ++k) {
+    x1 = 2.0 * xo_uniform(s) - 1.0;
+    x2 = 2.0 * xo_uniform(s) - 1.0;
+    q = x1 * x1 + x2 * x2;
+    ok = q < 1.0 && q > 0.0;
+  }
+  if (!ok) {
+    out[0] = 0.0; out[1] = 0.0; out[2] = 1.0;
+    return;
+  }
+  const double w = 2.0 * sqrt(1.0 - q);
+  v3 d = {x1 * w, x2 * w, 1.0 - 2.0 * q};
+  d = normalize(d);
+  out[0] = d.x; out[1] = d.y; out[2] = d.z;
+}
+
+/* one event of tools/walk_elements.h:75-87 inside the mesh; returns 0 to go
+ * on, else a status (particle stops) */
+static int transport_event(const xo_tetmesh* m, int32_t* elem, v3* r, v3* u, uint64_t* rng,
+                           double mfp, double* distance, double* tally) {
+  int32_t nxt;
+  double ex;
+  next_element(m, *elem, *r, *u, &nxt, &ex);
+  const double c = xo_sample_collision(rng, mfp);
+  if (c < ex) {
+    *r = add(*r, scl(c, *u));
+    *distance += c;
+    if (tally) {
+#pragma omp atomic
+      tally[*elem] += c;
+    }
+    double d[3];
+    xo_sample_direction(rng, d);
+    *u = mk(d);
+    return 0;
+  }
+  if (ex >= XO_INFTY) return XO_NO_EXIT_FACE;
+  *r = add(*r, scl(ex, *u));
+  *distance += ex;
+  if (tally) {
+#pragma omp atomic
+    tally[*elem] += ex;
+  }
+  *elem = nxt;
+  return 0;
+}
+
+void xo_transport_elements(const xo_tetmesh* m, int64_t n, int32_t* elem, double* pos,
+                           double* dir, uint64_t* rng, double mfp, int32_t max_events,
+                           double* distance, int32_t* events, double* tally,
+                           int32_t* status, int n_threads) {
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads > 0 ? n_threads : 1)
+  for (int64_t i = 0; i < n; ++i) {
+    v3 r = mk(pos + 3 * i), u = mk(dir + 3 * i);
+    int32_t e = elem[i];
+    int st = XO_OK;
+    while (e >= 0) {
+      if (events[i] >= max_events) { st = XO_EVENT_LIMIT; break; }
+      st = transport_event(m, &e, &r, &u, &rng[i], mfp, &distance[i], tally);
+      if (st) break;
+      events[i]++;
+    }
+    elem[i] = e;
+    pos[3 * i] = r.x; pos[3 * i + 1] = r.y; pos[3 * i + 2] = r.z;
+    dir[3 * i] = u.x; dir[3 * i + 1] = u.y; dir[3 * i + 2] = u.z;
+    if (status) status[i] = st;
+  }
+}
+
+void xo_walk_particles(const xo_tetmesh* m, const xo_tree* ipc, const xo_tree* etree, int64_t n,
+                       int32_t* elem, double* pos, double* dir, uint64_t* rng, double mfp,
+                       int32_t max_events, double* distance, int32_t* events, int32_t* status,
+                       int n_threads) {
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads > 0 ? n_threads : 1)
+  for (int64_t i = 0; i < n; ++i) {
+    v3 r = mk(pos + 3 * i), u = mk(dir + 3 * i);
+    int32_t e = elem[i];
+    int st = XO_OK;
+    int32_t prims[64];
+    int32_t nprim = 0;
+    while (e != XO_ID_NONE) {  /* :73 */
+      if (events[i] >= max_events) { st = XO_EVENT_LIMIT; break; }
+      st = transport_event(m, &e, &r, &u, &rng[i], mfp, &distance[i], NULL);
+      if (st) break;
+      /* :88-94 re-entry through the implicit complement */
+      while (e == XO_ID_NONE) {
+        double o[3] = {r.x, r.y, r.z}, d[3] = {u.x, u.y, u.z}, t;
+        int32_t off[2] = {0, nprim}, surf, face;
+        xo_ray_fire(ipc, 1, o, d, NULL, XO_EXITING, off, prims, &t, &surf, &face, 1);
+        if (surf == XO_ID_NONE) break;
+        r = add(r, scl(t, u)); /* r += u * ray_hit.first */
+        distance[i] += t;
+        if (nprim < 64) prims[nprim++] = face; /* ray_fire appends the hit to primitives */
+        const v3 q = add(r, scl(1e-10, u)); /* r + u*TINY_BIT */
+        double qq[3] = {q.x, q.y, q.z};
+        int32_t id, idx;
+        xo_find_element(etree, 1, qq, &id, &idx, 1);
+        e = idx;
+        if (nprim >= 64 && e == XO_ID_NONE) break;
+      }
+      nprim = 0; /* primitives.clear() */
+      events[i]++;
+    }
+    elem[i] = e;
+    pos[3 * i] = r.x; pos[3 * i + 1] = r.y; pos[3 * i + 2] = r.z;
+    dir[3 * i] = u.x; dir[3 * i + 1] = u.y; dir[3 * i + 2] = u.z;
+    if (status) status[i] = st;
+  }
+}
+
 int xo_version(void) { return 1; }

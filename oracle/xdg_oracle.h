@@ -38,6 +38,8 @@ enum {
   XO_OK = 0,
   XO_WALK_LIMIT = 4,     /* walk stopped at the caller's segment capacity */
   XO_NO_EXIT_FACE = 5,   /* next_element found no exiting face */
+  XO_EVENT_LIMIT = 7,    /* particle stopped at max_events */
+  XO_LOST = 8,           /* particle_sim: no surface ahead */
 };
 
 /* ---- single-primitive kernels ------------------------------------------ */
@@ -144,6 +146,39 @@ void xo_walk_elements(const xo_tetmesh* mesh, int64_t n, const int32_t* start_el
                       const double* start, const double* u, const double* distance,
                       int32_t max_segs, int32_t* seg_elem, double* seg_len,
                       int32_t* seg_count, int32_t* status, int n_threads);
+
+/* ---- particle loops ------------------------------------------------------ */
+
+/* Random sampling of the engine's particle loops (the engine gives each
+ * particle its own SplitMix64 stream where the reference tools share one
+ * drand48() stream): uniform in [0,1), -log(1-U)*mfp with the series
+ * logarithm, Marsaglia isotropic direction + Vec3da::normalize. */
+double xo_uniform(uint64_t* state);
+double xo_series_log(double x);
+double xo_sample_collision(uint64_t* state, double mfp);
+void xo_sample_direction(uint64_t* state, double dir[3]);
+
+/* The in-mesh part of the walk_elements tool loop (tools/walk_elements.h:
+ * 73-87): per particle, events until it leaves the mesh (elem = -1) or
+ * reaches max_events (XO_EVENT_LIMIT).  State arrays are updated in place;
+ * tally (may be NULL) gets each event's length added to its tet. */
+void xo_transport_elements(const xo_tetmesh* mesh, int64_t n, int32_t* elem, double* pos,
+                           double* dir, uint64_t* rng, double mfp, int32_t max_events,
+                           double* distance, int32_t* events, double* tally,
+                           int32_t* status, int n_threads);
+
+/* The whole walk_elements tool loop (tools/walk_elements.h:60-96) for
+ * particles that start in tet elem[i]: the in-mesh loop above, and after
+ * leaving the mesh the re-entry search -- ray_fire in the implicit
+ * complement's tree (EXITING, the hit faces of this search excluded), move
+ * to the hit, find_element(r + u*TINY_BIT) in elem_tree -- repeated until an
+ * element is found or nothing is hit (the particle ends).  events counts one
+ * per loop iteration as the tool does; elem_tree's primitive index must be
+ * the tet index. */
+void xo_walk_particles(const xo_tetmesh* mesh, const struct xo_tree* ipc_tree,
+                       const struct xo_tree* elem_tree, int64_t n, int32_t* elem, double* pos,
+                       double* dir, uint64_t* rng, double mfp, int32_t max_events,
+                       double* distance, int32_t* events, int32_t* status, int n_threads);
 
 /* Library self-description for tests. */
 int xo_version(void);

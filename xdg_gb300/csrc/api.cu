@@ -1550,4 +1550,95 @@ int xdgcu_walk_elements(xdgcu_ctx* c, int64_t n, const int32_t* start_index, con
                     seg_count, nullptr, nullptr, status, precision, stream);
 }
 
+// ---------------------------------------------------------------------------
+// device particle loop over the tet mesh
+// ---------------------------------------------------------------------------
+
+int xdgcu_seed_streams(uint64_t seed, int64_t n, uint64_t* states) {
+  if (n < 0 || (n > 0 && !states)) return set_err(XDGCU_ERR_INVALID_ARG, "bad seed arguments");
+  for (int64_t i = 0; i < n; ++i) {
+    // SplitMix64's output function applied to seed + (i + 1) * golden gamma
+    uint64_t z = seed + (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    states[i] = z ^ (z >> 31);
+  }
+  return XDGCU_OK;
+}
+
+int xdgcu_transport_elements(xdgcu_ctx* c, int64_t n, int32_t* elem_index, double* position,
+                             double* direction, uint64_t* rng_state, double mean_free_path,
+                             int32_t max_events, double* distance, int32_t* events,
+                             double* elem_tally, int32_t* status, int32_t precision,
+                             void* stream) {
+  CHECK_CTX(c);
+  if (n < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative particle count");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (!c->has_tets) return set_err(XDGCU_ERR_STATE, "no tet mesh set");
+  if (!(mean_free_path > 0.0) || !(mean_free_path < 1e300))
+    return set_err(XDGCU_ERR_INVALID_ARG, "mean_free_path must be positive and finite");
+  if (max_events < 0) return set_err(XDGCU_ERR_INVALID_ARG, "max_events must be >= 0");
+  if (n == 0) return XDGCU_OK;
+  if (!elem_index || !position || !direction || !rng_state || !distance || !events)
+    return set_err(XDGCU_ERR_INVALID_ARG, "null particle state");
+  const int kind = classify({elem_index, position, direction, rng_state, distance, events,
+                             elem_tally, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  TransportArgs t{};
+  WalkArgs& a = t.mesh;
+  a.xyz = c->d_xyz.p;
+  a.xyz32 = c->d_xyz32.p;
+  a.conn = c->d_conn.p;
+  a.adj = c->d_adj.p;
+  a.elem_ids = c->d_elem_ids.p;
+  a.n_tets = (int32_t)c->n_tet;
+  std::memcpy(a.face, c->face, sizeof(a.face));
+  t.n = n;
+  t.mfp = mean_free_path;
+  t.max_events = max_events;
+  const bool mixed = precision == XDGCU_MIXED;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 1) {
+    t.elem = elem_index;
+    t.pos = position;
+    t.dir = direction;
+    t.rng = (unsigned long long*)rng_state;
+    t.distance = distance;
+    t.events = events;
+    t.tally = elem_tally;
+    t.status = status;
+    int rc = begin_query(c, st, &t.counters);
+    if (rc) return rc;
+    API_CUDA(launch_transport(mixed, c->face_order, t, st), "transport launch");
+    return XDGCU_OK;
+  }
+  Slot* s = get_slot(c);
+  if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  if (!st) st = s->stream;
+  // the particle state is read and written back: copied in and out
+  Arr A_e{elem_index, elem_index, sizeof(int32_t) * n};
+  Arr A_p{position, position, sizeof(double) * 3 * n}, A_d{direction, direction, sizeof(double) * 3 * n};
+  Arr A_r{rng_state, rng_state, sizeof(uint64_t) * n};
+  Arr A_l{distance, distance, sizeof(double) * n};
+  Arr A_v{events, events, sizeof(int32_t) * n};
+  Arr A_t{elem_tally, elem_tally, elem_tally ? sizeof(double) * c->n_tet : 0};
+  Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
+  std::vector<Arr*> all = {&A_e, &A_p, &A_d, &A_r, &A_l, &A_v, &A_t, &A_st};
+  int rc = stage_in(s, all, st);
+  if (rc) return rc;
+  t.elem = (int32_t*)A_e.dev;
+  t.pos = (double*)A_p.dev;
+  t.dir = (double*)A_d.dev;
+  t.rng = (unsigned long long*)A_r.dev;
+  t.distance = (double*)A_l.dev;
+  t.events = (int32_t*)A_v.dev;
+  t.tally = (double*)A_t.dev;
+  t.status = (int32_t*)A_st.dev;
+  rc = begin_query(c, st, &t.counters);
+  if (rc) return rc;
+  API_CUDA(launch_transport(mixed, c->face_order, t, st), "transport launch");
+  return stage_out(all, st);
+}
+
 }  // extern "C"

@@ -84,6 +84,8 @@ enum : int32_t {
   RAY_WALK_LIMIT = 4,
   RAY_NO_EXIT_FACE = 5,
   RAY_OUTPUT_FULL = 6,
+  RAY_EVENT_LIMIT = 7,
+  RAY_LOST = 8,
 };
 
 // work counters (xdgcu_get_counters)

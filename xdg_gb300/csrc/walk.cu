@@ -27,6 +27,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include "internal.cuh"
+#include "sample.cuh"
 
 namespace xdgcu {
 
@@ -785,6 +786,155 @@ cudaError_t launch_walk(bool mixed, int face_order, const WalkArgs& a, cudaStrea
     case 1: return q ? launch_walk_t<0, true, true>(a, st) : launch_walk_t<0, true, false>(a, st);
     case 2: return launch_walk_t<1, false, false>(a, st);
     default: return q ? launch_walk_t<1, true, true>(a, st) : launch_walk_t<1, true, false>(a, st);
+  }
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Device particle loop over the tet mesh: the body of the walk_elements tool
+// (tools/walk_elements.h:73-95) for particles inside the mesh.  Per event:
+//   (next, exit) = next_element(elem, r, u)             (next_face above)
+//   c = -log(1 - U) * mfp                                (sample.cuh)
+//   c < exit: r += u c, distance += c, u = new isotropic direction
+//   else:     r += u exit, distance += exit, elem = next
+//   events++
+// until the particle leaves the mesh (elem = -1, status OK: the caller
+// decides on re-entry, which the tool does by ray_fire in the implicit
+// complement and find_element, :88-94) or reaches max_events
+// (RAY_EVENT_LIMIT).  With `tally`, each event adds its path length to the
+// tet it was made in (atomicAdd, so the sums' rounding depends on the order).
+// Warps own contiguous chunks of particles and refill lanes as particles
+// finish, as in k_walk.
+// ---------------------------------------------------------------------------
+
+template <int FO, bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t chunk) {
+  const WalkArgs& a = t.mesh;
+  const int lane = threadIdx.x & 31;
+  const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int64_t cursor = gwarp * chunk;
+  const int64_t end = min(t.n, cursor + chunk);
+  StepCnt cnt = {0, 0};
+  unsigned long long parts = 0;
+  bool has = false;
+  int64_t i = 0;
+  d3 r = mk3(0, 0, 0), u = mk3(0, 0, 0);
+  double dist = 0.0;
+  int32_t elem = -1, ev = 0, st = RAY_OK;
+  unsigned long long rs = 0;
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, !has);
+    if (need != 0u && cursor < end) {
+      if (!has) {
+        unsigned lt;
+        asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+        const int64_t kk = cursor + __popc(need & lt);
+        if (kk < end) {
+          i = kk;
+          has = true;
+          elem = t.elem[i];
+          r = load3(t.pos, i);
+          u = load3(t.dir, i);
+          rs = t.rng[i];
+          dist = t.distance[i];
+          ev = t.events[i];
+          st = RAY_OK;
+          if (elem >= a.n_tets || !finite3(r) || !finite3(u) || nan_bits(dist)) st = RAY_INVALID;
+        }
+      }
+      cursor += __popc(need);
+    }
+    if (__ballot_sync(0xffffffffu, has) == 0u) break;
+    if (has) {
+      bool done = st != RAY_OK || elem < 0;  // nothing to do outside the mesh
+      if (!done && ev >= t.max_events) {
+        st = RAY_EVENT_LIMIT;
+        done = true;
+      }
+      if (!done) {
+        cnt.steps++;
+        double ex;
+        const int f = next_face<FO, MIXED>(a, elem, r, u, &ex, cnt);
+        const double c = sample_collision(rs, t.mfp);
+        if (dlt(c, ex)) {
+          // collision inside the tet (:81-85)
+          r = add3(r, scl3(c, u));
+          dist += c;
+          if (t.tally) atomicAdd(&t.tally[elem], c);
+          u = sample_direction(rs);
+        } else if (f < 0) {
+          st = RAY_NO_EXIT_FACE;  // exit = INFTY and c >= INFTY: no finite step exists
+          done = true;
+        } else {
+          // to the exit face and into the neighbour (:86-90)
+          const int4 ad = __ldg(&a.adj[elem]);
+          const int32_t nxt = f == 0 ? ad.x : (f == 1 ? ad.y : (f == 2 ? ad.z : ad.w));
+          r = add3(r, scl3(ex, u));
+          dist += ex;
+          if (t.tally) atomicAdd(&t.tally[elem], ex);
+          if (nxt < -1 || nxt >= a.n_tets) {
+            st = RAY_INVALID;  // corrupt adjacency
+            done = true;
+          } else {
+            elem = nxt;
+            if (elem < 0) done = true;
+          }
+        }
+        if (st == RAY_OK) ++ev;
+      }
+      if (done) {
+        t.elem[i] = elem;
+        t.pos[3 * i] = r.x;
+        t.pos[3 * i + 1] = r.y;
+        t.pos[3 * i + 2] = r.z;
+        t.dir[3 * i] = u.x;
+        t.dir[3 * i + 1] = u.y;
+        t.dir[3 * i + 2] = u.z;
+        t.rng[i] = rs;
+        t.distance[i] = dist;
+        t.events[i] = ev;
+        if (t.status) t.status[i] = st;
+        has = false;
+        parts++;
+      }
+    }
+  }
+  if (t.counters) flush(t.counters, cnt, parts);
+}
+
+template <int FO, bool MIXED>
+cudaError_t launch_transport_t(const TransportArgs& a, cudaStream_t st) {
+  static int num_sms = 0, per_sm = 0;
+  auto kern = k_transport<FO, MIXED>;
+  if (per_sm == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaError_t e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+  }
+  int64_t blocks = (int64_t)num_sms * per_sm;
+  const int64_t max_blocks = (a.n + kBlock - 1) / kBlock;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks < 1) blocks = 1;
+  const int64_t warps = blocks * (kBlock / 32);
+  const int64_t chunk = (a.n + warps - 1) / warps;
+  kern<<<(unsigned)blocks, kBlock, 0, st>>>(a, chunk);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_transport(bool mixed, int face_order, const TransportArgs& a, cudaStream_t st) {
+  if (a.n <= 0) return cudaSuccess;
+  switch ((face_order == 0 ? 0 : 2) + (mixed ? 1 : 0)) {
+    case 0: return launch_transport_t<0, false>(a, st);
+    case 1: return launch_transport_t<0, true>(a, st);
+    case 2: return launch_transport_t<1, false>(a, st);
+    default: return launch_transport_t<1, true>(a, st);
   }
 }
 

@@ -44,6 +44,26 @@ struct WalkArgs {
 
 enum : int32_t { WALK_STRIDED = 0, WALK_COUNT = 1, WALK_PACKED = 2 };
 
+// Device particle loop over the tet mesh (tools/walk_elements.h:53-96): the
+// per-particle state is read and written back in place.
+struct TransportArgs {
+  WalkArgs mesh;             // mesh arrays and face table (n, start, ... unused)
+  int64_t n;
+  int32_t* elem;             // tet index; -1 = outside the mesh
+  double* pos;               // 3 per particle
+  double* dir;               // 3 per particle (unit)
+  unsigned long long* rng;   // SplitMix64 state per particle
+  double* distance;          // accumulated path length
+  int32_t* events;           // accumulated events
+  int32_t* status;           // per particle (may be null)
+  double* tally;             // per-tet track length, accumulated with atomics (may be null)
+  double mfp;
+  int32_t max_events;
+  unsigned long long* counters;
+};
+
+cudaError_t launch_transport(bool mixed, int face_order, const TransportArgs& a, cudaStream_t st);
+
 // In-place exclusive scan of offsets[0..n) with offsets[n] = total.
 // block_sums needs scan_scratch_entries(n) int64 entries.
 int64_t scan_scratch_entries(int64_t n);

@@ -430,6 +430,27 @@ class CudaRayTracer:
         return se, sl, sc, st
 
 
+    def seed_streams(self, seed, n):
+        """xdgcu_seed_streams: n independent random-stream states (uint64)."""
+        st = np.zeros(int(n), dtype=np.uint64)
+        self._check(self.L.xdgcu_seed_streams(ctypes.c_uint64(int(seed) & (2**64 - 1)), int(n),
+                                              _addr(st)), "seed_streams")
+        return st
+
+    def transport_elements(self, elem_index, pos, dirs, rng, mfp, max_events, distance, events,
+                           tally=None, precision=MIXED, stream=None):
+        """xdgcu_transport_elements: updates the particle state in place
+        (torch CUDA tensors or NumPy arrays; rng as int64/uint64 bits).
+        Returns the per-particle status array."""
+        n = len(elem_index)
+        out = _Out(pos)
+        st = out.i32(n)
+        self._check(self.L.xdgcu_transport_elements(
+            self.ctx, n, _addr(elem_index), _addr(pos), _addr(dirs), _addr(rng), float(mfp),
+            int(max_events), _addr(distance), _addr(events), _addr(tally), _addr(st),
+            int(precision), stream if stream is not None else out.stream()), "transport_elements")
+        return st
+
     def walk_elements_packed(self, start_index, start, u, distance, capacity, max_segs=4096,
                              precision=MIXED, stream=None):
         """Packed walk: returns (seg_elem [capacity], seg_len, offsets [n+1], status)."""
@@ -678,6 +699,77 @@ class XDG:
         offsets = np.zeros(n + 1, dtype=np.int64)
         offsets[1:] = np.cumsum(np.bincount(trk, minlength=n))
         return el, ln, offsets
+
+    def walk_particles(self, elem_index, pos, dirs, rng, mfp=1.0, max_events=1_000_000,
+                       precision=MIXED, tally=False, max_reentries=64):
+        """The walk_elements tool loop (tools/walk_elements.h:60-96) for
+        particles starting in tets ``elem_index`` (tet indices) at ``pos``
+        along ``dirs``, with per-particle random streams ``rng``.
+
+        Every in-mesh event of every particle runs in device launches of
+        xdgcu_transport_elements; a particle that leaves the mesh looks for
+        re-entry as the tool does -- ray_fire in the implicit complement
+        (EXITING, excluding the faces this search hit), move to the hit,
+        find_element(r + u*TINY_BIT) -- and, when it finds an element, goes
+        back to the device loop.  Returns a dict of NumPy arrays: elem (final
+        tet, -1 outside), pos, dir, rng, distance, events, status; and
+        tally (track length per tet) when asked for."""
+        import torch
+        dev = torch.device("cuda", self.rti.device)
+        n = len(elem_index)
+        e = torch.as_tensor(np.ascontiguousarray(elem_index, dtype=np.int32), device=dev)
+        r = torch.as_tensor(_host(pos, np.float64, (-1, 3)), device=dev).contiguous()
+        u = torch.as_tensor(_host(dirs, np.float64, (-1, 3)), device=dev).contiguous()
+        s = torch.as_tensor(np.ascontiguousarray(rng, dtype=np.uint64).view(np.int64),
+                            device=dev).contiguous()
+        d = torch.zeros(n, dtype=torch.float64, device=dev)
+        ev = torch.zeros(n, dtype=torch.int32, device=dev)
+        ty = torch.zeros(len(self.model.tets.conn), dtype=torch.float64, device=dev) if tally \
+            else None
+        ipc_tree = self.volume_to_surface_tree[self.model.implicit_complement]
+        gtree = self.rti.global_element_tree
+        final = np.zeros(n, dtype=np.int32)
+        ended = np.asarray(elem_index) < 0  # outside the mesh with no re-entry left
+        for _ in range(max_reentries + 1):
+            st = self.rti.transport_elements(e, r, u, s, mfp, max_events, d, ev, ty, precision)
+            torch.cuda.synchronize(dev)
+            final = st.cpu().numpy()
+            # particles that left the mesh in this launch
+            out = np.nonzero((e.cpu().numpy() < 0) & (final == 0) & ~ended)[0]
+            if len(out) == 0:
+                break
+            idx = torch.as_tensor(out, device=dev)
+            rr, uu, dd = r[idx].cpu().numpy(), u[idx].cpu().numpy(), d[idx].cpu().numpy()
+            ee = np.full(len(out), -1, dtype=np.int32)
+            excl = [[] for _ in range(len(out))]
+            pend = np.arange(len(out))
+            while len(pend):
+                t, surf, face = self.rti.ray_fire(ipc_tree, rr[pend], uu[pend], None, EXITING,
+                                                  [excl[k] for k in pend], precision)
+                hit = surf != ID_NONE
+                pend = pend[hit]
+                if len(pend) == 0:
+                    break
+                th = t[hit]
+                rr[pend] = rr[pend] + uu[pend] * th[:, None]   # r += u * ray_hit.first
+                dd[pend] = dd[pend] + th
+                for k, f in zip(pend, face[hit]):
+                    excl[k].append(int(f))
+                _, eidx = self.rti.find_element(gtree, rr[pend] + uu[pend] * TINY_BIT, precision)
+                ee[pend] = eidx
+                pend = pend[(eidx < 0) & np.array([len(excl[k]) < 64 for k in pend], dtype=bool)]
+            r[idx] = torch.as_tensor(rr, device=dev)
+            d[idx] = torch.as_tensor(dd, device=dev)
+            e[idx] = torch.as_tensor(ee, device=dev)
+            ended[out[ee < 0]] = True
+            if (ee < 0).all():
+                break
+        res = dict(elem=e.cpu().numpy(), pos=r.cpu().numpy(), dir=u.cpu().numpy(),
+                   rng=s.cpu().numpy().view(np.uint64), distance=d.cpu().numpy(),
+                   events=ev.cpu().numpy(), status=final)
+        if tally:
+            res["tally"] = ty.cpu().numpy()
+        return res
 
     def _walk_packed(self, elem_index, r, u, dist, precision):
         """Packed walk of host arrays sized in one pass when the first guess
