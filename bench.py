@@ -60,6 +60,11 @@ MFP = 1.0                   # tools/walk_elements.cpp: --mfp default
 MAX_EVENTS = 1_000_000
 TRANSPORT_CHECK = 2_000     # particles checked bit for bit against the oracle
 TRANSPORT_CPU_SAMPLE = 50_000
+SURF_WORKLOAD = "nested_spheres_8x_icosphere_L6_3.7e6_sources_mfp1_ipc_graveyard_particle_sim"
+SURF_PARTICLES = 10_000_000  # ray origins of the headline workload used as sources
+SURF_HIST = 16
+SURF_CHECK = 1_000
+SURF_CPU_SAMPLE = 20_000
 REF_STEP_SAMPLE = 1_000_000  # rays per step of --impl reference
 BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
 BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
@@ -340,6 +345,92 @@ def bench_many_surfaces(torch, L, dev, stream, args, rank, world):
     }
 
 
+def bench_surface_transport(torch, L, x, model, dev, stream, sptr, p, d, trees_h, args, rank,
+                            world):
+    """The particle_sim tool loop (tools/particle_sim.h:128-141) on the
+    nested-sphere model: the ray origins of the headline workload that lie
+    inside the spheres (3.7e6 of the 1e7) are particle sources (their volume from
+    find_volume, the ray's direction), mean free path 1, transmission on
+    every surface and the implicit complement as graveyard (the tool's
+    --ipc-graveyard): each particle flies (ray_fire in its volume, history
+    excluded), collides or crosses into the next shell until it leaves the
+    outer sphere, all in one xdgcu_transport_surfaces launch per step."""
+    from xdg_gb300 import _lib
+    from xdg_gb300.engine import FP64, MIXED
+    grave = x.volume_to_surface_tree[model.implicit_complement]
+    sel_h = np.nonzero(trees_h[:SURF_PARTICLES] != grave)[0]
+    n = len(sel_h)
+    sel = torch.from_numpy(sel_h).to(dev)
+    t0 = torch.from_numpy(trees_h[sel_h].astype(np.int32)).to(dev)
+    p0, d0 = p[sel].contiguous(), d[sel].contiguous()
+    seeds_h = x.rti.seed_streams(dist.rank_seed(4048, rank), n)
+    s0 = torch.from_numpy(seeds_h.view(np.int64)).to(dev)
+    T = {"tree": torch.empty_like(t0), "pos": torch.empty_like(p0), "dir": torch.empty_like(d0),
+         "rng": torch.empty_like(s0),
+         "hist": torch.zeros((n, SURF_HIST), dtype=torch.int32, device=dev),
+         "hc": torch.empty(n, dtype=torch.int32, device=dev),
+         "dist": torch.empty(n, dtype=torch.float64, device=dev),
+         "ev": torch.empty(n, dtype=torch.int32, device=dev),
+         "st": torch.empty(n, dtype=torch.int32, device=dev)}
+
+    def step(prec):
+        def go():
+            T["tree"].copy_(t0)
+            T["pos"].copy_(p0)
+            T["dir"].copy_(d0)
+            T["rng"].copy_(s0)
+            T["hc"].zero_()
+            T["dist"].zero_()
+            T["ev"].zero_()
+            a = [ctypes.c_void_p(T[k].data_ptr()) for k in ("tree", "pos", "dir", "rng")]
+            rc = L.xdgcu_transport_surfaces(
+                x.rti.ctx, n, *a, MFP, MAX_EVENTS, grave, SURF_HIST,
+                ctypes.c_void_p(T["hist"].data_ptr()), ctypes.c_void_p(T["hc"].data_ptr()),
+                ctypes.c_void_p(T["dist"].data_ptr()), ctypes.c_void_p(T["ev"].data_ptr()), None,
+                ctypes.c_void_p(T["st"].data_ptr()), prec, sptr)
+            _lib.check(rc, x.rti.ctx, "transport_surfaces")
+        return go
+
+    ms = timed(torch, step(MIXED), max(3, args.steps // 4), args.warmup, world, stream)
+    events = int(T["ev"].sum().item())
+    bad = int((T["st"] != 0).sum().item())
+    keys = ("tree", "pos", "dir", "rng", "dist", "ev")
+    mixed_state = {k: T[k].clone() for k in keys}
+    ms64 = timed(torch, step(FP64), 3, 1, world, stream)
+    mism = sum(int((mixed_state[k] != T[k]).reshape(n, -1).any(1).sum().item()) for k in keys)
+    total = dist.sum_over_ranks(events, world)
+    out = {
+        "workload": SURF_WORKLOAD, "unit": "Mevents/s",
+        "value": total / (ms / 1e3) / 1e6, "fp64_value": total / (ms64 / 1e3) / 1e6,
+        "ms_per_step": ms, "fp64_ms_per_step": ms64, "particles": n, "events": events,
+        "events_per_particle": events / max(1, n), "speedup_mixed_vs_fp64": ms64 / ms,
+        "particles_differing_mixed_vs_fp64": mism, "particles_with_status": bad,
+        "step": "reset sources + one xdgcu_transport_surfaces launch (all events)",
+    }
+    if rank == 0 and not args.no_oracle:
+        from oracle import oracle as xo
+        sim = xo.SurfaceTransport(model, x.volume_to_surface_tree)
+        k = min(SURF_CHECK, n)
+        o = sim.run(t0[:k].cpu().numpy(), p0[:k].cpu().numpy(), d0[:k].cpu().numpy(),
+                    seeds_h[:k], MFP, MAX_EVENTS, graveyard_tree=grave)
+        got = [mixed_state[kk][:k].cpu().numpy() for kk in keys]
+        got[3] = got[3].view(np.uint64)
+        out["oracle_check"] = {"particles": k, "mismatches": int(sum(
+            int((np.asarray(a) != np.asarray(b)).reshape(k, -1).any(1).sum())
+            for a, b in zip(got, o[:6])))}
+        kc = min(SURF_CPU_SAMPLE, n)
+        cores = os.cpu_count() or 1
+        tc = time.perf_counter()
+        oc = sim.run(t0[:kc].cpu().numpy(), p0[:kc].cpu().numpy(), d0[:kc].cpu().numpy(),
+                     seeds_h[:kc], MFP, MAX_EVENTS, graveyard_tree=grave, threads=cores)
+        dtc = time.perf_counter() - tc
+        out["cpu_baseline"] = {"value": float(oc[5].sum()) / dtc / 1e6, "unit": "Mevents/s",
+                               "cores": cores, "kind": "port",
+                               "sample": f"first {kc} particles, FP64 particle_sim loop, BVH, "
+                                         "OpenMP"}
+    return out
+
+
 def bench_transport(torch, L, wr, dev, stream, sptr, ws, wu, we_idx, tm, args, rank, world):
     """The walk_elements tool loop (tools/walk_elements.h:60-96) on the
     750,000-tet cube: the walk's 1e6 track starts as particle sources,
@@ -536,6 +627,10 @@ def run_engine(args, rank, world, local):
     ms_fv_loop = timed(torch, fv_per_volume, 3, 1, world, stream)
     fv_same = bool(torch.equal(fv, fv_loop))
     fv_host_same = bool(np.array_equal(fv.cpu().numpy(), vols_h))
+
+    # particle_sim loop on the same model
+    surface_transport = bench_surface_transport(torch, L, x, model, dev, stream, sptr, p, d,
+                                                trees_h, args, rank, world)
 
     # algorithmic work counters (untimed run)
     rti.set_counting(True)
@@ -762,6 +857,7 @@ def run_engine(args, rank, world, local):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "matches_device_path": e2e_ok},
         "transport": transport,
+        "surface_transport": surface_transport,
         "many_surfaces": many,
         "tuning": tuning,
         "gpu_launches": args.steps * launches_per_step,

@@ -63,7 +63,8 @@ enum {
   XDGCU_RAY_NO_EXIT_FACE = 5,   /* next_element found no exiting face */
   XDGCU_RAY_OUTPUT_FULL = 6,    /* packed walk output capacity exceeded */
   XDGCU_RAY_EVENT_LIMIT = 7,    /* particle stopped at max_events */
-  XDGCU_RAY_LOST = 8            /* particle found no surface ahead (particle_sim's "lost") */
+  XDGCU_RAY_LOST = 8,           /* particle found no surface ahead (particle_sim's "lost") */
+  XDGCU_RAY_STUCK = 9           /* particle's next surface hit at distance 0 ("stuck") */
 };
 
 /* shared_enums.h:11-15 */
@@ -274,6 +275,51 @@ int xdgcu_transport_elements(xdgcu_ctx* ctx, int64_t n, int32_t* elem_index, dou
                              double* elem_tally, int32_t* status, int32_t precision,
                              void* stream);
 
+/* Surface boundary conditions of the surface-tracking particle loop
+ * (MeshManager::get_surface_property(surface, BOUNDARY_CONDITION),
+ * mesh_manager_interface.cpp:98-104: "transmission" unless set). */
+enum { XDGCU_BC_TRANSMISSION = 0, XDGCU_BC_VACUUM = 1, XDGCU_BC_REFLECTING = 2 };
+
+/* Sets the boundary condition of n registered surfaces (by surface id). */
+int xdgcu_set_surface_boundary(xdgcu_ctx* ctx, int32_t n, const int32_t* surface_ids,
+                               const int32_t* conditions);
+
+/* The particle loop of the particle_sim tool (tools/particle_sim.h:128-141)
+ * on the device: surface tracking through the volumes' surface trees, every
+ * event of every particle in one launch.  Per event: ray_fire in the
+ * particle's volume (EXITING, the history of faces crossed since the last
+ * collision excluded; the hit face is appended to it); a collision distance
+ * c = -log(1 - U) * mean_free_path; if c < hit distance the particle moves c,
+ * takes a new isotropic direction and clears its history (collide), else it
+ * moves to the surface and crosses it: reflecting -> mirror the direction in
+ * the hit face's normal (XDG::surface_normal with the history, xdg.cpp:
+ * 272-289) and keep only the last face in the history; vacuum -> the
+ * particle ends; transmission -> the other parent volume of the surface
+ * (MeshManager::next_volume); entering graveyard_tree (> 0, e.g. the
+ * implicit complement's tree, the tool's --ipc-graveyard) or no volume ends
+ * the particle.  events += 1 per event.
+ * State, read and written back in place (n particles):
+ *   tree        surface tree id of the particle's volume; -1 once it ended
+ *               (particles with tree -1 are skipped)
+ *   position, direction (n x 3), rng_state (as in xdgcu_transport_elements),
+ *   history     n x history_cap face ids (the most recent history_cap
+ *               crossings are kept: older faces are behind the particle on
+ *               the same straight flight and cannot be hit again),
+ *   history_count  faces appended since the last clear (start with 0),
+ *   distance, events.
+ * tree_tally (may be NULL): n_surface_trees + 1 doubles indexed by tree id,
+ * the path length per volume (the tool's cell_tracks), atomic additions.
+ * status: XDGCU_RAY_OK (ended), XDGCU_RAY_EVENT_LIMIT (stopped alive; call
+ * again to continue), XDGCU_RAY_LOST / XDGCU_RAY_STUCK (the tool's fatal
+ * errors, :36-45: the particle stops), XDGCU_RAY_INVALID.  The tool reads
+ * max_events but never stops on it; here it bounds each call. */
+int xdgcu_transport_surfaces(xdgcu_ctx* ctx, int64_t n, int32_t* tree, double* position,
+                             double* direction, uint64_t* rng_state, double mean_free_path,
+                             int32_t max_events, int32_t graveyard_tree, int32_t history_cap,
+                             int32_t* history, int32_t* history_count, double* distance,
+                             int32_t* events, double* tree_tally, int32_t* status,
+                             int32_t precision, void* stream);
+
 /* Largest batch of xdgcu_walk_elements_packed_noalloc. */
 #define XDGCU_NOALLOC_MAX_TRACKS 4194304
 
@@ -330,6 +376,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      the batch fixed at launch; > 0 (a multiple of 32): warps
  *                      take this many rays at a time from a device work queue,
  *                      which balances batches of very uneven per-ray cost
+ *   "particle_event_wait"  particle loop of xdgcu_transport_surfaces: lanes
+ *                      whose flights have ended that a warp gathers before it
+ *                      runs their events together (1..32, default 16)
  *   "trace_sort_min"   batches of at least this many rays (default 0 = never)
  *                      are traversed in a coherent order: sorted on the device
  *                      by tree, direction octant and the Morton code of the

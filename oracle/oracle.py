@@ -93,6 +93,8 @@ def lib():
         L.xo_sample_direction.argtypes = [_U64, _D]
         L.xo_transport_elements.argtypes = [_VP, _i64, _I, _D, _D, _U64, _dbl, _i32, _D, _I, _D,
                                             _I, _int]
+        L.xo_transport_surfaces.argtypes = [_VP, _i32, _I, _I, _I, _i32, _D, _i32, _i64, _I, _D,
+                                            _D, _U64, _dbl, _i32, _i32, _D, _I, _D, _I, _int]
         L.xo_walk_particles.argtypes = [_VP, _VP, _VP, _i64, _I, _D, _D, _U64, _dbl, _i32, _D,
                                         _I, _I, _int]
         _lib = L
@@ -357,6 +359,52 @@ class TetWalker:
                                 _p(u, _D), _p(s, U64), float(mfp), int(max_events), _p(d, _D),
                                 _p(ev, _I), _p(st, _I), threads or n_threads_default())
         return e, r, u, s, d, ev, st
+
+
+class SurfaceTransport:
+    """The particle_sim tool loop over oracle volume trees
+    (xo_transport_surfaces).  ``tree_of_volume`` maps each volume to the
+    engine's surface tree id, so particle states use the same tree ids;
+    ``bc`` maps surface ids to 0 transmission / 1 vacuum / 2 reflecting."""
+
+    def __init__(self, model, tree_of_volume, bc=None):
+        bc = bc or {}
+        self.n_trees = max(tree_of_volume.values())
+        self.trees = [None] * self.n_trees
+        for v, t in tree_of_volume.items():
+            self.trees[t - 1] = volume_tree(model, v)
+        self._ptrs = (ctypes.c_void_p * self.n_trees)(
+            *[t.h if t is not None else None for t in self.trees])
+        ns = max(s.surface_id for s in model.surfaces) + 1
+        self.fwd = np.full(ns, -1, dtype=np.int32)
+        self.rev = np.full(ns, -1, dtype=np.int32)
+        self.bc = np.zeros(ns, dtype=np.int32)
+        nf = max(int(s.face_ids.max()) for s in model.surfaces) + 1
+        self.face_xyz = np.zeros((nf, 9))
+        for srf in model.surfaces:
+            self.fwd[srf.surface_id] = tree_of_volume.get(srf.forward_volume, -1)
+            self.rev[srf.surface_id] = tree_of_volume.get(srf.reverse_volume, -1)
+            self.bc[srf.surface_id] = bc.get(srf.surface_id, 0)
+            self.face_xyz[srf.face_ids] = srf.tri_xyz()
+
+    def run(self, tree, pos, dirs, rng, mfp, max_events, graveyard_tree=0, threads=None):
+        """Returns (tree, pos, dir, rng, distance, events, status, tally)."""
+        U64 = ctypes.POINTER(ctypes.c_uint64)
+        t = _i32a(tree).copy()
+        n = len(t)
+        r, u = _f64(pos, (-1, 3)).copy(), _f64(dirs, (-1, 3)).copy()
+        s = np.ascontiguousarray(rng, dtype=np.uint64).copy()
+        d = np.zeros(n)
+        ev = np.zeros(n, dtype=np.int32)
+        st = np.zeros(n, dtype=np.int32)
+        tally = np.zeros(self.n_trees + 1)
+        lib().xo_transport_surfaces(
+            ctypes.cast(self._ptrs, _VP), self.n_trees, _p(self.fwd, _I), _p(self.rev, _I),
+            _p(self.bc, _I), len(self.fwd), _p(self.face_xyz, _D), len(self.face_xyz), n,
+            _p(t, _I), _p(r, _D), _p(u, _D), _p(s, U64), float(mfp), int(max_events),
+            int(graveyard_tree), _p(d, _D), _p(ev, _I), _p(tally, _D), _p(st, _I),
+            threads or n_threads_default())
+        return t, r, u, s, d, ev, st, tally
 
 
 def series_log(x):

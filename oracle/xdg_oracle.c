@@ -1069,4 +1069,85 @@ void xo_walk_particles(const xo_tetmesh* m, const xo_tree* ipc, const xo_tree* e
   }
 }
 
+/* tools/particle_sim.h:128-141 (Particle::surf_dist / advance / collide /
+ * cross_surface) for particles given in a volume's tree, with the engine's
+ * per-particle streams.  trees[k] is the tree of tree id k+1; the surface
+ * tables are indexed by surface id, face_xyz by face id. */
+void xo_transport_surfaces(const xo_tree* const* trees, int32_t n_trees, const int32_t* surf_fwd,
+                           const int32_t* surf_rev, const int32_t* surf_bc, int32_t n_surf_ids,
+                           const double* face_xyz, int32_t n_face_ids, int64_t n, int32_t* tree,
+                           double* pos, double* dir, uint64_t* rng, double mfp,
+                           int32_t max_events, int32_t graveyard_tree, double* distance,
+                           int32_t* events, double* tally, int32_t* status, int n_threads) {
+#pragma omp parallel for schedule(dynamic, 16) num_threads(n_threads > 0 ? n_threads : 1)
+  for (int64_t i = 0; i < n; ++i) {
+    v3 r = mk(pos + 3 * i), u = mk(dir + 3 * i);
+    int32_t t = tree[i];
+    int st = XO_OK;
+    int32_t cap = 64, nh = 0;
+    int32_t* hist = (int32_t*)malloc(sizeof(int32_t) * cap);
+    int alive = t > 0;
+    if (alive && events[i] >= max_events) { st = XO_EVENT_LIMIT; alive = 0; }
+    while (alive) {
+      if (t < 1 || t > n_trees) { st = 1; break; }
+      /* surf_dist: ray_fire(volume, r, u, INFTY, EXITING, &history) */
+      double o[3] = {r.x, r.y, r.z}, d[3] = {u.x, u.y, u.z}, th;
+      int32_t off[2] = {0, nh}, surf, face;
+      xo_ray_fire(trees[t - 1], 1, o, d, NULL, XO_EXITING, off, hist, &th, &surf, &face, 1);
+      if (surf != XO_ID_NONE && th == 0.0) { st = 9; break; }  /* stuck */
+      if (surf == XO_ID_NONE) { st = XO_LOST; break; }           /* lost */
+      if (nh == cap) { cap *= 2; hist = (int32_t*)realloc(hist, sizeof(int32_t) * cap); }
+      hist[nh++] = face;
+      const double c = xo_sample_collision(&rng[i], mfp);
+      if (c < th) {
+        r = add(r, scl(c, u));
+        distance[i] += c;
+        if (tally) {
+#pragma omp atomic
+          tally[t] += c;
+        }
+        events[i]++;
+        double nd[3];
+        xo_sample_direction(&rng[i], nd);
+        u = mk(nd);
+        nh = 0;
+      } else {
+        r = add(r, scl(th, u));
+        distance[i] += th;
+        if (tally) {
+#pragma omp atomic
+          tally[t] += th;
+        }
+        events[i]++;
+        const int bc = (surf >= 0 && surf < n_surf_ids) ? surf_bc[surf] : 0;
+        if (bc == 2) {
+          const double* f = face_xyz + 9 * (int64_t)hist[nh - 1];
+          v3 nrm = face_normal(mk(f), mk(f + 3), mk(f + 6));
+          const double proj = dot(nrm, u);
+          const double mag = length(nrm);
+          nrm = scl(2.0 * proj / mag, nrm);
+          u = normalize(sub(u, nrm));
+          hist[0] = hist[nh - 1];
+          nh = 1;
+        } else if (bc == 1) {
+          alive = 0;
+        } else {
+          const int32_t fw = surf_fwd[surf], rv = surf_rev[surf];
+          if (fw == t) t = rv;
+          else if (rv == t) t = fw;
+          else { st = 1; alive = 0; }
+          if (alive && (t < 1 || t == graveyard_tree)) { t = -1; alive = 0; }
+        }
+        (void)n_face_ids;
+      }
+      if (alive && events[i] >= max_events) { st = XO_EVENT_LIMIT; alive = 0; }
+    }
+    free(hist);
+    tree[i] = t;
+    pos[3 * i] = r.x; pos[3 * i + 1] = r.y; pos[3 * i + 2] = r.z;
+    dir[3 * i] = u.x; dir[3 * i + 1] = u.y; dir[3 * i + 2] = u.z;
+    if (status) status[i] = st;
+  }
+}
+
 int xo_version(void) { return 1; }

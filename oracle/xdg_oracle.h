@@ -180,6 +180,22 @@ void xo_walk_particles(const xo_tetmesh* mesh, const struct xo_tree* ipc_tree,
                        double* dir, uint64_t* rng, double mfp, int32_t max_events,
                        double* distance, int32_t* events, int32_t* status, int n_threads);
 
+/* The particle_sim tool loop (tools/particle_sim.h:128-141) with the
+ * engine's per-particle streams: per event ray_fire in the particle's volume
+ * tree (EXITING, history excluded, hit appended), collision sampling,
+ * advance, then collide (new direction, history cleared) or cross the
+ * surface by its boundary condition (surf_bc: 0 transmission -> next volume
+ * by surf_fwd/surf_rev tree ids, 1 vacuum, 2 reflecting).  trees[k] is the
+ * volume tree of tree id k+1; surface tables are indexed by surface id and
+ * face_xyz (9 doubles) by face id.  tally (may be NULL) is indexed by tree
+ * id.  Statuses: 0, XO_EVENT_LIMIT, XO_LOST, 9 (stuck), 1 (invalid). */
+void xo_transport_surfaces(const xo_tree* const* trees, int32_t n_trees, const int32_t* surf_fwd,
+                           const int32_t* surf_rev, const int32_t* surf_bc, int32_t n_surf_ids,
+                           const double* face_xyz, int32_t n_face_ids, int64_t n, int32_t* tree,
+                           double* pos, double* dir, uint64_t* rng, double mfp,
+                           int32_t max_events, int32_t graveyard_tree, double* distance,
+                           int32_t* events, double* tally, int32_t* status, int n_threads);
+
 /* Library self-description for tests. */
 int xo_version(void);
 

@@ -137,3 +137,128 @@ def test_walk_particles_reentry_matches_oracle(cuda, oracle, prec):
     assert (got["distance"] > first[4]).sum() > n // 10  # many crossed a gap
     # the tally holds the in-mesh path only: the gaps crossed are not in it
     assert 0.0 < got["tally"].sum() < got["distance"].sum()
+
+
+# --------------------------------------------------------------------------
+# particle_sim surface-tracking loop (tools/particle_sim.h:128-141)
+# --------------------------------------------------------------------------
+
+SNAMES = ["tree", "pos", "dir", "rng", "distance", "events", "status"]
+
+
+def _same_tally(got, ref):
+    """Per-tree path length, summed with atomics: within 1e-12 relative.
+    The engine's array also has a slot for the global tree, never entered."""
+    assert np.allclose(got[:len(ref)], ref, rtol=1e-12, atol=0)
+    assert (got[len(ref):] == 0).all()
+
+
+def _surface_run(x, prec, tree, p, u, seeds, mfp, max_events, grave=0, cap=16):
+    n = len(tree)
+    t, r, d, s = tree.copy(), p.copy(), u.copy(), seeds.copy()
+    hist = np.zeros((n, cap), dtype=np.int32)
+    hc = np.zeros(n, dtype=np.int32)
+    dist, ev = np.zeros(n), np.zeros(n, dtype=np.int32)
+    tally = np.zeros(x.rti.num_registered_surface_trees() + 1)
+    st = x.rti.transport_surfaces(t, r, d, s, mfp, max_events, hist, hc, dist, ev, tally,
+                                  grave, prec)
+    return [t, r, d, s, dist, ev, st, tally, hist, hc]
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+@pytest.mark.parametrize("case", ["vacuum", "graveyard", "reflecting"])
+def test_transport_surfaces_sphere_in_box(cuda, oracle, prec, case):
+    from xdg_gb300.engine import BC_REFLECTING, BC_VACUUM
+    m = synth.single_sphere_in_box(level=3, radius=10.0, half_width=20.0)
+    x = XDG(m)
+    x.prepare_raytracer()
+    bc = {2: BC_VACUUM} if case == "vacuum" else ({2: BC_REFLECTING} if case == "reflecting"
+                                                   else {})
+    if bc:
+        x.rti.set_surface_boundary(bc)
+    n = 3000
+    rng0 = np.random.default_rng(4)
+    p = rng0.uniform(-6.0, 6.0, (n, 3))
+    u = synth.isotropic_dirs(rng0, n)
+    seeds = x.rti.seed_streams(99, n)
+    tree = np.full(n, x.volume_to_surface_tree[1], dtype=np.int32)
+    grave = x.volume_to_surface_tree[3] if case == "graveyard" else 0
+    max_ev = 300 if case == "reflecting" else 1_000_000
+    got = _surface_run(x, prec, tree, p, u, seeds, 5.0, max_ev, grave)
+    sim = oracle.SurfaceTransport(m, x.volume_to_surface_tree, bc)
+    o = sim.run(tree, p, u, seeds, 5.0, max_ev, graveyard_tree=grave)
+    for k, name in enumerate(SNAMES):
+        assert_same(got[k], o[k], name)
+    _same_tally(got[7], o[7])
+    assert (got[6] == (7 if case == "reflecting" else 0)).all()
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_transport_surfaces_nested_spheres(cuda, oracle, prec):
+    """Eight nested shells, transmission everywhere, the implicit complement
+    as graveyard; the device path, the host-array path and a run cut at
+    max_events then resumed all equal the oracle."""
+    import torch
+    m = synth.nested_spheres(n=8, level=3, jitter=1e-3, seed=7)
+    x = XDG(m)
+    x.prepare_raytracer()
+    n = 4000
+    rng0 = np.random.default_rng(8)
+    p = rng0.uniform(-7.5, 7.5, (n, 3))
+    u = synth.isotropic_dirs(rng0, n)
+    vols = x.find_volume(p, u)
+    keep = vols != m.implicit_complement
+    p, u, vols = p[keep], u[keep], vols[keep]
+    n = len(p)
+    tree = x._trees(vols).astype(np.int32)
+    seeds = x.rti.seed_streams(7, n)
+    grave = x.volume_to_surface_tree[m.implicit_complement]
+    sim = oracle.SurfaceTransport(m, x.volume_to_surface_tree)
+    o = sim.run(tree, p, u, seeds, 0.7, 1_000_000, graveyard_tree=grave)
+    # host arrays
+    got = _surface_run(x, prec, tree, p, u, seeds, 0.7, 1_000_000, grave)
+    for k, name in enumerate(SNAMES):
+        assert_same(got[k], o[k], name)
+    _same_tally(got[7], o[7])
+    assert (got[0] == -1).all() and got[5].mean() > 10
+    # events run one lane at a time or a whole warp at a time: same results
+    for wait in (1, 32):
+        x.rti.set_tuning("particle_event_wait", wait)
+        try:
+            g2 = _surface_run(x, prec, tree, p, u, seeds, 0.7, 1_000_000, grave)
+        finally:
+            x.rti.set_tuning("particle_event_wait", 16)
+        for k, name in enumerate(SNAMES):
+            assert_same(g2[k], o[k], f"{name} event_wait={wait}")
+    # device tensors, cut at 5 events then resumed with the saved history
+    dev = torch.device("cuda", 0)
+    T = [torch.as_tensor(a, device=dev).clone() for a in
+         (tree, p, u, seeds.view(np.int64), np.zeros((n, 16), np.int32), np.zeros(n, np.int32),
+          np.zeros(n), np.zeros(n, np.int32))]
+    st1 = x.rti.transport_surfaces(*T[:4], 0.7, 5, T[4], T[5], T[6], T[7], None, grave, prec)
+    torch.cuda.synchronize()
+    assert int((st1 == 7).sum()) > n // 2
+    st2 = x.rti.transport_surfaces(*T[:4], 0.7, 1_000_000, T[4], T[5], T[6], T[7], None, grave,
+                                   prec)
+    res = [T[0].cpu().numpy(), T[1].cpu().numpy(), T[2].cpu().numpy(),
+           T[3].cpu().numpy().view(np.uint64), T[6].cpu().numpy(), T[7].cpu().numpy(),
+           st2.cpu().numpy()]
+    for k, name in enumerate(SNAMES):
+        assert_same(res[k], o[k], "resumed " + name)
+
+
+def test_simulate_particles_facade(cuda):
+    from xdg_gb300.engine import BC_VACUUM
+    m = synth.single_sphere_in_box(level=3, radius=10.0, half_width=20.0)
+    x = XDG(m)
+    x.prepare_raytracer()
+    x.rti.set_surface_boundary({2: BC_VACUUM})
+    n = 500
+    p = np.zeros((n, 3))
+    u = np.tile([1.0, 0.0, 0.0], (n, 1))   # the tool's initial particle
+    res = x.simulate_particles(np.ones(n, dtype=np.int32), p, u, x.rti.seed_streams(3, n),
+                               mfp=1.0, tally=True)
+    assert (res["status"] == 0).all() and (res["volume"] == 2).all()
+    assert abs(sum(res["tally"].values()) - res["distance"].sum()) < 1e-9 * res["distance"].sum()
+    with pytest.raises(Exception):
+        x.rti.set_surface_boundary({77: BC_VACUUM})

@@ -149,3 +149,63 @@ def test_walk_particles_reenters_across_gaps(oracle):
     assert crossed.sum() > n // 10
     # a particle that crossed continued its own random stream
     assert not np.array_equal(a[3][crossed], b[3][crossed])
+
+
+# --------------------------------------------------------------------------
+# particle_sim surface-tracking loop (tools/particle_sim.h:128-141)
+# --------------------------------------------------------------------------
+
+def _sphere_sources(n, seed):
+    rng = np.random.default_rng(seed)
+    p = rng.uniform(-6.0, 6.0, (n, 3))          # inside the radius-10 sphere
+    return p, synth.isotropic_dirs(rng, n)
+
+
+@pytest.mark.parametrize("case", ["vacuum", "graveyard", "reflecting"])
+def test_surface_loop_boundaries(oracle, case):
+    m = synth.single_sphere_in_box(level=3, radius=10.0, half_width=20.0)
+    trees = {1: 1, 2: 2, 3: 3}
+    bc = {2: 1} if case == "vacuum" else ({2: 2} if case == "reflecting" else {})
+    sim = oracle.SurfaceTransport(m, trees, bc)
+    n = 200
+    p, u = _sphere_sources(n, 4)
+    rng = np.arange(1, n + 1, dtype=np.uint64) * np.uint64(2654435761)
+    max_ev = 400 if case == "reflecting" else 1_000_000
+    t, r, d, s, dist, ev, st, tally = sim.run(np.ones(n, dtype=np.int32), p, u, rng, 5.0, max_ev,
+                                             graveyard_tree=3 if case == "graveyard" else 0)
+    assert abs(tally.sum() - dist.sum()) <= 1e-12 * dist.sum()
+    assert np.abs(np.sqrt((d ** 2).sum(1)) - 1.0).max() < 4e-16
+    edge = np.abs(r).max(1)
+    if case == "reflecting":
+        assert (st == 7).all() and (ev == max_ev).all() and (t >= 1).all()
+        assert edge.max() <= 20.0 + 1e-9            # never leaves the box
+        assert tally[3] == 0.0
+    else:
+        assert (st == 0).all()
+        assert np.abs(edge - 20.0).max() < 1e-9      # every particle ends on the box
+        assert (t == (2 if case == "vacuum" else -1)).all()
+        assert tally[1] > 0 and tally[2] > 0 and tally[3] == 0.0
+
+
+def test_surface_loop_without_collisions_is_a_ray_fire_chain(oracle):
+    """With a huge mean free path each event is one surface crossing: the
+    particle's distance is the sum of the chain of ray_fire distances."""
+    m = synth.nested_spheres(n=4, level=2, jitter=1e-3, seed=7)
+    trees = {v: v for v in m.volumes}
+    sim = oracle.SurfaceTransport(m, trees)
+    n = 50
+    rng0 = np.random.default_rng(2)
+    p = rng0.uniform(-0.4, 0.4, (n, 3))
+    u = synth.isotropic_dirs(rng0, n)
+    rng = np.arange(1, n + 1, dtype=np.uint64)
+    t, r, d, s, dist, ev, st, _ = sim.run(np.ones(n, dtype=np.int32), p, u, rng, 1e300, 1000,
+                                         graveyard_tree=5)
+    assert (st == 0).all() and (t == -1).all() and (ev == 4).all()
+    for i in range(n):
+        o, acc, excl = p[i].copy(), 0.0, []
+        for k in range(1, 5):
+            th, sid, fid = oracle.volume_tree(m, k).ray_fire(o[None], u[i][None], excl=[excl])
+            o = o + th[0] * u[i]
+            acc += th[0]
+            excl = excl + [int(fid[0])]
+        assert dist[i] == acc and np.array_equal(r[i], o)

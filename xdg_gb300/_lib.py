@@ -23,7 +23,8 @@ _dbl = ctypes.c_double
 OK = 0
 RAY_OK, RAY_INVALID, RAY_STACK_OVERFLOW, RAY_WALK_LIMIT, RAY_NO_EXIT_FACE = 0, 1, 2, 4, 5
 RAY_OUTPUT_FULL = 6
-RAY_EVENT_LIMIT, RAY_LOST = 7, 8
+RAY_EVENT_LIMIT, RAY_LOST, RAY_STUCK = 7, 8, 9
+BC_TRANSMISSION, BC_VACUUM, BC_REFLECTING = 0, 1, 2
 ANY, EXITING, ENTERING = -1, 0, 1
 FP64, MIXED = 0, 1
 QUERY_RAY_FIRE, QUERY_POINT_IN_VOLUME, QUERY_OCCLUDED, QUERY_FIND_VOLUME = 0, 1, 2, 3
@@ -58,6 +59,9 @@ SIGNATURES = {
                                           _VP, _VP, _i32, _VP]),
     "xdgcu_walk_elements_packed_noalloc": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _i64,
                                                   _VP, _VP, _VP, _VP, _i32, _VP]),
+    "xdgcu_set_surface_boundary": (_int, [_VP, _i32, _VP, _VP]),
+    "xdgcu_transport_surfaces": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _dbl, _i32, _i32, _i32,
+                                        _VP, _VP, _VP, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_seed_streams": (_int, [ctypes.c_uint64, _i64, _VP]),
     "xdgcu_transport_elements": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _dbl, _i32, _VP, _VP,
                                         _VP, _VP, _i32, _VP]),

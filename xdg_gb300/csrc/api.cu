@@ -42,6 +42,7 @@ struct SurfaceRec {
   int64_t count;
   int32_t fwd_tree = -1;
   int32_t rev_tree = -1;
+  int32_t bc = 0;  // boundary condition for the particle loop (xdgcu_set_surface_boundary)
   double bump = 0.0;
 };
 
@@ -291,7 +292,7 @@ struct xdgcu_ctx {
   std::vector<double> h_tri_xyz;
   std::vector<int32_t> h_tri_face, h_tri_surf;
   DevMem<double> d_tri_xyz;
-  DevMem<int32_t> d_tri_face, d_tri_surf, d_surf_id, d_surf_rev;
+  DevMem<int32_t> d_tri_face, d_tri_surf, d_surf_id, d_surf_rev, d_surf_fwd, d_surf_bc;
   bool tri_dirty = true, surf_dirty = true;
   // tet mesh
   bool has_tets = false;
@@ -319,6 +320,7 @@ struct xdgcu_ctx {
   int32_t trace_stack = 48;      // shared-memory stack entries per lane
   int32_t trace_grab = 0;        // 0: one contiguous chunk per warp; > 0: device work queue
   int64_t trace_sort_min = 0;    // batches of at least this many rays run in coherent order (0 = never)
+  int32_t particle_event_wait = 16;  // particle loop: lanes gathered before their events run
   int32_t leaf_max = 4;
   int32_t walk_queue = 1;
   int32_t walk_flush_wait = 8;
@@ -353,17 +355,26 @@ int sync_surfaces(xdgcu_ctx* c) {
   }
   if (c->surf_dirty) {
     const int64_t ns = (int64_t)c->surfs.size();
-    std::vector<int32_t> ids(std::max<int64_t>(1, ns)), rev(std::max<int64_t>(1, ns));
+    const size_t m = (size_t)std::max<int64_t>(1, ns);
+    std::vector<int32_t> ids(m), rev(m), fwd(m), bc(m);
     for (int64_t s = 0; s < ns; ++s) {
       ids[s] = c->surfs[s].id;
       rev[s] = c->surfs[s].rev_tree;
+      fwd[s] = c->surfs[s].fwd_tree;
+      bc[s] = c->surfs[s].bc;
     }
-    API_CUDA(c->d_surf_id.alloc(std::max<int64_t>(1, ns)), "alloc surfaces");
-    API_CUDA(c->d_surf_rev.alloc(std::max<int64_t>(1, ns)), "alloc surfaces");
-    API_CUDA(cudaMemcpy(c->d_surf_id.p, ids.data(), sizeof(int32_t) * ids.size(),
-                        cudaMemcpyHostToDevice), "upload surfaces");
-    API_CUDA(cudaMemcpy(c->d_surf_rev.p, rev.data(), sizeof(int32_t) * rev.size(),
-                        cudaMemcpyHostToDevice), "upload surfaces");
+    API_CUDA(c->d_surf_id.alloc((int64_t)m), "alloc surfaces");
+    API_CUDA(c->d_surf_rev.alloc((int64_t)m), "alloc surfaces");
+    API_CUDA(c->d_surf_fwd.alloc((int64_t)m), "alloc surfaces");
+    API_CUDA(c->d_surf_bc.alloc((int64_t)m), "alloc surfaces");
+    API_CUDA(cudaMemcpy(c->d_surf_id.p, ids.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice),
+             "upload surfaces");
+    API_CUDA(cudaMemcpy(c->d_surf_rev.p, rev.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice),
+             "upload surfaces");
+    API_CUDA(cudaMemcpy(c->d_surf_fwd.p, fwd.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice),
+             "upload surfaces");
+    API_CUDA(cudaMemcpy(c->d_surf_bc.p, bc.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice),
+             "upload surfaces");
     c->surf_dirty = false;
   }
   return XDGCU_OK;
@@ -665,11 +676,11 @@ int with_length_order(xdgcu_ctx* c, WalkArgs& a, cudaStream_t s, Body body) {
 // batch is large enough (trace_sort_min) a coherent ray order, both in one
 // stream-ordered scratch allocation freed after the launch.
 cudaError_t launch_trace(xdgcu_ctx* c, int mode, bool mixed, SurfArgs a, double extent,
-                         cudaStream_t s) {
+                         cudaStream_t s, int32_t min_grab = 0) {
   if (a.n <= 0) return cudaSuccess;
   const bool sort = c->trace_sort_min > 0 && a.n >= c->trace_sort_min && a.n < ((int64_t)1 << 31) &&
                     extent > 0.0;
-  a.grab = c->trace_grab;
+  a.grab = std::max(c->trace_grab, min_grab);
   a.work = nullptr;
   a.order = nullptr;
   if (a.grab == 0 && !sort) return launch_surface_query(mode, mixed, a, s);
@@ -998,6 +1009,10 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     if (value < 0 || value > (1 << 20) || value % 32 != 0)
       return set_err(XDGCU_ERR_INVALID_ARG, "trace_grab must be 0 or a multiple of 32 up to 2^20");
     c->trace_grab = (int32_t)value;
+  } else if (k == "particle_event_wait") {
+    if (value < 1 || value > 32)
+      return set_err(XDGCU_ERR_INVALID_ARG, "particle_event_wait must be 1..32");
+    c->particle_event_wait = (int32_t)value;
   } else if (k == "trace_sort_min") {
     if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "trace_sort_min must be >= 0");
     c->trace_sort_min = value;
@@ -1029,6 +1044,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "trace_stack") *value = c->trace_stack;
   else if (k == "trace_grab") *value = c->trace_grab;
   else if (k == "trace_sort_min") *value = c->trace_sort_min;
+  else if (k == "particle_event_wait") *value = c->particle_event_wait;
   else if (k == "leaf_max") *value = c->leaf_max;
   else if (k == "walk_queue") *value = c->walk_queue;
   else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
@@ -1553,6 +1569,127 @@ int xdgcu_walk_elements(xdgcu_ctx* c, int64_t n, const int32_t* start_index, con
 // ---------------------------------------------------------------------------
 // device particle loop over the tet mesh
 // ---------------------------------------------------------------------------
+
+int xdgcu_set_surface_boundary(xdgcu_ctx* c, int32_t n, const int32_t* surface_ids,
+                               const int32_t* conditions) {
+  CHECK_CTX(c);
+  if (n < 0 || (n > 0 && (!surface_ids || !conditions)))
+    return set_err(XDGCU_ERR_INVALID_ARG, "bad boundary condition arguments");
+  std::lock_guard<std::mutex> g(c->mu);
+  for (int32_t k = 0; k < n; ++k) {
+    if (conditions[k] < XDGCU_BC_TRANSMISSION || conditions[k] > XDGCU_BC_REFLECTING)
+      return set_err(XDGCU_ERR_INVALID_ARG, "unknown boundary condition");
+    auto it = c->surf_index.find(surface_ids[k]);
+    if (it == c->surf_index.end())
+      return set_err(XDGCU_ERR_NOT_FOUND, "boundary condition for an unregistered surface");
+  }
+  for (int32_t k = 0; k < n; ++k) c->surfs[c->surf_index[surface_ids[k]]].bc = conditions[k];
+  c->surf_dirty = true;
+  return sync_surfaces(c);
+}
+
+int xdgcu_transport_surfaces(xdgcu_ctx* c, int64_t n, int32_t* tree, double* position,
+                             double* direction, uint64_t* rng_state, double mean_free_path,
+                             int32_t max_events, int32_t graveyard_tree, int32_t history_cap,
+                             int32_t* history, int32_t* history_count, double* distance,
+                             int32_t* events, double* tree_tally, int32_t* status,
+                             int32_t precision, void* stream) {
+  CHECK_CTX(c);
+  if (n < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative particle count");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (!(mean_free_path > 0.0) || !(mean_free_path < 1e300))
+    return set_err(XDGCU_ERR_INVALID_ARG, "mean_free_path must be positive and finite");
+  if (max_events < 0) return set_err(XDGCU_ERR_INVALID_ARG, "max_events must be >= 0");
+  if (history_cap < 1 || history_cap > 4096)
+    return set_err(XDGCU_ERR_INVALID_ARG, "history_cap must be 1..4096");
+  if (n == 0) return XDGCU_OK;
+  if (!tree || !position || !direction || !rng_state || !history || !history_count ||
+      !distance || !events)
+    return set_err(XDGCU_ERR_INVALID_ARG, "null particle state");
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    int rc = sync_surfaces(c);
+    if (rc) return rc;
+    rc = sync_tree_tables(c);
+    if (rc) return rc;
+  }
+  const int kind = classify({tree, position, direction, rng_state, history, history_count,
+                             distance, events, tree_tally, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  SurfArgs a{};
+  a.trees = c->d_surf_trees.p;
+  a.n_trees = (int32_t)c->surf_trees.size();
+  a.n = n;
+  a.orientation = XDGCU_EXITING;
+  a.tri_face = c->d_tri_face.p;
+  a.tri_surf = c->d_tri_surf.p;
+  a.surf_id = c->d_surf_id.p;
+  a.surf_rev_tree = c->d_surf_rev.p;
+  a.surf_fwd_tree = c->d_surf_fwd.p;
+  a.surf_bc = c->d_surf_bc.p;
+  a.tri_xyz = c->d_tri_xyz.p;
+  a.occupancy = c->trace_occupancy;
+  a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
+  a.flush_wait = c->trace_flush_wait;
+  a.stack = c->trace_stack;
+  a.mfp = mean_free_path;
+  a.max_events = max_events;
+  a.graveyard_tree = graveyard_tree;
+  a.hist_cap = history_cap;
+  a.event_wait = c->particle_event_wait;
+  const bool mixed = precision == XDGCU_MIXED;
+  cudaStream_t st = (cudaStream_t)stream;
+  auto bind = [&](char* const* p) {
+    a.p_tree = (int32_t*)p[0];
+    a.p_pos = (double*)p[1];
+    a.p_dir = (double*)p[2];
+    a.p_rng = (unsigned long long*)p[3];
+    a.p_hist = (int32_t*)p[4];
+    a.p_hcount = (int32_t*)p[5];
+    a.p_dist = (double*)p[6];
+    a.p_events = (int32_t*)p[7];
+    a.p_tally = (double*)p[8];
+    a.status = (int32_t*)p[9];
+  };
+  if (kind == 1) {
+    char* p[10] = {(char*)tree, (char*)position, (char*)direction, (char*)rng_state,
+                   (char*)history, (char*)history_count, (char*)distance, (char*)events,
+                   (char*)tree_tally, (char*)status};
+    bind(p);
+    int rc = begin_query(c, st, &a.counters);
+    if (rc) return rc;
+    // particle histories differ in length by orders of magnitude: warps
+    // always take particles from the work queue, 32 at a time at least
+    API_CUDA(launch_trace(c, MODE_PARTICLE, mixed, a, 0.0, st, 32), "particle launch");
+    return XDGCU_OK;
+  }
+  Slot* s = get_slot(c);
+  if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  if (!st) st = s->stream;
+  const size_t un = (size_t)n;
+  Arr A[10] = {{tree, tree, 4 * un},
+               {position, position, 24 * un},
+               {direction, direction, 24 * un},
+               {rng_state, rng_state, 8 * un},
+               {history, history, 4 * un * (size_t)history_cap},
+               {history_count, history_count, 4 * un},
+               {distance, distance, 8 * un},
+               {events, events, 4 * un},
+               {tree_tally, tree_tally, tree_tally ? 8 * (c->surf_trees.size() + 1) : 0},
+               {nullptr, status, status ? 4 * un : 0}};
+  std::vector<Arr*> all;
+  for (auto& x : A) all.push_back(&x);
+  int rc = stage_in(s, all, st);
+  if (rc) return rc;
+  char* p[10];
+  for (int k = 0; k < 10; ++k) p[k] = (char*)A[k].dev;
+  bind(p);
+  rc = begin_query(c, st, &a.counters);
+  if (rc) return rc;
+  API_CUDA(launch_trace(c, MODE_PARTICLE, mixed, a, 0.0, st, 32), "particle launch");
+  return stage_out(all, st);
+}
 
 int xdgcu_seed_streams(uint64_t seed, int64_t n, uint64_t* states) {
   if (n < 0 || (n > 0 && !states)) return set_err(XDGCU_ERR_INVALID_ARG, "bad seed arguments");

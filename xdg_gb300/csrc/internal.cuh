@@ -86,6 +86,7 @@ enum : int32_t {
   RAY_OUTPUT_FULL = 6,
   RAY_EVENT_LIMIT = 7,
   RAY_LOST = 8,
+  RAY_STUCK = 9,
 };
 
 // work counters (xdgcu_get_counters)

@@ -9,7 +9,16 @@
 
 namespace xdgcu {
 
-enum QueryMode : int { MODE_RAY_FIRE = 0, MODE_PIV = 1, MODE_OCCLUDED = 2, MODE_FIND_VOLUME = 3 };
+enum QueryMode : int {
+  MODE_RAY_FIRE = 0,
+  MODE_PIV = 1,
+  MODE_OCCLUDED = 2,
+  MODE_FIND_VOLUME = 3,
+  MODE_PARTICLE = 4  // the particle_sim loop: every ray is one flight of a particle
+};
+
+// boundary conditions of the particle loop (MeshManager surface property)
+enum : int32_t { BC_TRANSMISSION = 0, BC_VACUUM = 1, BC_REFLECTING = 2 };
 
 struct SurfArgs {
   const TreeDev* trees;  // indexed by tree id - 1
@@ -49,6 +58,25 @@ struct SurfArgs {
   const int32_t* vol_trees;
   int32_t n_vols;
   int32_t ipc_volume;
+  // MODE_PARTICLE: per-particle state, read at the start and written back
+  // when the particle stops
+  double* p_pos;
+  double* p_dir;
+  int32_t* p_tree;              // surface tree of the particle's volume (-1: ended outside)
+  unsigned long long* p_rng;    // SplitMix64 state
+  double* p_dist;               // path length so far
+  int32_t* p_events;
+  int32_t* p_hist;              // exclusion history: hist_cap entries per particle, a ring
+  int32_t* p_hcount;            // faces appended since the history was last cleared
+  int32_t hist_cap;
+  double* p_tally;              // track length per tree id (atomics), or null
+  double mfp;
+  int32_t max_events;
+  int32_t graveyard_tree;       // > 0: a particle that would enter this tree ends
+  int32_t event_wait;           // lanes whose flights ended before the warp runs their events
+  const int32_t* surf_fwd_tree;
+  const int32_t* surf_bc;
+  const double* tri_xyz;        // 9 doubles per global triangle, mesh vertex order
 };
 
 struct PointArgs {

@@ -44,6 +44,7 @@
 // keeps its near distance so entries beyond a closer hit found meanwhile are
 // discarded without fetching the node.  A deeper stack costs shared memory
 // and so resident blocks; overflow ends the ray with RAY_STACK_OVERFLOW.
+#include "sample.cuh"
 #include "traverse.cuh"
 
 namespace xdgcu {
@@ -64,6 +65,7 @@ struct WarpQueue {
   int32_t rface[32];
   int32_t rsurf[32];
   int32_t rflags[32];  // bit 0: accepted, bit 1: dot(d, n) > 0
+  int32_t rtri[32];    // global triangle of the result (particle mode: face normal)
   uint32_t head, tail;
   int32_t pad[2];
 };
@@ -120,6 +122,11 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
   bool bhas = false, bdot = false;
   const int32_t* excl = nullptr;
   int32_t nexcl = 0;
+  // MODE_PARTICLE: the particle's stream, path length, events, history count
+  // and the triangle of the best hit
+  unsigned long long rs = 0ull;
+  double pdist = 0.0;
+  int32_t pev = 0, hc = 0, btri = -1;
   BoxRay32 br32;
   Ray32 r32;
   BoxRay64 br64;
@@ -178,7 +185,18 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
 
   while (true) {
     // ---- finalize finished rays ----
-    if (has_ray && !trav && npend == 0) {
+    bool fin = has_ray && !trav && npend == 0;
+    if (MODE == MODE_PARTICLE) {
+      // A particle's event (sampling, logarithm, normalisation: ~100 FP64
+      // instructions) is run for many lanes at once: a lane whose flight has
+      // ended waits until event_wait lanes are ready or no lane of the warp
+      // has traversal work left.  FP64 instructions cost the same issue time
+      // however few lanes are active.
+      const unsigned fm = __ballot_sync(kFull, fin);
+      const unsigned wm = __ballot_sync(kFull, has_ray && (trav || npend > 0));
+      if (!(__popc(fm) >= a.event_wait || wm == 0u)) fin = false;
+    }
+    if (fin) {
       bool done = true;
       if (MODE == MODE_RAY_FIRE) {
         a.t_out[ray] = bhas ? bt : INFTY;
@@ -204,6 +222,105 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
           done = false;
         } else {
           a.flag_out[ray] = inside ? a.vol_ids[vk] : a.ipc_volume;
+        }
+      } else if (MODE == MODE_PARTICLE) {
+        // one event of tools/particle_sim.h:128-141 after the flight's
+        // ray_fire (EXITING, history excluded)
+        bool alive = false;
+        if (status == RAY_OK && tid > 0) {
+          if (bhas && bt == 0.0) {
+            status = RAY_STUCK;  // :36-40
+          } else if (!bhas) {
+            status = RAY_LOST;   // :41-45
+          } else {
+            // ray_fire appended the hit face to the history
+            a.p_hist[ray * a.hist_cap + (hc % a.hist_cap)] = bface;
+            ++hc;
+            const double c = sample_collision(rs, a.mfp);  // :47-49
+            alive = true;
+            if (dlt(c, bt)) {
+              // advance + collide (:66-70, :57-64)
+              o = add3(o, scl3(c, d));
+              pdist += c;
+              if (a.p_tally) atomicAdd(&a.p_tally[tid], c);
+              ++pev;
+              d = sample_direction(rs);
+              hc = 0;
+            } else {
+              // advance to the surface + cross_surface (:71-75, :78-118)
+              o = add3(o, scl3(bt, d));
+              pdist += bt;
+              if (a.p_tally) atomicAdd(&a.p_tally[tid], bt);
+              ++pev;
+              const int32_t sidx = __ldg(&a.tri_surf[btri]);
+              const int32_t bc = __ldg(&a.surf_bc[sidx]);
+              if (bc == BC_REFLECTING) {
+                // surface_normal(surface, r, &history) = face_normal(history.back())
+                // (xdg.cpp:272-289); reflect and renormalise (:88-96)
+                d3 v0, v1, v2;
+                const double* tx9 = a.tri_xyz + 9 * (int64_t)btri;
+                v0 = mk3(tx9[0], tx9[1], tx9[2]);
+                v1 = mk3(tx9[3], tx9[4], tx9[5]);
+                v2 = mk3(tx9[6], tx9[7], tx9[8]);
+                d3 nrm = face_normal64(v0, v1, v2);
+                const double proj = dot3(nrm, d);
+                const double mag = sqrt(nrm.x * nrm.x + nrm.y * nrm.y + nrm.z * nrm.z);
+                nrm = scl3(2.0 * proj / mag, nrm);
+                d = normalize64(sub3(d, nrm));
+                a.p_hist[ray * a.hist_cap] = bface;  // history = {history.back()}
+                hc = 1;
+              } else if (bc == BC_VACUUM) {
+                alive = false;
+              } else {
+                // MeshManager::next_volume (mesh_manager_interface.cpp:202-214)
+                const int32_t fwd = __ldg(&a.surf_fwd_tree[sidx]);
+                const int32_t rev = __ldg(&a.surf_rev_tree[sidx]);
+                if (fwd == tid) {
+                  tid = rev;
+                } else if (rev == tid) {
+                  tid = fwd;
+                } else {
+                  status = RAY_INVALID;  // not a parent volume of the surface
+                  alive = false;
+                }
+                if (alive && (tid < 1 || tid == a.graveyard_tree)) {
+                  tid = -1;  // :112-116
+                  alive = false;
+                }
+              }
+            }
+            if (alive && pev >= a.max_events) {
+              status = RAY_EVENT_LIMIT;
+              alive = false;
+            }
+          }
+        }
+        if (alive) {
+          // next flight from the new position in the (new) volume
+          bt = INFTY;
+          bhas = false;
+          bdot = false;
+          bface = -1;
+          bsurf = -1;
+          btri = -1;
+          sp = 0;
+          leaf_p = leaf_end = 0;
+          excl = a.p_hist + ray * a.hist_cap;
+          nexcl = min(hc, a.hist_cap);
+          begin_tree();
+          done = false;
+        } else {
+          a.p_pos[3 * ray] = o.x;
+          a.p_pos[3 * ray + 1] = o.y;
+          a.p_pos[3 * ray + 2] = o.z;
+          a.p_dir[3 * ray] = d.x;
+          a.p_dir[3 * ray + 1] = d.y;
+          a.p_dir[3 * ray + 2] = d.z;
+          a.p_tree[ray] = tid;
+          a.p_rng[ray] = rs;
+          a.p_dist[ray] = pdist;
+          a.p_events[ray] = pev;
+          a.p_hcount[ray] = hc;
         }
       } else {
         a.flag_out[ray] = bhas ? 1 : 0;
@@ -245,26 +362,46 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
           bsurf = -1;
           leaf_p = leaf_end = 0;
           vk = 0;
-          tid = (MODE == MODE_FIND_VOLUME) ? (a.n_vols > 0 ? a.vol_trees[0] : 0)
-                                           : (a.ray_trees ? a.ray_trees[idx] : a.tree);
-          o = load3(a.org, idx);
-          if ((MODE == MODE_PIV || MODE == MODE_FIND_VOLUME) && a.dir == nullptr)
-            d = mk3(1. / sqrt(2.0), 1 / sqrt(2.0), 0.0);  // embree/ray_tracer.cpp:268
-          else
-            d = load3(a.dir, idx);
+          if (MODE == MODE_PARTICLE) {
+            tid = a.p_tree[idx];
+            o = load3(a.p_pos, idx);
+            d = load3(a.p_dir, idx);
+            rs = a.p_rng[idx];
+            pdist = a.p_dist[idx];
+            pev = a.p_events[idx];
+            hc = a.p_hcount[idx];
+            btri = -1;
+          } else {
+            tid = (MODE == MODE_FIND_VOLUME) ? (a.n_vols > 0 ? a.vol_trees[0] : 0)
+                                             : (a.ray_trees ? a.ray_trees[idx] : a.tree);
+            o = load3(a.org, idx);
+            if ((MODE == MODE_PIV || MODE == MODE_FIND_VOLUME) && a.dir == nullptr)
+              d = mk3(1. / sqrt(2.0), 1 / sqrt(2.0), 0.0);  // embree/ray_tracer.cpp:268
+            else
+              d = load3(a.dir, idx);
+          }
           bt = (MODE == MODE_RAY_FIRE && a.tmax) ? a.tmax[idx] : INFTY;
           excl = nullptr;
           nexcl = 0;
-          if (MODE != MODE_OCCLUDED && MODE != MODE_FIND_VOLUME && a.excl_off) {
+          if (MODE == MODE_PARTICLE) {
+            excl = a.p_hist + idx * a.hist_cap;
+            nexcl = hc < 0 ? 0 : min(hc, a.hist_cap);
+          } else if (MODE != MODE_OCCLUDED && MODE != MODE_FIND_VOLUME && a.excl_off) {
             const int32_t e0 = a.excl_off[idx];
             excl = a.excl_ids + e0;
             nexcl = a.excl_off[idx + 1] - e0;
           }
-          if (!finite3(o) || !finite3(d) || nan_bits(bt)) {
+          if (!finite3(o) || !finite3(d) || nan_bits(bt) ||
+              (MODE == MODE_PARTICLE && (hc < 0 || nan_bits(pdist)))) {
             status = RAY_INVALID;
             trav = false;
           } else if (MODE == MODE_FIND_VOLUME && a.n_vols == 0) {
             trav = false;  // no volume to try: the implicit complement
+          } else if (MODE == MODE_PARTICLE && tid < 0) {
+            trav = false;  // the particle ended earlier: left as it is
+          } else if (MODE == MODE_PARTICLE && pev >= a.max_events) {
+            status = RAY_EVENT_LIMIT;
+            trav = false;
           } else {
             begin_tree();
           }
@@ -406,7 +543,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
       const int32_t onexcl = __shfl_sync(kFull, nexcl, owner);
       int32_t flags = 0;
       double rt = 0.0;
-      int32_t rface = -1, rsurf = -1;
+      int32_t rface = -1, rsurf = -1, rtri = -1;
       if (mine) {
         const double* op64 = otree->prim64;
         const int32_t* opref = otree->prim_ref;
@@ -428,7 +565,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
               int sg = normal_dot_sign(od, v0, v1, v2);
               if (__ldg(&a.surf_rev_tree[sidx]) == otid) sg = -sg;
               bool keep = true;
-              if (MODE == MODE_RAY_FIRE) {  // orientation_cull, :12-24
+              if (MODE == MODE_RAY_FIRE || MODE == MODE_PARTICLE) {  // orientation_cull, :12-24
                 if (a.orientation == 0 && sg < 0) keep = false;   // dot < 0
                 if (a.orientation == 1 && sg >= 0) keep = false;  // dot >= 0
               }
@@ -439,6 +576,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
                 rt = t;
                 rface = fid;
                 rsurf = __ldg(&a.surf_id[sidx]);
+                rtri = gtri;
               }
             }
           }
@@ -448,6 +586,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
       Q.rt[lane] = rt;
       Q.rface[lane] = rface;
       Q.rsurf[lane] = rsurf;
+      if (MODE == MODE_PARTICLE) Q.rtri[lane] = rtri;
       const int my_owner = owner;
       __syncwarp();
       // each ray merges its own results in queue order
@@ -470,6 +609,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
           bt = t;
           bface = f;
           bsurf = Q.rsurf[j];
+          if (MODE == MODE_PARTICLE) btri = Q.rtri[j];
           bdot = (fl & 2) != 0;
           changed = true;
         }
@@ -488,8 +628,8 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
 
 int g_num_sms = 0;
 // resident blocks per SM, by kernel variant, MINB and stack depth (8..64 step 8)
-int g_blocks_per_sm[8][3][kTStackMax / 8 + 1] = {};
-bool g_smem_attr[8][3] = {};
+int g_blocks_per_sm[10][3][kTStackMax / 8 + 1] = {};
+bool g_smem_attr[10][3] = {};
 
 template <int MODE, bool MIXED, int MINB>
 cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
@@ -548,6 +688,8 @@ cudaError_t launch_surface_query(int mode, bool mixed, const SurfArgs& a, cudaSt
     case 5: return launch_one<MODE_OCCLUDED, true>(a, st, 5);
     case 6: return launch_one<MODE_FIND_VOLUME, false>(a, st, 6);
     case 7: return launch_one<MODE_FIND_VOLUME, true>(a, st, 7);
+    case 8: return launch_one<MODE_PARTICLE, false>(a, st, 8);
+    case 9: return launch_one<MODE_PARTICLE, true>(a, st, 9);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -18,11 +18,12 @@ import numpy as np
 from . import _lib
 from ._lib import ANY, ENTERING, EXITING, FP64, MIXED, check  # noqa: F401
 from ._lib import (QUERY_FIND_VOLUME, QUERY_OCCLUDED, QUERY_POINT_IN_VOLUME,  # noqa: F401
-                   QUERY_RAY_FIRE)
+                   QUERY_RAY_FIRE, BC_REFLECTING, BC_TRANSMISSION, BC_VACUUM)
 
 # keys of xdgcu_set_tuning / xdgcu_get_tuning
 TUNING_KEYS = ("trace_occupancy", "trace_node_iters", "trace_node_iters_fp64",
-               "trace_flush_wait", "trace_stack", "trace_grab", "trace_sort_min", "leaf_max",
+               "trace_flush_wait", "trace_stack", "trace_grab", "trace_sort_min",
+               "particle_event_wait", "leaf_max",
                "walk_queue", "walk_flush_wait", "walk_sort_min")
 
 INFTY = np.finfo(np.float64).max
@@ -451,6 +452,31 @@ class CudaRayTracer:
             int(precision), stream if stream is not None else out.stream()), "transport_elements")
         return st
 
+    def set_surface_boundary(self, conditions: dict):
+        """xdgcu_set_surface_boundary: {surface id: BC_TRANSMISSION /
+        BC_VACUUM / BC_REFLECTING}."""
+        ids = np.array(list(conditions.keys()), dtype=np.int32)
+        bc = np.array([conditions[k] for k in conditions], dtype=np.int32)
+        self._check(self.L.xdgcu_set_surface_boundary(self.ctx, len(ids), _addr(ids), _addr(bc)),
+                    "set_surface_boundary")
+
+    def transport_surfaces(self, tree, pos, dirs, rng, mfp, max_events, history, history_count,
+                           distance, events, tally=None, graveyard_tree=0, precision=MIXED,
+                           stream=None):
+        """xdgcu_transport_surfaces: updates the particle state in place
+        (torch CUDA tensors or NumPy arrays).  ``history`` is n x cap.
+        Returns the per-particle status array."""
+        n = len(tree)
+        out = _Out(pos)
+        st = out.i32(n)
+        cap = int(history.shape[1])
+        self._check(self.L.xdgcu_transport_surfaces(
+            self.ctx, n, _addr(tree), _addr(pos), _addr(dirs), _addr(rng), float(mfp),
+            int(max_events), int(graveyard_tree), cap, _addr(history), _addr(history_count),
+            _addr(distance), _addr(events), _addr(tally), _addr(st), int(precision),
+            stream if stream is not None else out.stream()), "transport_surfaces")
+        return st
+
     def walk_elements_packed(self, start_index, start, u, distance, capacity, max_segs=4096,
                              precision=MIXED, stream=None):
         """Packed walk: returns (seg_elem [capacity], seg_len, offsets [n+1], status)."""
@@ -769,6 +795,36 @@ class XDG:
                    events=ev.cpu().numpy(), status=final)
         if tally:
             res["tally"] = ty.cpu().numpy()
+        return res
+
+    def simulate_particles(self, volumes, pos, dirs, rng, mfp=1.0, max_events=1_000_000,
+                           ipc_graveyard=False, precision=MIXED, history_cap=16, tally=False):
+        """The particle_sim tool loop (tools/particle_sim.h:128-141) for
+        particles in ``volumes`` (one volume id per particle) at ``pos`` along
+        ``dirs`` with per-particle streams ``rng``, every event on the device
+        (xdgcu_transport_surfaces).  Boundary conditions come from
+        CudaRayTracer.set_surface_boundary.  Returns a dict of NumPy arrays:
+        volume (ID_NONE once a particle left through the graveyard or had no
+        next volume), pos, dir, rng, distance, events, status and, when asked
+        for, tally (path length per volume id, the tool's cell_tracks)."""
+        n = len(pos)
+        tree = self._trees(np.asarray(volumes)).astype(np.int32)
+        r = _host(pos, np.float64, (-1, 3)).copy()
+        u = _host(dirs, np.float64, (-1, 3)).copy()
+        s = np.ascontiguousarray(rng, dtype=np.uint64).copy()
+        hist = np.zeros((n, history_cap), dtype=np.int32)
+        hc = np.zeros(n, dtype=np.int32)
+        d = np.zeros(n)
+        ev = np.zeros(n, dtype=np.int32)
+        ty = np.zeros(self.rti.num_registered_surface_trees() + 1) if tally else None
+        grave = self.volume_to_surface_tree[self.model.implicit_complement] if ipc_graveyard else 0
+        st = self.rti.transport_surfaces(tree, r, u, s, mfp, max_events, hist, hc, d, ev, ty,
+                                         grave, precision)
+        vol_of = {t: v for v, t in self.volume_to_surface_tree.items()}
+        res = dict(volume=np.array([vol_of.get(int(t), ID_NONE) for t in tree], dtype=np.int32),
+                   tree=tree, pos=r, dir=u, rng=s, distance=d, events=ev, status=st)
+        if tally:
+            res["tally"] = {v: ty[t] for v, t in self.volume_to_surface_tree.items()}
         return res
 
     def _walk_packed(self, elem_index, r, u, dist, precision):
