@@ -51,8 +51,8 @@ MANY_SURFACES = 256
 MANY_WORKLOAD = "256_surfaces_sphere_torus_tris_10^U(3,5.7)_rays_10^U(3,6)"
 TUNE_RAYS = 1_000_000       # autotuner sample (same distribution, its own seed)
 TUNE_TRACKS = 1_000_000     # the walk's length order pays off only on large batches
-TRACE_KEYS = ("trace_occupancy", "trace_stack", "trace_node_iters", "trace_node_iters_fp64",
-              "trace_flush_wait", "trace_grab", "trace_sort_min")
+TRACE_KEYS = ("node_width", "trace_occupancy", "trace_stack", "trace_node_iters",
+              "trace_node_iters_fp64", "trace_flush_wait", "trace_grab", "trace_sort_min")
 WALK_KEYS = ("walk_queue", "walk_flush_wait", "walk_sort_min")
 CPU_SAMPLE = 4_000_000      # rays of the same workload timed on the host cores
 TRANSPORT_WORKLOAD = "tet_cube_50^3x6_kuhn_jitter0.2_1e6_particles_mfp1_walk_elements_tool"
@@ -393,6 +393,13 @@ def bench_surface_transport(torch, L, x, model, dev, stream, sptr, p, d, trees_h
 
     ms = timed(torch, step(MIXED), max(3, args.steps // 4), args.warmup, world, stream)
     events = int(T["ev"].sum().item())
+    # work per event (untimed counting run): nodes, triangles, FP64 escalations
+    x.rti.set_counting(True)
+    step(MIXED)()
+    torch.cuda.synchronize()
+    cnt = x.rti.counters()
+    x.rti.set_counting(False)
+    per_event = {k: cnt[k] / max(1, events) for k in ("node", "prim", "escalate")}
     bad = int((T["st"] != 0).sum().item())
     keys = ("tree", "pos", "dir", "rng", "dist", "ev")
     mixed_state = {k: T[k].clone() for k in keys}
@@ -406,6 +413,7 @@ def bench_surface_transport(torch, L, x, model, dev, stream, sptr, p, d, trees_h
         "events_per_particle": events / max(1, n), "speedup_mixed_vs_fp64": ms64 / ms,
         "particles_differing_mixed_vs_fp64": mism, "particles_with_status": bad,
         "step": "reset sources + one xdgcu_transport_surfaces launch (all events)",
+        "per_event": per_event,
     }
     if rank == 0 and not args.no_oracle:
         from oracle import oracle as xo

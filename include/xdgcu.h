@@ -385,6 +385,8 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      origin.  Results are written at the callers' indices
  *                      and do not depend on it
  *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4)
+ *   "node_width"       children per BVH node for trees built (or rebuilt,
+ *                      xdgcu_rebuild_trees) afterwards: 4 (default) or 8
  *   "walk_queue"       mixed-precision walk: 1 (default) runs the FP64 face
  *                      tests of a warp's tracks 32 at a time from a per-warp
  *                      queue, 0 lets each lane evaluate its own faces
@@ -412,7 +414,9 @@ enum {
  * trace_occupancy, trace_stack, trace_node_iters (or trace_node_iters_fp64
  * for XDGCU_FP64), trace_flush_wait, trace_grab and, for samples of at least
  * 65,536 rays, trace_sort_min, one key at a time, and leaves the context set
- * to the fastest combination found.  Each setting is timed as the median of
+ * to the fastest combination found.  With tune_width != 0 it does so for
+ * node_width 4 and 8, rebuilding the surface trees for each
+ * (xdgcu_rebuild_trees), and keeps the faster width.  Each setting is timed as the median of
  * `reps` launches after one untimed launch.  Every setting must reproduce
  * the first run's outputs byte for byte (XDGCU_ERR_STATE otherwise); settings
  * whose smaller stack overflows are skipped.  When the coherent order wins,
@@ -421,7 +425,7 @@ enum {
  * queries of this context meanwhile. */
 int xdgcu_autotune_trace(xdgcu_ctx* ctx, int32_t query, int32_t tree, const int32_t* ray_trees,
                          int64_t n, const double* origins, const double* directions,
-                         int32_t precision, int32_t reps, double* best_ms);
+                         int32_t precision, int32_t reps, int32_t tune_width, double* best_ms);
 
 /* Autotuner of the walk launch parameters (no counterpart in the reference):
  * walk_queue (mixed precision only), walk_flush_wait and, for samples of at
@@ -433,8 +437,15 @@ int xdgcu_autotune_walk(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
                         const double* start, const double* u, const double* distance,
                         int32_t max_segs, int32_t precision, int32_t reps, double* best_ms);
 
+/* Rebuilds the existing trees (kinds: 1 = surface trees, 2 = element trees,
+ * 3 = both) with the current "node_width" and "leaf_max", keeping their ids
+ * and members.  No counterpart in the reference (Embree trees are built
+ * once); the autotuner uses it to compare node widths.  Must not run while
+ * queries of this context are running. */
+int xdgcu_rebuild_trees(xdgcu_ctx* ctx, int32_t kinds);
+
 /* Tree statistics: out[0] = nodes, [1] = primitives, [2] = depth,
- * [3] = bytes of FP32 nodes, [4] = bytes of FP64 nodes. */
+ * [3] = bytes of FP32 nodes, [4] = bytes of FP64 nodes, [5] = node width. */
 int xdgcu_surface_tree_info(const xdgcu_ctx* ctx, int32_t tree, int64_t out[8]);
 int xdgcu_element_tree_info(const xdgcu_ctx* ctx, int32_t tree, int64_t out[8]);
 

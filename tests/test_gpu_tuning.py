@@ -184,3 +184,82 @@ def test_autotune_walk(cuda, prec):
         assert_same(l1.cpu().numpy()[mask], l0.cpu().numpy()[mask], "lengths")
     finally:
         _restore(x.rti, old)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_node_width_8(cuda, oracle, prec):
+    """Trees built 8-wide (two 4-wide records per node) and rebuilt 4-wide
+    give the same ids and distances for every query, equal to the oracle."""
+    m = synth.nested_spheres(n=8, level=3, jitter=1e-3, seed=7)
+    x8 = XDG(m)
+    x8.rti.set_tuning("node_width", 8)
+    x8.prepare_raytracer()
+    assert x8.rti.tree_info(1)["width"] == 8
+    x4 = XDG(m)
+    x4.prepare_raytracer()
+    assert x4.rti.tree_info(1)["width"] == 4
+    rng = np.random.default_rng(23)
+    n = 60_000
+    p = rng.uniform(-9, 9, (n, 3))
+    d = synth.isotropic_dirs(rng, n)
+    vols = x4.find_volume(p, d, precision=prec)
+    assert_same(x8.find_volume(p, d, precision=prec), vols, "find_volume")
+    r8 = x8.ray_fire(vols, p, d, precision=prec)
+    r4 = x4.ray_fire(vols, p, d, precision=prec)
+    for a, b, what in zip(r8, r4, ("t", "surface", "face")):
+        assert_same(a, b, what)
+    k = np.nonzero(vols[:5000] == 4)[0]
+    ot, os_, of = oracle.volume_tree(m, 4).ray_fire(p[k], d[k])
+    assert_same(r8[0][k], ot, "t vs oracle")
+    assert_same(r8[2][k], of, "face vs oracle")
+    assert_same(x8.point_in_volume(5, p, precision=prec), x4.point_in_volume(5, p, precision=prec),
+                "piv")
+    c8, c4 = x8.closest(3, p[:5000], precision=prec), x4.closest(3, p[:5000], precision=prec)
+    assert_same(c8[0], c4[0], "closest distance")
+    assert_same(c8[1], c4[1], "closest face")
+    o8, o4 = x8.occluded(2, p, d, precision=prec), x4.occluded(2, p, d, precision=prec)
+    assert_same(o8[0], o4[0], "occluded")
+    # back to 4-wide by a rebuild: same results again
+    x8.rti.set_tuning("node_width", 4)
+    x8.rti.rebuild_trees(3)
+    assert x8.rti.tree_info(1)["width"] == 4
+    for a, b, what in zip(x8.ray_fire(vols, p, d, precision=prec), r4, ("t", "surface", "face")):
+        assert_same(a, b, "rebuilt " + what)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_node_width_8_elements(cuda, prec):
+    tm = synth.tet_cube(n=12, size=10.0, jitter=0.2, seed=11)
+    m = synth.model_from_tets(tm, np.ones(len(tm.conn), dtype=np.int32))
+    x8 = XDG(m)
+    x8.rti.set_tuning("node_width", 8)
+    x8.prepare_raytracer()
+    x4 = XDG(m)
+    x4.prepare_raytracer()
+    rng = np.random.default_rng(5)
+    p = rng.uniform(-0.5, 10.5, (50_000, 3))
+    a, b = x8.find_element(p, precision=prec), x4.find_element(p, precision=prec)
+    assert_same(a[0], b[0], "element id")
+    assert_same(a[1], b[1], "element index")
+    assert (a[0] >= 0).sum() > 35_000  # (10/11)^3 of the points lie in the cube
+
+
+def test_autotune_width(nested):
+    """The width search rebuilds the trees and keeps results unchanged."""
+    import torch
+    m, x, p, d, vols = nested
+    pd, dd = torch.from_numpy(p).cuda(), torch.from_numpy(d).cuda()
+    td = torch.from_numpy(x._trees(vols)).cuda()
+    t0, s0, f0 = x.rti.ray_fire(0, pd, dd, ray_trees=td)
+    old = x.rti.tuning()
+    try:
+        ms, tuned = x.rti.autotune_trace(QUERY_RAY_FIRE, 0, pd, dd, ray_trees=td, reps=2,
+                                         tune_width=True)
+        assert tuned["node_width"] in (4, 8)
+        assert x.rti.tree_info(1)["width"] == tuned["node_width"]
+        t1, s1, f1 = x.rti.ray_fire(0, pd, dd, ray_trees=td)
+        torch.cuda.synchronize()
+        assert torch.equal(t0, t1) and torch.equal(s0, s1) and torch.equal(f0, f1)
+    finally:
+        _restore(x.rti, old)
+        x.rti.rebuild_trees(3)

@@ -67,7 +67,8 @@ SIGNATURES = {
                                         _VP, _VP, _i32, _VP]),
     "xdgcu_set_tuning": (_int, [_VP, ctypes.c_char_p, _i64]),
     "xdgcu_get_tuning": (_int, [_VP, ctypes.c_char_p, _I64]),
-    "xdgcu_autotune_trace": (_int, [_VP, _i32, _i32, _VP, _i64, _VP, _VP, _i32, _i32, _D]),
+    "xdgcu_autotune_trace": (_int, [_VP, _i32, _i32, _VP, _i64, _VP, _VP, _i32, _i32, _i32, _D]),
+    "xdgcu_rebuild_trees": (_int, [_VP, _i32]),
     "xdgcu_autotune_walk": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _i32, _i32, _D]),
     "xdgcu_set_counting": (_int, [_VP, _i32]),
     "xdgcu_get_counters": (_int, [_VP, _I64]),

@@ -58,6 +58,7 @@ struct TreeHost {
   int32_t depth = 0;
   TreeDev dev{};
   std::vector<int32_t> members;  // surfaces (surface tree) or tet indices (element tree)
+  double bump_arg = 0.0;         // surface trees: the bump the tree was created with
   ~TreeHost() {
     if (n32) cudaFree(n32);
     if (n64) cudaFree(n64);
@@ -322,6 +323,7 @@ struct xdgcu_ctx {
   int64_t trace_sort_min = 0;    // batches of at least this many rays run in coherent order (0 = never)
   int32_t particle_event_wait = 16;  // particle loop: lanes gathered before their events run
   int32_t leaf_max = 4;
+  int32_t node_width = 4;        // children per BVH node (4 or 8) of trees built afterwards
   int32_t walk_queue = 1;
   int32_t walk_flush_wait = 8;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
@@ -418,6 +420,7 @@ void fill_dev(TreeHost& t, const BuiltTree& b, double min_bump) {
   d.depth = b.depth;
   d.tree_id = t.id;
   d.kind = t.kind;
+  d.width = b.width;
   double m = 0.0;
   for (int k = 0; k < 6; ++k) m = std::max(m, std::fabs(b.bounds[k]));
   d.max_abs = (float)(m * (1.0 + 1e-6));
@@ -448,7 +451,7 @@ int build_surface_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tri
     API_CUDA(cudaGetLastError(), "triangle boxes");
   }
   BuiltTree b;
-  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, st, &b), "bvh build");
+  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, st, &b), "bvh build");
   API_CUDA(t.prim32.alloc(3 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim64.alloc(kPrim64Stride * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
@@ -478,7 +481,7 @@ int build_element_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tet
     API_CUDA(cudaGetLastError(), "tet boxes");
   }
   BuiltTree b;
-  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, st, &b), "bvh build");
+  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, st, &b), "bvh build");
   API_CUDA(t.prim64.alloc(12 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim32.alloc(4 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
@@ -809,6 +812,7 @@ static int create_surface_tree_impl(xdgcu_ctx* c, const std::vector<int32_t>& si
   t->id = (int32_t)c->surf_trees.size() + 1;
   t->kind = TREE_SURFACE;
   t->members = sidx;
+  t->bump_arg = bump;
   // parent tree ids and box dilation (embree/ray_tracer.cpp:76-99)
   if (!global) {
     for (size_t k = 0; k < sidx.size(); ++k) {
@@ -975,8 +979,9 @@ static int tree_info(const std::vector<std::unique_ptr<TreeHost>>& v, int32_t tr
   out[0] = t.n_nodes;
   out[1] = t.prim_ref.n;
   out[2] = t.depth;
-  out[3] = (int64_t)sizeof(Node32) * t.n_nodes;
-  out[4] = (int64_t)sizeof(Node64) * t.n_nodes;
+  out[3] = (int64_t)sizeof(Node32) * t.n_nodes * (t.dev.width / kWidth);
+  out[4] = (int64_t)sizeof(Node64) * t.n_nodes * (t.dev.width / kWidth);
+  out[5] = t.dev.width;
   return XDGCU_OK;
 }
 
@@ -987,6 +992,47 @@ int xdgcu_surface_tree_info(const xdgcu_ctx* c, int32_t tree, int64_t out[8]) {
 int xdgcu_element_tree_info(const xdgcu_ctx* c, int32_t tree, int64_t out[8]) {
   if (!c) return set_err(XDGCU_ERR_INVALID_ARG, "null context");
   return tree_info(c->elem_trees, tree, out);
+}
+
+int xdgcu_rebuild_trees(xdgcu_ctx* c, int32_t kinds) {
+  CHECK_CTX(c);
+  if (kinds < 0 || kinds > 3) return set_err(XDGCU_ERR_INVALID_ARG, "kinds must be 0..3");
+  std::lock_guard<std::mutex> g(c->mu);
+  int rc = sync_surfaces(c);
+  if (rc) return rc;
+  for (auto& tp : c->surf_trees) {
+    if (!(kinds & 1)) break;
+    TreeHost& t = *tp;
+    std::vector<int32_t> tris;
+    std::vector<double> bumps;
+    for (int32_t sx : t.members) {
+      const SurfaceRec& r = c->surfs[sx];
+      const double b = r.bump > 0 ? r.bump : (t.bump_arg > 0 ? t.bump_arg : 1e-3);
+      for (int64_t k = 0; k < r.count; ++k) {
+        tris.push_back((int32_t)(r.first + k));
+        bumps.push_back(b);
+      }
+    }
+    if (t.n32) cudaFree(t.n32);
+    if (t.n64) cudaFree(t.n64);
+    t.n32 = nullptr;
+    t.n64 = nullptr;
+    rc = build_surface_bvh(c, t, tris, bumps);
+    if (rc) return rc;
+  }
+  for (auto& tp : c->elem_trees) {
+    if (!(kinds & 2)) break;
+    TreeHost& t = *tp;
+    if (t.n32) cudaFree(t.n32);
+    if (t.n64) cudaFree(t.n64);
+    t.n32 = nullptr;
+    t.n64 = nullptr;
+    rc = build_element_bvh(c, t, t.members);
+    if (rc) return rc;
+  }
+  c->surf_trees_dirty = true;
+  c->elem_trees_dirty = true;
+  return sync_tree_tables(c);
 }
 
 int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
@@ -1016,6 +1062,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "trace_sort_min") {
     if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "trace_sort_min must be >= 0");
     c->trace_sort_min = value;
+  } else if (k == "node_width") {
+    if (value != 4 && value != 8) return set_err(XDGCU_ERR_INVALID_ARG, "node_width must be 4 or 8");
+    c->node_width = (int32_t)value;
   } else if (k == "leaf_max") {
     if (value < 1 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "leaf_max must be 1..4");
     c->leaf_max = (int32_t)value;
@@ -1046,6 +1095,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "trace_sort_min") *value = c->trace_sort_min;
   else if (k == "particle_event_wait") *value = c->particle_event_wait;
   else if (k == "leaf_max") *value = c->leaf_max;
+  else if (k == "node_width") *value = c->node_width;
   else if (k == "walk_queue") *value = c->walk_queue;
   else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
   else if (k == "walk_sort_min") *value = c->walk_sort_min;

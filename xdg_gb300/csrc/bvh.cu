@@ -9,10 +9,12 @@
 //      primitive position so the tree is well formed for duplicates
 //   5. bottom-up box refit: one thread per leaf climbs, the second thread to
 //      reach a node computes its box (atomic arrival counter)
-//   6. collapse to 4-wide nodes top-down, one level per launch: a wide node
-//      repeatedly opens the child with the largest surface area (the SAH
-//      weight) until it has four children; subtrees with at most kLeafMax
-//      primitives become leaves (they are contiguous in sorted order).
+//   6. collapse to W-wide nodes (W = 4 or 8) top-down, one level per launch:
+//      a wide node repeatedly opens the child with the largest surface area
+//      (the SAH weight) until it has W children; subtrees with at most
+//      leaf_max primitives become leaves (they are contiguous in sorted
+//      order).  An 8-wide node is stored as two consecutive 4-wide records
+//      (children 0-3 and 4-7), so node index k occupies records 2k and 2k+1.
 // Every loop is bounded by the primitive count; no thread waits on another.
 #include <cub/device/device_radix_sort.cuh>
 
@@ -186,6 +188,7 @@ __device__ __forceinline__ double half_area(const double* b) {
   return dx * dy + dy * dz + dz * dx;
 }
 
+template <int W>
 __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t n_in,
                            int2* __restrict__ out) {
   int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
@@ -194,11 +197,11 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t 
   const int32_t n = A.n;
   auto is_inner = [&](int32_t c) { return c < n - 1; };
   auto count_of = [&](int32_t c) { return is_inner(c) ? A.last[c] - A.first[c] + 1 : 1; };
-  int32_t ch[kWidth];
+  int32_t ch[W];
   int cnt = 2;
   ch[0] = A.left[b];
   ch[1] = A.right[b];
-  while (cnt < kWidth) {
+  while (cnt < W) {
     int best = -1;
     double best_area = -1.0;
     for (int k = 0; k < cnt; ++k) {
@@ -216,45 +219,48 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t 
     ch[best] = A.left[c];
     ch[cnt++] = A.right[c];
   }
+  for (int rec = 0; rec < W / kWidth; ++rec) {
   Node32 n32;
   Node64 n64;
   float* f32[6] = {&n32.lox.x, &n32.hix.x, &n32.loy.x, &n32.hiy.x, &n32.loz.x, &n32.hiz.x};
   double* f64[6] = {n64.lox, n64.hix, n64.loy, n64.hiy, n64.loz, n64.hiz};
   int refs[kWidth];
-  for (int k = 0; k < kWidth; ++k) {
+  for (int kk = 0; kk < kWidth; ++kk) {
+    const int k = rec * kWidth + kk;
     if (k < cnt) {
       const int32_t c = ch[k];
       const double* bx = A.nbox + 6 * (int64_t)c;
       for (int a = 0; a < 3; ++a) {
-        f64[2 * a][k] = bx[a];
-        f64[2 * a + 1][k] = bx[3 + a];
-        f32[2 * a][k] = __double2float_rd(bx[a]);
-        f32[2 * a + 1][k] = __double2float_ru(bx[3 + a]);
+        f64[2 * a][kk] = bx[a];
+        f64[2 * a + 1][kk] = bx[3 + a];
+        f32[2 * a][kk] = __double2float_rd(bx[a]);
+        f32[2 * a + 1][kk] = __double2float_ru(bx[3 + a]);
       }
       const int32_t cc = count_of(c);
       if (!is_inner(c) || cc <= A.leaf_max) {
         const int32_t f = is_inner(c) ? A.first[c] : c - (n - 1);
-        refs[k] = make_leaf(f, cc);
+        refs[kk] = make_leaf(f, cc);
       } else {
         const int32_t nw = atomicAdd(A.node_counter, 1);
         const int32_t slot = atomicAdd(A.out_count, 1);
         out[slot] = make_int2(c, nw);
-        refs[k] = nw;
+        refs[kk] = nw;
       }
     } else {
       for (int a = 0; a < 3; ++a) {
-        f64[2 * a][k] = INFINITY;
-        f64[2 * a + 1][k] = -INFINITY;
-        f32[2 * a][k] = INFINITY;
-        f32[2 * a + 1][k] = -INFINITY;
+        f64[2 * a][kk] = INFINITY;
+        f64[2 * a + 1][kk] = -INFINITY;
+        f32[2 * a][kk] = INFINITY;
+        f32[2 * a + 1][kk] = -INFINITY;
       }
-      refs[k] = CHILD_EMPTY;
+      refs[kk] = CHILD_EMPTY;
     }
   }
   n32.child = make_int4(refs[0], refs[1], refs[2], refs[3]);
   n64.child = n32.child;
-  A.n32[w] = n32;
-  A.n64[w] = n64;
+  A.n32[(int64_t)w * (W / kWidth) + rec] = n32;
+  A.n64[(int64_t)w * (W / kWidth) + rec] = n64;
+  }
 }
 
 }  // namespace
@@ -265,8 +271,10 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t 
     if (e_ != cudaSuccess) return e_;         \
   } while (0)
 
-cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, cudaStream_t st,
-                           BuiltTree* out) {
+cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, int32_t width,
+                           cudaStream_t st, BuiltTree* out) {
+  if (width != 4 && width != 8) return cudaErrorInvalidValue;
+  out->width = width;
   out->n32 = nullptr;
   out->n64 = nullptr;
   out->order = nullptr;
@@ -362,8 +370,9 @@ cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, c
 
   // collapse, level by level
   const int32_t cap = n;  // inner wide nodes < n
-  BVH_CHECK(cudaMalloc(&out->n32, sizeof(Node32) * cap));
-  BVH_CHECK(cudaMalloc(&out->n64, sizeof(Node64) * cap));
+  const int64_t recs = (int64_t)cap * (width / kWidth);
+  BVH_CHECK(cudaMalloc(&out->n32, sizeof(Node32) * recs));
+  BVH_CHECK(cudaMalloc(&out->n64, sizeof(Node64) * recs));
   DevMem<int2> qa(cap), qb(cap);
   DevMem<int32_t> counters(2);  // [0] node counter, [1] out count
   BVH_CHECK(qa.alloc());
@@ -381,7 +390,10 @@ cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, c
   int2* qout = qb.p;
   while (n_in > 0) {
     BVH_CHECK(cudaMemsetAsync(counters.p + 1, 0, sizeof(int32_t), st));
-    k_collapse<<<(n_in + 127) / 128, 128, 0, st>>>(A, qin, n_in, qout);
+    if (width == 8)
+      k_collapse<8><<<(n_in + 127) / 128, 128, 0, st>>>(A, qin, n_in, qout);
+    else
+      k_collapse<4><<<(n_in + 127) / 128, 128, 0, st>>>(A, qin, n_in, qout);
     BVH_CHECK(cudaGetLastError());
     BVH_CHECK(cudaMemcpyAsync(hc, counters.p, sizeof hc, cudaMemcpyDeviceToHost, st));
     BVH_CHECK(cudaStreamSynchronize(st));

@@ -61,11 +61,12 @@ struct BuiltTree {
   int32_t n_nodes;
   int32_t depth;
   int32_t root;
+  int32_t width;     // children per node: 4 (one record) or 8 (two records)
   double bounds[6];  // union of the primitive boxes
 };
 
 // d_boxes: 6 doubles per primitive (lo.xyz, hi.xyz), already dilated.
-cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, cudaStream_t st,
-                           BuiltTree* out);
+cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, int32_t width,
+                           cudaStream_t st, BuiltTree* out);
 
 }  // namespace xdgcu

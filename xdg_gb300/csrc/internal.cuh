@@ -1,6 +1,7 @@
 // internal.cuh -- data layout of the ray-query engine in device memory.
 //
-// Trees are 4-wide BVHs stored twice: once with FP32 boxes rounded outward
+// Trees are 4- or 8-wide BVHs (an 8-wide node is two consecutive 4-wide
+// records) stored twice: once with FP32 boxes rounded outward
 // (the mixed-precision path) and once with FP64 boxes (the all-FP64 path).
 // A node holds its four children's boxes as six float4 (or 6x4 double)
 // vectors -- lo.x of children 0..3, hi.x, lo.y, hi.y, lo.z, hi.z -- followed
@@ -71,7 +72,7 @@ struct TreeDev {
   float bump;        // box dilation used for this tree (FP32, rounded down)
   float max_abs;     // max |coordinate| over the tree's (bumped) bounds
   int32_t kind;
-  int32_t pad;
+  int32_t width;     // 4 or 8 children per node; node k = records k*width/4 ..
 };
 
 constexpr int kPrim64Stride = 10;  // doubles per triangle in prim64

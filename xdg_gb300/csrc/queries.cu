@@ -1,7 +1,7 @@
 // queries.cu -- point-query kernels: closest (embree/ray_tracer.cpp:328-345)
 // and find_element (embree/ray_tracer.cpp:226-257).
 //
-// One thread owns one query point for its whole traversal of a 4-wide BVH
+// One thread owns one query point for its whole traversal of a 4- or 8-wide BVH
 // with a private stack, visiting the nearest children first (closest) or
 // every child whose box contains the point (find_element).  The FP32 node
 // tests are conservative -- boxes are rounded outward at build time and a
@@ -44,12 +44,17 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
       bool run = ref != CHILD_EMPTY;
       while (run) {
         if (!ref_is_leaf(ref)) {
+          // the node's records (one for 4-wide, two for 8-wide trees): the
+          // hits of each are pushed nearest last, so the nearest is popped first
+          const int nrec = T.width / kWidth;
+          bool overflow = false;
+          for (int rec = 0; rec < nrec; ++rec) {
           cnt.node++;
           cnt.box += 4;
           int32_t cr[4];
           int nhit = 0;
           if (MIXED) {
-            const Node32* np = T.n32 + ref;
+            const Node32* np = T.n32 + (int64_t)ref * nrec + rec;
             const float4 lx = __ldg(&np->lox), hx = __ldg(&np->hix), ly = __ldg(&np->loy),
                          hy = __ldg(&np->hiy), lz = __ldg(&np->loz), hz = __ldg(&np->hiz);
             const int4 c = __ldg(&np->child);
@@ -81,7 +86,7 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
             sort4(key, cr);
             for (int k = 0; k < 4; ++k) nhit += key[k] < INFINITY ? 1 : 0;
           } else {
-            const Node64* np = T.n64 + ref;
+            const Node64* np = T.n64 + (int64_t)ref * nrec + rec;
             const int4 c = __ldg(&np->child);
             const int32_t ca[4] = {c.x, c.y, c.z, c.w};
             double key[4];
@@ -106,14 +111,15 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
             sort4d(key, cr);
             for (int k = 0; k < 4; ++k) nhit += key[k] < INFINITY ? 1 : 0;
           }
-          if (nhit > 0) {
-            if (sp + nhit - 1 > kStackSize) {
-              st = RAY_STACK_OVERFLOW;
-              break;
-            }
-            for (int k = nhit - 1; k >= 1; --k) stack[sp++] = cr[k];
-            ref = cr[0];
-            continue;
+          if (sp + nhit > kStackSize) {
+            overflow = true;
+            break;
+          }
+          for (int k = nhit - 1; k >= 0; --k) stack[sp++] = cr[k];
+          }
+          if (overflow) {
+            st = RAY_STACK_OVERFLOW;
+            break;
           }
         } else {
           const int32_t first = leaf_first(ref), count = leaf_count(ref);
@@ -171,12 +177,15 @@ __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
       bool run = ref != CHILD_EMPTY;
       while (run) {
         if (!ref_is_leaf(ref)) {
+          const int nrec = T.width / kWidth;
+          bool overflow = false;
+          for (int rec = 0; rec < nrec; ++rec) {
           cnt.node++;
           cnt.box += 4;
           int32_t cr[4];
           int nhit = 0;
           if (MIXED) {
-            const Node32* np = T.n32 + ref;
+            const Node32* np = T.n32 + (int64_t)ref * nrec + rec;
             const float4 lx = __ldg(&np->lox), hx = __ldg(&np->hix), ly = __ldg(&np->loy),
                          hy = __ldg(&np->hiy), lz = __ldg(&np->loz), hz = __ldg(&np->hiz);
             const int4 c = __ldg(&np->child);
@@ -189,7 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
             for (int k = 0; k < 4; ++k)
               if (in[k]) cr[nhit++] = ca[k];
           } else {
-            const Node64* np = T.n64 + ref;
+            const Node64* np = T.n64 + (int64_t)ref * nrec + rec;
             const int4 c = __ldg(&np->child);
             const int32_t ca[4] = {c.x, c.y, c.z, c.w};
             for (int k = 0; k < 4; ++k) {
@@ -199,14 +208,15 @@ __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
               if (in) cr[nhit++] = ca[k];
             }
           }
-          if (nhit > 0) {
-            if (sp + nhit - 1 > kStackSize) {
-              st = RAY_STACK_OVERFLOW;
-              break;
-            }
-            for (int k = nhit - 1; k >= 1; --k) stack[sp++] = cr[k];
-            ref = cr[0];
-            continue;
+          if (sp + nhit > kStackSize) {
+            overflow = true;
+            break;
+          }
+          for (int k = nhit - 1; k >= 0; --k) stack[sp++] = cr[k];
+          }
+          if (overflow) {
+            st = RAY_STACK_OVERFLOW;
+            break;
           }
         } else {
           const int32_t first = leaf_first(ref), count = leaf_count(ref);

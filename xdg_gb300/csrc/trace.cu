@@ -39,6 +39,9 @@
 // ray for which 8u(max|coordinate| + |o|_inf) is not below the bump tests FP64
 // boxes instead (checked per ray, `use64`).
 //
+// Nodes are 4- or 8-wide per tree (an 8-wide node's two records are tested,
+// sorted and merged).
+//
 // Stack: `stack` entries per lane (16..64, a launch parameter) in dynamic
 // shared memory, [entry][thread] so that lanes hit distinct banks; each entry
 // keeps its near distance so entries beyond a closer hit found meanwhile are
@@ -122,6 +125,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
   bool bhas = false, bdot = false;
   const int32_t* excl = nullptr;
   int32_t nexcl = 0;
+  bool wide8 = false;  // the lane's tree has 8-wide nodes
   // MODE_PARTICLE: the particle's stream, path length, events, history count
   // and the triangle of the best hit
   unsigned long long rs = 0ull;
@@ -163,6 +167,7 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
     tree = T;
     n32 = T->n32;
     prim32 = T->prim32;
+    wide8 = T->width == 8;
     const int32_t root = T->root;
     bt32 = (MODE == MODE_OCCLUDED) ? INFINITY : f32_up(bt);
     if (MIXED) {
@@ -421,33 +426,52 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
       if (__ballot_sync(kFull, want) == 0u) break;
       if (want) {
         cnt.node++;
-        cnt.box += 4;
-        int32_t cr[4];
-        float key[4];
-        if (MIXED && !use64) {
-          node_test32(n32 + cur, br32, bt32, key, cr);
-        } else {
-          double tn[4];
-          if (MIXED) br64 = make_boxray64(o, d);  // rare: rays failing the FP32 safety test
-          node_test64(tree->n64 + cur, br64, (MODE == MODE_OCCLUDED) ? INFTY : bt, tn, cr);
+        cnt.box += wide8 ? 8 : 4;
+        // an 8-wide node is two 4-wide records, each tested and sorted, then
+        // merged; a 4-wide node leaves the upper half empty
+        int32_t cr[8];
+        float key[8];
 #pragma unroll
-          for (int k = 0; k < 4; ++k)
-            key[k] = tn[k] < INFINITY ? __double2float_rd(tn[k]) : INFINITY;
+        for (int r = 0; r < 2; ++r) {
+          if (r == 1 && !wide8) {
+#pragma unroll
+            for (int k = 4; k < 8; ++k) {
+              key[k] = INFINITY;
+              cr[k] = CHILD_EMPTY;
+            }
+            continue;
+          }
+          const int64_t rec = wide8 ? 2 * (int64_t)cur + r : (int64_t)cur;
+          if (MIXED && !use64) {
+            node_test32(n32 + rec, br32, bt32, key + 4 * r, cr + 4 * r);
+          } else {
+            double tn[4];
+            if (MIXED) br64 = make_boxray64(o, d);  // rare: rays failing the FP32 safety test
+            node_test64(tree->n64 + rec, br64, (MODE == MODE_OCCLUDED) ? INFTY : bt, tn,
+                        cr + 4 * r);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              key[4 * r + k] = tn[k] < INFINITY ? __double2float_rd(tn[k]) : INFINITY;
+          }
+          sort4(key + 4 * r, cr + 4 * r);
         }
-        sort4(key, cr);
+        if (wide8) merge8(key, cr);
         int nhit = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) nhit += key[k] < INFINITY ? 1 : 0;
+        for (int k = 0; k < 8; ++k) nhit += key[k] < INFINITY ? 1 : 0;
         if (nhit == 0) {
           pop();
         } else if (sp + nhit - 1 > kstack) {
           status = RAY_STACK_OVERFLOW;
           trav = false;
         } else {
-          for (int k = nhit - 1; k >= 1; --k) {
-            sref[sp * kTBlock + tx] = cr[k];
-            stn[sp * kTBlock + tx] = key[k];
-            ++sp;
+#pragma unroll
+          for (int k = 7; k >= 1; --k) {
+            if (k < nhit) {  // static indices keep key/cr in registers
+              sref[sp * kTBlock + tx] = cr[k];
+              stn[sp * kTBlock + tx] = key[k];
+              ++sp;
+            }
           }
           if (ref_is_leaf(cr[0])) {
             cur = CHILD_EMPTY;

@@ -58,6 +58,46 @@ __device__ __forceinline__ void sort4(float* k, int32_t* r) {
 #undef XDG_CSWAP
 }
 
+// Merges two ascending (key, ref) lists k[0..3] and k[4..7] into one
+// ascending list of eight (bitonic merge: reverse the second half, then
+// compare-exchange at distances 4, 2, 1).
+__device__ __forceinline__ void merge8(float* k, int32_t* r) {
+#define XDG_CSWAP(a, b)                 \
+  if (k[b] < k[a]) {                    \
+    float tk = k[a];                    \
+    k[a] = k[b];                        \
+    k[b] = tk;                          \
+    int32_t tr = r[a];                  \
+    r[a] = r[b];                        \
+    r[b] = tr;                          \
+  }
+#define XDG_SWAP(a, b)                  \
+  {                                     \
+    float tk = k[a];                    \
+    k[a] = k[b];                        \
+    k[b] = tk;                          \
+    int32_t tr = r[a];                  \
+    r[a] = r[b];                        \
+    r[b] = tr;                          \
+  }
+  XDG_SWAP(4, 7);
+  XDG_SWAP(5, 6);
+  XDG_CSWAP(0, 4);
+  XDG_CSWAP(1, 5);
+  XDG_CSWAP(2, 6);
+  XDG_CSWAP(3, 7);
+  XDG_CSWAP(0, 2);
+  XDG_CSWAP(1, 3);
+  XDG_CSWAP(4, 6);
+  XDG_CSWAP(5, 7);
+  XDG_CSWAP(0, 1);
+  XDG_CSWAP(2, 3);
+  XDG_CSWAP(4, 5);
+  XDG_CSWAP(6, 7);
+#undef XDG_SWAP
+#undef XDG_CSWAP
+}
+
 __device__ __forceinline__ void sort4d(double* k, int32_t* r) {
 #define XDG_CSWAP(a, b)                 \
   if (k[b] < k[a]) {                    \

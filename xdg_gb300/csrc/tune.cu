@@ -8,6 +8,9 @@
 // setting as the median of `reps` launches after one untimed launch, with
 // CUDA events on a private stream.
 //
+// With tune_width the search runs once per BVH node width (4 and 8), the
+// surface trees rebuilt for each, and the faster width is kept.
+//
 // Every setting must give the same results: the tuner compares each run's
 // outputs byte for byte with the first run's and fails with XDGCU_ERR_STATE
 // if they differ.  The one accepted difference is a smaller stack that makes
@@ -168,7 +171,7 @@ extern "C" {
 
 int xdgcu_autotune_trace(xdgcu_ctx* c, int32_t query, int32_t tree, const int32_t* ray_trees,
                          int64_t n, const double* origins, const double* directions,
-                         int32_t precision, int32_t reps, double* best_ms) {
+                         int32_t precision, int32_t reps, int32_t tune_width, double* best_ms) {
   if (!c) return set_last_error(XDGCU_ERR_INVALID_ARG, "null context");
   if (query < XDGCU_QUERY_RAY_FIRE || query > XDGCU_QUERY_FIND_VOLUME)
     return set_last_error(XDGCU_ERR_INVALID_ARG, "autotune: unknown query");
@@ -238,8 +241,37 @@ int xdgcu_autotune_trace(xdgcu_ctx* c, int32_t query, int32_t tree, const int32_
       {"trace_grab", {0, 64, 256, 1024, 4096}},
   };
   if (n >= 65536) knobs.push_back({"trace_sort_min", {0, n}});
-  int rc = descend(c, knobs, measure, best_ms);
+  int64_t w0 = 4;
+  int rc = xdgcu_get_tuning(c, "node_width", &w0);
   if (rc) return rc;
+  std::vector<int64_t> widths = {w0};
+  if (tune_width) widths.push_back(w0 == 4 ? 8 : 4);
+  double best = -1.0;
+  int64_t best_w = w0;
+  std::vector<int64_t> best_vals(knobs.size());
+  for (int64_t w : widths) {
+    if (w != w0) {
+      rc = xdgcu_set_tuning(c, "node_width", w);
+      if (!rc) rc = xdgcu_rebuild_trees(c, 1);
+      if (rc) return rc;
+    }
+    double ms = 0.0;
+    rc = descend(c, knobs, measure, &ms);
+    if (rc) return rc;
+    if (best < 0.0 || ms < 0.99 * best) {
+      best = ms;
+      best_w = w;
+      for (size_t k = 0; k < knobs.size(); ++k) xdgcu_get_tuning(c, knobs[k].key, &best_vals[k]);
+    }
+  }
+  const int64_t cur_w = widths.back();
+  if (best_w != cur_w) {
+    rc = xdgcu_set_tuning(c, "node_width", best_w);
+    if (!rc) rc = xdgcu_rebuild_trees(c, 1);
+    if (rc) return rc;
+  }
+  for (size_t k = 0; k < knobs.size(); ++k) xdgcu_set_tuning(c, knobs[k].key, best_vals[k]);
+  if (best_ms) *best_ms = best;
   // a coherent order that paid off on this sample is kept for batches of at
   // least a quarter of its size (and never below 65,536 rays)
   int64_t sm = 0;

@@ -23,7 +23,7 @@ from ._lib import (QUERY_FIND_VOLUME, QUERY_OCCLUDED, QUERY_POINT_IN_VOLUME,  # 
 # keys of xdgcu_set_tuning / xdgcu_get_tuning
 TUNING_KEYS = ("trace_occupancy", "trace_node_iters", "trace_node_iters_fp64",
                "trace_flush_wait", "trace_stack", "trace_grab", "trace_sort_min",
-               "particle_event_wait", "leaf_max",
+               "particle_event_wait", "leaf_max", "node_width",
                "walk_queue", "walk_flush_wait", "walk_sort_min")
 
 INFTY = np.finfo(np.float64).max
@@ -245,7 +245,8 @@ class CudaRayTracer:
         out = (ctypes.c_int64 * 8)()
         fn = self.L.xdgcu_element_tree_info if element else self.L.xdgcu_surface_tree_info
         self._check(fn(self.ctx, int(tree), out), "tree_info")
-        return dict(nodes=out[0], prims=out[1], depth=out[2], bytes32=out[3], bytes64=out[4])
+        return dict(nodes=out[0], prims=out[1], depth=out[2], bytes32=out[3], bytes64=out[4],
+                    width=out[5])
 
     def set_tuning(self, key: str, value: int):
         self._check(self.L.xdgcu_set_tuning(self.ctx, key.encode(), int(value)), "set_tuning")
@@ -259,8 +260,13 @@ class CudaRayTracer:
         """Every tuning key with its current value."""
         return {k: self.get_tuning(k) for k in TUNING_KEYS}
 
+    def rebuild_trees(self, kinds=3):
+        """xdgcu_rebuild_trees (1 surface, 2 element, 3 both) with the
+        current node_width / leaf_max."""
+        self._check(self.L.xdgcu_rebuild_trees(self.ctx, int(kinds)), "rebuild_trees")
+
     def autotune_trace(self, query, tree, origins, dirs=None, precision=MIXED, ray_trees=None,
-                       reps=5):
+                       reps=5, tune_width=True):
         """xdgcu_autotune_trace on a sample batch (torch CUDA tensors).  Leaves
         the context tuned; returns (sample ms under the chosen settings,
         tuning dict)."""
@@ -270,7 +276,8 @@ class CudaRayTracer:
         ms = ctypes.c_double()
         self._check(self.L.xdgcu_autotune_trace(self.ctx, int(query), int(tree or 0), _addr(rt),
                                                 o.shape[0], _addr(o), _addr(d), int(precision),
-                                                int(reps), ctypes.byref(ms)), "autotune_trace")
+                                                int(reps), 1 if tune_width else 0,
+                                                ctypes.byref(ms)), "autotune_trace")
         return ms.value, self.tuning()
 
     def autotune_walk(self, start_index, start, u, distance, max_segs=256, precision=MIXED,
