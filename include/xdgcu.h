@@ -379,6 +379,10 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *   "particle_event_wait"  particle loop of xdgcu_transport_surfaces: lanes
  *                      whose flights have ended that a warp gathers before it
  *                      runs their events together (1..32, default 16)
+ *   "transport_event_wait" particle loop of xdgcu_transport_elements, mixed
+ *                      precision: lanes whose events need the FP64 sample
+ *                      (collisions, uncertain exits) that a warp gathers
+ *                      before it runs them together (1..32, default 4)
  *   "trace_sort_min"   batches of at least this many rays (default 0 = never)
  *                      are traversed in a coherent order: sorted on the device
  *                      by tree, direction octant and the Morton code of the

@@ -71,6 +71,23 @@ def test_transport_elements_matches_oracle(cube, oracle, prec, mfp):
     for k, name in enumerate(NAMES):
         assert_same(got[k], o[k], name)
     assert (got[0] == -1).all() and (got[6] == 0).all()
+    # events run at once or gathered across the warp: same histories
+    for wait in (1, 32):
+        x.rti.set_tuning("transport_event_wait", wait)
+        try:
+            e2, r2, d2, s2 = e.clone(), r.clone(), d.clone(), s.clone()
+            e2.copy_(torch.as_tensor(elem, device=dev))
+            r2.copy_(torch.as_tensor(p, device=dev))
+            d2.copy_(torch.as_tensor(u, device=dev))
+            s2.copy_(torch.as_tensor(seeds.view(np.int64), device=dev))
+            dist2, ev2 = torch.zeros_like(dist), torch.zeros_like(ev)
+            x.rti.transport_elements(e2, r2, d2, s2, mfp, 1_000_000, dist2, ev2, None,
+                                     precision=prec)
+            torch.cuda.synchronize()
+            assert torch.equal(e2, e) and torch.equal(r2, r) and torch.equal(s2, s)
+            assert torch.equal(dist2, dist) and torch.equal(ev2, ev)
+        finally:
+            x.rti.set_tuning("transport_event_wait", 4)
     ty = tally.cpu().numpy()
     assert np.allclose(ty, o[7], rtol=1e-12, atol=1e-300)
     assert abs(ty.sum() - got[4].sum()) <= 1e-12 * got[4].sum()

@@ -321,7 +321,8 @@ struct xdgcu_ctx {
   int32_t trace_stack = 48;      // shared-memory stack entries per lane
   int32_t trace_grab = 0;        // 0: one contiguous chunk per warp; > 0: device work queue
   int64_t trace_sort_min = 0;    // batches of at least this many rays run in coherent order (0 = never)
-  int32_t particle_event_wait = 16;  // particle loop: lanes gathered before their events run
+  int32_t particle_event_wait = 16;  // particle_sim loop: lanes gathered before their events run
+  int32_t transport_event_wait = 4;  // walk_elements tool loop (mixed): the same
   int32_t leaf_max = 4;
   int32_t node_width = 4;        // children per BVH node (4 or 8) of trees built afterwards
   int32_t walk_queue = 1;
@@ -1055,6 +1056,10 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     if (value < 0 || value > (1 << 20) || value % 32 != 0)
       return set_err(XDGCU_ERR_INVALID_ARG, "trace_grab must be 0 or a multiple of 32 up to 2^20");
     c->trace_grab = (int32_t)value;
+  } else if (k == "transport_event_wait") {
+    if (value < 1 || value > 32)
+      return set_err(XDGCU_ERR_INVALID_ARG, "transport_event_wait must be 1..32");
+    c->transport_event_wait = (int32_t)value;
   } else if (k == "particle_event_wait") {
     if (value < 1 || value > 32)
       return set_err(XDGCU_ERR_INVALID_ARG, "particle_event_wait must be 1..32");
@@ -1094,6 +1099,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "trace_grab") *value = c->trace_grab;
   else if (k == "trace_sort_min") *value = c->trace_sort_min;
   else if (k == "particle_event_wait") *value = c->particle_event_wait;
+  else if (k == "transport_event_wait") *value = c->transport_event_wait;
   else if (k == "leaf_max") *value = c->leaf_max;
   else if (k == "node_width") *value = c->node_width;
   else if (k == "walk_queue") *value = c->walk_queue;
@@ -1784,6 +1790,9 @@ int xdgcu_transport_elements(xdgcu_ctx* c, int64_t n, int32_t* elem_index, doubl
   t.n = n;
   t.mfp = mean_free_path;
   t.max_events = max_events;
+  // FP64 steps are FP64-bound themselves: idle waiting lanes cost more than
+  // the batching saves, so the all-FP64 loop runs each event at once
+  t.event_wait = precision == XDGCU_MIXED ? c->transport_event_wait : 1;
   const bool mixed = precision == XDGCU_MIXED;
   cudaStream_t st = (cudaStream_t)stream;
   if (kind == 1) {

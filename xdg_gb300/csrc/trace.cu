@@ -241,9 +241,21 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
             // ray_fire appended the hit face to the history
             a.p_hist[ray * a.hist_cap + (hc % a.hist_cap)] = bface;
             ++hc;
-            const double c = sample_collision(rs, a.mfp);  // :47-49
+            // :47-49.  The FP64 series logarithm is needed only when the
+            // particle may collide: an FP32 logarithm with a certified margin
+            // (|c32 - c| <= 6.1e-8 mfp + 3.7e-7 c; margin 1.1e-6 (c32 + mfp))
+            // first tests c >= hit distance.
+            const double U = uniform53(rs);
+            bool cross = false;
+            if (a.mfp < 1e30) {
+              const float mfp32 = (float)a.mfp;
+              const float c32 = -logf(__double2float_rn(1.0 - U)) * mfp32;
+              cross = dlt(bt, (double)(c32 - 1.1e-6f * (c32 + mfp32)));
+            }
+            double c = 0.0;
+            if (!cross) c = -series_log(1.0 - U) * a.mfp;  // sample_collision's value
             alive = true;
-            if (dlt(c, bt)) {
+            if (!cross && dlt(c, bt)) {
               // advance + collide (:66-70, :57-64)
               o = add3(o, scl3(c, d));
               pdist += c;

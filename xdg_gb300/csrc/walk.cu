@@ -805,13 +805,14 @@ namespace {
 // (RAY_EVENT_LIMIT).  With `tally`, each event adds its path length to the
 // tet it was made in (atomicAdd, so the sums' rounding depends on the order).
 // Warps own contiguous chunks of particles and refill lanes as particles
-// finish, as in k_walk.
+// finish, as in k_walk.  The collision sample's FP64 logarithm and the new
+// direction are only computed where needed (see the FP32 test below) and for
+// many lanes at once.
 // ---------------------------------------------------------------------------
 
 template <int FO, bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t chunk) {
   const WalkArgs& a = t.mesh;
-  const int lane = threadIdx.x & 31;
   const int64_t gwarp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   int64_t cursor = gwarp * chunk;
   const int64_t end = min(t.n, cursor + chunk);
@@ -823,6 +824,35 @@ __global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t c
   double dist = 0.0;
   int32_t elem = -1, ev = 0, st = RAY_OK;
   unsigned long long rs = 0;
+  // an event whose FP64 part waits for the warp's batch: its uniform draw,
+  // exit distance and exit face
+  bool pend = false;
+  double pu = 0.0, pex = 0.0;
+  int pf = -1;
+  const float mfp32 = (float)t.mfp;
+  const bool quick = t.mfp < 1e30;
+
+  // moves the particle to the exit face and into the neighbour (:86-90);
+  // returns true when it stops
+  auto exit_step = [&](double ex, int f) -> bool {
+    if (f < 0) {
+      st = RAY_NO_EXIT_FACE;  // exit = INFTY and c >= INFTY: no finite step exists
+      return true;
+    }
+    const int4 ad = __ldg(&a.adj[elem]);
+    const int32_t nxt = f == 0 ? ad.x : (f == 1 ? ad.y : (f == 2 ? ad.z : ad.w));
+    r = add3(r, scl3(ex, u));
+    dist += ex;
+    if (t.tally) atomicAdd(&t.tally[elem], ex);
+    if (nxt < -1 || nxt >= a.n_tets) {
+      st = RAY_INVALID;  // corrupt adjacency
+      return true;
+    }
+    elem = nxt;
+    ++ev;
+    return elem < 0;
+  };
+
   while (true) {
     const unsigned need = __ballot_sync(0xffffffffu, !has);
     if (need != 0u && cursor < end) {
@@ -833,6 +863,7 @@ __global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t c
         if (kk < end) {
           i = kk;
           has = true;
+          pend = false;
           elem = t.elem[i];
           r = load3(t.pos, i);
           u = load3(t.dir, i);
@@ -846,8 +877,9 @@ __global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t c
       cursor += __popc(need);
     }
     if (__ballot_sync(0xffffffffu, has) == 0u) break;
-    if (has) {
-      bool done = st != RAY_OK || elem < 0;  // nothing to do outside the mesh
+    bool done = false;
+    if (has && !pend) {
+      done = st != RAY_OK || elem < 0;  // nothing to do outside the mesh
       if (!done && ev >= t.max_events) {
         st = RAY_EVENT_LIMIT;
         done = true;
@@ -856,48 +888,64 @@ __global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t c
         cnt.steps++;
         double ex;
         const int f = next_face<FO, MIXED>(a, elem, r, u, &ex, cnt);
-        const double c = sample_collision(rs, t.mfp);
-        if (dlt(c, ex)) {
-          // collision inside the tet (:81-85)
-          r = add3(r, scl3(c, u));
-          dist += c;
-          if (t.tally) atomicAdd(&t.tally[elem], c);
-          u = sample_direction(rs);
-        } else if (f < 0) {
-          st = RAY_NO_EXIT_FACE;  // exit = INFTY and c >= INFTY: no finite step exists
-          done = true;
+        const double U = uniform53(rs);
+        // Most events leave the tet: an FP32 logarithm with a certified
+        // margin decides c >= exit without the FP64 series.  |c32 - c| <=
+        // 6.1e-8 mfp + 3.7e-7 c (rounding 1 - U to FP32, logf within 2 ulp,
+        // two FP32 products); the margin below is 1.1e-6 (c32 + mfp).
+        bool leaves = false;
+        if (quick) {
+          const float c32 = -logf(__double2float_rn(1.0 - U)) * mfp32;
+          const float lo = c32 - 1.1e-6f * (c32 + mfp32);
+          leaves = dlt(ex, (double)lo);  // c >= lo > exit
+        }
+        if (leaves) {
+          done = exit_step(ex, f);
         } else {
-          // to the exit face and into the neighbour (:86-90)
-          const int4 ad = __ldg(&a.adj[elem]);
-          const int32_t nxt = f == 0 ? ad.x : (f == 1 ? ad.y : (f == 2 ? ad.z : ad.w));
-          r = add3(r, scl3(ex, u));
-          dist += ex;
-          if (t.tally) atomicAdd(&t.tally[elem], ex);
-          if (nxt < -1 || nxt >= a.n_tets) {
-            st = RAY_INVALID;  // corrupt adjacency
-            done = true;
+          pend = true;  // the exact sample and the event run with the warp's batch
+          pu = U;
+          pex = ex;
+          pf = f;
+        }
+      }
+    }
+    // Events that need the FP64 sample (collisions, and exits the FP32 test
+    // could not certify) run together once event_wait lanes wait or no lane
+    // can step: FP64 instructions cost the same issue time for 1 or 32 lanes.
+    const unsigned pm = __ballot_sync(0xffffffffu, has && pend);
+    if (pm != 0u) {
+      const unsigned run = __ballot_sync(0xffffffffu, has && !pend && !done);
+      if (__popc(pm) >= t.event_wait || run == 0u) {
+        if (has && pend) {
+          pend = false;
+          const double c = -series_log(1.0 - pu) * t.mfp;  // sample_collision's value
+          if (dlt(c, pex)) {
+            // collision inside the tet (:81-85)
+            r = add3(r, scl3(c, u));
+            dist += c;
+            if (t.tally) atomicAdd(&t.tally[elem], c);
+            u = sample_direction(rs);
+            ++ev;
           } else {
-            elem = nxt;
-            if (elem < 0) done = true;
+            done = exit_step(pex, pf);
           }
         }
-        if (st == RAY_OK) ++ev;
       }
-      if (done) {
-        t.elem[i] = elem;
-        t.pos[3 * i] = r.x;
-        t.pos[3 * i + 1] = r.y;
-        t.pos[3 * i + 2] = r.z;
-        t.dir[3 * i] = u.x;
-        t.dir[3 * i + 1] = u.y;
-        t.dir[3 * i + 2] = u.z;
-        t.rng[i] = rs;
-        t.distance[i] = dist;
-        t.events[i] = ev;
-        if (t.status) t.status[i] = st;
-        has = false;
-        parts++;
-      }
+    }
+    if (has && done) {
+      t.elem[i] = elem;
+      t.pos[3 * i] = r.x;
+      t.pos[3 * i + 1] = r.y;
+      t.pos[3 * i + 2] = r.z;
+      t.dir[3 * i] = u.x;
+      t.dir[3 * i + 1] = u.y;
+      t.dir[3 * i + 2] = u.z;
+      t.rng[i] = rs;
+      t.distance[i] = dist;
+      t.events[i] = ev;
+      if (t.status) t.status[i] = st;
+      has = false;
+      parts++;
     }
   }
   if (t.counters) flush(t.counters, cnt, parts);

@@ -59,6 +59,7 @@ struct TransportArgs {
   double* tally;             // per-tet track length, accumulated with atomics (may be null)
   double mfp;
   int32_t max_events;
+  int32_t event_wait;        // lanes gathered before their FP64 event work runs
   unsigned long long* counters;
 };
 
