@@ -168,6 +168,18 @@ int xdgcu_point_in_volume(xdgcu_ctx* ctx, int32_t tree, const int32_t* ray_trees
                           const int32_t* excl_offsets, const int32_t* excl_ids,
                           int32_t* inside_out, int32_t* status, int32_t precision, void* stream);
 
+/* RayTracer::point_in_volume (embree/ray_tracer.cpp:259-287) of each of n
+ * points in each of n_trees surface trees (the host array `trees`), in one
+ * launch: the lane restarts the point in the next tree.  inside_out[i *
+ * n_trees + k] = 1 when point i is inside tree k's volume.  directions may be
+ * NULL (the default (1/sqrt(2), 1/sqrt(2), 0)).  This is the inner loop of
+ * the overlap_check tool (tools/overlap.cpp:9-60, every volume for every
+ * point). */
+int xdgcu_point_in_volumes(xdgcu_ctx* ctx, int64_t n, const double* points,
+                           const double* directions, int32_t n_trees, const int32_t* trees,
+                           uint8_t* inside_out, int32_t* status, int32_t precision,
+                           void* stream);
+
 /* Sets the volumes XDG::find_volume tries, in order, with their surface
  * trees (XDG::volume_to_surface_tree_map_, xdg.h:125, filled by
  * prepare_raytracer, xdg.cpp:37-47).  Entries equal to implicit_complement

@@ -1626,6 +1626,92 @@ int xdgcu_walk_elements(xdgcu_ctx* c, int64_t n, const int32_t* start_index, con
 // device particle loop over the tet mesh
 // ---------------------------------------------------------------------------
 
+int xdgcu_point_in_volumes(xdgcu_ctx* c, int64_t n, const double* points,
+                           const double* directions, int32_t n_trees, const int32_t* trees,
+                           uint8_t* inside_out, int32_t* status, int32_t precision,
+                           void* stream) {
+  CHECK_CTX(c);
+  if (n < 0 || n_trees < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative count");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (n == 0 || n_trees == 0) return XDGCU_OK;
+  if (!points || !trees || !inside_out) return set_err(XDGCU_ERR_INVALID_ARG, "null argument");
+  for (int32_t k = 0; k < n_trees; ++k)
+    if (trees[k] < 1 || trees[k] > (int32_t)c->surf_trees.size())
+      return set_err(XDGCU_ERR_NOT_FOUND, "point_in_volumes: no such surface tree");
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    int rc = sync_surfaces(c);
+    if (rc) return rc;
+    rc = sync_tree_tables(c);
+    if (rc) return rc;
+  }
+  const int kind = classify({points, directions, inside_out, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  SurfArgs a{};
+  a.trees = c->d_surf_trees.p;
+  a.n_trees = (int32_t)c->surf_trees.size();
+  a.n = n;
+  a.tri_face = c->d_tri_face.p;
+  a.tri_surf = c->d_tri_surf.p;
+  a.surf_id = c->d_surf_id.p;
+  a.surf_rev_tree = c->d_surf_rev.p;
+  a.occupancy = c->trace_occupancy;
+  a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
+  a.flush_wait = c->trace_flush_wait;
+  a.stack = c->trace_stack;
+  a.n_vols = n_trees;
+  a.vol_stride = n_trees;
+  const bool mixed = precision == XDGCU_MIXED;
+  double extent = 0.0;
+  for (auto& t : c->surf_trees) extent = std::max(extent, (double)t->dev.max_abs);
+  cudaStream_t st = (cudaStream_t)stream;
+  Slot* s = nullptr;
+  if (kind == 0) {
+    s = get_slot(c);
+    if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  }
+  // the tree list, in stream order before the launches
+  cudaStream_t ls = kind == 1 ? st : s->stream;
+  int32_t* d_list = nullptr;
+  API_CUDA(cudaMallocAsync((void**)&d_list, sizeof(int32_t) * n_trees, ls), "tree list");
+  API_CUDA(cudaMemcpyAsync(d_list, trees, sizeof(int32_t) * n_trees, cudaMemcpyHostToDevice, ls),
+           "tree list");
+  a.vol_trees = d_list;
+  int rc = XDGCU_OK;
+  if (kind == 1) {
+    a.org = points;
+    a.dir = directions;
+    a.vol_inside = inside_out;
+    a.status = status;
+    rc = begin_query(c, st, &a.counters);
+    if (!rc) {
+      const cudaError_t e = launch_trace(c, MODE_ALL_VOLUMES, mixed, a, extent, st);
+      if (e != cudaSuccess) rc = cuda_err(e, "query launch");
+    }
+    cudaFreeAsync(d_list, st);
+    return rc;
+  }
+  RayArr R_p{points, nullptr, 24}, R_d{directions, nullptr, directions ? 24u : 0u};
+  RayArr R_in{nullptr, inside_out, (size_t)n_trees};
+  RayArr R_st{nullptr, status, status ? 4u : 0u};
+  auto at = [](const RayArr& r, int64_t first) -> char* {
+    return r.dev ? r.dev + r.per_ray * first : nullptr;
+  };
+  rc = run_staged(c, s, st, n, {}, {&R_p, &R_d, &R_in, &R_st}, &a.counters,
+                  [&](int64_t first, int64_t cnt, cudaStream_t cs) {
+                    SurfArgs b = a;
+                    b.n = cnt;
+                    b.org = (const double*)at(R_p, first);
+                    b.dir = (const double*)at(R_d, first);
+                    b.vol_inside = (uint8_t*)at(R_in, first);
+                    b.status = (int32_t*)at(R_st, first);
+                    return launch_trace(c, MODE_ALL_VOLUMES, mixed, b, extent, cs);
+                  });
+  cudaFreeAsync(d_list, s->stream);
+  return rc;
+}
+
 int xdgcu_set_surface_boundary(xdgcu_ctx* c, int32_t n, const int32_t* surface_ids,
                                const int32_t* conditions) {
   CHECK_CTX(c);

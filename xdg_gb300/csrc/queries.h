@@ -14,7 +14,8 @@ enum QueryMode : int {
   MODE_PIV = 1,
   MODE_OCCLUDED = 2,
   MODE_FIND_VOLUME = 3,
-  MODE_PARTICLE = 4  // the particle_sim loop: every ray is one flight of a particle
+  MODE_PARTICLE = 4,    // the particle_sim loop: every ray is one flight of a particle
+  MODE_ALL_VOLUMES = 5  // point_in_volume of each point in every volume of a list
 };
 
 // boundary conditions of the particle loop (MeshManager surface property)
@@ -58,6 +59,10 @@ struct SurfArgs {
   const int32_t* vol_trees;
   int32_t n_vols;
   int32_t ipc_volume;
+  // MODE_ALL_VOLUMES: inside flags, point i's flag for list entry k at
+  // vol_inside[i * vol_stride + k] (the list is vol_trees[0 .. n_vols))
+  uint8_t* vol_inside;
+  int64_t vol_stride;
   // MODE_PARTICLE: per-particle state, read at the start and written back
   // when the particle stops
   double* p_pos;

@@ -228,6 +228,23 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
         } else {
           a.flag_out[ray] = inside ? a.vol_ids[vk] : a.ipc_volume;
         }
+      } else if (MODE == MODE_ALL_VOLUMES) {
+        // point_in_volume in list entry vk (embree/ray_tracer.cpp:282-286),
+        // then the lane restarts the same point in the next entry's tree
+        a.vol_inside[ray * a.vol_stride + vk] = (bhas && bdot) ? 1 : 0;
+        if (status == RAY_OK && vk + 1 < a.n_vols) {
+          ++vk;
+          tid = a.vol_trees[vk];
+          bt = INFTY;
+          bhas = false;
+          bdot = false;
+          bface = -1;
+          bsurf = -1;
+          sp = 0;
+          leaf_p = leaf_end = 0;
+          begin_tree();
+          done = false;
+        }
       } else if (MODE == MODE_PARTICLE) {
         // one event of tools/particle_sim.h:128-141 after the flight's
         // ray_fire (EXITING, history excluded)
@@ -389,10 +406,12 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
             hc = a.p_hcount[idx];
             btri = -1;
           } else {
-            tid = (MODE == MODE_FIND_VOLUME) ? (a.n_vols > 0 ? a.vol_trees[0] : 0)
-                                             : (a.ray_trees ? a.ray_trees[idx] : a.tree);
+            tid = (MODE == MODE_FIND_VOLUME || MODE == MODE_ALL_VOLUMES)
+                      ? (a.n_vols > 0 ? a.vol_trees[0] : 0)
+                      : (a.ray_trees ? a.ray_trees[idx] : a.tree);
             o = load3(a.org, idx);
-            if ((MODE == MODE_PIV || MODE == MODE_FIND_VOLUME) && a.dir == nullptr)
+            if ((MODE == MODE_PIV || MODE == MODE_FIND_VOLUME || MODE == MODE_ALL_VOLUMES) &&
+                a.dir == nullptr)
               d = mk3(1. / sqrt(2.0), 1 / sqrt(2.0), 0.0);  // embree/ray_tracer.cpp:268
             else
               d = load3(a.dir, idx);
@@ -403,7 +422,8 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
           if (MODE == MODE_PARTICLE) {
             excl = a.p_hist + idx * a.hist_cap;
             nexcl = hc < 0 ? 0 : min(hc, a.hist_cap);
-          } else if (MODE != MODE_OCCLUDED && MODE != MODE_FIND_VOLUME && a.excl_off) {
+          } else if (MODE != MODE_OCCLUDED && MODE != MODE_FIND_VOLUME &&
+                     MODE != MODE_ALL_VOLUMES && a.excl_off) {
             const int32_t e0 = a.excl_off[idx];
             excl = a.excl_ids + e0;
             nexcl = a.excl_off[idx + 1] - e0;
@@ -412,8 +432,8 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
               (MODE == MODE_PARTICLE && (hc < 0 || nan_bits(pdist)))) {
             status = RAY_INVALID;
             trav = false;
-          } else if (MODE == MODE_FIND_VOLUME && a.n_vols == 0) {
-            trav = false;  // no volume to try: the implicit complement
+          } else if ((MODE == MODE_FIND_VOLUME || MODE == MODE_ALL_VOLUMES) && a.n_vols == 0) {
+            trav = false;  // no volume to try (find_volume: the implicit complement)
           } else if (MODE == MODE_PARTICLE && tid < 0) {
             trav = false;  // the particle ended earlier: left as it is
           } else if (MODE == MODE_PARTICLE && pev >= a.max_events) {
@@ -664,8 +684,8 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
 
 int g_num_sms = 0;
 // resident blocks per SM, by kernel variant, MINB and stack depth (8..64 step 8)
-int g_blocks_per_sm[10][3][kTStackMax / 8 + 1] = {};
-bool g_smem_attr[10][3] = {};
+int g_blocks_per_sm[12][3][kTStackMax / 8 + 1] = {};
+bool g_smem_attr[12][3] = {};
 
 template <int MODE, bool MIXED, int MINB>
 cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
@@ -726,6 +746,8 @@ cudaError_t launch_surface_query(int mode, bool mixed, const SurfArgs& a, cudaSt
     case 7: return launch_one<MODE_FIND_VOLUME, true>(a, st, 7);
     case 8: return launch_one<MODE_PARTICLE, false>(a, st, 8);
     case 9: return launch_one<MODE_PARTICLE, true>(a, st, 9);
+    case 10: return launch_one<MODE_ALL_VOLUMES, false>(a, st, 10);
+    case 11: return launch_one<MODE_ALL_VOLUMES, true>(a, st, 11);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -346,6 +346,23 @@ class CudaRayTracer:
                     "point_in_volume")
         return r
 
+    def point_in_volumes(self, points, trees, dirs=None, precision=MIXED, stream=None):
+        """xdgcu_point_in_volumes: (n, len(trees)) uint8 inside flags."""
+        p = _prep(points, np.float64, 3)
+        d = _prep(dirs, np.float64, 3)
+        n = p.shape[0]
+        tl = np.ascontiguousarray(trees, dtype=np.int32)
+        out = _Out(p)
+        if out.torch:
+            res = out._torch.zeros((n, len(tl)), dtype=out._torch.uint8, device=out.device)
+        else:
+            res = np.zeros((n, len(tl)), dtype=np.uint8)
+        self._check(self.L.xdgcu_point_in_volumes(self.ctx, n, _addr(p), _addr(d), len(tl),
+                                                  _addr(tl), _addr(res), None, int(precision),
+                                                  stream if stream is not None else out.stream()),
+                    "point_in_volumes")
+        return res
+
     def set_volume_map(self, volume_ids, surface_trees, implicit_complement):
         """The volumes find_volume tries, in order, and their surface trees."""
         ids = _host(volume_ids, np.int32)
@@ -833,6 +850,83 @@ class XDG:
         if tally:
             res["tally"] = {v: ty[t] for v, t in self.volume_to_surface_tree.items()}
         return res
+
+    def check_overlaps(self, check_edges=False, precision=MIXED, max_batch=4_000_000):
+        """The overlap_check tool (tools/overlap.cpp:62-191) with every
+        point_in_volume / ray_fire of a stage in one batch.
+
+        Vertex check: every vertex of every face of every surface, moved
+        1e-9 along dir = normalize(0.1, 0.1, 0.1) and then 2e-9 back along
+        -dir, is tested in every volume (the implicit complement included)
+        with that direction; a point inside more than one volume is an
+        overlap.  Edge check (check_edges): a ray along each face edge, as
+        long as the edge, is fired in every volume that is not a parent of
+        the edge's surface; the first of those volumes (in volume order) with
+        a hit reports {forward volume of the hit surface, forward volume of
+        the edge's surface}.  Returns {frozenset(volume ids): location}; of
+        the locations that found a set the first one (vertex order, then
+        edge order) is kept, where the reference keeps whichever its threads
+        wrote last."""
+        vols = list(self.model.volumes)
+        trees = np.array([self.volume_to_surface_tree[v] for v in vols], dtype=np.int32)
+        verts = np.concatenate([s.tri_xyz().reshape(-1, 3) for s in self.model.surfaces])
+        d = _normalize_rows(np.array([[0.1, 0.1, 0.1]]))[0]
+        bump = 1e-9
+        loc1 = verts + d * bump                    # loc += dir * bump
+        d2 = -d                                    # dir *= -1
+        loc2 = loc1 + (d2 * 2.0) * bump            # loc += dir * 2.0 * bump
+        found = {}
+        n = len(verts)
+        step = max(1, max_batch // max(1, len(vols)))
+        for k0 in range(0, n, step):
+            k1 = min(n, k0 + step)
+            pts = np.empty((2 * (k1 - k0), 3))
+            pts[0::2] = loc1[k0:k1]
+            pts[1::2] = loc2[k0:k1]
+            dirs = np.empty_like(pts)
+            dirs[0::2] = d
+            dirs[1::2] = d2
+            inside = self.rti.point_in_volumes(pts, trees, dirs, precision)
+            multi = np.nonzero(inside.sum(1) > 1)[0]
+            for j in multi:
+                key = frozenset(vols[m] for m in np.nonzero(inside[j])[0])
+                found.setdefault(key, pts[j].copy())
+        if not check_edges:
+            return found
+        parents = {s.surface_id: (s.forward_volume, s.reverse_volume) for s in self.model.surfaces}
+        for s in self.model.surfaces:
+            pf, pr = parents[s.surface_id]
+            check = [v for v in vols if v != pf and v != pr]
+            if not check:
+                continue
+            tri = s.tri_xyz().reshape(-1, 3, 3)
+            v1 = tri.reshape(-1, 3)
+            v2 = tri[:, [1, 2, 0], :].reshape(-1, 3)
+            dv = v2 - v1
+            ln = np.sqrt(dv[:, 0] * dv[:, 0] + dv[:, 1] * dv[:, 1] + dv[:, 2] * dv[:, 2])
+            dv = dv / ln[:, None]                   # dir /= edgeLength
+            ne, nv = len(v1), len(check)
+            ctrees = np.array([self.volume_to_surface_tree[v] for v in check], dtype=np.int32)
+            estep = max(1, max_batch // nv)
+            for e0 in range(0, ne, estep):
+                e1 = min(ne, e0 + estep)
+                m = e1 - e0
+                o = np.repeat(v1[e0:e1], nv, axis=0)
+                dd = np.repeat(dv[e0:e1], nv, axis=0)
+                dl = np.repeat(ln[e0:e1], nv)
+                rt = np.tile(ctrees, m)
+                t, surf, face = self.rti.ray_fire(0, o, dd, dl, EXITING, None, precision,
+                                                  ray_trees=rt)
+                hit = (surf != ID_NONE).reshape(m, nv)
+                for j in np.nonzero(hit.any(1))[0]:
+                    kk = int(np.argmax(hit[j]))     # the first volume with a hit
+                    r = j * nv + kk
+                    sh = int(surf[r])
+                    org, dirv, th = o[r], dd[r], t[r]
+                    loc = np.array([org[0] + th * dirv[0], org[1] + th * dirv[1],
+                                    org[2] + th * dirv[2]])
+                    found.setdefault(frozenset({parents[sh][0], pf}), loc)
+        return found
 
     def _walk_packed(self, elem_index, r, u, dist, precision):
         """Packed walk of host arrays sized in one pass when the first guess
