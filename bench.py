@@ -60,6 +60,8 @@ MFP = 1.0                   # tools/walk_elements.cpp: --mfp default
 MAX_EVENTS = 1_000_000
 TRANSPORT_CHECK = 2_000     # particles checked bit for bit against the oracle
 TRANSPORT_CPU_SAMPLE = 50_000
+OVERLAP_WORKLOAD = "nested_spheres_8x_icosphere_L6_overlap_check_vertices_and_edges"
+OVERLAP_CPU_SAMPLE = 200_000
 SURF_WORKLOAD = "nested_spheres_8x_icosphere_L6_3.7e6_sources_mfp1_ipc_graveyard_particle_sim"
 SURF_PARTICLES = 10_000_000  # ray origins of the headline workload used as sources
 SURF_HIST = 16
@@ -345,6 +347,132 @@ def bench_many_surfaces(torch, L, dev, stream, args, rank, world):
     }
 
 
+def bench_small_configs(torch, L, dev, stream, sptr, args, rank, world):
+    """The two small configurations, reported per configuration with the
+    mixed path's escalation fraction and its agreement with the FP64 path
+    and the oracle:
+      C1 sphere in box: level-4 icosphere r 10 in a cube of half-width 20,
+         1e5 rays from the ball r <= 9.9 (the ray-benchmark sampler, seed
+         12345), ray_fire EXITING in the sphere's volume;
+      C3 degenerate hits: level-6 icosphere r 5, 1e6 rays aimed at vertices
+         (40 %), edge midpoints (40 %) and centroids (20 %) with a 10^U(-12,-6)
+         jitter; every ray must hit (no lost hits)."""
+    from xdg_gb300 import _lib
+    from xdg_gb300.engine import FP64, MIXED, XDG
+    out = {}
+    cases = []
+    m1 = synth.single_sphere_in_box(level=4, radius=10.0, half_width=20.0)
+    o1, d1 = synth.lcg_benchmark_rays(100_000, (0.0, 0.0, 0.0), 9.9, seed=12345)
+    cases.append(("C1_sphere_in_box_L4_1e5_rays", m1, o1, d1))
+    v, tri = synth.icosphere(6, 5.0)
+    m3 = synth.Model()
+    m3.surfaces.append(synth.Surface(1, v, tri, np.arange(len(tri), dtype=np.int32), 1, 2))
+    m3.volumes = [1, 2]
+    m3.implicit_complement = 2
+    o3, d3, _ = synth.watertight_rays(v, tri, 1_000_000, 4.99, seed=4)
+    cases.append(("C3_degenerate_hits_L6_1e6_rays", m3, o3, d3))
+    for name, m, o_h, d_h in cases:
+        x = XDG(m, device=dev.index)
+        x.prepare_raytracer()
+        n = len(o_h)
+        o, d = torch.from_numpy(o_h).to(dev), torch.from_numpy(d_h).to(dev)
+        tree = x.volume_to_surface_tree[1]
+        t = {p: torch.empty(n, dtype=torch.float64, device=dev) for p in (MIXED, FP64)}
+        sf = {p: torch.empty(n, dtype=torch.int32, device=dev) for p in (MIXED, FP64)}
+        fc = {p: torch.empty(n, dtype=torch.int32, device=dev) for p in (MIXED, FP64)}
+
+        def rf(prec):
+            def go():
+                rc = L.xdgcu_ray_fire(x.rti.ctx, tree, None, n, ctypes.c_void_p(o.data_ptr()),
+                                      ctypes.c_void_p(d.data_ptr()), None, 0, None, None,
+                                      ctypes.c_void_p(t[prec].data_ptr()),
+                                      ctypes.c_void_p(sf[prec].data_ptr()),
+                                      ctypes.c_void_p(fc[prec].data_ptr()), None, prec, sptr)
+                _lib.check(rc, x.rti.ctx, "ray_fire")
+            return go
+
+        ms = {p: timed(torch, rf(p), max(3, args.steps // 2), 3, world, stream)
+              for p in (MIXED, FP64)}
+        x.rti.set_counting(True)
+        rf(MIXED)()
+        torch.cuda.synchronize()
+        cnt = x.rti.counters()
+        x.rti.set_counting(False)
+        rays = max(1, cnt["rays"])
+        res = {
+            "rays": n, "unit": "Mrays/s",
+            "value": n / (ms[MIXED] / 1e3) / 1e6, "fp64_value": n / (ms[FP64] / 1e3) / 1e6,
+            "escalations_per_ray": cnt["escalate"] / rays,
+            "escalated_fraction_of_triangle_tests": cnt["escalate"] / max(1, cnt["prim"]),
+            "id_mismatches_mixed_vs_fp64": int((sf[MIXED] != sf[FP64]).sum().item()
+                                               + (fc[MIXED] != fc[FP64]).sum().item()),
+            "t_mismatches_mixed_vs_fp64": int((t[MIXED] != t[FP64]).sum().item()),
+            "max_rel_t_error_mixed_vs_fp64": float(((t[MIXED] - t[FP64]).abs()
+                                                   / t[FP64].abs()).max().item()),
+            "lost_hits": int((sf[MIXED] != 1).sum().item()),
+        }
+        if rank == 0 and not args.no_oracle:
+            from oracle import oracle as xo
+            k = min(n, 200_000)
+            ot, os_, of = xo.volume_tree(m, 1).ray_fire(o_h[:k], d_h[:k],
+                                                         threads=os.cpu_count() or 1)
+            res["oracle_check"] = {"rays": k, "mismatches": int(
+                (t[MIXED][:k].cpu().numpy() != ot).sum() + (fc[MIXED][:k].cpu().numpy() != of).sum())}
+        out[name] = res
+    return out
+
+
+def bench_overlap(torch, x, model, args, rank):
+    """The overlap_check tool (tools/overlap.cpp:62-191) on the nested-sphere
+    model through XDG.check_overlaps: every face vertex moved +/-1e-9 along
+    normalize(0.1, 0.1, 0.1) and tested in all 9 volumes (3.9e6 points,
+    3.5e7 point_in_volume queries), then a ray along every face edge in the 7
+    volumes that are not its surface's parents (1.4e7 ray_fire queries).
+    Timed end to end from host arrays (host-side batching included), best of
+    three."""
+    from xdg_gb300.engine import FP64, MIXED
+    n_vert = 3 * sum(len(s.face_ids) for s in model.surfaces)
+    nv = len(model.volumes)
+    piv_q = 2 * n_vert * nv
+    edge_q = sum(3 * len(s.face_ids) * (nv - 2) for s in model.surfaces)
+    out = {"workload": OVERLAP_WORKLOAD, "unit": "Mqueries/s",
+           "point_in_volume_queries": piv_q, "edge_ray_queries": edge_q}
+    for name, prec in (("mixed", MIXED), ("fp64", FP64)):
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            found = x.check_overlaps(check_edges=True, precision=prec)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        out[f"seconds_{name}"] = best
+        out["value" if name == "mixed" else "fp64_value"] = (piv_q + edge_q) / best / 1e6
+        out[f"overlaps_found_{name}"] = len(found)
+    if rank == 0 and not args.no_oracle:
+        from oracle import oracle as xo
+        cores = os.cpu_count() or 1
+        verts = np.concatenate([s.tri_xyz().reshape(-1, 3) for s in model.surfaces])
+        k = min(OVERLAP_CPU_SAMPLE, len(verts))
+        dd = np.array([0.1, 0.1, 0.1])
+        dd = dd / np.sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2])
+        pts = verts[:k] + dd * 1e-9
+        dirs = np.tile(dd, (k, 1))
+        trees = [xo.volume_tree(model, v) for v in model.volumes]
+        tc = time.perf_counter()
+        inside = np.stack([t.point_in_volume(pts, dirs, threads=cores) for t in trees], 1)
+        dtc = time.perf_counter() - tc
+        got = x.rti.point_in_volumes(pts, [x.volume_to_surface_tree[v] for v in model.volumes],
+                                     dirs)
+        out["oracle_check"] = {"points": k, "volumes": nv,
+                               "mismatches": int((got != inside).any(1).sum())}
+        out["cpu_baseline"] = {"value": k * nv / dtc / 1e6, "unit": "Mqueries/s",
+                               "cores": cores, "kind": "port",
+                               "sample": f"vertex stage, first {k} vertices x {nv} volumes, "
+                                         "FP64, BVH, OpenMP"}
+    return out
+
+
 def bench_surface_transport(torch, L, x, model, dev, stream, sptr, p, d, trees_h, args, rank,
                             world):
     """The particle_sim tool loop (tools/particle_sim.h:128-141) on the
@@ -588,6 +716,9 @@ def run_engine(args, rank, world, local):
                     stream)
     id_mism = int((s_out != s_mixed).sum().item()) + int((f_out != f_mixed).sum().item())
     t_mism = int((t_out != t_mixed).sum().item())
+    hitm = s_mixed >= 0
+    max_rel_t = float(((t_mixed[hitm] - t_out[hitm]).abs() / t_out[hitm].abs()).max().item()) \
+        if bool(hitm.any()) else 0.0
     hit_frac = float((s_mixed >= 0).float().mean().item())
 
     # point_in_volume of the same points in their own volume (all must be inside)
@@ -639,6 +770,12 @@ def run_engine(args, rank, world, local):
     # particle_sim loop on the same model
     surface_transport = bench_surface_transport(torch, L, x, model, dev, stream, sptr, p, d,
                                                 trees_h, args, rank, world)
+
+    # the small configurations, per configuration
+    small_configs = bench_small_configs(torch, L, dev, stream, sptr, args, rank, world)
+
+    # overlap_check tool on the same model (vertex and edge stages)
+    overlap = bench_overlap(torch, x, model, args, rank)
 
     # algorithmic work counters (untimed run)
     rti.set_counting(True)
@@ -820,6 +957,7 @@ def run_engine(args, rank, world, local):
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "id_mismatches_mixed_vs_fp64": id_mism,
         "t_mismatches_mixed_vs_fp64": t_mism,
+        "max_rel_t_error_mixed_vs_fp64": max_rel_t,
         "hit_fraction": hit_frac,
         "oracle_check": oracle_mism,
         "escalations_per_ray": per_ray["escalate"],
@@ -864,6 +1002,8 @@ def run_engine(args, rank, world, local):
         "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "matches_device_path": e2e_ok},
+        "configs_small": small_configs,
+        "overlap_check": overlap,
         "transport": transport,
         "surface_transport": surface_transport,
         "many_surfaces": many,
