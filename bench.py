@@ -51,7 +51,7 @@ MANY_SURFACES = 256
 MANY_WORKLOAD = "256_surfaces_sphere_torus_tris_10^U(3,5.7)_rays_10^U(3,6)"
 TUNE_RAYS = 1_000_000       # autotuner sample (same distribution, its own seed)
 TUNE_TRACKS = 1_000_000     # the walk's length order pays off only on large batches
-TRACE_KEYS = ("node_width", "trace_occupancy", "trace_stack", "trace_node_iters",
+TRACE_KEYS = ("node_width", "leaf_max", "trace_occupancy", "trace_stack", "trace_node_iters",
               "trace_node_iters_fp64", "trace_flush_wait", "trace_grab", "trace_sort_min")
 WALK_KEYS = ("walk_queue", "walk_flush_wait", "walk_sort_min")
 CPU_SAMPLE = 4_000_000      # rays of the same workload timed on the host cores

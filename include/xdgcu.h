@@ -373,17 +373,22 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
 /* Launch and build parameters picked by an autotuner (no counterpart in the
  * reference, whose Embree backend has no tunables).  Keys:
  *   "trace_occupancy"  resident blocks per SM the ray-traversal kernel is
- *                      compiled for (2, 3 or 4; more blocks = fewer registers)
+ *                      compiled for (2, 3 or 4, default 4; more blocks = fewer
+ *                      registers)
  *   "trace_node_iters" inner-node steps a lane takes between two leaf phases
- *                      of the warp-synchronous traversal, mixed precision (1..64)
+ *                      of the warp-synchronous traversal, mixed precision
+ *                      (1..64, default 8; the FP64 path's default is 1)
  *   "trace_node_iters_fp64"  the same for the all-FP64 path
  *   "trace_flush_wait" number of lanes (1..32) whose rays wait only on queued
  *                      FP64 candidate tests before the warp drains a partly
  *                      filled queue
  *   "trace_stack"      shared-memory traversal stack entries per ray (16..64,
- *                      steps of 8; default 48).  Deeper stacks take shared
- *                      memory and so resident blocks; a ray whose traversal
- *                      needs more gets XDGCU_RAY_STACK_OVERFLOW
+ *                      steps of 8; default 40).  Deeper stacks take shared
+ *                      memory and so resident blocks.  A launch raises it to
+ *                      (node width - 1) x (depth of the deepest surface tree),
+ *                      which no traversal can exceed, up to 64; only trees
+ *                      deeper than that can make a ray end with
+ *                      XDGCU_RAY_STACK_OVERFLOW
  *   "trace_grab"       0 (default): each warp walks one contiguous slice of
  *                      the batch fixed at launch; > 0 (a multiple of 32): warps
  *                      take this many rays at a time from a device work queue,
@@ -400,7 +405,8 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      by tree, direction octant and the Morton code of the
  *                      origin.  Results are written at the callers' indices
  *                      and do not depend on it
- *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4)
+ *   "leaf_max"         primitives per BVH leaf for trees built afterwards (1..4,
+ *                      default 2)
  *   "node_width"       children per BVH node for trees built (or rebuilt,
  *                      xdgcu_rebuild_trees) afterwards: 4 (default) or 8
  *   "walk_queue"       mixed-precision walk: 1 (default) runs the FP64 face
@@ -430,9 +436,9 @@ enum {
  * trace_occupancy, trace_stack, trace_node_iters (or trace_node_iters_fp64
  * for XDGCU_FP64), trace_flush_wait, trace_grab and, for samples of at least
  * 65,536 rays, trace_sort_min, one key at a time, and leaves the context set
- * to the fastest combination found.  With tune_width != 0 it does so for
- * node_width 4 and 8, rebuilding the surface trees for each
- * (xdgcu_rebuild_trees), and keeps the faster width.  Each setting is timed as the median of
+ * to the fastest combination found.  With tune_tree != 0 it does so for
+ * every tree shape -- node_width 4 or 8, leaf_max 2, 3 or 4 -- rebuilding
+ * the surface trees for each (xdgcu_rebuild_trees), and keeps the fastest.  Each setting is timed as the median of
  * `reps` launches after one untimed launch.  Every setting must reproduce
  * the first run's outputs byte for byte (XDGCU_ERR_STATE otherwise); settings
  * whose smaller stack overflows are skipped.  When the coherent order wins,
@@ -441,7 +447,7 @@ enum {
  * queries of this context meanwhile. */
 int xdgcu_autotune_trace(xdgcu_ctx* ctx, int32_t query, int32_t tree, const int32_t* ray_trees,
                          int64_t n, const double* origins, const double* directions,
-                         int32_t precision, int32_t reps, int32_t tune_width, double* best_ms);
+                         int32_t precision, int32_t reps, int32_t tune_tree, double* best_ms);
 
 /* Autotuner of the walk launch parameters (no counterpart in the reference):
  * walk_queue (mixed precision only), walk_flush_wait and, for samples of at

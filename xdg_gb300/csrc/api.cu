@@ -314,16 +314,17 @@ struct xdgcu_ctx {
   int32_t ipc_volume = -1;
   bool has_volume_map = false;
   // tuning (xdgcu_set_tuning)
-  int32_t trace_occupancy = 3;
-  int32_t trace_node_iters = 4;       // mixed precision
+  int32_t trace_occupancy = 4;
+  int32_t trace_node_iters = 8;       // mixed precision
   int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
   int32_t trace_flush_wait = 8;
-  int32_t trace_stack = 48;      // shared-memory stack entries per lane
+  int32_t trace_stack = 40;      // shared-memory stack entries per lane
   int32_t trace_grab = 0;        // 0: one contiguous chunk per warp; > 0: device work queue
   int64_t trace_sort_min = 0;    // batches of at least this many rays run in coherent order (0 = never)
+  int32_t surf_stack_bound = 0;       // largest (width - 1) * depth of the surface trees
   int32_t particle_event_wait = 16;  // particle_sim loop: lanes gathered before their events run
   int32_t transport_event_wait = 4;  // walk_elements tool loop (mixed): the same
-  int32_t leaf_max = 4;
+  int32_t leaf_max = 2;
   int32_t node_width = 4;        // children per BVH node (4 or 8) of trees built afterwards
   int32_t walk_queue = 1;
   int32_t walk_flush_wait = 8;
@@ -386,7 +387,12 @@ int sync_surfaces(xdgcu_ctx* c) {
 int sync_tree_tables(xdgcu_ctx* c) {
   if (c->surf_trees_dirty) {
     std::vector<TreeDev> t;
-    for (auto& p : c->surf_trees) t.push_back(p->dev);
+    c->surf_stack_bound = 0;
+    for (auto& p : c->surf_trees) {
+      t.push_back(p->dev);
+      // a traversal holds at most (width - 1) entries per inner level
+      c->surf_stack_bound = std::max(c->surf_stack_bound, (p->dev.width - 1) * p->depth);
+    }
     if (t.empty()) t.push_back(TreeDev{});
     API_CUDA(c->d_surf_trees.alloc((int64_t)t.size()), "alloc tree table");
     API_CUDA(cudaMemcpy(c->d_surf_trees.p, t.data(), sizeof(TreeDev) * t.size(),
@@ -679,6 +685,14 @@ int with_length_order(xdgcu_ctx* c, WalkArgs& a, cudaStream_t s, Body body) {
 // the device work queue is on (trace_grab > 0) a zeroed cursor, and when the
 // batch is large enough (trace_sort_min) a coherent ray order, both in one
 // stream-ordered scratch allocation freed after the launch.
+// Stack entries of a traversal launch: the requested depth, raised to the
+// surface trees' bound (width - 1) * depth -- which no traversal can exceed --
+// as far as the 64-entry maximum allows.
+int32_t trace_stack_for(const xdgcu_ctx* c) {
+  const int32_t need = std::min(64, (c->surf_stack_bound + 7) / 8 * 8);
+  return std::max(c->trace_stack, need);
+}
+
 cudaError_t launch_trace(xdgcu_ctx* c, int mode, bool mixed, SurfArgs a, double extent,
                          cudaStream_t s, int32_t min_grab = 0) {
   if (a.n <= 0) return cudaSuccess;
@@ -1178,7 +1192,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.occupancy = c->trace_occupancy;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
-  a.stack = c->trace_stack;
+  a.stack = trace_stack_for(c);
   a.vol_ids = c->d_vol_ids.p;
   a.vol_trees = c->d_vol_trees.p;
   a.n_vols = c->n_vols;
@@ -1659,7 +1673,7 @@ int xdgcu_point_in_volumes(xdgcu_ctx* c, int64_t n, const double* points,
   a.occupancy = c->trace_occupancy;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
-  a.stack = c->trace_stack;
+  a.stack = trace_stack_for(c);
   a.n_vols = n_trees;
   a.vol_stride = n_trees;
   const bool mixed = precision == XDGCU_MIXED;
@@ -1774,7 +1788,7 @@ int xdgcu_transport_surfaces(xdgcu_ctx* c, int64_t n, int32_t* tree, double* pos
   a.occupancy = c->trace_occupancy;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
-  a.stack = c->trace_stack;
+  a.stack = trace_stack_for(c);
   a.mfp = mean_free_path;
   a.max_events = max_events;
   a.graveyard_tree = graveyard_tree;

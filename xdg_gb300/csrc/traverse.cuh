@@ -17,14 +17,17 @@ struct Hit {
   bool dotpos;
 };
 
+// per-thread work counts (32-bit: a thread's share of one launch stays far
+// below 2^32; the launch totals are 64-bit)
 struct Counters {
-  unsigned long long box, node, prim, esc;
+  uint32_t box, node, prim, esc;
 };
 
 __device__ __forceinline__ void flush_counters(unsigned long long* g, const Counters& c,
                                                unsigned long long rays) {
   if (!g) return;
-  unsigned long long v[5] = {c.box, c.node, c.prim, c.esc, rays};
+  unsigned long long v[5] = {(unsigned long long)c.box, (unsigned long long)c.node,
+                            (unsigned long long)c.prim, (unsigned long long)c.esc, rays};
   for (int k = 0; k < 5; ++k) {
     unsigned long long x = v[k];
     for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(__activemask(), x, off);

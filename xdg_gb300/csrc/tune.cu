@@ -8,8 +8,9 @@
 // setting as the median of `reps` launches after one untimed launch, with
 // CUDA events on a private stream.
 //
-// With tune_width the search runs once per BVH node width (4 and 8), the
-// surface trees rebuilt for each, and the faster width is kept.
+// With tune_tree the search runs once per tree shape -- node width 4 or 8,
+// leaf size 2, 3 or 4 -- the surface trees rebuilt for each, and the fastest
+// shape is kept.
 //
 // Every setting must give the same results: the tuner compares each run's
 // outputs byte for byte with the first run's and fails with XDGCU_ERR_STATE
@@ -21,6 +22,7 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "xdgcu.h"
@@ -171,7 +173,7 @@ extern "C" {
 
 int xdgcu_autotune_trace(xdgcu_ctx* c, int32_t query, int32_t tree, const int32_t* ray_trees,
                          int64_t n, const double* origins, const double* directions,
-                         int32_t precision, int32_t reps, int32_t tune_width, double* best_ms) {
+                         int32_t precision, int32_t reps, int32_t tune_tree, double* best_ms) {
   if (!c) return set_last_error(XDGCU_ERR_INVALID_ARG, "null context");
   if (query < XDGCU_QUERY_RAY_FIRE || query > XDGCU_QUERY_FIND_VOLUME)
     return set_last_error(XDGCU_ERR_INVALID_ARG, "autotune: unknown query");
@@ -241,32 +243,40 @@ int xdgcu_autotune_trace(xdgcu_ctx* c, int32_t query, int32_t tree, const int32_
       {"trace_grab", {0, 64, 256, 1024, 4096}},
   };
   if (n >= 65536) knobs.push_back({"trace_sort_min", {0, n}});
-  int64_t w0 = 4;
+  // tree shapes: the current one first, then (tune_tree) every node width
+  // and leaf size; each shape rebuilds the surface trees
+  int64_t w0 = 4, l0 = 4;
   int rc = xdgcu_get_tuning(c, "node_width", &w0);
+  if (!rc) rc = xdgcu_get_tuning(c, "leaf_max", &l0);
   if (rc) return rc;
-  std::vector<int64_t> widths = {w0};
-  if (tune_width) widths.push_back(w0 == 4 ? 8 : 4);
+  std::vector<std::pair<int64_t, int64_t>> shapes = {{w0, l0}};
+  if (tune_tree)
+    for (int64_t w : {4, 8})
+      for (int64_t l : {2, 3, 4})
+        if (!(w == w0 && l == l0)) shapes.push_back({w, l});
   double best = -1.0;
-  int64_t best_w = w0;
+  std::pair<int64_t, int64_t> best_shape = shapes[0], cur_shape = shapes[0];
   std::vector<int64_t> best_vals(knobs.size());
-  for (int64_t w : widths) {
-    if (w != w0) {
-      rc = xdgcu_set_tuning(c, "node_width", w);
+  for (const auto& sh : shapes) {
+    if (sh != cur_shape) {
+      rc = xdgcu_set_tuning(c, "node_width", sh.first);
+      if (!rc) rc = xdgcu_set_tuning(c, "leaf_max", sh.second);
       if (!rc) rc = xdgcu_rebuild_trees(c, 1);
       if (rc) return rc;
+      cur_shape = sh;
     }
     double ms = 0.0;
     rc = descend(c, knobs, measure, &ms);
     if (rc) return rc;
     if (best < 0.0 || ms < 0.99 * best) {
       best = ms;
-      best_w = w;
+      best_shape = sh;
       for (size_t k = 0; k < knobs.size(); ++k) xdgcu_get_tuning(c, knobs[k].key, &best_vals[k]);
     }
   }
-  const int64_t cur_w = widths.back();
-  if (best_w != cur_w) {
-    rc = xdgcu_set_tuning(c, "node_width", best_w);
+  if (best_shape != cur_shape) {
+    rc = xdgcu_set_tuning(c, "node_width", best_shape.first);
+    if (!rc) rc = xdgcu_set_tuning(c, "leaf_max", best_shape.second);
     if (!rc) rc = xdgcu_rebuild_trees(c, 1);
     if (rc) return rc;
   }

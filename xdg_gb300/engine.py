@@ -266,7 +266,7 @@ class CudaRayTracer:
         self._check(self.L.xdgcu_rebuild_trees(self.ctx, int(kinds)), "rebuild_trees")
 
     def autotune_trace(self, query, tree, origins, dirs=None, precision=MIXED, ray_trees=None,
-                       reps=5, tune_width=True):
+                       reps=5, tune_tree=True):
         """xdgcu_autotune_trace on a sample batch (torch CUDA tensors).  Leaves
         the context tuned; returns (sample ms under the chosen settings,
         tuning dict)."""
@@ -276,7 +276,7 @@ class CudaRayTracer:
         ms = ctypes.c_double()
         self._check(self.L.xdgcu_autotune_trace(self.ctx, int(query), int(tree or 0), _addr(rt),
                                                 o.shape[0], _addr(o), _addr(d), int(precision),
-                                                int(reps), 1 if tune_width else 0,
+                                                int(reps), 1 if tune_tree else 0,
                                                 ctypes.byref(ms)), "autotune_trace")
         return ms.value, self.tuning()
 
