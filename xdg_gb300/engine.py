@@ -867,30 +867,39 @@ class XDG:
         the locations that found a set the first one (vertex order, then
         edge order) is kept, where the reference keeps whichever its threads
         wrote last."""
+        import torch
+        dev = torch.device("cuda", self.rti.device)
         vols = list(self.model.volumes)
         trees = np.array([self.volume_to_surface_tree[v] for v in vols], dtype=np.int32)
-        verts = np.concatenate([s.tri_xyz().reshape(-1, 3) for s in self.model.surfaces])
-        d = _normalize_rows(np.array([[0.1, 0.1, 0.1]]))[0]
+        # the arithmetic below runs elementwise on the device, one IEEE
+        # operation per step as in the reference's Vec3da expressions
+        verts = torch.from_numpy(
+            np.concatenate([s.tri_xyz().reshape(-1, 3) for s in self.model.surfaces])).to(dev)
+        d = torch.from_numpy(_normalize_rows(np.array([[0.1, 0.1, 0.1]]))[0]).to(dev)
         bump = 1e-9
         loc1 = verts + d * bump                    # loc += dir * bump
         d2 = -d                                    # dir *= -1
         loc2 = loc1 + (d2 * 2.0) * bump            # loc += dir * 2.0 * bump
         found = {}
         n = len(verts)
-        step = max(1, max_batch // max(1, len(vols)))
+        step = max(1, max_batch // max(1, 2 * len(vols)))
         for k0 in range(0, n, step):
             k1 = min(n, k0 + step)
-            pts = np.empty((2 * (k1 - k0), 3))
+            pts = torch.empty((2 * (k1 - k0), 3), dtype=torch.float64, device=dev)
             pts[0::2] = loc1[k0:k1]
             pts[1::2] = loc2[k0:k1]
-            dirs = np.empty_like(pts)
+            dirs = torch.empty_like(pts)
             dirs[0::2] = d
             dirs[1::2] = d2
             inside = self.rti.point_in_volumes(pts, trees, dirs, precision)
-            multi = np.nonzero(inside.sum(1) > 1)[0]
-            for j in multi:
-                key = frozenset(vols[m] for m in np.nonzero(inside[j])[0])
-                found.setdefault(key, pts[j].copy())
+            multi = torch.nonzero(inside.sum(1) > 1).flatten()
+            if multi.numel() == 0:
+                continue
+            rows = inside[multi].cpu().numpy()
+            locs = pts[multi].cpu().numpy()
+            for j in range(len(rows)):
+                key = frozenset(vols[m] for m in np.nonzero(rows[j])[0])
+                found.setdefault(key, locs[j].copy())
         if not check_edges:
             return found
         parents = {s.surface_id: (s.forward_volume, s.reverse_volume) for s in self.model.surfaces}
@@ -899,33 +908,38 @@ class XDG:
             check = [v for v in vols if v != pf and v != pr]
             if not check:
                 continue
-            tri = s.tri_xyz().reshape(-1, 3, 3)
+            tri = torch.from_numpy(s.tri_xyz().reshape(-1, 3, 3)).to(dev)
             v1 = tri.reshape(-1, 3)
             v2 = tri[:, [1, 2, 0], :].reshape(-1, 3)
             dv = v2 - v1
-            ln = np.sqrt(dv[:, 0] * dv[:, 0] + dv[:, 1] * dv[:, 1] + dv[:, 2] * dv[:, 2])
+            ln = torch.sqrt(dv[:, 0] * dv[:, 0] + dv[:, 1] * dv[:, 1] + dv[:, 2] * dv[:, 2])
             dv = dv / ln[:, None]                   # dir /= edgeLength
             ne, nv = len(v1), len(check)
-            ctrees = np.array([self.volume_to_surface_tree[v] for v in check], dtype=np.int32)
+            ctrees = torch.tensor([self.volume_to_surface_tree[v] for v in check],
+                                  dtype=torch.int32, device=dev)
             estep = max(1, max_batch // nv)
             for e0 in range(0, ne, estep):
                 e1 = min(ne, e0 + estep)
                 m = e1 - e0
-                o = np.repeat(v1[e0:e1], nv, axis=0)
-                dd = np.repeat(dv[e0:e1], nv, axis=0)
-                dl = np.repeat(ln[e0:e1], nv)
-                rt = np.tile(ctrees, m)
+                o = torch.repeat_interleave(v1[e0:e1], nv, dim=0)
+                dd = torch.repeat_interleave(dv[e0:e1], nv, dim=0)
+                dl = torch.repeat_interleave(ln[e0:e1], nv)
+                rt = ctrees.repeat(m)
                 t, surf, face = self.rti.ray_fire(0, o, dd, dl, EXITING, None, precision,
                                                   ray_trees=rt)
                 hit = (surf != ID_NONE).reshape(m, nv)
-                for j in np.nonzero(hit.any(1))[0]:
-                    kk = int(np.argmax(hit[j]))     # the first volume with a hit
-                    r = j * nv + kk
-                    sh = int(surf[r])
-                    org, dirv, th = o[r], dd[r], t[r]
+                edges = torch.nonzero(hit.any(1)).flatten()
+                if edges.numel() == 0:
+                    continue
+                first = torch.argmax(hit[edges].to(torch.int32), dim=1)  # first volume with a hit
+                r = (edges * nv + first).cpu().numpy()
+                sh_all, o_h = surf[r].cpu().numpy(), o[r].cpu().numpy()
+                d_h, t_h = dd[r].cpu().numpy(), t[r].cpu().numpy()
+                for j in range(len(r)):
+                    org, dirv, th = o_h[j], d_h[j], t_h[j]
                     loc = np.array([org[0] + th * dirv[0], org[1] + th * dirv[1],
                                     org[2] + th * dirv[2]])
-                    found.setdefault(frozenset({parents[sh][0], pf}), loc)
+                    found.setdefault(frozenset({parents[int(sh_all[j])][0], pf}), loc)
         return found
 
     def _walk_packed(self, elem_index, r, u, dist, precision):
