@@ -59,11 +59,14 @@ class CudaRayTracer : public RayTracer {
                              void* stream = nullptr) const;
 
   xdgcu_ctx* context() const { return ctx_; }
+  int precision() const { return precision_; }
+  // the engine's tet index of an element of the element trees, and back
+  int32_t tet_index(MeshID element) const;
+  MeshID tet_id(int32_t index) const { return index < 0 ? ID_NONE : tet_ids_.at(index); }
+  void check(int rc, const char* what) const;
 
  private:
-  void check(int rc, const char* what) const;
   void upload_tet_mesh(const MeshManager* mm);
-  int32_t tet_index(MeshID element) const;
 
   xdgcu_ctx* ctx_ = nullptr;
   int precision_;

@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <map>
 #include <memory>
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -47,6 +48,8 @@ struct Vec3da {
 inline Vec3da operator-(const Vec3da& a, const Vec3da& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 inline Vec3da operator+(const Vec3da& a, const Vec3da& b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 inline Vec3da operator*(const Vec3da& a, double s) { return {s * a.x, s * a.y, s * a.z}; }
+inline Vec3da operator*(double s, const Vec3da& a) { return {s * a.x, s * a.y, s * a.z}; }
+inline Vec3da operator-(const Vec3da& a) { return {-a.x, -a.y, -a.z}; }
 using Position = Vec3da;
 using Direction = Vec3da;
 using Vertex = Vec3da;
@@ -69,7 +72,15 @@ struct BoundingBox {
   double dilation() const { return max_chord_length() * 1e-6; }
 };
 
-// The MeshManager queries a ray tracer reads (mesh_manager_interface.h).
+// constants.h:95-113
+enum class PropertyType { BOUNDARY_CONDITION = -1, MATERIAL = 0, DENSITY = 1, TEMPERATURE = 2 };
+struct Property {
+  PropertyType type;
+  std::string value;
+};
+
+// The MeshManager queries a ray tracer and the tools read
+// (mesh_manager_interface.h).
 class MeshManager {
  public:
   virtual ~MeshManager() = default;
@@ -84,6 +95,18 @@ class MeshManager {
   virtual MeshID adjacent_element(MeshID element, int face) const = 0;
   virtual MeshLibrary mesh_library() const = 0;
   const std::vector<MeshID>& volumes() const { return volumes_; }
+  const std::vector<MeshID>& surfaces() const { return surfaces_; }
+  MeshID implicit_complement() const { return implicit_complement_; }
+  // mesh_manager_interface.cpp: the forward-sense parent, then the reverse
+  std::pair<MeshID, MeshID> get_parent_volumes(MeshID surface) const {
+    return surface_senses(surface);
+  }
+  // mesh_manager_interface.cpp:98-104
+  Property get_surface_property(MeshID surface, PropertyType type) const {
+    auto it = surface_metadata_.find({surface, type});
+    if (it == surface_metadata_.end()) return {PropertyType::BOUNDARY_CONDITION, "transmission"};
+    return it->second;
+  }
   // mesh_manager_interface.cpp:236-245: the box starts at zero
   BoundingBox volume_bounding_box(MeshID volume) const {
     BoundingBox bb;
@@ -95,6 +118,9 @@ class MeshManager {
 
  protected:
   std::vector<MeshID> volumes_;
+  std::vector<MeshID> surfaces_;
+  MeshID implicit_complement_{ID_NONE};
+  std::map<std::pair<MeshID, PropertyType>, Property> surface_metadata_;
 };
 
 // element_face_accessor.h: face vertices of an element in the library's
@@ -133,6 +159,8 @@ class RayTracer {
                         double& dist) const = 0;
   virtual RTLibrary library() const = 0;
 
+  SurfaceTreeID global_surface_tree() const { return global_surface_tree_; }
+  ElementTreeID global_element_tree() const { return global_element_tree_; }
   int num_registered_trees() const { return (int)(surface_trees_.size() + element_trees_.size()); }
   int num_registered_surface_trees() const { return (int)surface_trees_.size(); }
   int num_registered_element_trees() const { return (int)element_trees_.size(); }
