@@ -10,15 +10,18 @@
 //   n_bc, (surface id, 0 transmission / 1 vacuum / 2 reflecting) pairs
 //   has_tets; if so: n_vertices, coordinates, n_tets, connectivity (4 per
 //     tet), adjacency (4 tet indices per tet, -1 on the boundary, MOAB face
-//     order), element ids, and per volume (in volume order) its tet count
-//     and tet indices
-// JOB: job (1 walk_particles, 2 simulate_particles, 3 check_overlaps),
-//   precision; for 1 and 2: n, n cells (element / volume ids), n x 3
-//   positions, n x 3 directions, n stream states (uint64), mfp, max_events,
-//   and for 2 the graveyard flag; for 3 the check_edges flag.
+//     order), element ids, per volume (in volume order) its tet count and
+//     tet indices, and n_bfe, the tet index behind each face id
+//     0 .. n_bfe-1 (-1: none; MeshManager::get_boundary_face_element)
+// JOB: job (1 walk_particles, 2 simulate_particles, 3 check_overlaps,
+//   4 track_segments), precision; for 1 and 2: n, n cells (element / volume
+//   ids), n x 3 positions, n x 3 directions, n stream states (uint64), mfp,
+//   max_events, and for 2 the graveyard flag; for 3 the check_edges flag;
+//   for 4: n, n x 3 starts, n x 3 ends.
 // OUT: for 1 and 2 the bank (cells, positions, directions, streams,
 //   distances, events, statuses); for 3 the number of sets, then per set its
-//   size, the volume ids and the location.
+//   size, the volume ids and the location; for 4 the n + 1 offsets (int64),
+//   the segments' element ids and lengths.
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -106,6 +109,8 @@ class FileMesh : public MeshManager {
         const std::vector<int32_t> tets = r.vec<int32_t>(c);
         for (int32_t t : tets) elements_[v].push_back(ids_[t]);
       }
+      const int32_t nb = r.get<int32_t>();
+      bfe_ = r.vec<int32_t>(nb);
     }
   }
   std::vector<MeshID> get_volume_surfaces(MeshID v) const override {
@@ -139,6 +144,10 @@ class FileMesh : public MeshManager {
     const int32_t nb = adj_[4 * index_.at(e) + face];
     return nb < 0 ? ID_NONE : ids_[nb];
   }
+  MeshID get_boundary_face_element(MeshID face) const override {
+    if (face < 0 || face >= (MeshID)bfe_.size() || bfe_[face] < 0) return ID_NONE;
+    return ids_[bfe_[face]];
+  }
   MeshLibrary mesh_library() const override { return MeshLibrary::MOAB; }
 
  private:
@@ -146,7 +155,7 @@ class FileMesh : public MeshManager {
   std::map<MeshID, std::vector<MeshID>> faces_;
   std::map<MeshID, std::array<Vertex, 3>> face_xyz_;
   std::vector<double> verts_;
-  std::vector<int32_t> conn_, adj_, ids_;
+  std::vector<int32_t> conn_, adj_, ids_, bfe_;
   std::map<MeshID, int32_t> index_;
   std::map<MeshID, std::vector<MeshID>> elements_;
 };
@@ -217,6 +226,15 @@ int main(int argc, char** argv) {
         w.put(kv.second.y);
         w.put(kv.second.z);
       }
+    } else if (job == 4) {
+      const int32_t n = rj.get<int32_t>();
+      const std::vector<double> a = rj.vec<double>(3 * (size_t)n);
+      const std::vector<double> b = rj.vec<double>(3 * (size_t)n);
+      const TrackSegments s = track_segments(rt, *mm, volume_trees.at(mm->implicit_complement()),
+                                             (size_t)n, a.data(), b.data());
+      w.vec(s.offsets);
+      w.vec(s.element);
+      w.vec(s.length);
     } else {
       std::fprintf(stderr, "unknown job %d\n", job);
       return 2;

@@ -79,6 +79,7 @@ class MockMesh : public MeshManager {
   }
   Vertex vertex_coordinates(MeshID v) const override { return vert(v); }
   MeshID adjacent_element(MeshID e, int face) const override { return ADJ[e][face]; }
+  MeshID get_boundary_face_element(MeshID) const override { return ID_NONE; }
   MeshLibrary mesh_library() const override { return MeshLibrary::MOCK; }
 
  private:

@@ -75,6 +75,10 @@ def write_model(path, m, bc=None):
             e = np.zeros(0, dtype=np.int32) if e is None else np.asarray(e, dtype=np.int32)
             out.append(_i32(len(e)))
             out.append(e.astype("<i4").tobytes())
+        bfe = m.boundary_face_element
+        bfe = np.zeros(0, dtype=np.int32) if bfe is None else np.asarray(bfe, dtype=np.int32)
+        out.append(_i32(len(bfe)))
+        out.append(bfe.astype("<i4").tobytes())
     with open(path, "wb") as f:
         f.write(b"".join(out))
 
@@ -215,3 +219,35 @@ def test_cpp_check_overlaps(cuda, tools_exe, tmp_path, prec):
     assert set(got) == set(ref) and frozenset({1, 2}) in got
     for key in got:
         assert np.array_equal(got[key], ref[key]), key
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [0, 1])
+def test_cpp_track_segments(cuda, tools_exe, tmp_path, prec):
+    """Tracks across three meshed blocks with gaps, starting and ending
+    inside, outside and between the blocks, some of zero length."""
+    from xdg_gb300.engine import XDG
+    m = synth.tet_blocks([((0.0, 0.0, 0.0), 6, 10.0), ((12.0, 0.0, 0.0), 5, 10.0),
+                          ((0.0, 11.0, 0.5), 4, 8.0)], jitter=0.2, seed=3)
+    x = XDG(m)
+    x.prepare_raytracer()
+    rng = np.random.default_rng(5)
+    n = 1500
+    a = rng.uniform([-4, -4, -4], [26, 23, 14], (n, 3))
+    b = rng.uniform([-4, -4, -4], [26, 23, 14], (n, 3))
+    b[:10] = a[:10]
+    el, ln, off = x.segments_global(a, b, precision=prec)
+    model_path, job_path = str(tmp_path / "m.bin"), str(tmp_path / "j.bin")
+    write_model(model_path, m)
+    with open(job_path, "wb") as f:
+        f.write(_i32(4, prec, n) + np.ascontiguousarray(a, dtype="<f8").tobytes()
+                + np.ascontiguousarray(b, dtype="<f8").tobytes())
+    raw = open(run(tools_exe, tmp_path, model_path, job_path), "rb").read()
+    got_off = np.frombuffer(raw, dtype="<i8", count=n + 1)
+    tot = int(got_off[-1])
+    got_el = np.frombuffer(raw, dtype="<i4", count=tot, offset=8 * (n + 1))
+    got_ln = np.frombuffer(raw, dtype="<f8", count=tot, offset=8 * (n + 1) + 4 * tot)
+    assert np.array_equal(got_off, off)
+    assert np.array_equal(got_el, el)
+    assert np.array_equal(got_ln, ln)
+    assert tot > n and (np.diff(off)[:10] == 0).all()

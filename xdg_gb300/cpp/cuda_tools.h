@@ -59,6 +59,26 @@ void simulate_particles(CudaRayTracer& rt, const MeshManager& mm,
                         std::map<MeshID, double>* cell_tracks = nullptr,
                         int32_t history_cap = 16);
 
+// Segments of n tracks: track i's are element[offsets[i] .. offsets[i+1]-1]
+// with the same lengths; offsets has n + 1 entries.
+struct TrackSegments {
+  std::vector<MeshID> element;
+  std::vector<double> length;
+  std::vector<int64_t> offsets;
+};
+
+// XDG::segments(start, end) (xdg.cpp:142-198) for the n tracks
+// starts[i] -> ends[i] (3 doubles each) across the meshed volumes and the
+// implicit complement between them.  All tracks advance together: each
+// round locates the active tracks in the global element tree
+// (xdgcu_find_element), fires the implicit-complement rays of the tracks
+// outside the mesh (xdgcu_ray_fire, EXITING) and re-enters through the
+// element behind the hit face (MeshManager::get_boundary_face_element), then
+// walks the rest in one packed launch (xdgcu_walk_elements_packed).
+TrackSegments track_segments(CudaRayTracer& rt, const MeshManager& mm, TreeID ipc_surface_tree,
+                             size_t n, const double* starts, const double* ends,
+                             int max_rounds = 10000);
+
 // The overlap_check tool (tools/overlap.cpp:62-191): every face vertex moved
 // 1e-9 along +/- normalize(0.1, 0.1, 0.1) and tested in every volume
 // (xdgcu_point_in_volumes); with check_edges a ray along every face edge in

@@ -93,6 +93,9 @@ class MeshManager {
   virtual std::vector<MeshID> element_connectivity(MeshID element) const = 0;
   virtual Vertex vertex_coordinates(MeshID vertex) const = 0;
   virtual MeshID adjacent_element(MeshID element, int face) const = 0;
+  // the element owning a boundary face, ID_NONE if none
+  // (mesh_manager_interface.h:153-157)
+  virtual MeshID get_boundary_face_element(MeshID face) const = 0;
   virtual MeshLibrary mesh_library() const = 0;
   const std::vector<MeshID>& volumes() const { return volumes_; }
   const std::vector<MeshID>& surfaces() const { return surfaces_; }
