@@ -829,26 +829,46 @@ def run_engine(args, rank, world, local):
     so_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
     fo_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
 
-    def e2e_call():
-        rc = L.xdgcu_ray_fire(rti.ctx, 0, ctypes.c_void_p(tr_h.data_ptr()), N_RAYS,
-                              ctypes.c_void_p(org_h.data_ptr()), ctypes.c_void_p(dir_h.data_ptr()),
-                              None, 0, None, None, ctypes.c_void_p(to_h.data_ptr()),
-                              ctypes.c_void_p(so_h.data_ptr()), ctypes.c_void_p(fo_h.data_ptr()),
+    def e2e_call(bufs):
+        tr, org, dr, to, so, fo = (ctypes.c_void_p(b.data_ptr()) if hasattr(b, "data_ptr")
+                                   else b.ctypes.data_as(ctypes.c_void_p) for b in bufs)
+        rc = L.xdgcu_ray_fire(rti.ctx, 0, tr, N_RAYS, org, dr, None, 0, None, None, to, so, fo,
                               None, MIXED, None)
         _lib.check(rc, rti.ctx, "ray_fire (host buffers)")
 
-    for _ in range(2):
-        e2e_call()
-    torch.cuda.synchronize()
-    dist.barrier(world)
-    te = time.perf_counter()
+    def e2e_ms(bufs, host_direct):
+        # host_direct 1: the kernel reads and writes page-locked host arrays
+        # in place; 0: staged copies in chunks; 2 (default): pageable arrays
+        # in place too when the device reads the host's page tables
+        old_hd = rti.get_tuning("host_direct")
+        rti.set_tuning("host_direct", host_direct)
+        for _ in range(2):
+            e2e_call(bufs)
+        torch.cuda.synchronize()
+        dist.barrier(world)
+        te = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_call(bufs)
+        torch.cuda.synchronize()
+        rti.set_tuning("host_direct", old_hd)
+        return dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world)
+
     e2e_steps = max(3, args.steps // 2)
-    for _ in range(e2e_steps):
-        e2e_call()
-    torch.cuda.synchronize()
-    ms_e2e = dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world)
+    pinned = (tr_h, org_h, dir_h, to_h, so_h, fo_h)
+    ms_e2e = e2e_ms(pinned, 1)
     e2e_ok = bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_staged = e2e_ms(pinned, 0)
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
     del org_h, dir_h, tr_h, to_h, so_h, fo_h
+    # the same call on pageable NumPy arrays
+    pg = (np.ascontiguousarray(trees_h), np.ascontiguousarray(p_h), np.ascontiguousarray(d_h),
+          np.empty(N_RAYS), np.empty(N_RAYS, np.int32), np.empty(N_RAYS, np.int32))
+    ms_e2e_pageable = e2e_ms(pg, 1)  # pageable arrays staged
+    e2e_ok = e2e_ok and bool(np.array_equal(pg[4], s_mixed.cpu().numpy()))
+    pageable_direct = bool(rti.get_tuning("pageable_direct"))
+    ms_e2e_pageable_direct = e2e_ms(pg, 2) if pageable_direct else None
+    e2e_ok = e2e_ok and bool(np.array_equal(pg[4], s_mixed.cpu().numpy()))
+    del pg
 
     # ---- C5: tet walk ------------------------------------------------------
     t0 = time.perf_counter()
@@ -1001,7 +1021,13 @@ def run_engine(args, rank, world, local):
         "cpu_baseline": cpu_baseline,
         "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "matches_device_path": e2e_ok},
+                "matches_device_path": e2e_ok,
+                "transfer": "page-locked host arrays read and written in place by the kernel "
+                            "over the host link (host_direct=1)",
+                "staged_value": total_rays / (ms_e2e_staged / 1e3) / 1e6,
+                "pageable_staged_value": total_rays / (ms_e2e_pageable / 1e3) / 1e6,
+                "pageable_direct_value": (total_rays / (ms_e2e_pageable_direct / 1e3) / 1e6
+                                          if ms_e2e_pageable_direct else None)},
         "configs_small": small_configs,
         "overlap_check": overlap,
         "transport": transport,

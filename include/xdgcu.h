@@ -418,7 +418,17 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      0 = never) are walked longest first: the tracks are
  *                      sorted by length on the device and dealt round-robin
  *                      to warps, so warps end on short tracks.  Results do not
- *                      depend on it. */
+ *                      depend on it.
+ *   "host_direct"      calls with host arrays: 1 lets the kernels read and
+ *                      write page-locked host arrays in place (no staging
+ *                      copies: each byte crosses the host link once, inside
+ *                      the kernel); 2 (default) does the same for pageable
+ *                      host memory when the device reads it through the
+ *                      host's page tables (read-only key "pageable_direct" =
+ *                      1, as on Grace systems); 0 stages every host array through
+ *                      device memory in chunks that overlap copies with
+ *                      compute.  Tallies updated atomically are always
+ *                      staged.  Results do not depend on it. */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);
 

@@ -328,6 +328,11 @@ struct xdgcu_ctx {
   int32_t node_width = 4;        // children per BVH node (4 or 8) of trees built afterwards
   int32_t walk_queue = 1;
   int32_t walk_flush_wait = 8;
+  // host arrays the kernels address directly instead of staging them:
+  // 0 none, 1 page-locked memory, 2 also pageable memory when the device
+  // reads it through the host's page tables (pageable_direct)
+  int32_t host_direct = 2;
+  bool pageable_direct = false;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
   bool counting = false;
@@ -513,7 +518,40 @@ struct Arr {
   void* host_out = nullptr;       // output to copy D2H
   size_t bytes = 0;
   void* dev = nullptr;
+  bool no_direct = false;  // kernels update it atomically: always staged
+  bool direct = false;     // dev is the host array's own device address
 };
+
+// The device address of host array p when the kernels can read and write it
+// in place (page-locked memory mapped into the device's address space, or
+// pageable memory on a device that walks the host's page tables), else
+// nullptr: the array is staged.  In-place access moves each byte over the
+// host link once, inside the kernel, with no staging copies or chunking.
+void* direct_ptr(const xdgcu_ctx* c, const void* p) {
+  if (!p || c->host_direct <= 0) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeHost) return at.devicePointer;
+  if (at.type == cudaMemoryTypeUnregistered && c->host_direct >= 2 && c->pageable_direct)
+    return const_cast<void*>(p);
+  return nullptr;
+}
+
+// Marks the arrays the kernels address in place (direct_ptr); an array that
+// is both read and written must be addressable for both.
+void resolve_direct(const xdgcu_ctx* c, Arr* a) {
+  if (a->no_direct || a->bytes == 0) return;
+  const void* p = a->host_in ? a->host_in : a->host_out;
+  if (!p || (a->host_in && a->host_out && a->host_in != a->host_out)) return;
+  void* d = direct_ptr(c, p);
+  if (d) {
+    a->dev = d;
+    a->direct = true;
+  }
+}
 
 // Decide the pointer kind of a call: 1 device, 0 host, -1 mixed (error).
 int classify(std::initializer_list<const void*> ptrs) {
@@ -543,15 +581,18 @@ Slot* get_slot(xdgcu_ctx* c) {
 }
 
 // Allocate device images of the arrays in the slot's workspace, upload inputs.
-int stage_in(Slot* s, std::vector<Arr*> arrs, cudaStream_t st) {
+int stage_in(const xdgcu_ctx* c, Slot* s, std::vector<Arr*> arrs, cudaStream_t st) {
   size_t total = 0;
-  for (Arr* a : arrs) total += (a->bytes + 255) & ~(size_t)255;
+  for (Arr* a : arrs) {
+    resolve_direct(c, a);
+    if (!a->direct) total += (a->bytes + 255) & ~(size_t)255;
+  }
   if ((int64_t)total > s->buf.n) {
     API_CUDA(s->buf.alloc((int64_t)std::max<size_t>(total, 1 << 20)), "workspace");
   }
   size_t off = 0;
   for (Arr* a : arrs) {
-    if (a->bytes == 0) continue;
+    if (a->bytes == 0 || a->direct) continue;
     a->dev = s->buf.p + off;
     off += (a->bytes + 255) & ~(size_t)255;
     if (a->host_in)
@@ -566,9 +607,13 @@ struct RayArr {
   void* host_out = nullptr;
   size_t per_ray = 0;
   char* dev = nullptr;
+  bool direct = false;  // dev is the host array's own device address
 };
 
-constexpr int64_t kChunkRays = 1 << 20;
+// Staged calls run in chunks of this many rays, at most kMaxChunks: 2^21 per
+// chunk ran ray_fire over 1e7 host rays in 10.1 ms, 2^20 in 10.7 ms and 2^19
+// in 12.6 ms (each chunk's launch ends with a tail of a few slow rays).
+constexpr int64_t kChunkRays = 1 << 21;
 constexpr int64_t kMaxChunks = 16;
 
 // Runs a per-ray query over host arrays in chunks: the inputs of chunk k+1
@@ -582,24 +627,46 @@ int begin_query(xdgcu_ctx* c, cudaStream_t st, unsigned long long** counters);
 template <typename Launch>
 int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<Arr*> whole,
                std::vector<RayArr*> rays, unsigned long long** counters, Launch launch) {
+  // arrays the kernels address in place take no workspace and no copies
+  bool all_direct = true;
+  for (Arr* a : whole) {
+    resolve_direct(c, a);
+    if (a->bytes && !a->direct) all_direct = false;
+  }
+  for (RayArr* r : rays) {
+    if (r->per_ray == 0) continue;
+    const void* p = r->host_in ? r->host_in : r->host_out;
+    void* d = (r->host_in && r->host_out && r->host_in != r->host_out) ? nullptr : direct_ptr(c, p);
+    if (d) {
+      r->dev = (char*)d;
+      r->direct = true;
+    } else {
+      all_direct = false;
+    }
+  }
   size_t total = 0;
-  for (Arr* a : whole) total += (a->bytes + 255) & ~(size_t)255;
-  for (RayArr* r : rays) total += (r->per_ray * (size_t)n + 255) & ~(size_t)255;
+  for (Arr* a : whole)
+    if (!a->direct) total += (a->bytes + 255) & ~(size_t)255;
+  for (RayArr* r : rays)
+    if (!r->direct) total += (r->per_ray * (size_t)n + 255) & ~(size_t)255;
   if ((int64_t)total > s->buf.n)
     API_CUDA(s->buf.alloc((int64_t)std::max<size_t>(total, 1 << 20)), "workspace");
   size_t off = 0;
   for (Arr* a : whole) {
-    if (a->bytes == 0) continue;
+    if (a->bytes == 0 || a->direct) continue;
     a->dev = s->buf.p + off;
     off += (a->bytes + 255) & ~(size_t)255;
   }
   for (RayArr* r : rays) {
-    if (r->per_ray == 0) continue;
+    if (r->per_ray == 0 || r->direct) continue;
     r->dev = s->buf.p + off;
     off += (r->per_ray * (size_t)n + 255) & ~(size_t)255;
   }
+  // chunks only overlap staging copies with compute: one launch when nothing is staged
   const int64_t chunks =
-      n <= 2 * kChunkRays ? 1 : std::min<int64_t>(kMaxChunks, (n + kChunkRays - 1) / kChunkRays);
+      all_direct || n <= 2 * kChunkRays
+          ? 1
+          : std::min<int64_t>(kMaxChunks, (n + kChunkRays - 1) / kChunkRays);
   const int64_t per = (n + chunks - 1) / chunks;
   if (!s->events((size_t)(2 * chunks + 1))) return set_err(XDGCU_ERR_CUDA, "event creation");
   // order after the caller's stream (if any)
@@ -608,7 +675,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
     API_CUDA(cudaStreamWaitEvent(s->copy_in, s->ev[2 * chunks], 0), "event wait");
   }
   for (Arr* a : whole)
-    if (a->host_in && a->bytes)
+    if (a->host_in && a->bytes && !a->direct)
       API_CUDA(cudaMemcpyAsync(a->dev, a->host_in, a->bytes, cudaMemcpyHostToDevice, s->copy_in),
                "H2D");
   int rc = begin_query(c, s->stream, counters);
@@ -618,7 +685,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
     const int64_t cnt = std::min<int64_t>(per, n - first);
     if (cnt <= 0) break;
     for (RayArr* r : rays)
-      if (r->host_in && r->per_ray)
+      if (r->host_in && r->per_ray && !r->direct)
         API_CUDA(cudaMemcpyAsync(r->dev + r->per_ray * first,
                                  (const char*)r->host_in + r->per_ray * first, r->per_ray * cnt,
                                  cudaMemcpyHostToDevice, s->copy_in),
@@ -629,7 +696,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
     API_CUDA(cudaEventRecord(s->ev[2 * k + 1], s->stream), "event");
     API_CUDA(cudaStreamWaitEvent(s->copy_out, s->ev[2 * k + 1], 0), "event wait");
     for (RayArr* r : rays)
-      if (r->host_out && r->per_ray)
+      if (r->host_out && r->per_ray && !r->direct)
         API_CUDA(cudaMemcpyAsync((char*)r->host_out + r->per_ray * first,
                                  r->dev + r->per_ray * first, r->per_ray * cnt,
                                  cudaMemcpyDeviceToHost, s->copy_out),
@@ -643,7 +710,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
 
 int stage_out(std::vector<Arr*> arrs, cudaStream_t st) {
   for (Arr* a : arrs)
-    if (a->host_out && a->bytes)
+    if (a->host_out && a->bytes && !a->direct)
       API_CUDA(cudaMemcpyAsync(a->host_out, a->dev, a->bytes, cudaMemcpyDeviceToHost, st), "D2H");
   API_CUDA(cudaStreamSynchronize(st), "sync");
   return XDGCU_OK;
@@ -774,6 +841,13 @@ int xdgcu_create(xdgcu_ctx** out, int device) {
   API_CUDA(cudaSetDevice(device), "cudaSetDevice");
   auto* c = new xdgcu_ctx();
   c->device = device;
+  int ats = 0;
+  if (cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    ats = 0;
+  }
+  c->pageable_direct = ats == 1;
   if (cudaStreamCreateWithFlags(&c->build_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return set_err(XDGCU_ERR_CUDA, "stream creation failed");
@@ -1096,6 +1170,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "walk_sort_min") {
     if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "walk_sort_min must be >= 0");
     c->walk_sort_min = value;
+  } else if (k == "host_direct") {
+    if (value < 0 || value > 2) return set_err(XDGCU_ERR_INVALID_ARG, "host_direct must be 0..2");
+    c->host_direct = (int32_t)value;
   } else {
     return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   }
@@ -1119,6 +1196,8 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "walk_queue") *value = c->walk_queue;
   else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
   else if (k == "walk_sort_min") *value = c->walk_sort_min;
+  else if (k == "host_direct") *value = c->host_direct;
+  else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   return XDGCU_OK;
 }
@@ -1495,7 +1574,7 @@ static int walk_query(xdgcu_ctx* c, bool walk, int64_t n, const int32_t* start, 
   Arr A_do{nullptr, dist_out, walk ? 0 : sizeof(double) * n};
   Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
   std::vector<Arr*> all = {&A_s, &A_o, &A_d, &A_l, &A_se, &A_sl, &A_sc, &A_no, &A_do, &A_st};
-  int rc = stage_in(s, all, st);
+  int rc = stage_in(c, s, all, st);
   if (rc) return rc;
   a.start = (const int32_t*)A_s.dev;
   a.org = (const double*)A_o.dev;
@@ -1594,7 +1673,7 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* c, int64_t n, const int32_t* start_ind
   Arr A_se{nullptr, nullptr, sizeof(int32_t) * capacity}, A_sl{nullptr, nullptr, sizeof(double) * capacity};
   Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
   std::vector<Arr*> all = {&A_s, &A_o, &A_d, &A_l, &A_off, &A_se, &A_sl, &A_st};
-  int rc = stage_in(s, all, st);
+  int rc = stage_in(c, s, all, st);
   if (rc) return rc;
   a.start = (const int32_t*)A_s.dev;
   a.org = (const double*)A_o.dev;
@@ -1834,9 +1913,10 @@ int xdgcu_transport_surfaces(xdgcu_ctx* c, int64_t n, int32_t* tree, double* pos
                {events, events, 4 * un},
                {tree_tally, tree_tally, tree_tally ? 8 * (c->surf_trees.size() + 1) : 0},
                {nullptr, status, status ? 4 * un : 0}};
+  A[8].no_direct = true;  // atomic tallies stay in device memory
   std::vector<Arr*> all;
   for (auto& x : A) all.push_back(&x);
-  int rc = stage_in(s, all, st);
+  int rc = stage_in(c, s, all, st);
   if (rc) return rc;
   char* p[10];
   for (int k = 0; k < 10; ++k) p[k] = (char*)A[k].dev;
@@ -1919,9 +1999,10 @@ int xdgcu_transport_elements(xdgcu_ctx* c, int64_t n, int32_t* elem_index, doubl
   Arr A_l{distance, distance, sizeof(double) * n};
   Arr A_v{events, events, sizeof(int32_t) * n};
   Arr A_t{elem_tally, elem_tally, elem_tally ? sizeof(double) * c->n_tet : 0};
+  A_t.no_direct = true;  // atomic tallies stay in device memory
   Arr A_st{nullptr, status, status ? sizeof(int32_t) * n : 0};
   std::vector<Arr*> all = {&A_e, &A_p, &A_d, &A_r, &A_l, &A_v, &A_t, &A_st};
-  int rc = stage_in(s, all, st);
+  int rc = stage_in(c, s, all, st);
   if (rc) return rc;
   t.elem = (int32_t*)A_e.dev;
   t.pos = (double*)A_p.dev;

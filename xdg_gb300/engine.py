@@ -24,7 +24,7 @@ from ._lib import (QUERY_FIND_VOLUME, QUERY_OCCLUDED, QUERY_POINT_IN_VOLUME,  # 
 TUNING_KEYS = ("trace_occupancy", "trace_node_iters", "trace_node_iters_fp64",
                "trace_flush_wait", "trace_stack", "trace_grab", "trace_sort_min",
                "particle_event_wait", "transport_event_wait", "leaf_max", "node_width",
-               "walk_queue", "walk_flush_wait", "walk_sort_min")
+               "walk_queue", "walk_flush_wait", "walk_sort_min", "host_direct")
 
 INFTY = np.finfo(np.float64).max
 TINY_BIT = 1e-10  # constants.h:32
@@ -51,7 +51,9 @@ def _host(a, dtype, shape=None):
 
 
 class _Out:
-    """Allocates outputs of the same kind (numpy / torch cuda) as the inputs."""
+    """Allocates outputs of the same kind as the inputs: NumPy arrays, torch
+    CUDA tensors, or torch CPU tensors (page-locked when the input is, so
+    that the kernels write them in place)."""
 
     def __init__(self, like):
         self.torch = _is_torch(like)
@@ -59,19 +61,27 @@ class _Out:
             import torch
             self._torch = torch
             self.device = like.device
+            self.cuda = like.is_cuda
+            self.pin = (not like.is_cuda) and like.is_pinned()
+
+    def empty(self, shape, dtype):
+        if self.torch:
+            return self._torch.empty(shape, dtype=dtype, device=self.device, pin_memory=self.pin)
+        return np.empty(shape, dtype=dtype)
+
+    def zeros(self, shape, dtype):
+        if self.torch:
+            return self._torch.zeros(shape, dtype=dtype, device=self.device, pin_memory=self.pin)
+        return np.zeros(shape, dtype=dtype)
 
     def f64(self, *shape):
-        if self.torch:
-            return self._torch.empty(shape, dtype=self._torch.float64, device=self.device)
-        return np.empty(shape, dtype=np.float64)
+        return self.empty(shape, self._torch.float64 if self.torch else np.float64)
 
     def i32(self, *shape):
-        if self.torch:
-            return self._torch.empty(shape, dtype=self._torch.int32, device=self.device)
-        return np.empty(shape, dtype=np.int32)
+        return self.empty(shape, self._torch.int32 if self.torch else np.int32)
 
     def stream(self):
-        if self.torch:
+        if self.torch and self.cuda:
             return ctypes.c_void_p(self._torch.cuda.current_stream(self.device).cuda_stream)
         return None
 
@@ -353,10 +363,7 @@ class CudaRayTracer:
         n = p.shape[0]
         tl = np.ascontiguousarray(trees, dtype=np.int32)
         out = _Out(p)
-        if out.torch:
-            res = out._torch.zeros((n, len(tl)), dtype=out._torch.uint8, device=out.device)
-        else:
-            res = np.zeros((n, len(tl)), dtype=np.uint8)
+        res = out.zeros((n, len(tl)), out._torch.uint8 if out.torch else np.uint8)
         self._check(self.L.xdgcu_point_in_volumes(self.ctx, n, _addr(p), _addr(d), len(tl),
                                                   _addr(tl), _addr(res), None, int(precision),
                                                   stream if stream is not None else out.stream()),
@@ -512,10 +519,7 @@ class CudaRayTracer:
                                                            np.float64)
         out = _Out(r)
         se, sl, st = out.i32(max(1, capacity)), out.f64(max(1, capacity)), out.i32(n)
-        if out.torch:
-            off = out._torch.empty(n + 1, dtype=out._torch.int64, device=out.device)
-        else:
-            off = np.empty(n + 1, dtype=np.int64)
+        off = out.empty(n + 1, out._torch.int64 if out.torch else np.int64)
         self._check(self.L.xdgcu_walk_elements_packed(self.ctx, n, _addr(e), _addr(r), _addr(uu),
                                                       _addr(dist), int(max_segs), int(capacity),
                                                       _addr(se), _addr(sl), _addr(off), _addr(st),
