@@ -918,6 +918,20 @@ def run_engine(args, rank, world, local):
     n_segs = int(seg_c.sum().item())
     walk_status_bad = int((wst != 0).sum().item())
     c_mixed = seg_c.clone()
+    # the same mixed walk with its FP64 edge coordinates computed from the
+    # vertices instead of the mesh's edge table
+    seg_ex, seg_lx, seg_cx = torch.empty_like(seg_e), torch.empty_like(seg_l), torch.empty_like(seg_c)
+    wr.rti.set_tuning("walk_edge_table", 0)
+    ms_walk_noedge = timed(torch, walk(MIXED, seg_ex, seg_lx, seg_cx), max(3, args.steps // 4), 1,
+                           world, stream)
+    wr.rti.set_tuning("walk_edge_table", 1)
+    vmask = torch.arange(MAX_SEGS, device=dev)[None, :] < c_mixed[:, None]
+    walk_edge_table_same = (bool(torch.equal(seg_cx, c_mixed))
+                            and bool(torch.equal(torch.where(vmask, seg_ex, 0),
+                                                 torch.where(vmask, seg_e, 0)))
+                            and bool(torch.equal(torch.where(vmask, seg_lx, 0.0),
+                                                 torch.where(vmask, seg_l, 0.0))))
+    del seg_ex, seg_lx, seg_cx, vmask
     # FP64 path into separate buffers for the sequence comparison
     seg_e64 = torch.empty_like(seg_e)
     seg_l64 = torch.empty_like(seg_l)
@@ -999,6 +1013,8 @@ def run_engine(args, rank, world, local):
             "workload": WALK_WORKLOAD,
             "value": total_segs / (ms_walk / 1e3) / 1e6, "unit": "Msegs/s",
             "fp64_value": total_segs / (ms_walk64 / 1e3) / 1e6,
+            "value_without_edge_table": total_segs / (ms_walk_noedge / 1e3) / 1e6,
+            "edge_table_same_segments": walk_edge_table_same,
             "ms_per_step": ms_walk, "fp64_ms_per_step": ms_walk64,
             "segments": n_segs, "tracks": N_TRACKS,
             "speedup_mixed_vs_fp64": ms_walk64 / ms_walk,

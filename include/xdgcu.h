@@ -419,6 +419,12 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      sorted by length on the device and dealt round-robin
  *                      to warps, so warps end on short tracks.  Results do not
  *                      depend on it.
+ *   "walk_edge_table"  mixed walk: 1 (default) takes the FP64 Plucker
+ *                      coordinates of a face's edges from the edge table built
+ *                      with the mesh (each edge's e and e x lo evaluated once,
+ *                      the same values), 0 computes them from the vertices;
+ *                      read-only "walk_edges" is the table's edge count (0
+ *                      when the mesh has none).  Results do not depend on it
  *   "host_direct"      calls with host arrays: 1 lets the kernels read and
  *                      write page-locked host arrays in place (no staging
  *                      copies: each byte crosses the host link once, inside

@@ -169,12 +169,19 @@ def tet_model():
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
-def test_find_element_and_walk_tet_cube(cuda, oracle, tet_model, prec):
+@pytest.mark.parametrize("settings", [{}, {"walk_edge_table": 0},
+                                      {"walk_queue": 0}, {"walk_queue": 0, "walk_edge_table": 0}])
+def test_find_element_and_walk_tet_cube(cuda, oracle, tet_model, prec, settings):
     """Scaled-down tet-walk configuration: find_element then the face-adjacency
-    walk; element sequences and lengths bit-identical to the oracle."""
+    walk; element sequences and lengths bit-identical to the oracle, with the
+    mixed walk's FP64 edge coordinates from the mesh's edge table or from the
+    vertices, through the per-warp FP64 queue or per lane."""
     tm = tet_model
     rti = CudaRayTracer()
     rti.set_tet_mesh(tm)
+    assert rti.get_tuning("walk_edges") > len(tm.conn)
+    for k, v in settings.items():
+        rti.set_tuning(k, v)
     m = synth.Model(volumes=[1], tets=tm, elements={1: np.arange(len(tm.conn), dtype=np.int32)})
     et = rti.create_element_tree(m, 1)
     rng = np.random.default_rng(23)

@@ -301,6 +301,10 @@ struct xdgcu_ctx {
   DevMem<double> d_xyz;
   DevMem<float4> d_xyz32;
   DevMem<int4> d_conn, d_adj;
+  // edge table for the mixed walk's FP64 face tests (build_edge_table)
+  DevMem<double> d_edge;
+  DevMem<int32_t> d_tet_edge;
+  int64_t n_edges = 0;
   DevMem<int32_t> d_elem_ids;
   int32_t face[12] = {0};
   int face_order = 0;
@@ -332,6 +336,7 @@ struct xdgcu_ctx {
   // 0 none, 1 page-locked memory, 2 also pageable memory when the device
   // reads it through the host's page tables (pageable_direct)
   int32_t host_direct = 2;
+  int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
   bool pageable_direct = false;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
@@ -807,6 +812,8 @@ const char* walk_args_for(const xdgcu_ctx* c, WalkArgs* a, int* face_order, int*
   if (!c->has_tets) return "no tet mesh set";
   a->xyz = c->d_xyz.p;
   a->xyz32 = c->d_xyz32.p;
+  a->edge = c->walk_edge_table ? c->d_edge.p : nullptr;
+  a->tet_edge = c->d_tet_edge.p;
   a->conn = c->d_conn.p;
   a->adj = c->d_adj.p;
   a->elem_ids = c->d_elem_ids.p;
@@ -1006,6 +1013,21 @@ int xdgcu_set_tet_mesh(xdgcu_ctx* c, int64_t n_vertices, const double* xyz, int6
              "upload tets");
     API_CUDA(cudaMemcpy(c->d_elem_ids.p, elem_ids, sizeof(int32_t) * n_tets, cudaMemcpyHostToDevice),
              "upload tets");
+    // meshes of 6 * n_tets >= 2^31 vertex pairs walk without the table
+    if (6 * n_tets < (1ll << 31)) {
+      double* edge = nullptr;
+      int32_t* tet_edge = nullptr;
+      int64_t ne = 0;
+      // without memory for it the walk computes the edges from the vertices
+      if (build_edge_table(c->d_xyz.p, c->d_conn.p, n_tets, &edge, &tet_edge, &ne,
+                           c->build_stream) != cudaSuccess)
+        cudaGetLastError();
+      c->d_edge.p = edge;
+      c->d_edge.n = 6 * ne;
+      c->d_tet_edge.p = tet_edge;
+      c->d_tet_edge.n = 6 * n_tets;
+      c->n_edges = ne;
+    }
   }
   std::memcpy(c->face, face_table, sizeof(c->face));
   c->face_order = std::memcmp(face_table, kMoabFaces, sizeof(kMoabFaces)) == 0 ? 0 : 1;
@@ -1170,6 +1192,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "walk_sort_min") {
     if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "walk_sort_min must be >= 0");
     c->walk_sort_min = value;
+  } else if (k == "walk_edge_table") {
+    if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "walk_edge_table must be 0 or 1");
+    c->walk_edge_table = (int32_t)value;
   } else if (k == "host_direct") {
     if (value < 0 || value > 2) return set_err(XDGCU_ERR_INVALID_ARG, "host_direct must be 0..2");
     c->host_direct = (int32_t)value;
@@ -1197,6 +1222,8 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
   else if (k == "walk_sort_min") *value = c->walk_sort_min;
   else if (k == "host_direct") *value = c->host_direct;
+  else if (k == "walk_edge_table") *value = c->walk_edge_table;
+  else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   return XDGCU_OK;
@@ -1525,6 +1552,8 @@ static int walk_query(xdgcu_ctx* c, bool walk, int64_t n, const int32_t* start, 
   WalkArgs a{};
   a.xyz = c->d_xyz.p;
   a.xyz32 = c->d_xyz32.p;
+  a.edge = c->walk_edge_table ? c->d_edge.p : nullptr;
+  a.tet_edge = c->d_tet_edge.p;
   a.conn = c->d_conn.p;
   a.adj = c->d_adj.p;
   a.elem_ids = c->d_elem_ids.p;
@@ -1620,6 +1649,8 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* c, int64_t n, const int32_t* start_ind
   WalkArgs a{};
   a.xyz = c->d_xyz.p;
   a.xyz32 = c->d_xyz32.p;
+  a.edge = c->walk_edge_table ? c->d_edge.p : nullptr;
+  a.tet_edge = c->d_tet_edge.p;
   a.conn = c->d_conn.p;
   a.adj = c->d_adj.p;
   a.elem_ids = c->d_elem_ids.p;
@@ -1962,6 +1993,8 @@ int xdgcu_transport_elements(xdgcu_ctx* c, int64_t n, int32_t* elem_index, doubl
   WalkArgs& a = t.mesh;
   a.xyz = c->d_xyz.p;
   a.xyz32 = c->d_xyz32.p;
+  a.edge = c->walk_edge_table ? c->d_edge.p : nullptr;
+  a.tet_edge = c->d_tet_edge.p;
   a.conn = c->d_conn.p;
   a.adj = c->d_adj.p;
   a.elem_ids = c->d_elem_ids.p;

@@ -125,15 +125,26 @@ __device__ __forceinline__ double plucker_edge64(d3 va, d3 vb, d3 ray, d3 rn) {
 // in so callers testing many triangles against one ray compute it once; the
 // value is identical to recomputing it per call.  `orient` is +1 or -1 when
 // use_or is set.
-__device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn, double t_max,
-                                          double t_min, bool use_or, int orient, double* t_out) {
-  // The three coordinates are evaluated unconditionally (the reference
-  // returns after the first one that fails, :83-113); the decisions below use
-  // the same values, so the outcome is the same, and lanes of a warp do not
-  // diverge in the FP64 part.
-  const double c0 = plucker_edge64(v0, v1, d, rn);
-  const double c1 = plucker_edge64(v1, v2, d, rn);
-  const double c2 = plucker_edge64(v2, v0, d, rn);
+// index of the largest |d| component, first maximum wins (plucker.h:132-134)
+__device__ __forceinline__ int plucker_axis(d3 d) {
+  const unsigned long long ax = absbits(d.x), ay = absbits(d.y), az = absbits(d.z);
+  int idx = 0;
+  unsigned long long mx = 0ull;
+  if (ax > mx) { idx = 0; mx = ax; }
+  if (ay > mx) { idx = 1; mx = ay; }
+  if (az > mx) { idx = 2; mx = az; }
+  return idx;
+}
+
+// plucker.h:83-161 from the three edge coordinates c0 = (v0, v1), c1 =
+// (v1, v2), c2 = (v2, v0) and component idx = plucker_axis(d) of the
+// vertices, origin and direction.  Only that component of the intersection
+// point is used; it is computed alone, with the reference's operations and
+// order.
+__device__ __forceinline__ bool plucker64_coords(double c0, double c1, double c2, double v0i,
+                                                 double v1i, double v2i, double oi, double di,
+                                                 double t_max, double t_min, bool use_or,
+                                                 int orient, double* t_out) {
   // orientation * c > 0
   auto exits = [&](double c) { return orient > 0 ? gt0(c) : lt0(c); };
   const bool p0 = gt0(c0), n0 = lt0(c0), p1 = gt0(c1), n1 = lt0(c1), p2 = gt0(c2), n2 = lt0(c2);
@@ -145,24 +156,45 @@ __device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn
   }
   if (rej || (is0(c0) && is0(c1) && is0(c2))) return false;
   const double inv = 1.0 / (c0 + c1 + c2);
-  // index of the largest |d| component, first maximum wins
-  const unsigned long long ax = absbits(d.x), ay = absbits(d.y), az = absbits(d.z);
-  int idx = 0;
-  unsigned long long mx = 0ull;
-  if (ax > mx) { idx = 0; mx = ax; }
-  if (ay > mx) { idx = 1; mx = ay; }
-  if (az > mx) { idx = 2; mx = az; }
-  // only component idx of the intersection point (plucker.h:132-134) is used;
-  // it is computed alone, with the same operations and order
   const double w0 = c0 * inv, w1 = c1 * inv, w2 = c2 * inv;
-  const double hit_i = (w0 * comp3(v2, idx) + w1 * comp3(v0, idx)) + w2 * comp3(v1, idx);
-  double dist = (hit_i - comp3(o, idx)) / comp3(d, idx);
+  const double hit_i = (w0 * v2i + w1 * v0i) + w2 * v1i;
+  double dist = (hit_i - oi) / di;
   const double u = w2;
   const double v = w0;
   if (lt0(u) || lt0(v) || dlt(1.0, u + v)) dist = -1.0;
   if (dlt(dist, t_min) || dlt(t_max, dist)) return false;
   *t_out = dist;
   return true;
+}
+
+__device__ __forceinline__ bool plucker64(d3 v0, d3 v1, d3 v2, d3 o, d3 d, d3 rn, double t_max,
+                                          double t_min, bool use_or, int orient, double* t_out) {
+  // The three coordinates are evaluated unconditionally (the reference
+  // returns after the first one that fails, :83-113); the decisions use the
+  // same values, so the outcome is the same, and lanes of a warp do not
+  // diverge in the FP64 part.
+  const double c0 = plucker_edge64(v0, v1, d, rn);
+  const double c1 = plucker_edge64(v1, v2, d, rn);
+  const double c2 = plucker_edge64(v2, v0, d, rn);
+  const int idx = plucker_axis(d);
+  return plucker64_coords(c0, c1, c2, comp3(v0, idx), comp3(v1, idx), comp3(v2, idx),
+                          comp3(o, idx), comp3(d, idx), t_max, t_min, use_or, orient, t_out);
+}
+
+// plucker.h:45-62 for an edge of a tet mesh whose edge vector e = hi - lo
+// and edge normal en = e x lo (lo, hi: its vertices in first() order) were
+// computed once when the mesh was set (6 doubles at E: e, then en).  The
+// same operations on the same values give the same coordinate as
+// plucker_edge64; `flip` is set when the test runs the edge from hi to lo.
+__device__ __forceinline__ double plucker_edge_pre(const double* E, bool flip, d3 ray, d3 rn) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(E));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(E + 2));
+  const double2 c = __ldg(reinterpret_cast<const double2*>(E + 4));
+  const d3 e = mk3(a.x, a.y, b.x), en = mk3(b.y, c.x, c.y);
+  double pip = dot3(ray, en) + dot3(rn, e);
+  pip = __longlong_as_double(__double_as_longlong(pip) ^ (flip ? (long long)0x8000000000000000ull : 0ll));
+  if (absbits(pip) < absbits(ZERO_TOL)) pip = 0.0;
+  return pip;
 }
 
 // Sign of dot(d, face_normal64(v0, v1, v2)) as the reference computes it

@@ -25,6 +25,7 @@
 #include "walk.h"
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "internal.cuh"
 #include "sample.cuh"
@@ -78,6 +79,31 @@ __device__ __forceinline__ int pair_index(int i, int j) {
 struct StepCnt {
   unsigned long long steps, esc;
 };
+
+// plucker64 for the face (l0, l1, l2) of tet `tet` (vertex indices ci), its
+// three edge coordinates taken from the mesh's edge table: the same values
+// plucker_edge64 computes from the vertices, for a third of the FP64
+// operations.  Only component plucker_axis(u) of the vertices is read.
+__device__ __forceinline__ bool plucker64_face_pre(const WalkArgs& a, int32_t tet,
+                                                   const int32_t ci[4], int l0, int l1, int l2,
+                                                   d3 r, d3 u, d3 rn, double* t) {
+  const int32_t* te = a.tet_edge + 6 * (int64_t)tet;
+  auto coord = [&](int la, int lb) {
+    const int32_t ref = __ldg(&te[pair_index(la, lb)]);
+    // the test runs la -> lb; the reference keeps the sign when la's vertex
+    // is the edge's lo (first(va, vb), plucker.h:48)
+    const bool second_is_lo = ref < 0;
+    const bool la_is_lo = second_is_lo == (la > lb);
+    return plucker_edge_pre(a.edge + 6 * (int64_t)(ref & 0x7fffffff), !la_is_lo, u, rn);
+  };
+  const double c0 = coord(l0, l1), c1 = coord(l1, l2), c2 = coord(l2, l0);
+  const int idx = plucker_axis(u);
+  const double v0i = __ldg(&a.xyz[3 * (int64_t)sel4(ci, l0) + idx]);
+  const double v1i = __ldg(&a.xyz[3 * (int64_t)sel4(ci, l1) + idx]);
+  const double v2i = __ldg(&a.xyz[3 * (int64_t)sel4(ci, l2) + idx]);
+  return plucker64_coords(c0, c1, c2, v0i, v1i, v2i, comp3(r, idx), comp3(u, idx), INFTY, 0.0,
+                          true, 1, t);
+}
 
 // MeshManager::next_element for tet `elem` at r along u.  Returns the face
 // index (or -1) and writes the exit distance.
@@ -156,11 +182,16 @@ __device__ __forceinline__ int next_face(const WalkArgs& a, int32_t elem, d3 r, 
       cnt.esc++;
       const int l0 = face_local<FO>(a, f, 0), l1 = face_local<FO>(a, f, 1),
                 l2 = face_local<FO>(a, f, 2);
-      const d3 f0 = load3(a.xyz, sel4(ci, l0));
-      const d3 f1 = load3(a.xyz, sel4(ci, l1));
-      const d3 f2 = load3(a.xyz, sel4(ci, l2));
       double t;
-      const bool hit = plucker64(f0, f1, f2, r, u, rn, INFTY, 0.0, true, 1, &t);
+      bool hit;
+      if (a.edge) {
+        hit = plucker64_face_pre(a, elem, ci, l0, l1, l2, r, u, rn, &t);
+      } else {
+        const d3 f0 = load3(a.xyz, sel4(ci, l0));
+        const d3 f1 = load3(a.xyz, sel4(ci, l1));
+        const d3 f2 = load3(a.xyz, sel4(ci, l2));
+        hit = plucker64(f0, f1, f2, r, u, rn, INFTY, 0.0, true, 1, &t);
+      }
       const double df = hit ? (gt0(t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
       if (dlt(df, best)) {
         best = df;
@@ -597,15 +628,21 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
       int32_t oc[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) oc[q] = __shfl_sync(0xffffffffu, ci[q], owner);
+      const int32_t oel = __shfl_sync(0xffffffffu, elem, owner);
       double df = INFTY;
       if (mine) {
         const int l0 = face_local<FO>(a, f, 0), l1 = face_local<FO>(a, f, 1),
                   l2 = face_local<FO>(a, f, 2);
-        const d3 f0 = load3(a.xyz, sel4(oc, l0));
-        const d3 f1 = load3(a.xyz, sel4(oc, l1));
-        const d3 f2 = load3(a.xyz, sel4(oc, l2));
         double t;
-        const bool hit = plucker64(f0, f1, f2, orr, ou, orn, INFTY, 0.0, true, 1, &t);
+        bool hit;
+        if (a.edge) {
+          hit = plucker64_face_pre(a, oel, oc, l0, l1, l2, orr, ou, orn, &t);
+        } else {
+          const d3 f0 = load3(a.xyz, sel4(oc, l0));
+          const d3 f1 = load3(a.xyz, sel4(oc, l1));
+          const d3 f2 = load3(a.xyz, sel4(oc, l2));
+          hit = plucker64(f0, f1, f2, orr, ou, orn, INFTY, 0.0, true, 1, &t);
+        }
         df = hit ? (gt0(t) ? t : 0.0) : INFTY;  // std::max(0.0, t)
       }
       Q.rd[lane] = df;
@@ -994,6 +1031,143 @@ __global__ void k_iota(int32_t* v, int64_t n) {
   if (i < n) v[i] = (int32_t)i;
 }
 }  // namespace
+
+namespace {
+
+// local vertex pairs of a tet in pair_index order
+__device__ __forceinline__ void pair_of(int p, int& i, int& j) {
+  i = p < 3 ? 0 : (p < 5 ? 1 : 2);
+  j = p < 3 ? p + 1 : (p < 5 ? p - 1 : 3);
+}
+
+__device__ __forceinline__ int32_t conn_at(int4 c, int k) {
+  return k == 0 ? c.x : (k == 1 ? c.y : (k == 2 ? c.z : c.w));
+}
+
+__global__ void k_edge_keys(const int4* __restrict__ conn, int64_t n_tets,
+                            unsigned long long* __restrict__ keys, int32_t* __restrict__ slots) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= 6 * n_tets) return;
+  const int4 c = conn[s / 6];
+  int i, j;
+  pair_of((int)(s % 6), i, j);
+  const unsigned a = (unsigned)conn_at(c, i), b = (unsigned)conn_at(c, j);
+  const unsigned lo = a < b ? a : b, hi = a < b ? b : a;
+  keys[s] = ((unsigned long long)lo << 32) | hi;
+  slots[s] = (int32_t)s;
+}
+
+__global__ void k_edge_heads(const unsigned long long* __restrict__ keys, int64_t n,
+                             int32_t* __restrict__ head) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  head[k] = (k == 0 || keys[k] != keys[k - 1]) ? 1 : 0;
+}
+
+// e = hi - lo and en = e x lo of each unique edge (plucker.h:45-62 with
+// first() ordering the two vertices); lo_vertex = the vertex index of lo
+__global__ void k_edge_data(const unsigned long long* __restrict__ keys,
+                            const int32_t* __restrict__ head, const int32_t* __restrict__ id,
+                            int64_t n, const double* __restrict__ xyz, double* __restrict__ edge,
+                            int32_t* __restrict__ lo_vertex) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n || !head[k]) return;
+  const int64_t e = id[k] - 1;
+  const int32_t ga = (int32_t)(keys[k] >> 32), gb = (int32_t)(keys[k] & 0xffffffffull);
+  const d3 va = load3(xyz, ga), vb = load3(xyz, gb);
+  const bool f = first_lower(va, vb);
+  const d3 lo = f ? va : vb;
+  const d3 hi = f ? vb : va;
+  const d3 ev = sub3(hi, lo);
+  const d3 en = cross3(ev, lo);
+  double* E = edge + 6 * e;
+  E[0] = ev.x;
+  E[1] = ev.y;
+  E[2] = ev.z;
+  E[3] = en.x;
+  E[4] = en.y;
+  E[5] = en.z;
+  lo_vertex[e] = f ? ga : gb;
+}
+
+__global__ void k_edge_scatter(const int32_t* __restrict__ slots, const int32_t* __restrict__ id,
+                               int64_t n, const int4* __restrict__ conn,
+                               const int32_t* __restrict__ lo_vertex,
+                               int32_t* __restrict__ tet_edge) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int32_t s = slots[k];
+  const int32_t e = id[k] - 1;
+  int i, j;
+  pair_of(s % 6, i, j);
+  const bool second_is_lo = conn_at(conn[s / 6], j) == lo_vertex[e];
+  tet_edge[s] = e | (second_is_lo ? (int32_t)0x80000000u : 0);
+}
+
+}  // namespace
+
+cudaError_t build_edge_table(const double* xyz, const int4* conn, int64_t n_tets, double** edge,
+                             int32_t** tet_edge, int64_t* n_edges, cudaStream_t st) {
+  *edge = nullptr;
+  *tet_edge = nullptr;
+  *n_edges = 0;
+  const int64_t n = 6 * n_tets;
+  if (n_tets <= 0 || n >= (1ll << 31)) return cudaErrorInvalidValue;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  unsigned long long *keys = nullptr, *keys2 = nullptr;
+  int32_t *slots = nullptr, *slots2 = nullptr, *head = nullptr, *id = nullptr, *lo = nullptr;
+  void* tmp = nullptr;
+  size_t tb_sort = 0, tb_scan = 0;
+  cudaError_t e = cub::DeviceRadixSort::SortPairs(nullptr, tb_sort, keys, keys2, slots, slots2,
+                                                  (int)n, 0, 64, st);
+  if (e == cudaSuccess) e = cub::DeviceScan::InclusiveSum(nullptr, tb_scan, head, id, (int)n, st);
+  const size_t tb = tb_sort > tb_scan ? tb_sort : tb_scan;
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&keys, sizeof(*keys) * n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&keys2, sizeof(*keys2) * n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&slots, sizeof(*slots) * n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&slots2, sizeof(*slots2) * n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&head, sizeof(*head) * n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&id, sizeof(*id) * n, st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&tmp, tb, st);
+  if (e == cudaSuccess) {
+    k_edge_keys<<<g, 256, 0, st>>>(conn, n_tets, keys, slots);
+    e = cudaGetLastError();
+  }
+  size_t t1 = tb;
+  if (e == cudaSuccess)
+    e = cub::DeviceRadixSort::SortPairs(tmp, t1, keys, keys2, slots, slots2, (int)n, 0, 64, st);
+  if (e == cudaSuccess) {
+    k_edge_heads<<<g, 256, 0, st>>>(keys2, n, head);
+    e = cudaGetLastError();
+  }
+  size_t t2 = tb;
+  if (e == cudaSuccess) e = cub::DeviceScan::InclusiveSum(tmp, t2, head, id, (int)n, st);
+  int32_t ne = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&ne, id + (n - 1), sizeof(ne), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaMalloc((void**)edge, sizeof(double) * 6 * (size_t)ne);
+  if (e == cudaSuccess) e = cudaMalloc((void**)tet_edge, sizeof(int32_t) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&lo, sizeof(int32_t) * (size_t)ne, st);
+  if (e == cudaSuccess) {
+    k_edge_data<<<g, 256, 0, st>>>(keys2, head, id, n, xyz, *edge, lo);
+    k_edge_scatter<<<g, 256, 0, st>>>(slots2, id, n, conn, lo, *tet_edge);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  for (void* p : {(void*)keys, (void*)keys2, (void*)slots, (void*)slots2, (void*)head, (void*)id,
+                  tmp, (void*)lo})
+    if (p) cudaFreeAsync(p, st);
+  cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    if (*edge) cudaFree(*edge);
+    if (*tet_edge) cudaFree(*tet_edge);
+    *edge = nullptr;
+    *tet_edge = nullptr;
+    return e;
+  }
+  *n_edges = ne;
+  return cudaSuccess;
+}
 
 size_t walk_order_scratch_bytes(int64_t n) {
   size_t tmp = 0;

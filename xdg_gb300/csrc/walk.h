@@ -13,6 +13,12 @@ struct WalkArgs {
   const int4* conn;      // 4 vertex indices per tet
   const int4* adj;       // 4 neighbour tets per tet (-1 boundary), face order
   const int32_t* elem_ids;
+  // edge table of the mesh (may be null): 6 doubles per unique edge (e = hi -
+  // lo, then e x lo, lo/hi in first() order) and 6 entries per tet for its
+  // local vertex pairs (0,1),(0,2),(0,3),(1,2),(1,3),(2,3): the edge index,
+  // bit 31 set when the pair's second vertex is the edge's lo
+  const double* edge;
+  const int32_t* tet_edge;
   int32_t n_tets;
   int32_t face[12];      // local face table
   int64_t n;
@@ -75,6 +81,14 @@ cudaError_t scan_offsets(int64_t* offsets, int64_t n, int64_t* block_sums, cudaS
 size_t walk_order_scratch_bytes(int64_t n);
 cudaError_t walk_order(const double* dist, int64_t n, int32_t* order, void* scratch,
                        size_t scratch_bytes, cudaStream_t st);
+
+// Builds the edge table of a tet mesh (WalkArgs::edge / tet_edge) on the
+// device: sorts the 6 vertex pairs of every tet, numbers the unique ones and
+// evaluates each edge's e and e x lo once, with plucker.h:45-62's operations.
+// *edge and *tet_edge are cudaMalloc'ed (the caller frees them).  Returns
+// cudaErrorInvalidValue without building anything when 6 * n_tets >= 2^31.
+cudaError_t build_edge_table(const double* xyz, const int4* conn, int64_t n_tets, double** edge,
+                             int32_t** tet_edge, int64_t* n_edges, cudaStream_t st);
 
 // face_order: 0 = the MOAB table {0,1,3},{1,2,3},{2,0,3},{0,2,1} (compiled in),
 // 1 = any other table (read from WalkArgs::face).
