@@ -712,6 +712,13 @@ def run_engine(args, rank, world, local):
         N_RAYS < rti.get_tuning("trace_sort_min") else 6
     clk = clocks.stop()
     t_mixed, s_mixed, f_mixed = t_out.clone(), s_out.clone(), f_out.clone()
+    # the same mixed launch with the triangles' FP64 terms computed from the
+    # vertices instead of read from the tree
+    rti.set_tuning("trace_edge_table", 0)
+    ms_mixed_noedge = timed(torch, rf(MIXED), max(3, args.steps // 4), 1, world, stream)
+    rti.set_tuning("trace_edge_table", 1)
+    edge_table_same = bool(torch.equal(t_out, t_mixed) and torch.equal(s_out, s_mixed)
+                           and torch.equal(f_out, f_mixed))
     ms_fp64 = timed(torch, rf(FP64), max(3, args.steps // 4), max(1, args.warmup // 2), world,
                     stream)
     id_mism = int((s_out != s_mixed).sum().item()) + int((f_out != f_mixed).sum().item())
@@ -988,6 +995,8 @@ def run_engine(args, rank, world, local):
         },
         "fp64": {"value": total_rays / (ms_fp64 / 1e3) / 1e6, "unit": "Mrays/s",
                  "ms_per_step": ms_fp64},
+        "mixed_without_edge_table": {"value": total_rays / (ms_mixed_noedge / 1e3) / 1e6,
+                                     "unit": "Mrays/s", "same_results": edge_table_same},
         "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
         "id_mismatches_mixed_vs_fp64": id_mism,
         "t_mismatches_mixed_vs_fp64": t_mism,

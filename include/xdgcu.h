@@ -419,6 +419,13 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      sorted by length on the device and dealt round-robin
  *                      to warps, so warps end on short tracks.  Results do not
  *                      depend on it.
+ *   "trace_edge_table" mixed ray_fire / point_in_volume / occluded /
+ *                      find_volume / particle loop: 1 (default) takes each
+ *                      triangle's ray-independent FP64 terms (edge vectors,
+ *                      edge normals, face normal) from the tree, where they
+ *                      were evaluated once at build time with the reference's
+ *                      operations; 0 computes them from the vertices.
+ *                      Results do not depend on it
  *   "walk_edge_table"  mixed walk: 1 (default) takes the FP64 Plucker
  *                      coordinates of a face's edges from the edge table built
  *                      with the mesh (each edge's e and e x lo evaluated once,

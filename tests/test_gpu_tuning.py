@@ -25,6 +25,8 @@ SETTINGS = [
     {"trace_stack": 32, "trace_occupancy": 4, "trace_node_iters": 1, "trace_node_iters_fp64": 4},
     {"trace_grab": 4096, "trace_node_iters": 16, "trace_flush_wait": 32, "trace_stack": 40},
     {"trace_flush_wait": 1, "trace_grab": 64},
+    {"trace_edge_table": 0},
+    {"trace_edge_table": 0, "trace_grab": 64, "trace_stack": 48},
 ]
 
 

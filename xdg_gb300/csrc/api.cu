@@ -53,6 +53,7 @@ struct TreeHost {
   Node64* n64 = nullptr;
   DevMem<float4> prim32;
   DevMem<double> prim64;
+  DevMem<double> prime;  // surface trees: TreeDev::prime
   DevMem<int32_t> prim_ref;
   int32_t n_nodes = 0;
   int32_t depth = 0;
@@ -129,7 +130,7 @@ __global__ void k_tri_boxes(const double* __restrict__ tri_xyz, const int32_t* _
 __global__ void k_tri_gather(const double* __restrict__ tri_xyz, const int32_t* __restrict__ tris,
                              const int32_t* __restrict__ order, int32_t n,
                              float4* __restrict__ prim32, double* __restrict__ prim64,
-                             int32_t* __restrict__ prim_ref) {
+                             double* __restrict__ prime, int32_t* __restrict__ prim_ref) {
   int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const int32_t g = tris[order[j]];
@@ -138,6 +139,35 @@ __global__ void k_tri_gather(const double* __restrict__ tri_xyz, const int32_t* 
   for (int k = 0; k < 9; ++k) o[k] = v[k];
   o[9] = 0.0;
   prim_ref[j] = g;
+  {
+    // the ray-independent parts of the FP64 test (TreeDev::prime), with the
+    // operations of plucker_edge64 and normal_dot_sign
+    const d3 V[3] = {mk3(v[0], v[1], v[2]), mk3(v[3], v[4], v[5]), mk3(v[6], v[7], v[8])};
+    double* pe = prime + kPrimEStride * (int64_t)j;
+    for (int k = 0; k < 3; ++k) {
+      const d3 va = V[k], vb = V[(k + 1) % 3];
+      const bool f = first_lower(va, vb);
+      const d3 lo = f ? va : vb;
+      const d3 hi = f ? vb : va;
+      d3 e = sub3(hi, lo);
+      d3 en = cross3(e, lo);
+      if (!f) {
+        e = mk3(-e.x, -e.y, -e.z);
+        en = mk3(-en.x, -en.y, -en.z);
+      }
+      pe[6 * k] = e.x;
+      pe[6 * k + 1] = e.y;
+      pe[6 * k + 2] = e.z;
+      pe[6 * k + 3] = en.x;
+      pe[6 * k + 4] = en.y;
+      pe[6 * k + 5] = en.z;
+    }
+    const d3 c = cross3(sub3(V[1], V[0]), sub3(V[2], V[0]));
+    pe[18] = c.x;
+    pe[19] = c.y;
+    pe[20] = c.z;
+    pe[21] = 0.0;
+  }
   const double e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
   const double e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
   double emax = 0.0;
@@ -337,6 +367,7 @@ struct xdgcu_ctx {
   // reads it through the host's page tables (pageable_direct)
   int32_t host_direct = 2;
   int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
+  int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from TreeDev::prime
   bool pageable_direct = false;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
@@ -431,6 +462,7 @@ void fill_dev(TreeHost& t, const BuiltTree& b, double min_bump) {
   d.n64 = b.n64;
   d.prim32 = t.prim32.p;
   d.prim64 = t.prim64.p;
+  d.prime = t.prime.p;
   d.prim_ref = t.prim_ref.p;
   d.root = b.root;
   d.n_prims = (int32_t)t.prim_ref.n;
@@ -471,10 +503,11 @@ int build_surface_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tri
   API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, st, &b), "bvh build");
   API_CUDA(t.prim32.alloc(3 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim64.alloc(kPrim64Stride * (int64_t)std::max(1, n)), "alloc prims");
+  API_CUDA(t.prime.alloc(kPrimEStride * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
   if (n > 0) {
     k_tri_gather<<<grid(n), 256, 0, st>>>(c->d_tri_xyz.p, d_tris.p, b.order, n, t.prim32.p,
-                                          t.prim64.p, t.prim_ref.p);
+                                          t.prim64.p, t.prime.p, t.prim_ref.p);
     API_CUDA(cudaGetLastError(), "gather");
   }
   API_CUDA(cudaStreamSynchronize(st), "build sync");
@@ -1192,6 +1225,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "walk_sort_min") {
     if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "walk_sort_min must be >= 0");
     c->walk_sort_min = value;
+  } else if (k == "trace_edge_table") {
+    if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "trace_edge_table must be 0 or 1");
+    c->trace_edge_table = (int32_t)value;
   } else if (k == "walk_edge_table") {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "walk_edge_table must be 0 or 1");
     c->walk_edge_table = (int32_t)value;
@@ -1223,6 +1259,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "walk_sort_min") *value = c->walk_sort_min;
   else if (k == "host_direct") *value = c->host_direct;
   else if (k == "walk_edge_table") *value = c->walk_edge_table;
+  else if (k == "trace_edge_table") *value = c->trace_edge_table;
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
@@ -1296,6 +1333,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.surf_id = c->d_surf_id.p;
   a.surf_rev_tree = c->d_surf_rev.p;
   a.occupancy = c->trace_occupancy;
+  a.prim_edges = c->trace_edge_table;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
   a.stack = trace_stack_for(c);
@@ -1781,6 +1819,7 @@ int xdgcu_point_in_volumes(xdgcu_ctx* c, int64_t n, const double* points,
   a.surf_id = c->d_surf_id.p;
   a.surf_rev_tree = c->d_surf_rev.p;
   a.occupancy = c->trace_occupancy;
+  a.prim_edges = c->trace_edge_table;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
   a.stack = trace_stack_for(c);
@@ -1896,6 +1935,7 @@ int xdgcu_transport_surfaces(xdgcu_ctx* c, int64_t n, int32_t* tree, double* pos
   a.surf_bc = c->d_surf_bc.p;
   a.tri_xyz = c->d_tri_xyz.p;
   a.occupancy = c->trace_occupancy;
+  a.prim_edges = c->trace_edge_table;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
   a.stack = trace_stack_for(c);

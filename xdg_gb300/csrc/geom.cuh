@@ -197,6 +197,21 @@ __device__ __forceinline__ double plucker_edge_pre(const double* E, bool flip, d
   return pip;
 }
 
+// plucker.h:45-62 for a triangle edge stored in test orientation: e and
+// e x lo of the edge's first() order, both negated when the test runs the
+// edge from hi to lo.  IEEE products and sums of negated operands are the
+// negated results, so this is plucker_edge64's value (a zero may differ in
+// sign before the snap to +0 below, not after).
+__device__ __forceinline__ double plucker_edge_oriented(const double* E, d3 ray, d3 rn) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(E));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(E + 2));
+  const double2 c = __ldg(reinterpret_cast<const double2*>(E + 4));
+  const d3 e = mk3(a.x, a.y, b.x), en = mk3(b.y, c.x, c.y);
+  double pip = dot3(ray, en) + dot3(rn, e);
+  if (absbits(pip) < absbits(ZERO_TOL)) pip = 0.0;
+  return pip;
+}
+
 // Sign of dot(d, face_normal64(v0, v1, v2)) as the reference computes it
 // (-1, 0, +1), without the square root and divisions of the normalisation
 // when the rounding bound allows.  With c = (v1-v0) x (v2-v0) rounded as the
@@ -205,8 +220,7 @@ __device__ __forceinline__ double plucker_edge_pre(const double* E, bool flip, d
 // |th_i| <= gamma_4; the FP64 sum s = fl(sum d_i c_i) is within gamma_3
 // sum |d_i c_i| of the exact sum.  If |s| > 8 eps sum |d_i c_i|, both have the
 // sign of s and neither is zero; otherwise the exact normalised value decides.
-__device__ __forceinline__ int normal_dot_sign(d3 d, d3 v0, d3 v1, d3 v2) {
-  const d3 c = cross3(sub3(v1, v0), sub3(v2, v0));
+__device__ __forceinline__ int normal_dot_sign_c(d3 d, d3 c) {
   const double p0 = d.x * c.x, p1 = d.y * c.y, p2 = d.z * c.z;
   const double s = p0 + p1 + p2;
   const double bound = (fabs(p0) + fabs(p1) + fabs(p2)) * (8.0 * DBL_EPSILON);
@@ -214,6 +228,12 @@ __device__ __forceinline__ int normal_dot_sign(d3 d, d3 v0, d3 v1, d3 v2) {
   if (absbits(s) > absbits(bound) && absbits(s) > 0x0100000000000000ull) return gt0(s) ? 1 : -1;
   const double dp = dot3(d, normalize64(c));
   return gt0(dp) ? 1 : (lt0(dp) ? -1 : 0);
+}
+
+// the same from the vertices: c = (v1 - v0) x (v2 - v0) as the reference
+// computes it (mesh_manager_interface.cpp:216-220)
+__device__ __forceinline__ int normal_dot_sign(d3 d, d3 v0, d3 v1, d3 v2) {
+  return normal_dot_sign_c(d, cross3(sub3(v1, v0), sub3(v2, v0)));
 }
 
 // tetrahedron_contain.cpp:11-43.  The reference solves T*lambda = p - v0 with

@@ -619,12 +619,31 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
       if (mine) {
         const double* op64 = otree->prim64;
         const int32_t* opref = otree->prim_ref;
-        d3 v0, v1, v2;
-        load_tri64(op64 + kPrim64Stride * (int64_t)prim, v0, v1, v2);
+        // the mixed path reads the triangle's ray-independent FP64 terms
+        // (edges, edge normals, face normal) from the tree; the all-FP64
+        // path computes them from the vertices, as the reference does
+        const double* pe =
+            (MIXED && a.prim_edges && otree->prime) ? otree->prime + kPrimEStride * (int64_t)prim
+                                                    : nullptr;
+        const double* pv = op64 + kPrim64Stride * (int64_t)prim;
+        d3 v0 = mk3(0, 0, 0), v1 = v0, v2 = v0;
         const d3 rn = cross3(od, oo);  // plucker.h:75
         double t;
         const double tmax = (MODE == MODE_OCCLUDED) ? INFTY : obt;
-        if (plucker64(v0, v1, v2, oo, od, rn, tmax, 0.0, false, 0, &t)) {
+        bool hit;
+        if (pe) {
+          const double c0 = plucker_edge_oriented(pe, od, rn);
+          const double c1 = plucker_edge_oriented(pe + 6, od, rn);
+          const double c2 = plucker_edge_oriented(pe + 12, od, rn);
+          const int idx = plucker_axis(od);
+          hit = plucker64_coords(c0, c1, c2, __ldg(&pv[idx]), __ldg(&pv[3 + idx]),
+                                 __ldg(&pv[6 + idx]), comp3(oo, idx), comp3(od, idx), tmax, 0.0,
+                                 false, 0, &t);
+        } else {
+          load_tri64(pv, v0, v1, v2);
+          hit = plucker64(v0, v1, v2, oo, od, rn, tmax, 0.0, false, 0, &t);
+        }
+        if (hit) {
           if (MODE == MODE_OCCLUDED) {
             flags = 1;
           } else if (!dlt(obt, t)) {  // triangle_intersect.cpp:78: t > dtfar rejects
@@ -634,7 +653,13 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
               // sign of dot(d, normal), normal flipped in the surface's
               // reverse-sense tree (:80, :84-87)
               const int32_t sidx = __ldg(&a.tri_surf[gtri]);
-              int sg = normal_dot_sign(od, v0, v1, v2);
+              int sg;
+              if (pe) {
+                const double2 cxy = __ldg(reinterpret_cast<const double2*>(pe + 18));
+                sg = normal_dot_sign_c(od, mk3(cxy.x, cxy.y, __ldg(&pe[20])));
+              } else {
+                sg = normal_dot_sign(od, v0, v1, v2);
+              }
               if (__ldg(&a.surf_rev_tree[sidx]) == otid) sg = -sg;
               bool keep = true;
               if (MODE == MODE_RAY_FIRE || MODE == MODE_PARTICLE) {  // orientation_cull, :12-24
