@@ -409,9 +409,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      default 2)
  *   "node_width"       children per BVH node for trees built (or rebuilt,
  *                      xdgcu_rebuild_trees) afterwards: 4 (default) or 8
- *   "walk_queue"       mixed-precision walk: 1 (default) runs the FP64 face
- *                      tests of a warp's tracks 32 at a time from a per-warp
- *                      queue, 0 lets each lane evaluate its own faces
+ *   "walk_queue"       mixed-precision walk: 1 runs the FP64 face tests of a
+ *                      warp's tracks 32 at a time from a per-warp queue, 0
+ *                      (default) lets each lane evaluate its own faces
  *   "walk_flush_wait"  number of tracks (1..32) waiting only on queued FP64
  *                      face tests before the warp runs a partly filled round
  *   "walk_sort_min"    batches of at least this many tracks (default 16384;
@@ -422,10 +422,10 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *   "trace_edge_table" mixed ray_fire / point_in_volume / occluded /
  *                      find_volume / particle loop: 1 (default) takes each
  *                      triangle's ray-independent FP64 terms (edge vectors,
- *                      edge normals, face normal) from the tree, where they
- *                      were evaluated once at build time with the reference's
- *                      operations; 0 computes them from the vertices.
- *                      Results do not depend on it
+ *                      edge normals, face normal) from a 256-byte record per
+ *                      triangle, evaluated once when the surfaces are
+ *                      uploaded, with the reference's operations; 0 computes
+ *                      them from the vertices.  Results do not depend on it
  *   "walk_edge_table"  mixed walk: 1 (default) takes the FP64 Plucker
  *                      coordinates of a face's edges from the edge table built
  *                      with the mesh (each edge's e and e x lo evaluated once,

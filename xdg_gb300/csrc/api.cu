@@ -53,7 +53,6 @@ struct TreeHost {
   Node64* n64 = nullptr;
   DevMem<float4> prim32;
   DevMem<double> prim64;
-  DevMem<double> prime;  // surface trees: TreeDev::prime
   DevMem<int32_t> prim_ref;
   int32_t n_nodes = 0;
   int32_t depth = 0;
@@ -130,7 +129,7 @@ __global__ void k_tri_boxes(const double* __restrict__ tri_xyz, const int32_t* _
 __global__ void k_tri_gather(const double* __restrict__ tri_xyz, const int32_t* __restrict__ tris,
                              const int32_t* __restrict__ order, int32_t n,
                              float4* __restrict__ prim32, double* __restrict__ prim64,
-                             double* __restrict__ prime, int32_t* __restrict__ prim_ref) {
+                             int32_t* __restrict__ prim_ref) {
   int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const int32_t g = tris[order[j]];
@@ -139,35 +138,6 @@ __global__ void k_tri_gather(const double* __restrict__ tri_xyz, const int32_t* 
   for (int k = 0; k < 9; ++k) o[k] = v[k];
   o[9] = 0.0;
   prim_ref[j] = g;
-  {
-    // the ray-independent parts of the FP64 test (TreeDev::prime), with the
-    // operations of plucker_edge64 and normal_dot_sign
-    const d3 V[3] = {mk3(v[0], v[1], v[2]), mk3(v[3], v[4], v[5]), mk3(v[6], v[7], v[8])};
-    double* pe = prime + kPrimEStride * (int64_t)j;
-    for (int k = 0; k < 3; ++k) {
-      const d3 va = V[k], vb = V[(k + 1) % 3];
-      const bool f = first_lower(va, vb);
-      const d3 lo = f ? va : vb;
-      const d3 hi = f ? vb : va;
-      d3 e = sub3(hi, lo);
-      d3 en = cross3(e, lo);
-      if (!f) {
-        e = mk3(-e.x, -e.y, -e.z);
-        en = mk3(-en.x, -en.y, -en.z);
-      }
-      pe[6 * k] = e.x;
-      pe[6 * k + 1] = e.y;
-      pe[6 * k + 2] = e.z;
-      pe[6 * k + 3] = en.x;
-      pe[6 * k + 4] = en.y;
-      pe[6 * k + 5] = en.z;
-    }
-    const d3 c = cross3(sub3(V[1], V[0]), sub3(V[2], V[0]));
-    pe[18] = c.x;
-    pe[19] = c.y;
-    pe[20] = c.z;
-    pe[21] = 0.0;
-  }
   const double e1[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
   const double e2[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
   double emax = 0.0;
@@ -187,6 +157,47 @@ __global__ void k_tri_gather(const double* __restrict__ tri_xyz, const int32_t* 
                                            __double2float_rn(e1[2]), emaxf);
   prim32[3 * (int64_t)j + 2] = make_float4(__double2float_rn(e2[0]), __double2float_rn(e2[1]),
                                            __double2float_rn(e2[2]), 0.0f);
+}
+
+// Per global triangle (kTriPrimeStride doubles), the ray-independent terms
+// of the FP64 test, with the operations of plucker_edge64 and
+// normal_dot_sign: for the test edges (v0,v1), (v1,v2), (v2,v0) e = hi - lo
+// and e x lo (lo, hi in first() order), both negated when the test runs the
+// edge from hi to lo (offsets 0, 6, 12); the normal (v1-v0) x (v2-v0)
+// (offset 18); the 9 vertex coordinates (offset 22).  A mixed FP64 test
+// reads this one 256-byte record.
+__global__ void k_tri_prime(const double* __restrict__ tri_xyz, int64_t n,
+                            double* __restrict__ out) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const double* v = tri_xyz + 9 * g;
+  const d3 V[3] = {mk3(v[0], v[1], v[2]), mk3(v[3], v[4], v[5]), mk3(v[6], v[7], v[8])};
+  double* pe = out + kTriPrimeStride * g;
+  for (int k = 0; k < 3; ++k) {
+    const d3 va = V[k], vb = V[(k + 1) % 3];
+    const bool f = first_lower(va, vb);
+    const d3 lo = f ? va : vb;
+    const d3 hi = f ? vb : va;
+    d3 e = sub3(hi, lo);
+    d3 en = cross3(e, lo);
+    if (!f) {
+      e = mk3(-e.x, -e.y, -e.z);
+      en = mk3(-en.x, -en.y, -en.z);
+    }
+    pe[6 * k] = e.x;
+    pe[6 * k + 1] = e.y;
+    pe[6 * k + 2] = e.z;
+    pe[6 * k + 3] = en.x;
+    pe[6 * k + 4] = en.y;
+    pe[6 * k + 5] = en.z;
+  }
+  const d3 c = cross3(sub3(V[1], V[0]), sub3(V[2], V[0]));
+  pe[18] = c.x;
+  pe[19] = c.y;
+  pe[20] = c.z;
+  pe[21] = 0.0;
+  for (int k = 0; k < 9; ++k) pe[22 + k] = v[k];
+  pe[31] = 0.0;
 }
 
 __global__ void k_tet_boxes(const double* __restrict__ xyz, const int4* __restrict__ conn,
@@ -324,6 +335,7 @@ struct xdgcu_ctx {
   std::vector<int32_t> h_tri_face, h_tri_surf;
   DevMem<double> d_tri_xyz;
   DevMem<int32_t> d_tri_face, d_tri_surf, d_surf_id, d_surf_rev, d_surf_fwd, d_surf_bc;
+  DevMem<double> d_tri_prime;  // kTriPrimeStride doubles per triangle (k_tri_prime)
   bool tri_dirty = true, surf_dirty = true;
   // tet mesh
   bool has_tets = false;
@@ -360,14 +372,14 @@ struct xdgcu_ctx {
   int32_t transport_event_wait = 4;  // walk_elements tool loop (mixed): the same
   int32_t leaf_max = 2;
   int32_t node_width = 4;        // children per BVH node (4 or 8) of trees built afterwards
-  int32_t walk_queue = 1;
+  int32_t walk_queue = 0;
   int32_t walk_flush_wait = 8;
   // host arrays the kernels address directly instead of staging them:
   // 0 none, 1 page-locked memory, 2 also pageable memory when the device
   // reads it through the host's page tables (pageable_direct)
   int32_t host_direct = 2;
   int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
-  int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from TreeDev::prime
+  int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from d_tri_prime
   bool pageable_direct = false;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
@@ -395,6 +407,10 @@ int sync_surfaces(xdgcu_ctx* c) {
                           cudaMemcpyHostToDevice), "upload face ids");
       API_CUDA(cudaMemcpy(c->d_tri_surf.p, c->h_tri_surf.data(), sizeof(int32_t) * nt,
                           cudaMemcpyHostToDevice), "upload surface index");
+      API_CUDA(c->d_tri_prime.alloc(kTriPrimeStride * nt), "alloc triangle terms");
+      k_tri_prime<<<grid(nt), 256, 0, c->build_stream>>>(c->d_tri_xyz.p, nt, c->d_tri_prime.p);
+      API_CUDA(cudaGetLastError(), "triangle terms");
+      API_CUDA(cudaStreamSynchronize(c->build_stream), "triangle terms");
     }
     c->tri_dirty = false;
   }
@@ -462,7 +478,6 @@ void fill_dev(TreeHost& t, const BuiltTree& b, double min_bump) {
   d.n64 = b.n64;
   d.prim32 = t.prim32.p;
   d.prim64 = t.prim64.p;
-  d.prime = t.prime.p;
   d.prim_ref = t.prim_ref.p;
   d.root = b.root;
   d.n_prims = (int32_t)t.prim_ref.n;
@@ -503,11 +518,10 @@ int build_surface_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tri
   API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, st, &b), "bvh build");
   API_CUDA(t.prim32.alloc(3 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim64.alloc(kPrim64Stride * (int64_t)std::max(1, n)), "alloc prims");
-  API_CUDA(t.prime.alloc(kPrimEStride * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
   if (n > 0) {
     k_tri_gather<<<grid(n), 256, 0, st>>>(c->d_tri_xyz.p, d_tris.p, b.order, n, t.prim32.p,
-                                          t.prim64.p, t.prime.p, t.prim_ref.p);
+                                          t.prim64.p, t.prim_ref.p);
     API_CUDA(cudaGetLastError(), "gather");
   }
   API_CUDA(cudaStreamSynchronize(st), "build sync");
@@ -1334,6 +1348,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   a.surf_rev_tree = c->d_surf_rev.p;
   a.occupancy = c->trace_occupancy;
   a.prim_edges = c->trace_edge_table;
+  a.tri_prime = c->d_tri_prime.p;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
   a.stack = trace_stack_for(c);
@@ -1820,6 +1835,7 @@ int xdgcu_point_in_volumes(xdgcu_ctx* c, int64_t n, const double* points,
   a.surf_rev_tree = c->d_surf_rev.p;
   a.occupancy = c->trace_occupancy;
   a.prim_edges = c->trace_edge_table;
+  a.tri_prime = c->d_tri_prime.p;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
   a.stack = trace_stack_for(c);
@@ -1936,6 +1952,7 @@ int xdgcu_transport_surfaces(xdgcu_ctx* c, int64_t n, int32_t* tree, double* pos
   a.tri_xyz = c->d_tri_xyz.p;
   a.occupancy = c->trace_occupancy;
   a.prim_edges = c->trace_edge_table;
+  a.tri_prime = c->d_tri_prime.p;
   a.node_iters = precision == XDGCU_MIXED ? c->trace_node_iters : c->trace_node_iters_fp64;
   a.flush_wait = c->trace_flush_wait;
   a.stack = trace_stack_for(c);

@@ -64,11 +64,6 @@ struct TreeDev {
   const Node64* n64;
   const float4* prim32;
   const double* prim64;
-  // surface trees: kPrimEStride doubles per triangle for the mixed path's
-  // FP64 tests (may be null): for the test edges (v0,v1), (v1,v2), (v2,v0)
-  // e = hi - lo and e x lo (plucker.h:45-62), both negated when the test
-  // runs the edge from hi to lo, then the normal (v1-v0) x (v2-v0)
-  const double* prime;
   const int32_t* prim_ref;
   int32_t root;      // a child reference (inner node 0, or a leaf, or CHILD_EMPTY)
   int32_t n_prims;
@@ -81,7 +76,9 @@ struct TreeDev {
 };
 
 constexpr int kPrim64Stride = 10;  // doubles per triangle in prim64
-constexpr int kPrimEStride = 22;   // doubles per triangle in prime (21 used)
+// doubles per global triangle in the mixed path's table of ray-independent
+// FP64 terms (k_tri_prime in api.cu)
+constexpr int kTriPrimeStride = 32;
 
 // status codes (mirrors xdgcu.h)
 enum : int32_t {

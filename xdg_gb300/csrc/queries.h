@@ -79,7 +79,8 @@ struct SurfArgs {
   int32_t max_events;
   int32_t graveyard_tree;       // > 0: a particle that would enter this tree ends
   int32_t event_wait;           // lanes whose flights ended before the warp runs their events
-  int32_t prim_edges;           // mixed FP64 tests read TreeDev::prime (when the tree has it)
+  int32_t prim_edges;           // mixed FP64 tests read tri_prime (1) or the vertices (0)
+  const double* tri_prime;      // kTriPrimeStride doubles per global triangle
   const int32_t* surf_fwd_tree;
   const int32_t* surf_bc;
   const double* tri_xyz;        // 9 doubles per global triangle, mesh vertex order

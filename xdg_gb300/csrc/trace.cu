@@ -620,12 +620,15 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
         const double* op64 = otree->prim64;
         const int32_t* opref = otree->prim_ref;
         // the mixed path reads the triangle's ray-independent FP64 terms
-        // (edges, edge normals, face normal) from the tree; the all-FP64
-        // path computes them from the vertices, as the reference does
-        const double* pe =
-            (MIXED && a.prim_edges && otree->prime) ? otree->prime + kPrimEStride * (int64_t)prim
-                                                    : nullptr;
+        // (edges, edge normals, face normal) and its vertices from one
+        // record per triangle; the all-FP64 path computes the terms from the
+        // vertices, as the reference does
+        const double* pe = nullptr;
         const double* pv = op64 + kPrim64Stride * (int64_t)prim;
+        if (MIXED && a.prim_edges && a.tri_prime) {
+          pe = a.tri_prime + kTriPrimeStride * (int64_t)__ldg(&opref[prim]);
+          pv = pe + 22;
+        }
         d3 v0 = mk3(0, 0, 0), v1 = v0, v2 = v0;
         const d3 rn = cross3(od, oo);  // plucker.h:75
         double t;
