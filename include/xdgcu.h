@@ -379,9 +379,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      of the warp-synchronous traversal, mixed precision
  *                      (1..64, default 8; the FP64 path's default is 1)
  *   "trace_node_iters_fp64"  the same for the all-FP64 path
- *   "trace_flush_wait" number of lanes (1..32) whose rays wait only on queued
- *                      FP64 candidate tests before the warp drains a partly
- *                      filled queue
+ *   "trace_flush_wait" number of lanes (1..32, default 4) whose rays wait
+ *                      only on queued FP64 candidate tests before the warp
+ *                      drains a partly filled queue
  *   "trace_stack"      shared-memory traversal stack entries per ray (16..64,
  *                      steps of 8; default 40).  Deeper stacks take shared
  *                      memory and so resident blocks.  A launch raises it to

@@ -363,7 +363,7 @@ struct xdgcu_ctx {
   int32_t trace_occupancy = 4;
   int32_t trace_node_iters = 8;       // mixed precision
   int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
-  int32_t trace_flush_wait = 8;
+  int32_t trace_flush_wait = 4;
   int32_t trace_stack = 40;      // shared-memory stack entries per lane
   int32_t trace_grab = 0;        // 0: one contiguous chunk per warp; > 0: device work queue
   int64_t trace_sort_min = 0;    // batches of at least this many rays run in coherent order (0 = never)
