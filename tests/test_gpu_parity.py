@@ -205,6 +205,65 @@ def test_find_element_and_walk_tet_cube(cuda, oracle, tet_model, prec, settings)
         assert np.array_equal(sl[k, :c], ol[k, :c]), f"track {k} lengths"
 
 
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_walk_degenerate_tracks(cuda, oracle, prec):
+    """Tracks through the vertices and along the edges and faces of an
+    unjittered tet cube (every coordinate a multiple of the cell size):
+    along grid lines, across cell diagonals, starting on vertices and faces.
+    Zero Plucker coordinates, ties between faces and zero-length segments are
+    the rule here; elements, lengths and statuses must equal the oracle's,
+    with the mixed walk's edge coordinates from the edge table and from the
+    vertices."""
+    tm = synth.tet_cube(n=6, size=6.0, jitter=0.0, seed=1)
+    rng = np.random.default_rng(41)
+    starts, dirs = [], []
+    g = np.arange(0, 7, dtype=np.float64)
+    axes = np.eye(3)
+    for _ in range(300):
+        p = rng.choice(g, 3)
+        p = np.clip(p, 0.0, 6.0)
+        kind = rng.integers(0, 4)
+        if kind == 0:
+            u = axes[rng.integers(0, 3)] * rng.choice([-1.0, 1.0])
+        elif kind == 1:
+            u = rng.choice([-1.0, 0.0, 1.0], 3)
+            if not u.any():
+                u = axes[0]
+        elif kind == 2:
+            p = p + rng.choice([0.0, 0.5], 3)
+            u = rng.choice([-1.0, 1.0, 2.0], 3)
+        else:
+            p = p + rng.uniform(0, 1, 3) * (rng.random(3) < 0.5)
+            u = rng.normal(size=3)
+        starts.append(np.clip(p, 0.0, 6.0))
+        dirs.append(u / np.linalg.norm(u))
+    start = np.array(starts)
+    u = np.array(dirs)
+    rti = CudaRayTracer()
+    rti.set_tet_mesh(tm)
+    m = synth.Model(volumes=[1], tets=tm, elements={1: np.arange(len(tm.conn), dtype=np.int32)})
+    et = rti.create_element_tree(m, 1)
+    eid, eidx = rti.find_element(et, start, prec)
+    oid, oidx = oracle.TetTree(tm.tet_xyz(), tm.elem_ids).find_element(start)
+    assert_same(eidx, oidx, "find_element index")
+    ok = eidx >= 0
+    assert ok.sum() > 250
+    length = np.full(len(start), 20.0)
+    w = oracle.TetWalker(tm.vertices, tm.conn, tm.adj, tm.face_table)
+    oe, ol, oc, ost = w.walk(oidx[ok], start[ok], u[ok], length[ok], 512)
+    for edges in (1, 0):
+        rti.set_tuning("walk_edge_table", edges)
+        for queue in (0, 1):
+            rti.set_tuning("walk_queue", queue)
+            se, sl, sc, st = rti.walk_elements(eidx[ok], start[ok], u[ok], length[ok], 512, prec)
+            assert_same(sc, oc, f"segment counts (edges {edges}, queue {queue})")
+            assert_same(st, ost, f"status (edges {edges}, queue {queue})")
+            for k in range(len(sc)):
+                c = sc[k]
+                assert np.array_equal(se[k, :c], tm.elem_ids[oe[k, :c]]), f"track {k} elements"
+                assert np.array_equal(sl[k, :c], ol[k, :c]), f"track {k} lengths"
+
+
 def _exit_distance(p, u, lo, hi):
     with np.errstate(divide="ignore", invalid="ignore"):
         t1 = (lo - p) / u
