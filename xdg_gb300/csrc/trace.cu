@@ -89,16 +89,30 @@ __host__ __device__ constexpr bool stack_keys() {
 }
 
 // Dynamic shared memory: the warp queues, each lane's FP64 ray (origin and
-// direction, [6][kTBlock]), then the stack's references [stack][kTBlock] and,
-// with keys, near distances [stack][kTBlock].  The FP64 ray is read only
+// direction, [6][kTBlock]), the lanes' LaneCold, then the stack's references
+// [stack][kTBlock] and, with keys, near distances [stack][kTBlock].  The FP64 ray is read only
 // when a traversal starts (its FP32 forms), by the FP64 tests of the drain
 // (any lane of the warp reads the owner's) and by the particle events;
 // keeping it out of the registers cut the 4-blocks-per-SM variant's spills
 // from 144 to 52 bytes per thread and raised ray_fire on 655k triangles
 // from 1275 to 1420 Mrays/s.
 constexpr size_t kRayBytes = 6 * sizeof(double) * kTBlock;
+
+// Per-lane state the traversal loop does not touch, in shared memory for the
+// same reason: the best hit so far, the tree, the exclusion list and the ray
+// index.  The drain reads the owner lane's entries directly instead of
+// shuffling them.  ray_fire 1404 -> 1447 Mrays/s (spills at 4 blocks per SM
+// 52 -> 16 bytes per thread).
+struct LaneCold {
+  double bt[kTBlock];
+  int64_t ray[kTBlock];
+  const TreeDev* tree[kTBlock];
+  const int32_t* excl[kTBlock];
+  int32_t tid[kTBlock], nexcl[kTBlock], bface[kTBlock], bsurf[kTBlock];
+};
+
 __host__ __device__ constexpr size_t trace_smem_bytes(int stack, bool keys) {
-  return sizeof(WarpQueue) * kTWarps + kRayBytes +
+  return sizeof(WarpQueue) * kTWarps + kRayBytes + sizeof(LaneCold) +
          (size_t)stack * kTBlock * (sizeof(int32_t) + (keys ? sizeof(uint16_t) : 0));
 }
 
@@ -116,8 +130,9 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
   const int tx = threadIdx.x;
   WarpQueue& Q = reinterpret_cast<WarpQueue*>(smem_raw)[wib];
   double* const sray = reinterpret_cast<double*>(smem_raw + sizeof(WarpQueue) * kTWarps);
-  int32_t* const sref =
-      reinterpret_cast<int32_t*>(smem_raw + sizeof(WarpQueue) * kTWarps + kRayBytes);
+  LaneCold& LC = *reinterpret_cast<LaneCold*>(smem_raw + sizeof(WarpQueue) * kTWarps + kRayBytes);
+  int32_t* const sref = reinterpret_cast<int32_t*>(smem_raw + sizeof(WarpQueue) * kTWarps +
+                                                   kRayBytes + sizeof(LaneCold));
   // the FP64 ray of lane slot t (this thread's: tx)
   auto ray_o = [&](int t) { return mk3(sray[t], sray[kTBlock + t], sray[2 * kTBlock + t]); };
   auto ray_d = [&](int t) {
@@ -152,19 +167,30 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
 
   // ---- lane state ----
   bool has_ray = false, trav = false, use64 = false;
-  int64_t ray = 0;
-  int32_t tid = 0, status = RAY_OK, npend = 0, vk = 0;
+  int32_t status = RAY_OK, npend = 0, vk = 0;
+  // (LaneCold entries of this lane)
+  int64_t& ray = LC.ray[tx];
+  int32_t& tid = LC.tid[tx];
+  const TreeDev*& tree = LC.tree[tx];
+  double& bt = LC.bt[tx];
+  int32_t& bface = LC.bface[tx];
+  int32_t& bsurf = LC.bsurf[tx];
+  const int32_t*& excl = LC.excl[tx];
+  int32_t& nexcl = LC.nexcl[tx];
+  ray = 0;
+  tid = 0;
+  tree = nullptr;
+  bt = INFTY;
+  bface = -1;
+  bsurf = -1;
+  excl = nullptr;
+  nexcl = 0;
   const Node32* n32 = nullptr;
   const float4* prim32 = nullptr;
-  const TreeDev* tree = nullptr;
   int32_t cur = CHILD_EMPTY, leaf_p = 0, leaf_end = 0;
   int sp = 0;
-  double bt = INFTY;
   float bt32 = INFINITY;
-  int32_t bface = -1, bsurf = -1;
   bool bhas = false, bdot = false;
-  const int32_t* excl = nullptr;
-  int32_t nexcl = 0;
   bool wide8 = false;  // the lane's tree has 8-wide nodes
   // MODE_PARTICLE: the particle's stream, path length, events, history count
   // and the triangle of the best hit
@@ -623,16 +649,16 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
       const int owner = (int)(ent >> 27);
       const int32_t prim = (int32_t)(ent & 0x7ffffffu);
       // the owner's ray, tree and current best
-      const d3 oo = ray_o((wib << 5) + owner), od = ray_d((wib << 5) + owner);
-      const double obt = __shfl_sync(kFull, bt, owner);
-      const int32_t obface = __shfl_sync(kFull, bface, owner);
+
       const bool obhas = __shfl_sync(kFull, bhas ? 1 : 0, owner) != 0;
-      const int32_t otid = __shfl_sync(kFull, tid, owner);
-      const TreeDev* otree = reinterpret_cast<const TreeDev*>(
-          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(tree), owner));
-      const int32_t* oexcl = reinterpret_cast<const int32_t*>(
-          __shfl_sync(kFull, reinterpret_cast<unsigned long long>(excl), owner));
-      const int32_t onexcl = __shfl_sync(kFull, nexcl, owner);
+      const int ot = (wib << 5) + owner;
+      const double obt = LC.bt[ot];
+      const int32_t obface = LC.bface[ot];
+      const int32_t otid = LC.tid[ot];
+      const TreeDev* otree = LC.tree[ot];
+      const int32_t* oexcl = LC.excl[ot];
+      const int32_t onexcl = LC.nexcl[ot];
+      const d3 oo = ray_o(ot), od = ray_d(ot);
       int32_t flags = 0;
       double rt = 0.0;
       int32_t rface = -1, rsurf = -1, rtri = -1;
