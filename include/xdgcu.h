@@ -432,16 +432,20 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      the same values), 0 computes them from the vertices;
  *                      read-only "walk_edges" is the table's edge count (0
  *                      when the mesh has none).  Results do not depend on it
- *   "host_direct"      calls with host arrays: 1 lets the kernels read and
- *                      write page-locked host arrays in place (no staging
- *                      copies: each byte crosses the host link once, inside
- *                      the kernel); 2 (default) does the same for pageable
- *                      host memory when the device reads it through the
- *                      host's page tables (read-only key "pageable_direct" =
- *                      1, as on Grace systems); 0 stages every host array through
- *                      device memory in chunks that overlap copies with
- *                      compute.  Tallies updated atomically are always
- *                      staged.  Results do not depend on it. */
+ *   "host_direct"      calls with host arrays: 0 stages every host array
+ *                      through device memory, in chunks that overlap copies
+ *                      with compute; 1 lets the kernels read and write
+ *                      page-locked arrays in place (each byte crosses the
+ *                      host link once, inside the kernel); 2 does the same
+ *                      for pageable memory too when the device reads it
+ *                      through the host's page tables (read-only key
+ *                      "pageable_direct" = 1, as on Grace systems); 3
+ *                      (default) keeps pageable arrays in place where it can
+ *                      and page-locked arrays in place unless the call is
+ *                      large enough (more than 2 chunks of 2^21 rays) for the
+ *                      staged pipeline to overlap its copies.  Tallies
+ *                      updated atomically are always staged.  Results do not
+ *                      depend on it. */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);
 
