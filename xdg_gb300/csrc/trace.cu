@@ -111,8 +111,19 @@ struct LaneCold {
   int32_t tid[kTBlock], nexcl[kTBlock], bface[kTBlock], bsurf[kTBlock];
 };
 
-__host__ __device__ constexpr size_t trace_smem_bytes(int stack, bool keys) {
+// The mixed particle loop's per-particle state, likewise: its random
+// stream, path length, events, history count and the triangle of the best
+// hit (spills at 4 blocks per SM 40 -> 16 bytes per thread; particle_sim
+// loop 468 -> 479 Mevents/s).
+struct ParticleCold {
+  unsigned long long rs[kTBlock];
+  double pdist[kTBlock];
+  int32_t pev[kTBlock], hc[kTBlock], btri[kTBlock];
+};
+
+__host__ __device__ constexpr size_t trace_smem_bytes(int stack, bool keys, bool particle) {
   return sizeof(WarpQueue) * kTWarps + kRayBytes + sizeof(LaneCold) +
+         (particle ? sizeof(ParticleCold) : 0) +
          (size_t)stack * kTBlock * (sizeof(int32_t) + (keys ? sizeof(uint16_t) : 0));
 }
 
@@ -131,8 +142,14 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
   WarpQueue& Q = reinterpret_cast<WarpQueue*>(smem_raw)[wib];
   double* const sray = reinterpret_cast<double*>(smem_raw + sizeof(WarpQueue) * kTWarps);
   LaneCold& LC = *reinterpret_cast<LaneCold*>(smem_raw + sizeof(WarpQueue) * kTWarps + kRayBytes);
+  // (the all-FP64 particle loop keeps this state in registers: it has no
+  // spills to remove, and the shared memory would cost it L1)
+  constexpr bool kPCold = MODE == MODE_PARTICLE && MIXED;
+  constexpr size_t kPC = kPCold ? sizeof(ParticleCold) : 0;
+  ParticleCold& PC = *reinterpret_cast<ParticleCold*>(smem_raw + sizeof(WarpQueue) * kTWarps +
+                                                     kRayBytes + sizeof(LaneCold));
   int32_t* const sref = reinterpret_cast<int32_t*>(smem_raw + sizeof(WarpQueue) * kTWarps +
-                                                   kRayBytes + sizeof(LaneCold));
+                                                   kRayBytes + sizeof(LaneCold) + kPC);
   // the FP64 ray of lane slot t (this thread's: tx)
   auto ray_o = [&](int t) { return mk3(sray[t], sray[kTBlock + t], sray[2 * kTBlock + t]); };
   auto ray_d = [&](int t) {
@@ -194,9 +211,21 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
   bool wide8 = false;  // the lane's tree has 8-wide nodes
   // MODE_PARTICLE: the particle's stream, path length, events, history count
   // and the triangle of the best hit
-  unsigned long long rs = 0ull;
-  double pdist = 0.0;
-  int32_t pev = 0, hc = 0, btri = -1;
+  unsigned long long rs_r = 0ull;
+  double pdist_r = 0.0;
+  int32_t pev_r = 0, hc_r = 0, btri_r = -1;
+  unsigned long long& rs = kPCold ? PC.rs[tx] : rs_r;
+  double& pdist = kPCold ? PC.pdist[tx] : pdist_r;
+  int32_t& pev = kPCold ? PC.pev[tx] : pev_r;
+  int32_t& hc = kPCold ? PC.hc[tx] : hc_r;
+  int32_t& btri = kPCold ? PC.btri[tx] : btri_r;
+  if (kPCold) {
+    rs = 0ull;
+    pdist = 0.0;
+    pev = 0;
+    hc = 0;
+    btri = -1;
+  }
   BoxRay32 br32;
   Ray32 r32;
   BoxRay64 br64;
@@ -782,11 +811,11 @@ cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
   if (a.stack < kTStackMin || a.stack > kTStackMax || a.stack % 8 != 0) return cudaErrorInvalidValue;
   if (a.grab > 0 && (a.work == nullptr || a.grab % 32 != 0)) return cudaErrorInvalidValue;
   constexpr bool keys = stack_keys<MODE, MIXED>();
-  const size_t smem = trace_smem_bytes(a.stack, keys);
+  const size_t smem = trace_smem_bytes(a.stack, keys, MODE == MODE_PARTICLE && MIXED);
   auto kern = k_trace<MODE, MIXED, MINB>;
   if (!g_smem_attr[slot][MINB - 2]) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)trace_smem_bytes(kTStackMax, keys));
+                                         (int)trace_smem_bytes(kTStackMax, keys, MODE == MODE_PARTICLE && MIXED));
     if (e != cudaSuccess) return e;
     g_smem_attr[slot][MINB - 2] = true;
   }
