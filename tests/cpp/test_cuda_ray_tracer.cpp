@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <memory>
+#include <thread>
+#include <vector>
 
 #include "cuda_ray_tracer.h"
 
@@ -291,6 +293,67 @@ void test_batch(int prec) {
   }
 }
 
+// The scalar methods called concurrently from several host threads on one
+// backend object, as the reference's OpenMP loops call them
+// (tools/ray_benchmark.cpp:209-213): every result equals the batched call's
+// (ray_fire, point_in_volume) or the single-threaded scalar call's
+// (find_element).
+void test_threads(int prec) {
+  auto mm = std::make_shared<MockMesh>(true);
+  CudaRayTracer rti(0, prec);
+  const auto trees = rti.register_volume(mm, 0);
+  const TreeID vt = trees.first, et = trees.second;
+  const int nth = 8, per = 300, n = nth * per;
+  std::vector<double> org(3 * n), dir(3 * n), dl(n, INFTY), t(n);
+  std::vector<int32_t> surf(n), face(n), inside(n);
+  unsigned long long s = 12345;
+  auto uni = [&s]() {
+    s = s * 6364136223846793005ull + 1442695040888963407ull;
+    return (double)(s >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (int i = 0; i < n; ++i) {
+    for (int c = 0; c < 3; ++c) org[3 * i + c] = LO[c] + 0.05 + (HI[c] - LO[c] - 0.1) * uni();
+    double d[3], len = 0.0;
+    do {
+      len = 0.0;
+      for (int c = 0; c < 3; ++c) {
+        d[c] = 2.0 * uni() - 1.0;
+        len += d[c] * d[c];
+      }
+    } while (len > 1.0 || len < 1e-6);
+    len = std::sqrt(len);
+    for (int c = 0; c < 3; ++c) dir[3 * i + c] = d[c] / len;
+  }
+  rti.ray_fire_batch(vt, nullptr, n, org.data(), dir.data(), dl.data(), HitOrientation::EXITING,
+                     t.data(), surf.data(), face.data());
+  rti.point_in_volume_batch(vt, nullptr, n, org.data(), nullptr, inside.data());
+  std::vector<double> tt(n);
+  std::vector<MeshID> ss(n), ee(n);
+  std::vector<int> in(n);
+  std::vector<std::thread> pool;
+  for (int k = 0; k < nth; ++k)
+    pool.emplace_back([&, k] {
+      for (int i = k * per; i < (k + 1) * per; ++i) {
+        const Position o{org[3 * i], org[3 * i + 1], org[3 * i + 2]};
+        const Direction d{dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]};
+        const auto h = rti.ray_fire(vt, o, d);
+        tt[i] = h.first;
+        ss[i] = h.second;
+        in[i] = rti.point_in_volume(vt, o) ? 1 : 0;
+        ee[i] = rti.find_element(et, o);
+      }
+    });
+  for (auto& th : pool) th.join();
+  int bad = 0;
+  for (int i = 0; i < n; ++i) {
+    const Position o{org[3 * i], org[3 * i + 1], org[3 * i + 2]};
+    if (tt[i] != t[i] || ss[i] != surf[i] || in[i] != inside[i] || ee[i] != rti.find_element(et, o))
+      ++bad;
+    if (ss[i] == ID_NONE || in[i] != 1 || ee[i] == ID_NONE) ++bad;
+  }
+  CHECK(bad == 0);
+}
+
 }  // namespace
 
 int main() {
@@ -302,6 +365,7 @@ int main() {
     test_closest(prec);
     test_walk(prec);
     test_batch(prec);
+    test_threads(prec);
   }
   std::printf("%d checks, %d failures\n", g_checks, g_failures);
   return g_failures == 0 ? 0 : 1;

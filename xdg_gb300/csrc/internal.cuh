@@ -76,6 +76,21 @@ struct TreeDev {
 };
 
 constexpr int kPrim64Stride = 10;  // doubles per triangle in prim64
+
+// Number of SMs of the device the process uses, read once (thread-safe
+// initialisation) for the persistent launches' grid sizes.
+inline int device_sm_count() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
 // doubles per global triangle in the mixed path's table of ray-independent
 // FP64 terms (k_tri_prime in api.cu)
 constexpr int kTriPrimeStride = 32;

@@ -49,6 +49,8 @@
 // the node (stack_keys below).  A deeper stack costs shared memory and so
 // resident blocks and L1 capacity; overflow ends the ray with
 // RAY_STACK_OVERFLOW.
+#include <atomic>
+
 #include "sample.cuh"
 #include "traverse.cuh"
 
@@ -801,10 +803,11 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
   }
 }
 
-int g_num_sms = 0;
-// resident blocks per SM, by kernel variant, MINB and stack depth (8..64 step 8)
-int g_blocks_per_sm[12][3][kTStackMax / 8 + 1] = {};
-bool g_smem_attr[12][3] = {};
+// resident blocks per SM, by kernel variant, MINB and stack depth (8..64
+// step 8), and whether the variant's shared-memory limit is raised; filled on
+// first use, from any host thread
+std::atomic<int> g_blocks_per_sm[12][3][kTStackMax / 8 + 1];
+std::atomic<bool> g_smem_attr[12][3];
 
 template <int MODE, bool MIXED, int MINB>
 cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
@@ -813,26 +816,23 @@ cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
   constexpr bool keys = stack_keys<MODE, MIXED>();
   const size_t smem = trace_smem_bytes(a.stack, keys, MODE == MODE_PARTICLE && MIXED);
   auto kern = k_trace<MODE, MIXED, MINB>;
-  if (!g_smem_attr[slot][MINB - 2]) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)trace_smem_bytes(kTStackMax, keys, MODE == MODE_PARTICLE && MIXED));
+  if (!g_smem_attr[slot][MINB - 2].load(std::memory_order_acquire)) {
+    cudaError_t e = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)trace_smem_bytes(kTStackMax, keys, MODE == MODE_PARTICLE && MIXED));
     if (e != cudaSuccess) return e;
-    g_smem_attr[slot][MINB - 2] = true;
+    g_smem_attr[slot][MINB - 2].store(true, std::memory_order_release);
   }
-  int* cache = &g_blocks_per_sm[slot][MINB - 2][a.stack / 8];
-  if (*cache == 0) {
-    cudaError_t e;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  std::atomic<int>& cache = g_blocks_per_sm[slot][MINB - 2][a.stack / 8];
+  int per_sm = cache.load(std::memory_order_acquire);
+  if (per_sm == 0) {
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTBlock, smem);
     if (e != cudaSuccess) return e;
-    int b = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kTBlock, smem);
-    if (e != cudaSuccess) return e;
-    *cache = b > 0 ? b : 1;
+    if (per_sm < 1) per_sm = 1;
+    cache.store(per_sm, std::memory_order_release);
   }
   const int64_t warps_needed = (a.n + 31) / 32;
-  int64_t blocks = (int64_t)g_num_sms * (*cache);
+  int64_t blocks = (int64_t)device_sm_count() * per_sm;
   const int64_t max_blocks = (warps_needed + kTWarps - 1) / kTWarps;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks < 1) blocks = 1;

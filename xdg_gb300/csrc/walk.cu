@@ -24,6 +24,8 @@
 // FP64 evaluation error and the 20*DBL_EPSILON snap are added as in geom.cuh).
 #include "walk.h"
 
+#include <atomic>
+
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -791,18 +793,16 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(int64_t* __restrict__
 
 template <int FO, bool MIXED, bool QUEUE>
 cudaError_t launch_walk_t(const WalkArgs& a, cudaStream_t st) {
-  static int num_sms = 0, per_sm = 0;
+  static std::atomic<int> cached{0};  // resident blocks per SM, filled on first use
   auto kern = QUEUE ? k_walk_q<FO> : k_walk<FO, MIXED>;
+  int per_sm = cached.load(std::memory_order_acquire);
   if (per_sm == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaError_t e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
+    cached.store(per_sm, std::memory_order_release);
   }
-  int64_t blocks = (int64_t)num_sms * per_sm;
+  int64_t blocks = (int64_t)device_sm_count() * per_sm;
   const int64_t max_blocks = (a.n + kBlock - 1) / kBlock;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks < 1) blocks = 1;
@@ -990,18 +990,16 @@ __global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t c
 
 template <int FO, bool MIXED>
 cudaError_t launch_transport_t(const TransportArgs& a, cudaStream_t st) {
-  static int num_sms = 0, per_sm = 0;
+  static std::atomic<int> cached{0};  // resident blocks per SM, filled on first use
   auto kern = k_transport<FO, MIXED>;
+  int per_sm = cached.load(std::memory_order_acquire);
   if (per_sm == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaError_t e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
+    cached.store(per_sm, std::memory_order_release);
   }
-  int64_t blocks = (int64_t)num_sms * per_sm;
+  int64_t blocks = (int64_t)device_sm_count() * per_sm;
   const int64_t max_blocks = (a.n + kBlock - 1) / kBlock;
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks < 1) blocks = 1;
