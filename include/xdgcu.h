@@ -439,10 +439,10 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      host link once, inside the kernel); 2 does the same
  *                      for pageable memory too when the device reads it
  *                      through the host's page tables (read-only key
- *                      "pageable_direct" = 1, as on Grace systems); 3
- *                      (default) keeps pageable arrays in place where it can
- *                      and page-locked arrays in place unless the call is
- *                      large enough (more than 2 chunks of 2^21 rays) for the
+ *                      "pageable_direct" = 1, as on Grace systems; the
+ *                      default); 3 keeps pageable arrays in place and
+ *                      page-locked arrays in place unless the call is large
+ *                      enough (more than 2 chunks of 2^21 rays) for the
  *                      staged pipeline to overlap its copies.  Tallies
  *                      updated atomically are always staged.  Results do not
  *                      depend on it. */

@@ -5,8 +5,8 @@ and as device arrays.
 ray_fire runs on 4.5e6 rays (more than two staging chunks) with the inputs
 and outputs in page-locked memory, pageable memory, or page-locked inputs
 with pageable outputs (some arrays in place, the rest staged), under each
-host_direct setting (3, the default, stages the page-locked arrays of this
-large call in overlapping chunks and keeps pageable ones in place).  The
+host_direct setting (2, the default, keeps both kinds in place; 3 stages
+the page-locked arrays of this large call in overlapping chunks).  The
 packed tet walk and the walk_elements particle loop
 (whose atomic tally is always staged) are checked the same way.
 """

@@ -377,7 +377,7 @@ struct xdgcu_ctx {
   // host arrays the kernels address directly instead of staging them:
   // 0 none, 1 page-locked memory, 2 also pageable memory when the device
   // reads it through the host's page tables (pageable_direct)
-  int32_t host_direct = 3;
+  int32_t host_direct = 2;
   int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
   int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from d_tri_prime
   bool pageable_direct = false;
@@ -580,12 +580,11 @@ struct Arr {
 // nullptr: the array is staged.  In-place access moves each byte over the
 // host link once, inside the kernel, with no staging copies or chunking.
 // `pipelined`: the call is large enough for the staged chunk pipeline to
-// overlap its copies with compute; under host_direct 3 (automatic)
-// page-locked arrays are staged then (ray_fire over 1e7 host rays: 1238
-// Mrays/s staged against 1192 in place), and read in place otherwise.
-// Pageable arrays staged by the runtime's own copies are much slower than in
-// place (542 against 1188), so they stay in place whenever the device can
-// address them.
+// overlap its copies with compute; under host_direct 3 page-locked arrays
+// are staged then.  Measured on ray_fire over 1e7 host rays, interleaved in
+// one process: page-locked 1319 Mrays/s in place against 1241 staged,
+// pageable 1334 in place against 846 staged (the default, 2, keeps both in
+// place).
 void* direct_ptr(const xdgcu_ctx* c, const void* p, bool pipelined) {
   if (!p || c->host_direct <= 0) return nullptr;
   cudaPointerAttributes at;
@@ -730,12 +729,25 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
       all_direct || n <= 2 * kChunkRays
           ? 1
           : std::min<int64_t>(kMaxChunks, (n + kChunkRays - 1) / kChunkRays);
+  // chunk k covers rays [starts[k], starts[k+1]).  With more than one, a
+  // first chunk of a quarter of the others starts the kernels after a short
+  // copy (ray_fire over 1e7 page-locked host rays: 1202 -> 1246 Mrays/s).
   const int64_t per = (n + chunks - 1) / chunks;
-  if (!s->events((size_t)(2 * chunks + 1))) return set_err(XDGCU_ERR_CUDA, "event creation");
+  std::vector<int64_t> starts;
+  if (chunks == 1) {
+    starts = {0, n};
+  } else {
+    const int64_t f = std::max<int64_t>(1 << 18, per / 4);
+    const int64_t per2 = (n - f + chunks - 1) / chunks;
+    starts.push_back(0);
+    for (int64_t k = 0; k <= chunks; ++k) starts.push_back(std::min<int64_t>(n, f + k * per2));
+  }
+  const int64_t nch = (int64_t)starts.size() - 1;
+  if (!s->events((size_t)(2 * nch + 1))) return set_err(XDGCU_ERR_CUDA, "event creation");
   // order after the caller's stream (if any)
   if (user) {
-    API_CUDA(cudaEventRecord(s->ev[2 * chunks], user), "event");
-    API_CUDA(cudaStreamWaitEvent(s->copy_in, s->ev[2 * chunks], 0), "event wait");
+    API_CUDA(cudaEventRecord(s->ev[2 * nch], user), "event");
+    API_CUDA(cudaStreamWaitEvent(s->copy_in, s->ev[2 * nch], 0), "event wait");
   }
   for (Arr* a : whole)
     if (a->host_in && a->bytes && !a->direct)
@@ -743,10 +755,10 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
                "H2D");
   int rc = begin_query(c, s->stream, counters);
   if (rc) return rc;
-  for (int64_t k = 0; k < chunks; ++k) {
-    const int64_t first = k * per;
-    const int64_t cnt = std::min<int64_t>(per, n - first);
-    if (cnt <= 0) break;
+  for (int64_t k = 0; k < nch; ++k) {
+    const int64_t first = starts[k];
+    const int64_t cnt = starts[k + 1] - first;
+    if (cnt <= 0) continue;
     for (RayArr* r : rays)
       if (r->host_in && r->per_ray && !r->direct)
         API_CUDA(cudaMemcpyAsync(r->dev + r->per_ray * first,
