@@ -68,6 +68,7 @@ SURF_HIST = 16
 SURF_CHECK = 1_000
 SURF_CPU_SAMPLE = 20_000
 REF_STEP_SAMPLE = 1_000_000  # rays per step of --impl reference
+CLOSEST_POINTS = 1_000_000   # closest-facet queries (the first points of the ray origins)
 BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
 BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
 BYTES_TRI64 = 76            # 72 B FP64 triangle + 4 B id (escalations)
@@ -746,6 +747,40 @@ def run_engine(args, rank, world, local):
     piv_inside_frac = float(piv_out[not_ipc].float().mean().item()) if not_ipc.any() else 1.0
     ms_piv64 = timed(torch, piv(FP64), 3, 1, world, stream)
 
+    # occluded (any hit, embree/ray_tracer.cpp:347-370) of the same rays, and
+    # closest (the nearest facet, :328-345) of the first CLOSEST_POINTS points
+    occ_out = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+
+    def occ(prec):
+        def go():
+            rc = L.xdgcu_occluded(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), N_RAYS,
+                                  ctypes.c_void_p(p.data_ptr()), ctypes.c_void_p(d.data_ptr()),
+                                  ctypes.c_void_p(occ_out.data_ptr()), None, None, prec, sptr)
+            _lib.check(rc, rti.ctx, "occluded")
+        return go
+
+    ms_occ = timed(torch, occ(MIXED), max(3, args.steps // 4), 2, world, stream)
+    occ_mixed = occ_out.clone()
+    ms_occ64 = timed(torch, occ(FP64), 3, 1, world, stream)
+    occ_same = bool(torch.equal(occ_out, occ_mixed))
+    n_clo = min(N_RAYS, CLOSEST_POINTS)
+    clo_d = torch.empty(n_clo, dtype=torch.float64, device=dev)
+    clo_f = torch.empty(n_clo, dtype=torch.int32, device=dev)
+
+    def clo(prec):
+        def go():
+            rc = L.xdgcu_closest(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), n_clo,
+                                 ctypes.c_void_p(p.data_ptr()), ctypes.c_void_p(clo_d.data_ptr()),
+                                 ctypes.c_void_p(clo_f.data_ptr()), None, prec, sptr)
+            _lib.check(rc, rti.ctx, "closest")
+        return go
+
+    ms_clo = timed(torch, clo(MIXED), 3, 2, world, stream)
+    clo_mixed = (clo_d.clone(), clo_f.clone())
+    ms_clo64 = timed(torch, clo(FP64), 3, 1, world, stream)
+    clo_same = bool(torch.equal(clo_d, clo_mixed[0]) and torch.equal(clo_f, clo_mixed[1]))
+    del occ_mixed, clo_mixed
+
     # find_volume of the same points: one fused launch vs one launch per volume
     fv = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
     fv_vols = [v for v in sorted(x.volume_to_surface_tree) if v != ipc]
@@ -1011,6 +1046,17 @@ def run_engine(args, rank, world, local):
             "value": total_rays / (ms_piv / 1e3) / 1e6, "unit": "Mpoints/s",
             "fp64_value": total_rays / (ms_piv64 / 1e3) / 1e6,
             "inside_fraction_own_volume": piv_inside_frac,
+        },
+        "occluded": {
+            "value": total_rays / (ms_occ / 1e3) / 1e6, "unit": "Mrays/s",
+            "fp64_value": total_rays / (ms_occ64 / 1e3) / 1e6,
+            "mixed_equals_fp64": occ_same,
+        },
+        "closest": {
+            "points": n_clo, "unit": "Mpoints/s",
+            "value": dist.sum_over_ranks(n_clo, world) / (ms_clo / 1e3) / 1e6,
+            "fp64_value": dist.sum_over_ranks(n_clo, world) / (ms_clo64 / 1e3) / 1e6,
+            "mixed_equals_fp64": clo_same,
         },
         "find_volume": {
             "value": total_rays / (ms_fv / 1e3) / 1e6, "unit": "Mpoints/s",
