@@ -369,3 +369,35 @@ def test_packed_walk_matches_strided(cuda, tet_model, prec):
     # empty batch
     e0, l0, off0, s0 = rti.walk_elements_packed(idx[:0], start[:0], u[:0], length[:0], 0, 512, prec)
     assert len(off0) == 1 and off0[0] == 0
+
+
+@pytest.mark.parametrize("shift", [0.0, 3.0e4])
+def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
+    """closest in mixed precision (an FP32 bound that skips the FP64 test of
+    triangles proven farther than the best so far) gives the FP64 answer bit
+    for bit and the oracle's: lattice points with exact ties between the two
+    triangles of a box face and between faces, points within 1e-9 of a
+    jittered sphere, and the same model moved far from the origin."""
+    c = np.array([shift, -0.5 * shift, 0.25 * shift])
+    m = synth.Model()
+    v, f = synth.icosphere(4, 3.0, center=tuple(c), jitter=1e-3, seed=21)
+    m.surfaces.append(synth.Surface(1, v, f, np.arange(len(f), dtype=np.int32), 1, 2))
+    bv, bf = synth.box_surface(c - 8.0, c + 8.0)
+    m.surfaces.append(synth.Surface(2, bv, bf, np.arange(len(f), len(f) + len(bf), dtype=np.int32), 2, 3))
+    m.volumes = [1, 2, 3]
+    m.implicit_complement = 3
+    x = XDG(m)
+    x.prepare_raytracer()
+    g = np.arange(-10.0, 10.5, 0.5)
+    lat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    rng = np.random.default_rng(4)
+    dirs = synth.isotropic_dirs(rng, 3000)
+    r = np.linalg.norm(v - c, axis=1).mean()
+    near = c + dirs * (r + rng.choice([-1e-9, 0.0, 1e-9], 3000))[:, None]
+    p = np.concatenate([lat + c, near, c + rng.uniform(-12, 12, (3000, 3))])
+    for vol in (1, 2, 3):
+        ocd, ocf = oracle.volume_tree(m, vol).closest(p)
+        res = {prec: x.closest(vol, p, prec) for prec in PRECISIONS}
+        for prec, (cd, cf) in res.items():
+            assert_same(cf, ocf, f"closest face vol {vol} prec {prec}")
+            assert_same(cd, ocd, f"closest distance vol {vol} prec {prec}")

@@ -200,6 +200,32 @@ __global__ void k_tri_prime(const double* __restrict__ tri_xyz, int64_t n,
   pe[31] = 0.0;
 }
 
+// closest's bound planes (PointArgs::tri_cb): computed in FP64 and rounded
+// to FP32; the query's margin covers the rounding.
+__global__ void k_tri_cbound(const double* __restrict__ tri_xyz, int64_t n,
+                             float4* __restrict__ out) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const double* v = tri_xyz + 9 * g;
+  const d3 V[3] = {mk3(v[0], v[1], v[2]), mk3(v[3], v[4], v[5]), mk3(v[6], v[7], v[8])};
+  const d3 nrm = cross3(sub3(V[1], V[0]), sub3(V[2], V[0]));
+  const double ln = sqrt(dot3(nrm, nrm));
+  bool ok = ln > 0.0 && ln < INFINITY;
+  float4 r[4];
+  const d3 nu = ok ? scl3(1.0 / ln, nrm) : mk3(0, 0, 0);
+  r[0] = make_float4((float)nu.x, (float)nu.y, (float)nu.z, (float)dot3(nu, V[0]));
+  for (int k = 0; k < 3; ++k) {
+    const d3 e = sub3(V[(k + 1) % 3], V[k]);
+    const d3 m = cross3(e, nrm);  // in the plane, pointing away from the triangle
+    const double lm = sqrt(dot3(m, m));
+    ok = ok && lm > 0.0 && lm < INFINITY;
+    const d3 mu = lm > 0.0 ? scl3(1.0 / lm, m) : mk3(0, 0, 0);
+    r[k + 1] = make_float4((float)mu.x, (float)mu.y, (float)mu.z, (float)dot3(mu, V[k]));
+  }
+  if (!ok) r[0].w = __int_as_float(0x7fc00000);  // NaN: the bound never prunes
+  for (int k = 0; k < 4; ++k) out[4 * g + k] = r[k];
+}
+
 __global__ void k_tet_boxes(const double* __restrict__ xyz, const int4* __restrict__ conn,
                             const int32_t* __restrict__ tets, int32_t n, double* __restrict__ box) {
   int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -336,6 +362,7 @@ struct xdgcu_ctx {
   DevMem<double> d_tri_xyz;
   DevMem<int32_t> d_tri_face, d_tri_surf, d_surf_id, d_surf_rev, d_surf_fwd, d_surf_bc;
   DevMem<double> d_tri_prime;  // kTriPrimeStride doubles per triangle (k_tri_prime)
+  DevMem<float4> d_tri_cb;     // 4 per triangle: closest's FP32 bound planes (k_tri_cbound)
   bool tri_dirty = true, surf_dirty = true;
   // tet mesh
   bool has_tets = false;
@@ -410,6 +437,9 @@ int sync_surfaces(xdgcu_ctx* c) {
       API_CUDA(c->d_tri_prime.alloc(kTriPrimeStride * nt), "alloc triangle terms");
       k_tri_prime<<<grid(nt), 256, 0, c->build_stream>>>(c->d_tri_xyz.p, nt, c->d_tri_prime.p);
       API_CUDA(cudaGetLastError(), "triangle terms");
+      API_CUDA(c->d_tri_cb.alloc(4 * nt), "alloc triangle bound planes");
+      k_tri_cbound<<<grid(nt), 256, 0, c->build_stream>>>(c->d_tri_xyz.p, nt, c->d_tri_cb.p);
+      API_CUDA(cudaGetLastError(), "triangle bound planes");
       API_CUDA(cudaStreamSynchronize(c->build_stream), "triangle terms");
     }
     c->tri_dirty = false;
@@ -1545,6 +1575,7 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
   a.tree = tree;
   a.n = n;
   a.tri_face = c->d_tri_face.p;
+  a.tri_cb = closest ? c->d_tri_cb.p : nullptr;
   a.elem_ids = c->d_elem_ids.p;
   cudaStream_t st = (cudaStream_t)stream;
   auto launch = [&]() -> cudaError_t {

@@ -38,6 +38,9 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
       const float px = __double2float_rn(p.x), py = __double2float_rn(p.y),
                   pz = __double2float_rn(p.z);
       const float pabs = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
+      // the FP32 triangle bound below, for coordinates far from FP32 overflow
+      const bool cbound = MIXED && a.tri_cb && pabs + T.max_abs < 1e18f;
+      const float cmargin = 48.0f * kU32 * (pabs + T.max_abs);
       int32_t stack[kStackSize];
       int sp = 0;
       int32_t ref = T.root;
@@ -125,11 +128,35 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
           const int32_t first = leaf_first(ref), count = leaf_count(ref);
           for (int32_t q = first; q < first + count; ++q) {
             cnt.prim++;
+            const int32_t gtri = __ldg(&T.prim_ref[q]);
+            if (cbound) {
+              // Certified FP32 lower bound of the distance to the triangle:
+              // sqrt(h^2 + m^2) with h the distance to its plane and m the
+              // largest distance beyond one of its edges in that plane
+              // (exact in the face and edge regions, below it at vertices).
+              // Each of h and m is within 24 u (|p| + max_abs) of its exact
+              // value (rounding of the stored planes, of p and of three
+              // FMAs); the triangle is skipped only when the bound, less
+              // twice that and the rounding of the root, still exceeds the
+              // best distance rounded up: its distance is then larger, so
+              // neither the minimum nor its tie rule can change.
+              const float4* cb = a.tri_cb + 4 * (int64_t)gtri;
+              const float4 pn = __ldg(cb), e0 = __ldg(cb + 1), e1 = __ldg(cb + 2),
+                           e2 = __ldg(cb + 3);
+              const float h = fabsf(__fmaf_rn(pn.x, px, __fmaf_rn(pn.y, py, __fmaf_rn(pn.z, pz, -pn.w))));
+              const float s0 = __fmaf_rn(e0.x, px, __fmaf_rn(e0.y, py, __fmaf_rn(e0.z, pz, -e0.w)));
+              const float s1 = __fmaf_rn(e1.x, px, __fmaf_rn(e1.y, py, __fmaf_rn(e1.z, pz, -e1.w)));
+              const float s2 = __fmaf_rn(e2.x, px, __fmaf_rn(e2.y, py, __fmaf_rn(e2.z, pz, -e2.w)));
+              const float mo = fmaxf(fmaxf(fmaxf(s0, s1), s2), 0.0f);
+              const float lb = __fsqrt_rn(__fmaf_rn(h, h, mo * mo));
+              if (lb * (1.0f - 8.0f * kU32) - cmargin > __double2float_ru(best)) continue;
+              cnt.esc++;
+            }
             d3 v0, v1, v2;
             load_tri64(T.prim64 + kPrim64Stride * (int64_t)q, v0, v1, v2);
             const d3 r = closest64(v0, v1, v2, p);
             const double dd = dist64(r, p);
-            const int32_t fid = __ldg(&a.tri_face[__ldg(&T.prim_ref[q])]);
+            const int32_t fid = __ldg(&a.tri_face[gtri]);
             // triangle_intersect.cpp:126-133 (strict <) plus the tie rule
             if (dd < best || (dd == best && best_face >= 0 && fid < best_face)) {
               best = dd;

@@ -94,6 +94,11 @@ struct PointArgs {
   int64_t n;
   const double* pts;
   const int32_t* tri_face;   // closest: face ids
+  // closest, mixed: per global triangle 4 float4 -- unit normal n and n.v0,
+  // then for the edges (v0,v1), (v1,v2), (v2,v0) the outward in-plane unit
+  // normal m and m.(edge start) -- for a certified FP32 lower bound of the
+  // distance (w = NaN for degenerate triangles: never pruned)
+  const float4* tri_cb;
   const int32_t* elem_ids;   // find_element: element mesh ids
   double* dist_out;
   int32_t* id_out;
