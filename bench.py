@@ -779,6 +779,10 @@ def run_engine(args, rank, world, local):
     clo_mixed = (clo_d.clone(), clo_f.clone())
     ms_clo64 = timed(torch, clo(FP64), 3, 1, world, stream)
     clo_same = bool(torch.equal(clo_d, clo_mixed[0]) and torch.equal(clo_f, clo_mixed[1]))
+    rti.set_tuning("closest_bound", 0)
+    ms_clo_nb = timed(torch, clo(MIXED), 3, 1, world, stream)
+    rti.set_tuning("closest_bound", 1)
+    clo_same = clo_same and bool(torch.equal(clo_d, clo_mixed[0]) and torch.equal(clo_f, clo_mixed[1]))
     del occ_mixed, clo_mixed
 
     # find_volume of the same points: one fused launch vs one launch per volume
@@ -1056,6 +1060,7 @@ def run_engine(args, rank, world, local):
             "points": n_clo, "unit": "Mpoints/s",
             "value": dist.sum_over_ranks(n_clo, world) / (ms_clo / 1e3) / 1e6,
             "fp64_value": dist.sum_over_ranks(n_clo, world) / (ms_clo64 / 1e3) / 1e6,
+            "value_without_triangle_bound": dist.sum_over_ranks(n_clo, world) / (ms_clo_nb / 1e3) / 1e6,
             "mixed_equals_fp64": clo_same,
         },
         "find_volume": {

@@ -426,6 +426,12 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      triangle, evaluated once when the surfaces are
  *                      uploaded, with the reference's operations; 0 computes
  *                      them from the vertices.  Results do not depend on it
+ *   "closest_bound"    mixed closest: 1 (default) skips the FP64 point-triangle
+ *                      test of triangles that a certified FP32 lower bound of
+ *                      the distance (four planes per triangle, evaluated once
+ *                      when the surfaces are uploaded) proves farther than the
+ *                      nearest so far; 0 tests every triangle the box pruning
+ *                      reaches.  Results do not depend on it
  *   "walk_edge_table"  mixed walk: 1 (default) takes the FP64 Plucker
  *                      coordinates of a face's edges from the edge table built
  *                      with the mesh (each edge's e and e x lo evaluated once,

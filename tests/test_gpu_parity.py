@@ -398,6 +398,11 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
     for vol in (1, 2, 3):
         ocd, ocf = oracle.volume_tree(m, vol).closest(p)
         res = {prec: x.closest(vol, p, prec) for prec in PRECISIONS}
+        x.rti.set_tuning("closest_bound", 0)
+        try:
+            res["mixed, no bound"] = x.closest(vol, p, MIXED)
+        finally:
+            x.rti.set_tuning("closest_bound", 1)
         for prec, (cd, cf) in res.items():
             assert_same(cf, ocf, f"closest face vol {vol} prec {prec}")
             assert_same(cd, ocd, f"closest distance vol {vol} prec {prec}")

@@ -407,6 +407,7 @@ struct xdgcu_ctx {
   int32_t host_direct = 2;
   int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
   int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from d_tri_prime
+  int32_t closest_bound = 1;     // mixed closest: FP32 triangle bound from d_tri_cb
   bool pageable_direct = false;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
@@ -1295,6 +1296,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "trace_edge_table") {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "trace_edge_table must be 0 or 1");
     c->trace_edge_table = (int32_t)value;
+  } else if (k == "closest_bound") {
+    if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "closest_bound must be 0 or 1");
+    c->closest_bound = (int32_t)value;
   } else if (k == "walk_edge_table") {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "walk_edge_table must be 0 or 1");
     c->walk_edge_table = (int32_t)value;
@@ -1327,6 +1331,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "host_direct") *value = c->host_direct;
   else if (k == "walk_edge_table") *value = c->walk_edge_table;
   else if (k == "trace_edge_table") *value = c->trace_edge_table;
+  else if (k == "closest_bound") *value = c->closest_bound;
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
@@ -1575,7 +1580,7 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
   a.tree = tree;
   a.n = n;
   a.tri_face = c->d_tri_face.p;
-  a.tri_cb = closest ? c->d_tri_cb.p : nullptr;
+  a.tri_cb = closest && c->closest_bound ? c->d_tri_cb.p : nullptr;
   a.elem_ids = c->d_elem_ids.p;
   cudaStream_t st = (cudaStream_t)stream;
   auto launch = [&]() -> cudaError_t {
