@@ -1,0 +1,192 @@
+"""The FP32 lower bound that lets mixed-precision closest skip a triangle's
+FP64 test (`k_closest` in queries.cu) never exceeds the FP64 point-triangle
+distance (closest.cpp:54-183 through the oracle), so a triangle it skips is
+one the FP64 test would not have taken: its distance is larger than the
+best so far.
+
+The planes come from the product's own `tri_cbound` (xdg_gb300/csrc/cbound.h,
+the function `k_tri_cbound` runs on the device), compiled here for the host
+with FP64 operations unfused as in the device build (-fmad=false).  The
+kernel's FP32 evaluation is restated in numpy: IEEE FP32 products, sums and
+square roots, and each `__fmaf_rn` as an exact FP64 product plus one FP64
+sum rounded to FP32 (double rounding can differ from a fused operation by
+one FP32 ulp, far inside the bound's margin).  Cases: random triangles of
+sizes 1e-4..1e2 placed up to 1e6 from the origin, needles down to 1e-12 of
+their length off a line (whose FP64 normals can be far off), and points on
+the plane, near vertices and edges (down to 1e-12 of the triangle's size)
+and far away.  The certificates the planes carry (face slab within
+7 u max|V|, every vertex inside the edge planes) are checked in exact
+rational arithmetic on a sample, the FP32 evaluation against 8 u (|p| + M),
+and the bound's use for points well away from the triangle.
+"""
+import ctypes
+import os
+import subprocess
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+U = np.float32(2.0 ** -24)
+
+
+def _fma32(a, b, c):
+    return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
+
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "xdg_gb300", "csrc")
+
+WRAP = r"""
+#include <cstdint>
+#include "cbound.h"
+extern "C" void cbound_all(const double* v, int64_t n, float* out) {
+  for (int64_t i = 0; i < n; ++i) xdgcu::tri_cbound(v + 9 * i, out + 16 * i);
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def cbound(tmp_path_factory):
+    d = str(tmp_path_factory.mktemp("cbound"))
+    src, so = os.path.join(d, "w.cpp"), os.path.join(d, "libcb.so")
+    with open(src, "w") as f:
+        f.write(WRAP)
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-ffp-contract=off", "-fPIC",
+                        "-shared", "-I", CSRC, src, "-o", so], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lib = ctypes.CDLL(so)
+    lib.cbound_all.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+
+    def planes(v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        out = np.zeros((len(v), 4, 4), dtype=np.float32)
+        lib.cbound_all(v.ctypes.data, len(v), out.ctypes.data)
+        return out
+
+    return planes
+
+
+def plane_dists32(pl, p):
+    """h and the three edge distances in the kernel's FP32 operations."""
+    px, py, pz = (p[:, k].astype(np.float32) for k in range(3))
+
+    def ev(k):
+        q = pl[:, k]
+        return _fma32(q[:, 0], px, _fma32(q[:, 1], py, _fma32(q[:, 2], pz, -q[:, 3])))
+
+    return np.abs(ev(0)), ev(1), ev(2), ev(3)
+
+
+def skip_value(pl, p, max_abs):
+    """The value the kernel compares with the best distance rounded up:
+    the triangle is skipped when it is larger."""
+    h, s0, s1, s2 = plane_dists32(pl, p)
+    mo = np.maximum(np.maximum(np.maximum(s0, s1), s2), np.float32(0))
+    lb = np.sqrt(_fma32(h, h, mo * mo))
+    pabs = np.abs(p.astype(np.float32)).max(1)
+    cmargin = (np.float32(48) * U) * (pabs + max_abs)
+    return lb * (np.float32(1) - np.float32(8) * U) - cmargin, pabs
+
+
+def _cases(rng, n):
+    scale = 10.0 ** rng.choice([0.0, 3.0, 4.5, 6.0], n)
+    size = 10.0 ** rng.uniform(-4, 2, n)
+    c = rng.uniform(-1, 1, (n, 3)) * scale[:, None]
+    v = c[:, None, :] + rng.normal(size=(n, 3, 3)) * size[:, None, None]
+    # needles: the third vertex on the first edge's line, nudged off it
+    nd = rng.random(n) < 0.15
+    t = rng.uniform(-0.5, 1.5, n)
+    nudge = 10.0 ** rng.uniform(-12, -3, n)
+    v[nd, 2] = (v[nd, 0] + t[nd, None] * (v[nd, 1] - v[nd, 0])
+                + nudge[nd, None] * size[nd, None] * rng.normal(size=(nd.sum(), 3)))
+    # points: near a vertex, near an edge, over the face, or far away
+    kind = rng.integers(0, 4, n)
+    w = rng.dirichlet([1, 1, 1], n)
+    face_pt = (w[:, :, None] * v).sum(1)
+    k = rng.integers(0, 3, n)
+    a, b = v[np.arange(n), k], v[np.arange(n), (k + 1) % 3]
+    edge_pt = a + rng.random(n)[:, None] * (b - a)
+    vert_pt = v[np.arange(n), k]
+    base = np.where((kind == 0)[:, None], vert_pt, np.where((kind == 1)[:, None], edge_pt, face_pt))
+    off = 10.0 ** rng.uniform(-12, 0, n)
+    off = np.where(kind == 3, 10.0 ** rng.uniform(0.5, 3, n), off)
+    p = base + (off * size)[:, None] * rng.normal(size=(n, 3))
+    return v, p
+
+
+def _fr(x):
+    return Fraction(float(x))
+
+
+def test_bound_never_exceeds_fp64_distance(oracle, cbound):
+    rng = np.random.default_rng(2024)
+    v, p = _cases(rng, 12000)
+    pl = cbound(v)
+    max_abs = np.abs(v).max((1, 2)).astype(np.float32)  # the smallest a tree's bound could be
+    sv, pabs = skip_value(pl, p, max_abs)
+    dd = np.empty(len(v))
+    for i in range(len(v)):
+        r = oracle.closest_on_tri(v[i].reshape(9), p[i])
+        w = r - p[i]
+        dd[i] = np.sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2])
+    fin = np.isfinite(sv)
+    assert fin.mean() > 0.9
+    bad = np.nonzero(fin & (sv.astype(np.float64) > dd))[0]
+    assert len(bad) == 0, f"bound above the distance at {bad[:5]}: {sv[bad[:3]]} vs {dd[bad[:3]]}"
+
+    # useful: for far points the bound is within 10 % of the distance for
+    # half of them (beyond a sharp vertex the largest edge distance
+    # underestimates), above half of it for nine in ten
+    size = np.abs(v - v.mean(1, keepdims=True)).max((1, 2))
+    far = fin & (dd > 30 * size) & (dd > 1e3 * U * (pabs.astype(np.float64) + max_abs))
+    assert far.sum() > 1000
+    ratio = sv[far] / dd[far]
+    assert np.median(ratio) >= 0.9 and np.percentile(ratio, 10) >= 0.5
+
+
+def test_plane_certificates_exact(cbound):
+    """What the proof uses, in exact rational arithmetic on a sample: the face
+    slab, the edge planes holding every vertex, near-orthonormal rows, and the
+    FP32 evaluation within 8 u (|p| + M) of the exact plane distances."""
+    rng = np.random.default_rng(77)
+    v, p = _cases(rng, 1500)
+    pl = cbound(v)
+    ok = np.isfinite(pl[:, 0, 3])
+    assert ok.mean() > 0.9
+    u = Fraction(1, 2 ** 24)
+    ev = plane_dists32(pl, p)
+    max_abs = np.abs(v).max((1, 2)).astype(np.float32)
+    pabs = np.abs(p.astype(np.float32)).max(1)
+    for i in np.nonzero(ok)[0]:
+        V = [[_fr(x) for x in v[i, k]] for k in range(3)]
+        vmax = max(abs(x) for row in V for x in row)
+        P = [[_fr(x) for x in pl[i, k]] for k in range(4)]
+        n, d = P[0][:3], P[0][3]
+        dot = lambda a, b: a[0] * b[0] + a[1] * b[1] + a[2] * b[2]  # noqa: E731
+        for Vk in V:
+            assert abs(dot(n, Vk) - d) <= 7 * u * vmax * (1 + Fraction(1, 10 ** 9)), i
+        assert dot(n, n) <= (1 + 4 * u) ** 2
+        for k in (1, 2, 3):
+            m, c = P[k][:3], P[k][3]
+            assert all(dot(m, Vq) <= c for Vq in V), (i, k)
+            assert dot(m, m) <= (1 + 4 * u) ** 2 and abs(dot(n, m)) <= 4 * u, (i, k)
+        pe = [_fr(x) for x in p[i]]
+        lim = 8 * u * (_fr(pabs[i]) + _fr(max_abs[i]))
+        assert abs(_fr(ev[0][i]) - abs(dot(n, pe) - d)) <= lim, i
+        for k in (1, 2, 3):
+            assert abs(_fr(ev[k][i]) - (dot(P[k][:3], pe) - P[k][3])) <= lim, (i, k)
+
+
+def test_degenerate_triangles_never_skip(cbound):
+    v = np.array([[[0, 0, 0], [1, 1, 1], [2, 2, 2]],      # collinear
+                  [[1, 2, 3], [1, 2, 3], [4, 5, 6]],      # repeated vertex
+                  [[5, 5, 5], [5, 5, 5], [5, 5, 5]],      # a point
+                  [[0, 0, 0], [1, 0, 0], [np.nan, 1, 0]],  # NaN
+                  [[0, 0, 0], [1e31, 0, 0], [0, 1, 0]]],   # beyond 1e30
+                 dtype=np.float64)
+    pl = cbound(v)
+    assert np.isnan(pl[:, 0, 3]).all()
+    p = np.array([[100.0, 0, 0], [0, 100.0, 0], [0, 0, 100.0], [3.0, 3, 3], [-5.0, 0, 0]])
+    sv, _ = skip_value(pl, p, np.float32(1e30))
+    assert not (sv > np.float32(0)).any()

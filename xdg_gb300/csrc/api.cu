@@ -27,6 +27,7 @@
 
 #include "../../include/xdgcu.h"
 #include "bvh.h"
+#include "cbound.h"
 #include "queries.h"
 #include "walk.h"
 
@@ -200,30 +201,15 @@ __global__ void k_tri_prime(const double* __restrict__ tri_xyz, int64_t n,
   pe[31] = 0.0;
 }
 
-// closest's bound planes (PointArgs::tri_cb): computed in FP64 and rounded
-// to FP32; the query's margin covers the rounding.
+// closest's bound planes (PointArgs::tri_cb), certified against each
+// triangle's vertices (tri_cbound)
 __global__ void k_tri_cbound(const double* __restrict__ tri_xyz, int64_t n,
                              float4* __restrict__ out) {
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (g >= n) return;
-  const double* v = tri_xyz + 9 * g;
-  const d3 V[3] = {mk3(v[0], v[1], v[2]), mk3(v[3], v[4], v[5]), mk3(v[6], v[7], v[8])};
-  const d3 nrm = cross3(sub3(V[1], V[0]), sub3(V[2], V[0]));
-  const double ln = sqrt(dot3(nrm, nrm));
-  bool ok = ln > 0.0 && ln < INFINITY;
-  float4 r[4];
-  const d3 nu = ok ? scl3(1.0 / ln, nrm) : mk3(0, 0, 0);
-  r[0] = make_float4((float)nu.x, (float)nu.y, (float)nu.z, (float)dot3(nu, V[0]));
-  for (int k = 0; k < 3; ++k) {
-    const d3 e = sub3(V[(k + 1) % 3], V[k]);
-    const d3 m = cross3(e, nrm);  // in the plane, pointing away from the triangle
-    const double lm = sqrt(dot3(m, m));
-    ok = ok && lm > 0.0 && lm < INFINITY;
-    const d3 mu = lm > 0.0 ? scl3(1.0 / lm, m) : mk3(0, 0, 0);
-    r[k + 1] = make_float4((float)mu.x, (float)mu.y, (float)mu.z, (float)dot3(mu, V[k]));
-  }
-  if (!ok) r[0].w = __int_as_float(0x7fc00000);  // NaN: the bound never prunes
-  for (int k = 0; k < 4; ++k) out[4 * g + k] = r[k];
+  float r[16];
+  tri_cbound(tri_xyz + 9 * g, r);
+  for (int k = 0; k < 4; ++k) out[4 * g + k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
 }
 
 __global__ void k_tet_boxes(const double* __restrict__ xyz, const int4* __restrict__ conn,

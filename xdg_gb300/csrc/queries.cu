@@ -130,16 +130,20 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
             cnt.prim++;
             const int32_t gtri = __ldg(&T.prim_ref[q]);
             if (cbound) {
-              // Certified FP32 lower bound of the distance to the triangle:
-              // sqrt(h^2 + m^2) with h the distance to its plane and m the
-              // largest distance beyond one of its edges in that plane
-              // (exact in the face and edge regions, below it at vertices).
-              // Each of h and m is within 24 u (|p| + max_abs) of its exact
-              // value (rounding of the stored planes, of p and of three
-              // FMAs); the triangle is skipped only when the bound, less
-              // twice that and the rounding of the root, still exceeds the
-              // best distance rounded up: its distance is then larger, so
-              // neither the minimum nor its tie rule can change.
+              // Certified FP32 lower bound of the distance to the triangle
+              // (planes from tri_cbound): sqrt(h^2 + m^2) with h the distance
+              // to its face plane and m the largest distance beyond one of
+              // its edge planes.  With p exact, the triangle lies within
+              // 8 u M of the face plane and inside the edge planes, and the
+              // rows are orthonormal to 4 u, so the distance is at least
+              // that root less 8 u M, over 1 + 6 u.  The FP32 evaluation
+              // (p's rounding and three FMAs) is within about 7 u (|p| + M)
+              // of h and of each edge distance (M = max_abs).  The bound,
+              // less 48 u (|p| + M) and the rounding of the root, undershoots
+              // the distance by at least 20 u (|p| + M), far beyond the FP64
+              // rounding of the exact test; the triangle is skipped only when
+              // it still exceeds the best distance rounded up, so neither
+              // the minimum nor its tie rule can change.
               const float4* cb = a.tri_cb + 4 * (int64_t)gtri;
               const float4 pn = __ldg(cb), e0 = __ldg(cb + 1), e1 = __ldg(cb + 2),
                            e2 = __ldg(cb + 3);
