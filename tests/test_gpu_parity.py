@@ -406,3 +406,20 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
         for prec, (cd, cf) in res.items():
             assert_same(cf, ocf, f"closest face vol {vol} prec {prec}")
             assert_same(cd, ocd, f"closest distance vol {vol} prec {prec}")
+
+
+def test_closest_far_points(cuda, oracle, sphere_box):
+    """Points 1e15..1e25 away: beyond about 1e19 a box distance squared
+    overflows FP32, and the mixed path then tests every triangle in FP64
+    instead of pruning; results equal FP64's and the oracle's."""
+    m, x = sphere_box
+    rng = np.random.default_rng(12)
+    n = 600
+    p = synth.isotropic_dirs(rng, n) * (10.0 ** rng.uniform(15, 25, n))[:, None]
+    for vol in (2, 3):
+        ocd, ocf = oracle.volume_tree(m, vol).closest(p)
+        assert (ocf >= 0).all()
+        for prec in PRECISIONS:
+            cd, cf = x.closest(vol, p, prec)
+            assert_same(cf, ocf, f"closest face vol {vol} prec {prec}")
+            assert_same(cd, ocd, f"closest distance vol {vol} prec {prec}")

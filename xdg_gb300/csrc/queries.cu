@@ -38,8 +38,11 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
       const float px = __double2float_rn(p.x), py = __double2float_rn(p.y),
                   pz = __double2float_rn(p.z);
       const float pabs = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
-      // the FP32 triangle bound below, for coordinates far from FP32 overflow
-      const bool cbound = MIXED && a.tri_cb && pabs + T.max_abs < 1e18f;
+      // FP32 box and triangle bounds only for coordinates far from FP32
+      // overflow (a box distance squared stays finite); beyond, the FP32
+      // box test prunes nothing and every triangle gets the exact test
+      const bool f32ok = pabs + T.max_abs < 1e18f;
+      const bool cbound = MIXED && a.tri_cb && f32ok;
       const float cmargin = 48.0f * kU32 * (pabs + T.max_abs);
       int32_t stack[kStackSize];
       int sp = 0;
@@ -83,7 +86,7 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
               }
               const float dist = sqrtf(s);
               const float lb = dist * (1.0f - 8.0f * kU32) - 4.0f * kU32 * pabs;
-              key[k] = (!empty && lb <= bestf) ? dist : INFINITY;
+              key[k] = (!empty && (lb <= bestf || !f32ok)) ? (f32ok ? dist : 0.0f) : INFINITY;
               cr[k] = ca[k];
             }
             sort4(key, cr);
