@@ -8,9 +8,7 @@ The planes come from the product's own `tri_cbound` (xdg_gb300/csrc/cbound.h,
 the function `k_tri_cbound` runs on the device), compiled here for the host
 with FP64 operations unfused as in the device build (-fmad=false).  The
 kernel's FP32 evaluation is restated in numpy: IEEE FP32 products, sums and
-square roots, and each `__fmaf_rn` as an exact FP64 product plus one FP64
-sum rounded to FP32 (double rounding can differ from a fused operation by
-one FP32 ulp, far inside the bound's margin).  Cases: random triangles of
+square roots, and each `__fmaf_rn` as a correctly rounded fused operation.  Cases: random triangles of
 sizes 1e-4..1e2 placed up to 1e6 from the origin, needles down to 1e-12 of
 their length off a line (whose FP64 normals can be far off), and points on
 the plane, near vertices and edges (down to 1e-12 of the triangle's size)
@@ -27,11 +25,7 @@ from fractions import Fraction
 import numpy as np
 import pytest
 
-U = np.float32(2.0 ** -24)
-
-
-def _fma32(a, b, c):
-    return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
+from fp32_emul import U, fma32
 
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -73,7 +67,7 @@ def plane_dists32(pl, p):
 
     def ev(k):
         q = pl[:, k]
-        return _fma32(q[:, 0], px, _fma32(q[:, 1], py, _fma32(q[:, 2], pz, -q[:, 3])))
+        return fma32(q[:, 0], px, fma32(q[:, 1], py, fma32(q[:, 2], pz, -q[:, 3])))
 
     return np.abs(ev(0)), ev(1), ev(2), ev(3)
 
@@ -83,7 +77,7 @@ def skip_value(pl, p, max_abs):
     the triangle is skipped when it is larger."""
     h, s0, s1, s2 = plane_dists32(pl, p)
     mo = np.maximum(np.maximum(np.maximum(s0, s1), s2), np.float32(0))
-    lb = np.sqrt(_fma32(h, h, mo * mo))
+    lb = np.sqrt(fma32(h, h, mo * mo))
     pabs = np.abs(p.astype(np.float32)).max(1)
     cmargin = (np.float32(48) * U) * (pabs + max_abs)
     return lb * (np.float32(1) - np.float32(8) * U) - cmargin, pabs

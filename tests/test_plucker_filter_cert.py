@@ -18,27 +18,9 @@ import ctypes
 
 import numpy as np
 
-F = np.float32
+from fp32_emul import F, f32_dir, f32_trunc
+
 DBL_MAX = np.finfo(np.float64).max
-
-
-def _f32_up(x):
-    f = x.astype(np.float32)
-    lo = f.astype(np.float64) < x
-    f[lo] = np.nextafter(f[lo], F(np.inf))
-    return f
-
-
-def _f32_trunc(x):
-    """Toward zero; magnitudes below FLT_MIN flush to zero; overflow to inf."""
-    with np.errstate(over="ignore"):
-        f = x.astype(np.float32)
-    big = np.abs(f.astype(np.float64)) > np.abs(x)
-    f[big & np.isfinite(f)] = np.nextafter(f[big & np.isfinite(f)], F(0))
-    ovf = np.abs(x) >= 2.0 ** 128
-    f[ovf] = np.copysign(F(np.inf), x[ovf]).astype(np.float32)
-    f[np.abs(x) < 2.0 ** -126] = F(0) * np.sign(x[np.abs(x) < 2.0 ** -126]).astype(np.float32)
-    return f
 
 
 def tri_records(v):
@@ -52,7 +34,7 @@ def tri_records(v):
         emax = np.fmax(emax, np.abs(e2[:, c] - e1[:, c]))
     v0 = v[:, 0].astype(np.float32)
     v0abs = np.abs(v0).max(1)
-    return v0, v0abs, e1.astype(np.float32), e2.astype(np.float32), _f32_up(emax * (1.0 + 9.5367431640625e-07))
+    return v0, v0abs, e1.astype(np.float32), e2.astype(np.float32), f32_dir(emax * (1.0 + 9.5367431640625e-07), up=True)
 
 
 def _triple(d, e, w):
@@ -64,7 +46,7 @@ def _triple(d, e, w):
 
 def certified_miss(v, o, d):
     v0, v0abs, e1, e2, emax = tri_records(v)
-    o32, d32 = _f32_trunc(o), _f32_trunc(d)
+    o32, d32 = f32_trunc(o), f32_trunc(d)
     dmax = np.abs(d32).max(1)
     du = dmax * (F(5.9604645e-08) * F(1.000001))
     oabs = np.abs(o32).max(1)

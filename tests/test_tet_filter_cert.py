@@ -15,15 +15,7 @@ inside, just inside and just outside faces (barycentric margins down to
 """
 import numpy as np
 
-F = np.float32
-U = F(5.9604645e-08)
-
-
-def _f32_up(x):
-    f = x.astype(np.float32)
-    lo = f.astype(np.float64) < x
-    f[lo] = np.nextafter(f[lo], F(np.inf))
-    return f
+from fp32_emul import F, U, f32_dir
 
 
 def tet_records(v):
@@ -67,11 +59,11 @@ def tet_records(v):
         ok = (det > 0) & np.isfinite(det) & (m < 1e20) & (krel < 1e6) & np.isfinite(e64)
         rec = np.zeros((len(v), 4, 4), dtype=np.float32)
         rec[:, 0, :3] = v0.astype(np.float32)
-        rec[:, 0, 3] = np.where(ok, _f32_up(np.where(ok, m * (1.0 + 1e-6), 0.0)), np.inf)
+        rec[:, 0, 3] = np.where(ok, f32_dir(np.where(ok, m * (1.0 + 1e-6), 0.0), up=True), np.inf)
         rec[:, 1, :3] = M[:, 0].astype(np.float32)
         rec[:, 1, 3] = np.abs(rec[:, 0, :3]).max(1)
         rec[:, 2, :3] = M[:, 1].astype(np.float32)
-        rec[:, 2, 3] = np.where(ok, _f32_up(np.where(ok, e64, 0.0)), np.inf)
+        rec[:, 2, 3] = np.where(ok, f32_dir(np.where(ok, e64, 0.0), up=True), np.inf)
         rec[:, 3, :3] = M[:, 2].astype(np.float32)
     return rec, lo - (w * 1e-6)[:, None], hi + (w * 1e-6)[:, None]
 
