@@ -25,7 +25,7 @@ from fractions import Fraction
 import numpy as np
 import pytest
 
-from fp32_emul import U, fma32
+from fp32_emul import U, f32_dir, fma32
 
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -184,3 +184,46 @@ def test_degenerate_triangles_never_skip(cbound):
     p = np.array([[100.0, 0, 0], [0, 100.0, 0], [0, 0, 100.0], [3.0, 3, 3], [-5.0, 0, 0]])
     sv, _ = skip_value(pl, p, np.float32(1e30))
     assert not (sv > np.float32(0)).any()
+
+
+def test_box_bound_never_exceeds_box_distance():
+    """closest's FP32 box pruning (k_closest): the distance from the point
+    rounded to FP32 to the box rounded outward, computed in FP32 (separate
+    products and sums, a correctly rounded root), less 8 u of itself and
+    4 u |p|, never exceeds the exact distance from the point to the FP64 box
+    (checked as squares in rational arithmetic), so a box holding a triangle
+    at the best distance is never pruned."""
+    rng = np.random.default_rng(9)
+    n = 4000
+    scale = 10.0 ** rng.choice([0.0, 3.0, 6.0, 9.0], n)
+    c = rng.uniform(-1, 1, (n, 3)) * scale[:, None]
+    half = np.abs(rng.normal(size=(n, 3))) * (10.0 ** rng.uniform(-4, 2, n))[:, None]
+    lo64, hi64 = c - half, c + half
+    # points inside, on a face, just outside, or far out
+    k = rng.integers(0, 4, n)
+    off = np.where(k[:, None] == 0, 0.0,
+                   (10.0 ** rng.uniform(-14, 3, n))[:, None] * np.abs(rng.normal(size=(n, 3))) * half)
+    side = rng.choice([-1.0, 1.0], (n, 3))
+    p = np.where(side > 0, hi64 + off, lo64 - off)
+    p = np.where((k == 0)[:, None], lo64 + rng.random((n, 3)) * (hi64 - lo64), p)
+    lo = f32_dir(lo64, up=False)
+    hi = f32_dir(hi64, up=True)
+    px = p.astype(np.float32)
+    pabs = np.abs(px).max(1)
+    s = np.zeros(n, dtype=np.float32)
+    for ax in range(3):
+        e = np.maximum(np.maximum(lo[:, ax] - px[:, ax], px[:, ax] - hi[:, ax]), np.float32(0))
+        s = s + e * e
+    dist = np.sqrt(s)
+    lb = dist * (np.float32(1) - np.float32(8) * U) - (np.float32(4) * U) * pabs
+    for i in range(n):
+        if lb[i] <= 0:
+            continue
+        d2 = Fraction(0)
+        for ax in range(3):
+            q, a, b = Fraction(float(p[i, ax])), Fraction(float(lo64[i, ax])), Fraction(float(hi64[i, ax]))
+            e = max(a - q, q - b, Fraction(0))
+            d2 += e * e
+        assert Fraction(float(lb[i])) ** 2 <= d2, i
+    assert (lb > 0).sum() > 500  # (at 1e9 from the origin the 4 u |p| term dominates)
+
