@@ -122,7 +122,8 @@ def test_small_stack_overflow_is_reported(nested):
 def test_bad_settings_rejected(nested):
     _, x, _, _, _ = nested
     for k, v in [("trace_stack", 12), ("trace_stack", 50), ("trace_stack", 72),
-                 ("trace_grab", 33), ("trace_grab", -32), ("trace_sort_min", -1)]:
+                 ("trace_grab", 33), ("trace_grab", -32), ("trace_sort_min", -1),
+                 ("closest_bound", 2), ("trace_edge_table", -1)]:
         with pytest.raises(Exception):
             x.rti.set_tuning(k, v)
     assert set(x.rti.tuning()) == set(TUNING_KEYS)
