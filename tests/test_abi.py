@@ -39,3 +39,17 @@ def test_create_without_gpu_fails_cleanly():
     rc = L.xdgcu_create(ctypes.byref(h), 0)
     assert rc != 0 and not h.value
     assert b"device" in L.xdgcu_last_error(None)
+
+
+def test_every_tuning_key_documented_and_handled():
+    """Each tuning key the Python layer lists is documented in the header and
+    handled by both xdgcu_set_tuning and xdgcu_get_tuning in the library
+    source."""
+    from xdg_gb300.engine import TUNING_KEYS
+    with open(os.path.join(ROOT, "include", "xdgcu.h")) as f:
+        header = f.read()
+    with open(os.path.join(ROOT, "xdg_gb300", "csrc", "api.cu")) as f:
+        src = f.read()
+    for k in TUNING_KEYS:
+        assert re.search(r'^\s*\*\s+"%s"' % re.escape(k), header, re.M), f"{k} not documented"
+        assert src.count('k == "%s"' % k) >= 2, f"{k} not handled by set and get"
