@@ -25,9 +25,11 @@
  * not be mixed within one call.
  *
  * Precision: XDGCU_FP64 evaluates everything in double precision (the plain
- * drop-in); XDGCU_MIXED runs FP32 box tests and an FP32 Plucker pre-filter
- * with a proven error bound, escalating to the FP64 test wherever the FP32
- * answer is not certain.  Both return bit-identical ids and distances.
+ * drop-in); XDGCU_MIXED runs FP32 box tests, an FP32 Plucker pre-filter (the
+ * walk: an FP32 face pre-filter; find_element: an FP32 containment
+ * pre-filter; closest: FP32 lower bounds of box and triangle distances) with
+ * a proven error bound, escalating to the FP64 test wherever the FP32 answer
+ * is not certain.  Both return bit-identical ids and distances.
  *
  * Tie rule: when two accepted candidates are at exactly the same distance,
  * the lowest mesh id wins (face id for ray_fire / point_in_volume / closest,
