@@ -11,7 +11,8 @@ FP32 with the kernel's operation order.  Cases: tets of sizes 1e-4..1e2 up
 to 1e6 from the origin, regular, slivers (the fourth vertex 1e-2..1e-9 of
 the size off the plane of the other three), needles and caps, with points
 inside, just inside and just outside faces (barycentric margins down to
-1e-14), near vertices and edges, and anywhere in the tet's dilated box.
+1e-14), near vertices and edges, anywhere in the tet's dilated box, and up
+to 1000 tet sizes away (what an FP32 box rounded outward admits).
 """
 import numpy as np
 
@@ -144,7 +145,14 @@ def _points(rng, v, lo, hi):
                     np.where((kind == 2)[:, None], vert, edge)))
     p = (bary[:, :, None] * v).sum(1)
     box = lo + rng.random((n, 3)) * (hi - lo)
-    return np.where((kind == 4)[:, None], box, p)
+    p = np.where((kind == 4)[:, None], box, p)
+    # up to 1000 tet sizes away: a tiny tet far from the origin has an FP32
+    # box (rounded outward) far wider than itself, and the filter sees every
+    # point inside that box
+    far = rng.random(n) < 0.15
+    size = np.abs(v - v.mean(1, keepdims=True)).max((1, 2))
+    return np.where(far[:, None], v.mean(1) + (10.0 ** rng.uniform(0, 3, n) * size)[:, None]
+                    * rng.uniform(-1, 1, (n, 3)), p)
 
 
 def test_filter_agrees_with_fp64_test(oracle):
