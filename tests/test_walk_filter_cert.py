@@ -17,14 +17,17 @@ to 1e-14 of the size), and directions at random or grazing a face.
 import ctypes
 
 import numpy as np
+import pytest
+
+from xdg_gb300.synth import MOCK_TET_FACES
 
 F = np.float32
 DBL_MAX = np.finfo(np.float64).max
-MOAB_FACES = [(0, 1, 3), (1, 2, 3), (2, 0, 3), (0, 2, 1)]
+MOAB_FACES = [(0, 1, 3), (1, 2, 3), (2, 0, 3), (0, 2, 1)]  # direct_access.h:181-183
 PAIRS = [(0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)]
 
 
-def face_early_exit(v, r, u):
+def face_early_exit(v, r, u, faces=MOAB_FACES):
     """(n, 4) bool: face f certified to be rejected by the FP64 test."""
     P = v.astype(np.float32)
     Pw = np.abs(P).max(2)
@@ -46,7 +49,7 @@ def face_early_exit(v, r, u):
         pe[(i, j)] = (u32[:, 0] * cx + u32[:, 1] * cy) + u32[:, 2] * cz
     coord = lambda a, b: pe[(a, b)] if a < b else -pe[(b, a)]  # noqa: E731
     out = np.zeros((len(v), 4), dtype=bool)
-    for f, (l0, l1, l2) in enumerate(MOAB_FACES):
+    for f, (l0, l1, l2) in enumerate(faces):
         out[:, f] = (coord(l0, l1) > thr) | (coord(l1, l2) > thr) | (coord(l2, l0) > thr)
     return out
 
@@ -106,17 +109,18 @@ def _cases(rng, n):
     return v, r, u
 
 
-def test_certified_exit_is_fp64_rejection(oracle):
+@pytest.mark.parametrize("faces", [MOAB_FACES, [tuple(f) for f in MOCK_TET_FACES]], ids=["moab", "mock"])
+def test_certified_exit_is_fp64_rejection(oracle, faces):
     rng = np.random.default_rng(23)
     n = 40000
     v, r, u = _cases(rng, n)
-    cert = face_early_exit(v, r, u)
+    cert = face_early_exit(v, r, u, faces)
     L = oracle.lib()
     D = ctypes.POINTER(ctypes.c_double)
     t = np.zeros(1)
     bad = []
     for i, f in zip(*np.nonzero(cert)):
-        fv = np.ascontiguousarray(v[i, list(MOAB_FACES[f])].reshape(9))
+        fv = np.ascontiguousarray(v[i, list(faces[f])].reshape(9))
         ri, ui = np.ascontiguousarray(r[i]), np.ascontiguousarray(u[i])
         if L.xo_plucker_ray_tri(fv.ctypes.data_as(D), ri.ctypes.data_as(D), ui.ctypes.data_as(D),
                                 DBL_MAX, -DBL_MAX, 1, 1, t.ctypes.data_as(D)):
