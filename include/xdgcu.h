@@ -20,9 +20,14 @@
  * `ray_trees` = NULL) or one tree per ray (`ray_trees` != NULL, `tree`
  * ignored).  Input and output pointers may be device memory (the fast path:
  * the work is enqueued on `stream` and the call returns without
- * synchronising) or host memory (the call stages through pinned buffers and
- * returns when the results are in the caller's arrays).  The two kinds may
- * not be mixed within one call.
+ * synchronising) or host memory (the call returns when the results are in
+ * the caller's arrays).  The two kinds may not be mixed within one call.
+ * Host arrays are read and written in place by the kernels where the device
+ * can address them (page-locked memory, and pageable memory on systems whose
+ * GPU walks the host page tables, such as Grace): the default tuning
+ * `host_direct` = 2.  Memory the device cannot address, or any host array
+ * under `host_direct` = 0, is staged through a per-thread device workspace in
+ * overlapping chunks.
  *
  * Precision: XDGCU_FP64 evaluates everything in double precision (the plain
  * drop-in); XDGCU_MIXED runs FP32 box tests, an FP32 Plucker pre-filter (the

@@ -40,11 +40,34 @@ def build(force: bool = False) -> None:
         subprocess.run(["make", "-s", "-C", HERE], check=True)
 
 
-def build_ref(ref_root: str = "/root/reference") -> bool:
-    if not os.path.isdir(ref_root):
+REF_ENV = "XDG_REFERENCE_DIR"   # the reference source tree, when it is present
+
+
+REF_DIR_NOTE = os.path.join(HERE, "_ref", "reference_dir")
+
+
+def reference_dir():
+    """The reference source tree: $XDG_REFERENCE_DIR, else the tree the last
+    build_ref() compiled from (recorded in oracle/_ref), else None."""
+    d = os.environ.get(REF_ENV)
+    if not d and os.path.exists(REF_DIR_NOTE):
+        with open(REF_DIR_NOTE) as f:
+            d = f.read().strip()
+    return d if d and os.path.isdir(d) else None
+
+
+def build_ref(ref_root: str | None = None) -> bool:
+    """Compile the reference harness from the tree `ref_root` (default
+    $XDG_REFERENCE_DIR); False when no tree is given or it is absent."""
+    ref_root = ref_root or reference_dir()
+    if not ref_root or not os.path.isdir(ref_root):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
-    return os.path.exists(REF_PATH)
+    if not os.path.exists(REF_PATH):
+        return False
+    with open(REF_DIR_NOTE, "w") as f:
+        f.write(os.path.abspath(ref_root))
+    return True
 
 
 def _p(a, t):

@@ -5,7 +5,7 @@ compiles from the reference's sources (include/xdg/geometry/plucker.h,
 src/geometry/closest.cpp, src/mesh_manager_interface.cpp, ...).  They pin the
 C oracle (and through it the CUDA engine) where the reference tree is absent.
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    XDG_REFERENCE_DIR=<reference tree> python tests/golden/make_golden.py
 """
 import os
 import sys
@@ -56,7 +56,8 @@ def plucker_cases(rng):
 
 def main():
     if not xo.build_ref():
-        raise SystemExit("reference sources not found; cannot generate golden vectors")
+        raise SystemExit("reference sources not found (set XDG_REFERENCE_DIR to the reference "
+                         "tree); cannot generate golden vectors")
     xo.build()
     R = xo.ref_lib()
     rng = np.random.default_rng(20241203)

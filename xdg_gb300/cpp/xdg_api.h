@@ -5,7 +5,7 @@
 //   #include "xdg/ray_tracing_interface.h"
 //   #include "xdg/mesh_manager_interface.h"
 //   #include "xdg/element_face_accessor.h"
-// and add CUDA to RTLibrary.
+// and add CUDA to RTLibrary in constants.h.
 #pragma once
 
 #include <array>

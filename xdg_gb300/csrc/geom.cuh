@@ -75,7 +75,7 @@ __host__ __device__ __forceinline__ d3 face_normal64(d3 v0, d3 v1, d3 v2) {
 // rate.  For non-NaN doubles the map okey() below is strictly monotone and
 // sends -0.0 and +0.0 to the same key, so every comparison of the reference's
 // code can be evaluated on integer keys with identical outcome.  The engine
-// rejects non-finite and huge (|x| >= 2^400) inputs at the C ABI, so no NaN
+// rejects non-finite and huge (|x| >= 2^300) inputs at the C ABI, so no NaN
 // can arise inside these routines.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
