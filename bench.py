@@ -73,6 +73,24 @@ BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
 BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
 BYTES_TRI64 = 76            # 72 B FP64 triangle + 4 B id (escalations)
 BYTES_IO = 68               # 48 B origin/dir + 4 B tree id in, 8 B t + 4 B surface + 4 B face out
+WALK_CHECK = 50_000          # C5 tracks walked by the oracle and compared bit for bit
+WALK_CPU_SAMPLE = 1_000_000  # C5 tracks of the walk's CPU baseline (all of them)
+FV_CHECK = 100_000           # headline points whose find_volume the oracle repeats
+NOALLOC_MAX_TRACKS = 4_194_304
+# Algorithmic work of one walk segment (one step of next_element +
+# walk_elements, mesh_manager_interface.cpp:106-200), in FP64 operations with
+# a division counted as one:
+#   per step: cross(u, r) 9 (plucker.h:75), r += len * u and distance -= len 7;
+#   per face tested exactly from the edge table: 3 coordinates x 11
+#   (dot(u, e x lo) + dot(u x r, e)) + 14 for the hit distance (sum, 1/sum,
+#   3 weights, the hit point component, its difference and quotient, u + v);
+#   the all-FP64 path computes each coordinate from the vertices (23: edge,
+#   cross, two dots, sum), 4 faces per step, one of which reaches the distance.
+WALK_FP64_OPS_STEP = 16
+WALK_FP64_OPS_FACE = 47
+WALK_FP64_OPS_FP64_PATH = 16 + 4 * 69 + 14
+# bytes per segment (conn 16 + adjacency 16 + 4 FP32 vertices 48 + output 12)
+WALK_BYTES_SEG_MIXED = 92
 
 
 def set_sizes(rays, tracks):
@@ -166,6 +184,28 @@ def measured_peaks():
             j = json.load(f)
         return float(j["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def measure_peaks(device):
+    """FP64/FP32 issue rates and L2 read bandwidth of this GPU, from the
+    microbenchmarks in xdg_gb300/csrc/peaks.cu (median of 5 launches)."""
+    from xdg_gb300 import build as b
+    lib = ctypes.CDLL(b.PEAKS_LIB)
+    lib.xdgpk_measure.restype = ctypes.c_int
+    lib.xdgpk_measure.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    out = {}
+    for kind, key, scale in ((0, "fp64_add_gops", 1e9), (1, "fp64_mul_gops", 1e9),
+                             (2, "fp64_fma_gops", 1e9), (3, "fp32_fma_gops", 1e9),
+                             (4, "l2_read_gbs", 1e9)):
+        v, ms = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        rc = lib.xdgpk_measure(device, kind, 5, ctypes.byref(v), ctypes.byref(ms))
+        if rc != 0:
+            raise RuntimeError(f"peaks microbenchmark {key}: CUDA error {rc}")
+        out[key] = v.value / scale
+    out["how"] = ("peaks.cu: 8 independent chains per thread, SMs x 2048 threads, median of 5 "
+                  "launches (CUDA events); L2: 32 MiB read 2048 times")
+    return out
 
 
 def profile_traffic():
@@ -414,11 +454,21 @@ def bench_small_configs(torch, L, dev, stream, sptr, args, rank, world):
         }
         if rank == 0 and not args.no_oracle:
             from oracle import oracle as xo
+            cores = os.cpu_count() or 1
             k = min(n, 200_000)
-            ot, os_, of = xo.volume_tree(m, 1).ray_fire(o_h[:k], d_h[:k],
-                                                         threads=os.cpu_count() or 1)
+            otree = xo.volume_tree(m, 1)
+            # the trace loop alone on the host cores (tools/ray_benchmark.cpp:209-230:
+            # the tree is built before the clock starts)
+            tc = time.perf_counter()
+            ot, os_, of = otree.ray_fire(o_h[:k], d_h[:k], threads=cores)
+            dtc = time.perf_counter() - tc
             res["oracle_check"] = {"rays": k, "mismatches": int(
-                (t[MIXED][:k].cpu().numpy() != ot).sum() + (fc[MIXED][:k].cpu().numpy() != of).sum())}
+                (t[MIXED][:k].cpu().numpy() != ot).sum() + (fc[MIXED][:k].cpu().numpy() != of).sum()
+                + (sf[MIXED][:k].cpu().numpy() != os_).sum())}
+            res["cpu_baseline"] = {"value": k / dtc / 1e6, "unit": "Mrays/s", "cores": cores,
+                                   "kind": "port",
+                                   "sample": f"first {k} rays, FP64 ray_fire, BVH, OpenMP, "
+                                             "trace loop only"}
         out[name] = res
     return out
 
@@ -656,6 +706,11 @@ def run_engine(args, rank, world, local):
     stream = torch.cuda.current_stream(dev)
     sptr = ctypes.c_void_p(stream.cuda_stream)
     L = _lib.load()
+    pclk = ClockSampler(local)
+    pclk.start()
+    peaks = measure_peaks(local)
+    peaks["clocks"] = pclk.stop()
+    log(f"[bench] peaks {peaks}")
 
     # ---- C2: nested spheres -------------------------------------------
     t0 = time.perf_counter()
@@ -836,6 +891,7 @@ def run_engine(args, rank, world, local):
 
     # oracle agreement on a sample (rank 0)
     oracle_mism = None
+    fv_oracle = None
     cpu_baseline = None
     if rank == 0 and not args.no_oracle:
         from oracle import oracle as xo
@@ -852,6 +908,14 @@ def run_engine(args, rank, world, local):
                 ot, os_, of = otrees[v].ray_fire(p_h[sel], d_h[sel], threads=cores)
                 mism += int((ot != th[sel]).sum() + (os_ != sh[sel]).sum())
         oracle_mism = {"rays": int(len(sample)), "mismatches": mism}
+        # find_volume of FV_CHECK of the headline points: the volume every
+        # ray above was fired in
+        fsel = np.arange(0, N_RAYS, max(1, N_RAYS // FV_CHECK))
+        ovols = oracle_find_volume(otrees, model, p_h[fsel], d_h[fsel], cores)
+        fv_h = fv.cpu().numpy()[fsel]
+        fv_oracle = {"points": int(len(fsel)), "mismatches": int((ovols != fv_h).sum()),
+                     "host_path_mismatches": int((ovols != vols_h[fsel]).sum()),
+                     "volumes_seen": int(len(np.unique(ovols)))}
         # CPU baseline: the oracle (C restatement of the FP64 path) on the host cores
         cs = min(CPU_SAMPLE, N_RAYS)
         tc = time.perf_counter()
@@ -901,6 +965,8 @@ def run_engine(args, rank, world, local):
         return dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world)
 
     e2e_steps = max(3, args.steps // 2)
+    e2e_transfer = ("page-locked host arrays read and written in place by the kernel over the "
+                    "host link (the library's default, host_direct=2)")
     pinned = (tr_h, org_h, dir_h, to_h, so_h, fo_h)
     ms_e2e = e2e_ms(pinned, rti.get_tuning("host_direct"))
     e2e_ok = bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
@@ -946,13 +1012,17 @@ def run_engine(args, rank, world, local):
         del sdev
         log(f"[bench] autotune walk {tuning['walk_seconds']:.1f}s: {tuning['walk']}")
 
-    def walk(prec, e=seg_e, ln=seg_l, c=seg_c):
+    def find_el(prec, idx):
         def go():
             rc = L.xdgcu_find_element(wr.rti.ctx, et, None, N_TRACKS, ctypes.c_void_p(ws.data_ptr()),
                                       ctypes.c_void_p(we_id.data_ptr()),
-                                      ctypes.c_void_p(we_idx.data_ptr()), None, prec, sptr)
+                                      ctypes.c_void_p(idx.data_ptr()), None, prec, sptr)
             _lib.check(rc, wr.rti.ctx, "find_element")
-            rc = L.xdgcu_walk_elements(wr.rti.ctx, N_TRACKS, ctypes.c_void_p(we_idx.data_ptr()),
+        return go
+
+    def walk(prec, idx, e=seg_e, ln=seg_l, c=seg_c):
+        def go():
+            rc = L.xdgcu_walk_elements(wr.rti.ctx, N_TRACKS, ctypes.c_void_p(idx.data_ptr()),
                                        ctypes.c_void_p(ws.data_ptr()), ctypes.c_void_p(wu.data_ptr()),
                                        ctypes.c_void_p(wl.data_ptr()), MAX_SEGS,
                                        ctypes.c_void_p(e.data_ptr()), ctypes.c_void_p(ln.data_ptr()),
@@ -961,16 +1031,33 @@ def run_engine(args, rank, world, local):
             _lib.check(rc, wr.rti.ctx, "walk_elements")
         return go
 
-    ms_walk = timed(torch, walk(MIXED), args.steps, args.warmup, world, stream)
+    # find_element of the track starts, then the walk alone (it reads the
+    # start elements find_element wrote and nothing else of it)
+    ms_find = timed(torch, find_el(MIXED, we_idx), max(3, args.steps // 4), 2, world, stream)
+    we_id_mixed = we_id.clone()
+    we_idx64 = torch.empty_like(we_idx)
+    ms_find64 = timed(torch, find_el(FP64, we_idx64), 3, 1, world, stream)
+    find_mism = int((we_idx64 != we_idx).sum().item()) + int((we_id != we_id_mixed).sum().item())
+    ms_walk = timed(torch, walk(MIXED, we_idx), args.steps, args.warmup, world, stream)
     n_segs = int(seg_c.sum().item())
     walk_status_bad = int((wst != 0).sum().item())
     c_mixed = seg_c.clone()
+    # FP64 operations of the mixed walk: per step the position update and
+    # cross(u, r), plus the exact Plucker test of every face the FP32 filter
+    # leaves open (the exit face: ~1.0004 faces per step)
+    wr.rti.set_counting(True)
+    walk(MIXED, we_idx)()
+    torch.cuda.synchronize()
+    wcnt = wr.rti.counters()
+    wr.rti.set_counting(False)
+    esc_per_step = wcnt["escalate"] / max(1, wcnt["steps"])
+    fp64_ops_per_seg = WALK_FP64_OPS_STEP + WALK_FP64_OPS_FACE * esc_per_step
     # the same mixed walk with its FP64 edge coordinates computed from the
     # vertices instead of the mesh's edge table
     seg_ex, seg_lx, seg_cx = torch.empty_like(seg_e), torch.empty_like(seg_l), torch.empty_like(seg_c)
     wr.rti.set_tuning("walk_edge_table", 0)
-    ms_walk_noedge = timed(torch, walk(MIXED, seg_ex, seg_lx, seg_cx), max(3, args.steps // 4), 1,
-                           world, stream)
+    ms_walk_noedge = timed(torch, walk(MIXED, we_idx, seg_ex, seg_lx, seg_cx),
+                           max(3, args.steps // 4), 1, world, stream)
     wr.rti.set_tuning("walk_edge_table", 1)
     vmask = torch.arange(MAX_SEGS, device=dev)[None, :] < c_mixed[:, None]
     walk_edge_table_same = (bool(torch.equal(seg_cx, c_mixed))
@@ -979,18 +1066,105 @@ def run_engine(args, rank, world, local):
                             and bool(torch.equal(torch.where(vmask, seg_lx, 0.0),
                                                  torch.where(vmask, seg_l, 0.0))))
     del seg_ex, seg_lx, seg_cx, vmask
-    # FP64 path into separate buffers for the sequence comparison
+    # FP64 path (its own find_element) into separate buffers for the sequence comparison
     seg_e64 = torch.empty_like(seg_e)
     seg_l64 = torch.empty_like(seg_l)
     seg_c64 = torch.empty_like(seg_c)
-    ms_walk64 = timed(torch, walk(FP64, seg_e64, seg_l64, seg_c64), max(3, args.steps // 4), 1,
-                      world, stream)
+    ms_walk64 = timed(torch, walk(FP64, we_idx64, seg_e64, seg_l64, seg_c64),
+                      max(3, args.steps // 4), 1, world, stream)
     cols = torch.arange(MAX_SEGS, device=dev)[None, :]
     valid = cols < c_mixed[:, None]
     walk_elem_mism = int((seg_c64 != c_mixed).sum().item()) + int(
         ((seg_e64 != seg_e) & valid).sum().item())
     walk_len_mism = int(((seg_l64 != seg_l) & valid).sum().item())
-    del seg_e64, seg_l64
+    del seg_e64, seg_l64, seg_c64, valid
+    # the packed walk (count, scan, emit) and its allocation-free variant
+    cap = int(n_segs + N_TRACKS)
+    pk_e = torch.empty(cap, dtype=torch.int32, device=dev)
+    pk_l = torch.empty(cap, dtype=torch.float64, device=dev)
+    pk_off = torch.empty(N_TRACKS + 1, dtype=torch.int64, device=dev)
+    pk_st = torch.empty(N_TRACKS, dtype=torch.int32, device=dev)
+
+    def packed(fn):
+        def go():
+            rc = fn(wr.rti.ctx, N_TRACKS, ctypes.c_void_p(we_idx.data_ptr()),
+                    ctypes.c_void_p(ws.data_ptr()), ctypes.c_void_p(wu.data_ptr()),
+                    ctypes.c_void_p(wl.data_ptr()), MAX_SEGS, cap, ctypes.c_void_p(pk_e.data_ptr()),
+                    ctypes.c_void_p(pk_l.data_ptr()), ctypes.c_void_p(pk_off.data_ptr()),
+                    ctypes.c_void_p(pk_st.data_ptr()), MIXED, sptr)
+            _lib.check(rc, wr.rti.ctx, "walk_elements_packed")
+        return go
+
+    ms_packed = timed(torch, packed(L.xdgcu_walk_elements_packed), max(3, args.steps // 4), 2,
+                      world, stream)
+    pk_ref = (pk_e[:n_segs].clone(), pk_l[:n_segs].clone(), pk_off.clone())
+    ms_packed_na = (timed(torch, packed(L.xdgcu_walk_elements_packed_noalloc),
+                          max(3, args.steps // 4), 2, world, stream)
+                    if N_TRACKS <= NOALLOC_MAX_TRACKS else None)
+    packed_same = (ms_packed_na is not None and bool(torch.equal(pk_off, pk_ref[2]))
+                   and bool(torch.equal(pk_e[:n_segs], pk_ref[0]))
+                   and bool(torch.equal(pk_l[:n_segs], pk_ref[1]))
+                   and int(pk_off[-1].item()) == n_segs)
+    del pk_e, pk_l, pk_off, pk_st, pk_ref
+
+    # oracle agreement at full size: find_element and the walk of WALK_CHECK
+    # tracks spread over the batch, element sequences (zero-length segments
+    # included), lengths and status bit for bit; and the oracle's own
+    # find_element + walk on the host cores (tools/tally_segments.h:50-62)
+    walk_oracle = None
+    walk_cpu = None
+    if rank == 0 and not args.no_oracle:
+        from oracle import oracle as xo
+        xo.build()
+        cores = os.cpu_count() or 1
+        t1 = time.perf_counter()
+        otree = xo.TetTree(tm.tet_xyz(), tm.elem_ids)
+        owalk = xo.TetWalker(tm.vertices, tm.conn, tm.adj, tm.face_table)
+        ksel = np.arange(0, N_TRACKS, max(1, N_TRACKS // WALK_CHECK))
+        oid, oidx = otree.find_element(s_h[ksel], threads=cores)
+        eid_h = we_id_mixed.cpu().numpy()[ksel]
+        eidx_h = we_idx.cpu().numpy()[ksel]
+        ok = oidx >= 0
+        oe, ol, oc, ost = owalk.walk(np.where(ok, oidx, 0).astype(np.int32), s_h[ksel], u_h[ksel],
+                                     np.where(ok, len_h[ksel], 0.0), max_segs=MAX_SEGS,
+                                     threads=cores)
+        kdev = torch.from_numpy(ksel).to(dev)
+        ce = seg_e[kdev].cpu().numpy()
+        cl = seg_l[kdev].cpu().numpy()
+        cc = c_mixed[kdev].cpu().numpy()
+        cs_ = wst[kdev].cpu().numpy()
+        oc = np.where(ok, oc, 0)
+        valid = np.arange(MAX_SEGS)[None, :] < oc[:, None]
+        oe_ids = np.where(valid, tm.elem_ids[np.clip(oe, 0, len(tm.elem_ids) - 1)], 0)
+        walk_oracle = {
+            "tracks": int(len(ksel)), "segments": int(oc.sum()),
+            "find_element_mismatches": int((oid != eid_h).sum() + (oidx != eidx_h).sum()),
+            "count_mismatches": int((cc != oc).sum()),
+            "element_mismatches": int(((np.where(valid, ce, 0) != oe_ids)).sum()),
+            "length_mismatches": int(((np.where(valid, cl, 0.0) != np.where(valid, ol, 0.0))).sum()),
+            "status_mismatches": int((cs_[ok] != ost[ok]).sum()),
+            "max_rel_length_error": float(np.max(np.abs(np.where(valid, cl - ol, 0.0))
+                                                 / np.maximum(np.abs(np.where(valid, ol, 1.0)), 1e-300),
+                                                 initial=0.0)),
+        }
+        del oe, ol, ce, cl, valid, oe_ids
+        # CPU baseline: find_element + walk of WALK_CPU_SAMPLE tracks
+        nb = min(WALK_CPU_SAMPLE, N_TRACKS)
+        tc = time.perf_counter()
+        segs_cpu = 0
+        for b0 in range(0, nb, 25_000):
+            sl_ = slice(b0, min(nb, b0 + 25_000))
+            _, bidx = otree.find_element(s_h[sl_], threads=cores)
+            bok = bidx >= 0
+            _, _, bc, _ = owalk.walk(np.where(bok, bidx, 0).astype(np.int32), s_h[sl_], u_h[sl_],
+                                     np.where(bok, len_h[sl_], 0.0), max_segs=MAX_SEGS,
+                                     threads=cores)
+            segs_cpu += int(bc[bok].sum())
+        dtc = time.perf_counter() - tc
+        walk_cpu = {"value": segs_cpu / dtc / 1e6, "unit": "Msegs/s", "cores": cores,
+                    "kind": "port",
+                    "sample": f"first {nb} tracks: find_element + walk_elements, FP64, BVH, OpenMP"}
+        log(f"[bench] walk oracle check + cpu baseline {time.perf_counter() - t1:.1f}s")
 
     # ---- device particle loop (walk_elements tool) over the same mesh ------
     transport = bench_transport(torch, L, wr, dev, stream, sptr, ws, wu, we_idx, tm, args, rank,
@@ -1002,6 +1176,7 @@ def run_engine(args, rank, world, local):
     # ---- report -------------------------------------------------------------
     total_rays = dist.sum_over_ranks(N_RAYS, world)
     total_segs = dist.sum_over_ranks(n_segs, world)
+    total_tracks = dist.sum_over_ranks(N_TRACKS, world)
     value = total_rays / (ms_mixed / 1e3) / 1e6
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_ray * N_RAYS / (ms_mixed / 1e3) / 1e9
@@ -1011,6 +1186,28 @@ def run_engine(args, rank, world, local):
         traffic = prof["dram_bytes_per_ray"] * N_RAYS
     h2d = N_RAYS * (24 + 24 + 4)
     d2h = N_RAYS * (8 + 4 + 4)
+    walk_value = total_segs / (ms_walk / 1e3) / 1e6
+    walk_fp64_value = total_segs / (ms_walk64 / 1e3) / 1e6
+    # the walk's roofline: FP64 operations per segment against the measured
+    # FP64 issue rate, and bytes per segment against HBM
+    fp64_peak = peaks.get("fp64_add_gops")
+    walk_fp64_achieved = fp64_ops_per_seg * n_segs / (ms_walk / 1e3) / 1e9
+    walk_hbm_achieved = WALK_BYTES_SEG_MIXED * n_segs / (ms_walk / 1e3) / 1e9
+    walk_roofline = {
+        "bound": "fp64", "kernel": "k_walk<MOAB, mixed>",
+        "achieved": walk_fp64_achieved, "peak": fp64_peak, "unit": "GFP64op/s",
+        "frac": walk_fp64_achieved / fp64_peak if fp64_peak else None,
+        "fp64_ops_per_segment": fp64_ops_per_seg,
+        "fp64_faces_per_step": esc_per_step,
+        "peak_kind": "measured in this run: FP64 add issue rate (peaks.cu)",
+        "hbm": {"achieved": walk_hbm_achieved, "peak": peak, "unit": "GB/s",
+                "frac": walk_hbm_achieved / peak, "bytes_per_segment": WALK_BYTES_SEG_MIXED},
+        "fp64_path": {
+            "achieved": WALK_FP64_OPS_FP64_PATH * n_segs / (ms_walk64 / 1e3) / 1e9,
+            "frac": (WALK_FP64_OPS_FP64_PATH * n_segs / (ms_walk64 / 1e3) / 1e9 / fp64_peak
+                     if fp64_peak else None),
+            "fp64_ops_per_segment": WALK_FP64_OPS_FP64_PATH},
+    }
     line = {
         "metric": METRIC,
         "value": value,
@@ -1033,19 +1230,37 @@ def run_engine(args, rank, world, local):
             "l2": "streamed inputs 520 MB > 129 MB L2 per step; no flush",
             "parallelism": f"replicas{world} (rays sharded by rank, geometry replicated)",
         },
-        "fp64": {"value": total_rays / (ms_fp64 / 1e3) / 1e6, "unit": "Mrays/s",
-                 "ms_per_step": ms_fp64},
+        "roofline": {
+            "bound": "hbm",
+            "achieved": achieved,
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": traffic,
+            "peak_kind": f"{peak_kind} HBM copy bandwidth",
+            "kernel": f"k_trace<RAY_FIRE, mixed, {rti.get_tuning('trace_occupancy')}>",
+            "algorithmic_bytes_per_ray": bytes_per_ray,
+        },
+        "cpu_baseline": cpu_baseline,
+        "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "matches_device_path": e2e_ok,
+                "transfer": e2e_transfer,
+                "staged_value": total_rays / (ms_e2e_staged / 1e3) / 1e6,
+                "pageable_staged_value": total_rays / (ms_e2e_pageable / 1e3) / 1e6,
+                "pageable_direct_value": (total_rays / (ms_e2e_pageable_direct / 1e3) / 1e6
+                                          if ms_e2e_pageable_direct else None)},
+        # secondary workloads first: the end of the line carries the headline
+        # comparisons and the parity checks
+        "configs_small": small_configs,
+        "overlap_check": overlap,
+        "transport": transport,
+        "surface_transport": surface_transport,
+        "many_surfaces": many,
+        "tuning": tuning,
+        "peaks_measured": peaks,
         "mixed_without_edge_table": {"value": total_rays / (ms_mixed_noedge / 1e3) / 1e6,
                                      "unit": "Mrays/s", "same_results": edge_table_same},
-        "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
-        "id_mismatches_mixed_vs_fp64": id_mism,
-        "t_mismatches_mixed_vs_fp64": t_mism,
-        "max_rel_t_error_mixed_vs_fp64": max_rel_t,
-        "hit_fraction": hit_frac,
-        "oracle_check": oracle_mism,
-        "escalations_per_ray": per_ray["escalate"],
-        "nodes_per_ray": per_ray["node"],
-        "prims_per_ray": per_ray["prim"],
         "point_in_volume": {
             "value": total_rays / (ms_piv / 1e3) / 1e6, "unit": "Mpoints/s",
             "fp64_value": total_rays / (ms_piv64 / 1e3) / 1e6,
@@ -1069,52 +1284,67 @@ def run_engine(args, rank, world, local):
             "ms_fused": ms_fv, "ms_per_volume": ms_fv_loop,
             "fused_equals_per_volume": fv_same, "device_equals_host_path": fv_host_same,
             "volumes_tried_in_order": len(fv_vols),
+            "oracle_check": fv_oracle,
         },
+        "escalations_per_ray": per_ray["escalate"],
+        "nodes_per_ray": per_ray["node"],
+        "prims_per_ray": per_ray["prim"],
+        "hit_fraction": hit_frac,
         "walk": {
             "workload": WALK_WORKLOAD,
-            "value": total_segs / (ms_walk / 1e3) / 1e6, "unit": "Msegs/s",
-            "fp64_value": total_segs / (ms_walk64 / 1e3) / 1e6,
+            "value": walk_value, "unit": "Msegs/s",
+            "fp64_value": walk_fp64_value,
+            "step": "walk_elements alone (k_walk); find_element timed separately",
+            "ms_per_step": ms_walk, "fp64_ms_per_step": ms_walk64,
+            "find_element": {"unit": "Mpoints/s", "ms": ms_find, "fp64_ms": ms_find64,
+                             "value": total_tracks / (ms_find / 1e3) / 1e6,
+                             "fp64_value": total_tracks / (ms_find64 / 1e3) / 1e6,
+                             "mismatches_mixed_vs_fp64": find_mism},
+            "with_find_element_value": total_segs / ((ms_walk + ms_find) / 1e3) / 1e6,
             "value_without_edge_table": total_segs / (ms_walk_noedge / 1e3) / 1e6,
             "edge_table_same_segments": walk_edge_table_same,
-            "ms_per_step": ms_walk, "fp64_ms_per_step": ms_walk64,
+            "packed_value": total_segs / (ms_packed / 1e3) / 1e6,
+            "packed_noalloc_value": (total_segs / (ms_packed_na / 1e3) / 1e6
+                                     if ms_packed_na else None),
+            "packed_noalloc_equals_packed": packed_same,
             "segments": n_segs, "tracks": N_TRACKS,
             "speedup_mixed_vs_fp64": ms_walk64 / ms_walk,
             "element_mismatches_mixed_vs_fp64": walk_elem_mism,
             "length_mismatches_mixed_vs_fp64": walk_len_mism,
             "tracks_with_status": walk_status_bad,
-            "step": "find_element + walk_elements",
+            "roofline": walk_roofline,
+            "cpu_baseline": walk_cpu,
+            "oracle_check": walk_oracle,
         },
-        "roofline": {
-            "bound": "hbm",
-            "achieved": achieved,
-            "peak": peak,
-            "unit": "GB/s",
-            "frac": achieved / peak,
-            "traffic": traffic,
-            "peak_kind": f"{peak_kind} HBM copy bandwidth",
-            "kernel": f"k_trace<RAY_FIRE, mixed, {rti.get_tuning('trace_occupancy')}>",
-            "algorithmic_bytes_per_ray": bytes_per_ray,
+        "fp64": {"value": total_rays / (ms_fp64 / 1e3) / 1e6, "unit": "Mrays/s",
+                 "ms_per_step": ms_fp64},
+        "speedup_mixed_vs_fp64": ms_fp64 / ms_mixed,
+        "id_mismatches_mixed_vs_fp64": id_mism,
+        "t_mismatches_mixed_vs_fp64": t_mism,
+        "max_rel_t_error_mixed_vs_fp64": max_rel_t,
+        "oracle_check": oracle_mism,
+        "summary": {
+            "ray_fire_Mrays_s": {"mixed": round(value, 1),
+                                 "fp64": round(total_rays / (ms_fp64 / 1e3) / 1e6, 1),
+                                 "e2e": round(total_rays / (ms_e2e / 1e3) / 1e6, 1)},
+            "walk_Msegs_s": {"mixed": round(walk_value, 1), "fp64": round(walk_fp64_value, 1),
+                             "fp64_frac": (round(walk_roofline["frac"], 3)
+                                           if walk_roofline["frac"] else None),
+                             "cpu": round(walk_cpu["value"], 1) if walk_cpu else None},
+            "oracle_mismatches": {
+                "ray_fire": oracle_mism["mismatches"] if oracle_mism else None,
+                "find_volume": fv_oracle["mismatches"] if fv_oracle else None,
+                "walk": (walk_oracle["count_mismatches"] + walk_oracle["element_mismatches"]
+                         + walk_oracle["length_mismatches"] + walk_oracle["status_mismatches"]
+                         + walk_oracle["find_element_mismatches"]) if walk_oracle else None},
+            "mixed_vs_fp64_mismatches": {"ray_fire": id_mism + t_mism,
+                                         "walk": walk_elem_mism + walk_len_mism},
         },
-        "cpu_baseline": cpu_baseline,
-        "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "matches_device_path": e2e_ok,
-                "transfer": "page-locked host arrays read and written in place by the kernel "
-                            "over the host link (the library's default, host_direct=2)",
-                "staged_value": total_rays / (ms_e2e_staged / 1e3) / 1e6,
-                "pageable_staged_value": total_rays / (ms_e2e_pageable / 1e3) / 1e6,
-                "pageable_direct_value": (total_rays / (ms_e2e_pageable_direct / 1e3) / 1e6
-                                          if ms_e2e_pageable_direct else None)},
-        "configs_small": small_configs,
-        "overlap_check": overlap,
-        "transport": transport,
-        "surface_transport": surface_transport,
-        "many_surfaces": many,
-        "tuning": tuning,
         "gpu_launches": args.steps * launches_per_step,
         "clocks": clk,
     }
     if rank == 0:
+        log(f"[bench] summary {json.dumps(line['summary'])}")
         print(json.dumps(line), flush=True)
     return 0
 

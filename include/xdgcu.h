@@ -36,6 +36,10 @@
  * a proven error bound, escalating to the FP64 test wherever the FP32 answer
  * is not certain.  Both return bit-identical ids and distances.
  *
+ * Devices: a context belongs to the device it was created on.  Every entry
+ * point makes that device current while it runs and makes the caller's
+ * current device current again before it returns.
+ *
  * Tie rule: when two accepted candidates are at exactly the same distance,
  * the lowest mesh id wins (face id for ray_fire / point_in_volume / closest,
  * element id for find_element).  The reference leaves this to Embree's
@@ -354,8 +358,16 @@ int xdgcu_transport_surfaces(xdgcu_ctx* ctx, int64_t n, int32_t* tree, double* p
  *     library, which every GPU that loads the library holds until exit;
  *   - n must not exceed XDGCU_NOALLOC_MAX_TRACKS (else XDGCU_ERR_INVALID_ARG);
  *   - all array arguments must be device (or managed) memory;
+ *   - all array arguments must be on the context's device;
+ *   - it never applies the longest-first track order the allocating walk
+ *     uses for batches of at least `walk_sort_min` tracks (that order sorts
+ *     the tracks into scratch memory), so `walk_sort_min` has no effect here:
+ *     the results are the same, large batches of uneven tracks run slower;
  *   - the first call on a device looks up the static array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream capture;
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *     The address stays valid for the device's primary context: after a
+ *     cudaDeviceReset the entry point cannot be used on that device again in
+ *     the same process;
  *   - all calls share the static array, so calls whose work overlaps on the
  *     GPU (other streams or host threads) race and must be serialised. */
 int xdgcu_walk_elements_packed_noalloc(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,

@@ -23,6 +23,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libxdgcu.so")
+# throughput microbenchmarks for the roofline denominators (not the engine)
+PEAKS_SRC = "peaks.cu"
+PEAKS_LIB = os.path.join(OUT_DIR, "libxdgpeaks.so")
 SOURCES = ["api.cu", "bvh.cu", "noalloc.cu", "order.cu", "queries.cu", "trace.cu", "tune.cu", "walk.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relaxed-constexpr",
@@ -69,6 +72,9 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
         if verbose:
             sys.stdout.write(r.stdout + r.stderr)
 
+    ps = os.path.join(CSRC, PEAKS_SRC)
+    if force or not _newer(PEAKS_LIB, [ps]):
+        jobs.append([nvcc()] + ARCH + NVCC_FLAGS + ["-shared", ps, "-o", PEAKS_LIB])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(run, jobs))

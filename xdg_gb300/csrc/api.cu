@@ -881,12 +881,12 @@ cudaError_t launch_trace(xdgcu_ctx* c, int mode, bool mixed, SurfArgs a, double 
   return e != cudaSuccess ? e : f;
 }
 
+// Entry points run with the context's device current and give the caller's
+// current device back on return (DeviceGuard).
 #define CHECK_CTX(c)                                                            \
-  do {                                                                          \
-    if (!(c)) return set_err(XDGCU_ERR_INVALID_ARG, "null context");            \
-    if (cudaSetDevice((c)->device) != cudaSuccess)                             \
-      return set_err(XDGCU_ERR_CUDA, "cudaSetDevice failed");                   \
-  } while (0)
+  if (!(c)) return set_err(XDGCU_ERR_INVALID_ARG, "null context");              \
+  DeviceGuard device_guard_((c)->device);                                       \
+  if (!device_guard_.ok()) return set_err(XDGCU_ERR_CUDA, "cudaSetDevice failed")
 
 }  // namespace
 
@@ -894,6 +894,8 @@ cudaError_t launch_trace(xdgcu_ctx* c, int mode, bool mixed, SurfArgs a, double 
 namespace xdgcu {
 
 int set_last_error(int code, const char* msg) { return set_err(code, msg); }
+
+int ctx_device(const xdgcu_ctx* c) { return c->device; }
 
 const char* walk_args_for(const xdgcu_ctx* c, WalkArgs* a, int* face_order, int* device) {
   if (!c->has_tets) return "no tet mesh set";
@@ -932,7 +934,8 @@ int xdgcu_create(xdgcu_ctx** out, int device) {
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0) return set_err(XDGCU_ERR_CUDA, "no CUDA device available");
   if (device < 0 || device >= n) return set_err(XDGCU_ERR_INVALID_ARG, "device out of range");
-  API_CUDA(cudaSetDevice(device), "cudaSetDevice");
+  DeviceGuard guard(device);
+  if (!guard.ok()) return set_err(XDGCU_ERR_CUDA, "cudaSetDevice failed");
   auto* c = new xdgcu_ctx();
   c->device = device;
   int ats = 0;
@@ -952,7 +955,7 @@ int xdgcu_create(xdgcu_ctx** out, int device) {
 
 int xdgcu_destroy(xdgcu_ctx* c) {
   if (!c) return XDGCU_OK;
-  cudaSetDevice(c->device);
+  DeviceGuard guard(c->device);
   cudaDeviceSynchronize();
   if (c->build_stream) cudaStreamDestroy(c->build_stream);
   delete c;

@@ -17,6 +17,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "geom.cuh"
@@ -77,20 +78,76 @@ struct TreeDev {
 
 constexpr int kPrim64Stride = 10;  // doubles per triangle in prim64
 
-// Number of SMs of the device the process uses, read once (thread-safe
-// initialisation) for the persistent launches' grid sizes.
-inline int device_sm_count() {
-  static const int n = [] {
-    int dev = 0, v = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-      cudaGetLastError();
-      v = 0;
-    }
-    return v > 0 ? v : 1;
-  }();
-  return n;
+// Devices a process can use with per-device launch caches (more are
+// served, with the caches bypassed).
+constexpr int kMaxDevices = 64;
+
+// The current device, or -1.
+inline int current_device() {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return dev;
 }
+
+// Number of SMs of the current device, read once per device (any host
+// thread) for the persistent launches' grid sizes.
+inline int device_sm_count() {
+  static std::atomic<int> cache[kMaxDevices];
+  const int dev = current_device();
+  if (dev >= 0 && dev < kMaxDevices) {
+    const int c = cache[dev].load(std::memory_order_acquire);
+    if (c > 0) return c;
+  }
+  int v = 0;
+  if (dev < 0 || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    v = 0;
+  }
+  v = v > 0 ? v : 1;
+  if (dev >= 0 && dev < kMaxDevices) cache[dev].store(v, std::memory_order_release);
+  return v;
+}
+
+// Resident blocks per SM of `kern` on the current device (`block` threads,
+// `smem` bytes of dynamic shared memory), looked up once per device in the
+// caller's `cache` (one per kernel variant and launch shape).
+template <typename K>
+cudaError_t occupancy_cached(std::atomic<int>* cache, K kern, int block, size_t smem,
+                             int& per_sm) {
+  const int dev = current_device();
+  const bool use = dev >= 0 && dev < kMaxDevices;
+  per_sm = use ? cache[dev].load(std::memory_order_acquire) : 0;
+  if (per_sm > 0) return cudaSuccess;
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  if (use) cache[dev].store(per_sm, std::memory_order_release);
+  return cudaSuccess;
+}
+
+// Makes `device` current for the scope of an entry point and makes the
+// caller's current device current again on the way out, so that a host
+// thread driving several GPUs keeps the device it selected.
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) : prev_(current_device()) {
+    ok_ = prev_ == device || cudaSetDevice(device) == cudaSuccess;
+    if (!ok_) cudaGetLastError();
+  }
+  ~DeviceGuard() {
+    if (prev_ >= 0 && current_device() != prev_) cudaSetDevice(prev_);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+  bool ok() const { return ok_; }
+
+ private:
+  int prev_;
+  bool ok_ = false;
+};
 // doubles per global triangle in the mixed path's table of ray-independent
 // FP64 terms (k_tri_prime in api.cu)
 constexpr int kTriPrimeStride = 32;

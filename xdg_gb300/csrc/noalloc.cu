@@ -13,7 +13,10 @@
 // loads this library keeps it until the process exits.  Host code cannot use
 // the array's name as a device address, so the first call on each device
 // looks the address up with cudaGetSymbolAddress (with that device current)
-// and caches it; that first call should come before any stream capture.
+// and caches it; that first call should come before any stream capture.  The
+// cached address belongs to the device's primary context: after a
+// cudaDeviceReset (or a reset of the primary context) the library cannot be
+// used on that device again in the same process.
 // All calls share the array and it keeps the last call's contents.  Nothing
 // in it needs to start at zero: the scan writes every block sum before it
 // reads it.  Calls whose work overlaps on the GPU (different streams, or
@@ -26,6 +29,7 @@
 #include <string>
 
 #include "../../include/xdgcu.h"
+#include "internal.cuh"
 #include "walk.h"
 
 namespace xdgcu {
@@ -37,7 +41,6 @@ static_assert(kNoAllocScratch >= 1, "scratch size");
 
 static __device__ __align__(256) int64_t g_walk_scan_scratch[kNoAllocScratch];
 
-constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 int64_t* g_scratch_ptr[kMaxDevices] = {};
 
@@ -88,8 +91,10 @@ extern "C" int xdgcu_walk_elements_packed_noalloc(
   if (const char* msg = walk_args_for(ctx, &a, &face_order, &dev))
     return set_last_error(XDGCU_ERR_STATE, msg);
   if (dev < 0 || dev >= kMaxDevices) return set_last_error(XDGCU_ERR_INVALID_ARG, "device id");
-  if (cudaSetDevice(dev) != cudaSuccess) return set_last_error(XDGCU_ERR_CUDA, "cudaSetDevice failed");
-  // device memory only: host pointers would need staging buffers
+  DeviceGuard guard(dev);
+  if (!guard.ok()) return set_last_error(XDGCU_ERR_CUDA, "cudaSetDevice failed");
+  // device memory of the context's device only: host pointers would need
+  // staging buffers, and another GPU's memory is not this device's to walk into
   for (const void* p : {(const void*)start_index, (const void*)start, (const void*)u,
                         (const void*)distance, (const void*)seg_elem, (const void*)seg_len,
                         (const void*)offsets, (const void*)status}) {
@@ -101,6 +106,10 @@ extern "C" int xdgcu_walk_elements_packed_noalloc(
       return set_last_error(XDGCU_ERR_INVALID_ARG,
                             "walk_elements_packed_noalloc takes device pointers only");
     }
+    if (at.type == cudaMemoryTypeDevice && at.device != dev)
+      return set_last_error(XDGCU_ERR_INVALID_ARG,
+                            "walk_elements_packed_noalloc: an array is on another device than "
+                            "the context's");
   }
   cudaStream_t st = (cudaStream_t)stream;
   if (n == 0) {

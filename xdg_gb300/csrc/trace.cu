@@ -804,10 +804,10 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
 }
 
 // resident blocks per SM, by kernel variant, MINB and stack depth (8..64
-// step 8), and whether the variant's shared-memory limit is raised; filled on
-// first use, from any host thread
-std::atomic<int> g_blocks_per_sm[12][3][kTStackMax / 8 + 1];
-std::atomic<bool> g_smem_attr[12][3];
+// step 8), per device, and whether the variant's shared-memory limit is
+// raised on a device; filled on first use, from any host thread
+std::atomic<int> g_blocks_per_sm[12][3][kTStackMax / 8 + 1][kMaxDevices];
+std::atomic<bool> g_smem_attr[12][3][kMaxDevices];
 
 template <int MODE, bool MIXED, int MINB>
 cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
@@ -816,20 +816,20 @@ cudaError_t launch_minb(const SurfArgs& a, cudaStream_t st, int slot) {
   constexpr bool keys = stack_keys<MODE, MIXED>();
   const size_t smem = trace_smem_bytes(a.stack, keys, MODE == MODE_PARTICLE && MIXED);
   auto kern = k_trace<MODE, MIXED, MINB>;
-  if (!g_smem_attr[slot][MINB - 2].load(std::memory_order_acquire)) {
+  const int dev = current_device();
+  const bool known = dev >= 0 && dev < kMaxDevices;
+  if (!known || !g_smem_attr[slot][MINB - 2][dev].load(std::memory_order_acquire)) {
     cudaError_t e = cudaFuncSetAttribute(
         kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
         (int)trace_smem_bytes(kTStackMax, keys, MODE == MODE_PARTICLE && MIXED));
     if (e != cudaSuccess) return e;
-    g_smem_attr[slot][MINB - 2].store(true, std::memory_order_release);
+    if (known) g_smem_attr[slot][MINB - 2][dev].store(true, std::memory_order_release);
   }
-  std::atomic<int>& cache = g_blocks_per_sm[slot][MINB - 2][a.stack / 8];
-  int per_sm = cache.load(std::memory_order_acquire);
-  if (per_sm == 0) {
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTBlock, smem);
+  int per_sm = 0;
+  {
+    const cudaError_t e =
+        occupancy_cached(g_blocks_per_sm[slot][MINB - 2][a.stack / 8], kern, kTBlock, smem, per_sm);
     if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    cache.store(per_sm, std::memory_order_release);
   }
   const int64_t warps_needed = (a.n + 31) / 32;
   int64_t blocks = (int64_t)device_sm_count() * per_sm;

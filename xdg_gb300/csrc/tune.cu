@@ -26,9 +26,11 @@
 #include <vector>
 
 #include "xdgcu.h"
+#include "internal.cuh"
 
 namespace xdgcu {
 int set_last_error(int code, const char* msg);
+int ctx_device(const xdgcu_ctx* c);
 }
 
 namespace {
@@ -175,6 +177,8 @@ int xdgcu_autotune_trace(xdgcu_ctx* c, int32_t query, int32_t tree, const int32_
                          int64_t n, const double* origins, const double* directions,
                          int32_t precision, int32_t reps, int32_t tune_tree, double* best_ms) {
   if (!c) return set_last_error(XDGCU_ERR_INVALID_ARG, "null context");
+  xdgcu::DeviceGuard guard(xdgcu::ctx_device(c));
+  if (!guard.ok()) return set_last_error(XDGCU_ERR_CUDA, "cudaSetDevice failed");
   if (query < XDGCU_QUERY_RAY_FIRE || query > XDGCU_QUERY_FIND_VOLUME)
     return set_last_error(XDGCU_ERR_INVALID_ARG, "autotune: unknown query");
   if (n <= 0 || !origins || (!directions && query != XDGCU_QUERY_POINT_IN_VOLUME &&
@@ -294,6 +298,8 @@ int xdgcu_autotune_walk(xdgcu_ctx* c, int64_t n, const int32_t* start_index, con
                         const double* u, const double* distance, int32_t max_segs,
                         int32_t precision, int32_t reps, double* best_ms) {
   if (!c) return set_last_error(XDGCU_ERR_INVALID_ARG, "null context");
+  xdgcu::DeviceGuard guard(xdgcu::ctx_device(c));
+  if (!guard.ok()) return set_last_error(XDGCU_ERR_CUDA, "cudaSetDevice failed");
   if (n <= 0 || !start_index || !start || !u || !distance || max_segs <= 0)
     return set_last_error(XDGCU_ERR_INVALID_ARG, "autotune: empty sample or bad arguments");
   if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)

@@ -793,15 +793,11 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(int64_t* __restrict__
 
 template <int FO, bool MIXED, bool QUEUE>
 cudaError_t launch_walk_t(const WalkArgs& a, cudaStream_t st) {
-  static std::atomic<int> cached{0};  // resident blocks per SM, filled on first use
+  static std::atomic<int> cached[kMaxDevices];  // resident blocks per SM, per device
   auto kern = QUEUE ? k_walk_q<FO> : k_walk<FO, MIXED>;
-  int per_sm = cached.load(std::memory_order_acquire);
-  if (per_sm == 0) {
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    cached.store(per_sm, std::memory_order_release);
-  }
+  int per_sm = 0;
+  const cudaError_t e = occupancy_cached(cached, kern, kBlock, 0, per_sm);
+  if (e != cudaSuccess) return e;
   int64_t blocks = (int64_t)device_sm_count() * per_sm;
   const int64_t max_blocks = (a.n + kBlock - 1) / kBlock;
   if (blocks > max_blocks) blocks = max_blocks;
@@ -990,15 +986,11 @@ __global__ void __launch_bounds__(kBlock) k_transport(TransportArgs t, int64_t c
 
 template <int FO, bool MIXED>
 cudaError_t launch_transport_t(const TransportArgs& a, cudaStream_t st) {
-  static std::atomic<int> cached{0};  // resident blocks per SM, filled on first use
+  static std::atomic<int> cached[kMaxDevices];  // resident blocks per SM, per device
   auto kern = k_transport<FO, MIXED>;
-  int per_sm = cached.load(std::memory_order_acquire);
-  if (per_sm == 0) {
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    cached.store(per_sm, std::memory_order_release);
-  }
+  int per_sm = 0;
+  const cudaError_t e = occupancy_cached(cached, kern, kBlock, 0, per_sm);
+  if (e != cudaSuccess) return e;
   int64_t blocks = (int64_t)device_sm_count() * per_sm;
   const int64_t max_blocks = (a.n + kBlock - 1) / kBlock;
   if (blocks > max_blocks) blocks = max_blocks;
