@@ -1,9 +1,16 @@
 // The reference's MeshMock Catch2 tests, replayed through the C++ backend
 // class xdg::CudaRayTracer (the RayTracer subclass over the C ABI), in both
-// precisions.  The mesh below restates the MeshMock fixture
-// (tests/mesh_mock.h:17-321): a box [-2,5]x[-3,6]x[-4,7] of six two-triangle
-// surfaces, forward-sensed to volume 0, split into twelve tets around the
-// centre.  Exit status 0 when every check passes.
+// precisions.  Exit status 0 when every check passes.
+//
+// Built two ways:
+//  - against the stand-in declarations of xdg_api.h: the mesh below restates
+//    the MeshMock fixture (tests/mesh_mock.h:17-321), a box
+//    [-2,5]x[-3,6]x[-4,7] of six two-triangle surfaces, forward-sensed to
+//    volume 0, split into twelve tets around the centre;
+//  - with XDGCU_WITH_XDG_HEADERS, against XDG's own headers: the backend
+//    derives from XDG's RayTracer and the tests run on the reference's own
+//    MeshMock (include/xdg/testing/mesh_mock.h) and its ElementFaceAccessor
+//    factory (src/element_face_accessor.cpp), linked from XDG's sources.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -12,6 +19,9 @@
 #include <vector>
 
 #include "cuda_ray_tracer.h"
+#ifdef XDGCU_WITH_XDG_HEADERS
+#include "xdg/testing/mesh_mock.h"
+#endif
 
 using namespace xdg;
 
@@ -56,6 +66,14 @@ const int ADJ[12][4] = {{-1, 1, 4, 11}, {-1, 9, 0, 7}, {-1, 5, 3, 10}, {-1, 2, 8
 const int TET_FACES[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
 
 Vertex vert(int i) { return {VERTS[i][0], VERTS[i][1], VERTS[i][2]}; }
+
+#ifdef XDGCU_WITH_XDG_HEADERS
+
+using MockMesh = ::MeshMock;  // the reference's own fixture
+
+}  // namespace
+
+#else
 
 class MockMesh : public MeshManager {
  public:
@@ -105,6 +123,8 @@ std::shared_ptr<ElementFaceAccessor> ElementFaceAccessor::create(const MeshManag
                                                                  MeshID element) {
   return std::make_shared<MockFaceAccessor>(mm, element);
 }
+
+#endif  // XDGCU_WITH_XDG_HEADERS
 
 namespace {
 

@@ -73,6 +73,7 @@ TreeID CudaRayTracer::create_surface_tree(const std::shared_ptr<MeshManager>& mm
   check(xdgcu_create_surface_tree(ctx_, ids.data(), sense.data(), (int32_t)ids.size(),
                                   bounding_box_bump(mm, volume), &tree),
         "create_surface_tree");
+  claim_surface_tree_id(tree);
   surface_trees_.push_back(tree);
   return tree;
 }
@@ -143,6 +144,7 @@ TreeID CudaRayTracer::create_element_tree(const std::shared_ptr<MeshManager>& mm
   TreeID tree = TREE_NONE;
   check(xdgcu_create_element_tree(ctx_, idx.data(), (int64_t)idx.size(), &tree),
         "create_element_tree");
+  claim_element_tree_id(tree);
   element_trees_.push_back(tree);
   return tree;
 }
@@ -150,6 +152,7 @@ TreeID CudaRayTracer::create_element_tree(const std::shared_ptr<MeshManager>& mm
 void CudaRayTracer::create_global_surface_tree() {
   TreeID tree = TREE_NONE;
   check(xdgcu_create_global_surface_tree(ctx_, &tree), "create_global_surface_tree");
+  claim_surface_tree_id(tree);
   surface_trees_.push_back(tree);
   global_surface_tree_ = tree;
 }
@@ -157,8 +160,22 @@ void CudaRayTracer::create_global_surface_tree() {
 void CudaRayTracer::create_global_element_tree() {
   TreeID tree = TREE_NONE;
   check(xdgcu_create_global_element_tree(ctx_, &tree), "create_global_element_tree");
+  claim_element_tree_id(tree);
   element_trees_.push_back(tree);
   global_element_tree_ = tree;
+}
+
+// The engine numbers each kind of tree from 1 in creation order, as the base
+// class's counters do (ray_tracing_interface.cpp:10-18); the backend takes
+// the base class's next id and checks that the engine gave the same one.
+void CudaRayTracer::claim_surface_tree_id(TreeID tree) {
+  if (tree != next_surface_tree_id())
+    throw std::runtime_error("CUDA backend: surface tree ids out of step with the engine");
+}
+
+void CudaRayTracer::claim_element_tree_id(TreeID tree) {
+  if (tree != next_element_tree_id())
+    throw std::runtime_error("CUDA backend: element tree ids out of step with the engine");
 }
 
 int32_t CudaRayTracer::tet_index(MeshID element) const {

@@ -40,7 +40,11 @@ class CudaRayTracer : public RayTracer {
   std::pair<double, MeshID> closest(TreeID tree, const Position& origin) override;
   bool occluded(TreeID tree, const Position& origin, const Direction& direction,
                 double& dist) const override;
-  RTLibrary library() const override { return RTLibrary::CUDA; }
+  RTLibrary library() const override { return XDGCU_RTLIBRARY; }
+
+  // the global trees (TREE_NONE until created)
+  SurfaceTreeID global_surface_tree_id() const { return global_surface_tree_; }
+  ElementTreeID global_element_tree_id() const { return global_element_tree_; }
 
   // MeshManager::next_element / walk_elements on the device, for the mesh
   // of the element trees (mesh_manager_interface.cpp:106-200).
@@ -67,6 +71,8 @@ class CudaRayTracer : public RayTracer {
 
  private:
   void upload_tet_mesh(const MeshManager* mm);
+  void claim_surface_tree_id(TreeID tree);
+  void claim_element_tree_id(TreeID tree);
 
   xdgcu_ctx* ctx_ = nullptr;
   int precision_;

@@ -11,8 +11,6 @@ namespace xdg {
 
 namespace {
 
-constexpr double TINY_BIT = 1e-10;  // constants.h:32
-
 // Vec3da::normalize (vec3da.h:61-66)
 Vec3da normalized(Vec3da v) {
   double len = std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
@@ -57,7 +55,7 @@ void walk_particles(CudaRayTracer& rt, TreeID ipc_surface_tree, ParticleBank& ba
   }
   double* tally = nullptr;
   if (element_tally) tally = element_tally->data();
-  const TreeID gtree = rt.global_element_tree();
+  const TreeID gtree = rt.global_element_tree_id();
   for (int round = 0; round <= max_reentries; ++round) {
     rt.check(xdgcu_transport_elements(ctx, (int64_t)n, idx.data(), bank.pos.data(),
                                       bank.dir.data(), bank.rng.data(), mfp, max_events,
@@ -178,7 +176,7 @@ TrackSegments track_segments(CudaRayTracer& rt, const MeshManager& mm, TreeID ip
                              size_t n, const double* starts, const double* ends, int max_rounds) {
   xdgcu_ctx* ctx = rt.context();
   const int prec = rt.precision();
-  const TreeID gtree = rt.global_element_tree();
+  const TreeID gtree = rt.global_element_tree_id();
   // u = end - start; distance = u.length(); u /= distance (xdg.cpp:150-153)
   std::vector<double> r(starts, starts + 3 * n), u(3 * n), dist(n);
   for (size_t i = 0; i < n; ++i) {

@@ -1,12 +1,29 @@
-// xdg_api.h -- the parts of XDG's public C++ interface the CUDA backend uses,
-// declared with the same names and signatures so that cuda_ray_tracer.cpp
-// compiles here without the XDG tree.  Inside XDG, replace this include with
-//   #include "xdg/constants.h"
-//   #include "xdg/ray_tracing_interface.h"
-//   #include "xdg/mesh_manager_interface.h"
-//   #include "xdg/element_face_accessor.h"
-// and add CUDA to RTLibrary in constants.h.
+// xdg_api.h -- XDG's public C++ interface as the CUDA backend sees it.
+//
+// Built with XDGCU_WITH_XDG_HEADERS defined (inside XDG, or against its
+// source tree) this includes XDG's own headers:
+//   xdg/constants.h, xdg/ray_tracing_interface.h, xdg/mesh_manager_interface.h,
+//   xdg/element_face_accessor.h.
+// Otherwise it declares the subset of them the backend uses, with the same
+// names, signatures and protected state, so that the backend and its tests
+// compile without the XDG tree.
+//
+// XDGCU_RTLIBRARY is the RTLibrary value the backend reports; XDG's
+// integration adds CUDA to RTLibrary in constants.h, after EMBREE and GPRT.
 #pragma once
+
+#ifdef XDGCU_WITH_XDG_HEADERS
+
+#include "xdg/constants.h"
+#include "xdg/element_face_accessor.h"
+#include "xdg/mesh_manager_interface.h"
+#include "xdg/ray_tracing_interface.h"
+
+#ifndef XDGCU_RTLIBRARY
+#define XDGCU_RTLIBRARY ::xdg::RTLibrary::CUDA
+#endif
+
+#else  // the stand-in declarations
 
 #include <array>
 #include <cfloat>
@@ -18,6 +35,10 @@
 #include <utility>
 #include <vector>
 
+#ifndef XDGCU_RTLIBRARY
+#define XDGCU_RTLIBRARY ::xdg::RTLibrary::CUDA
+#endif
+
 namespace xdg {
 
 // constants.h:15, 73-87
@@ -28,12 +49,13 @@ using SurfaceTreeID = TreeID;
 using ElementTreeID = TreeID;
 constexpr MeshID ID_NONE{-1};
 constexpr TreeID TREE_NONE{-1};
+constexpr double TINY_BIT{1e-10};  // constants.h:32
 
 // shared_enums.h:11-15
 enum HitOrientation : int { ANY = -1, EXITING = 0, ENTERING = 1 };
 enum class Sense { UNSET = -1, FORWARD = 0, REVERSE = 1 };
 enum class MeshLibrary { MOCK = 0, MOAB, LIBMESH };
-enum class RTLibrary { EMBREE, GPRT, CUDA };
+enum class RTLibrary { EMBREE, GPRT, CUDA };  // CUDA: the integration adds it
 
 // The subset of Vec3da (vec3da.h) the backend uses.
 struct Vec3da {
@@ -162,8 +184,6 @@ class RayTracer {
                         double& dist) const = 0;
   virtual RTLibrary library() const = 0;
 
-  SurfaceTreeID global_surface_tree() const { return global_surface_tree_; }
-  ElementTreeID global_element_tree() const { return global_element_tree_; }
   int num_registered_trees() const { return (int)(surface_trees_.size() + element_trees_.size()); }
   int num_registered_surface_trees() const { return (int)surface_trees_.size(); }
   int num_registered_element_trees() const { return (int)element_trees_.size(); }
@@ -173,11 +193,20 @@ class RayTracer {
   double bounding_box_bump(const std::shared_ptr<MeshManager> mm, MeshID volume) {
     return std::max(mm->volume_bounding_box(volume).dilation(), numerical_precision_);
   }
+  // ray_tracing_interface.cpp:10-18
+  SurfaceTreeID next_surface_tree_id() { return ++next_surface_tree_id_; }
+  ElementTreeID next_element_tree_id() { return ++next_element_tree_id_; }
   SurfaceTreeID global_surface_tree_{TREE_NONE};
   ElementTreeID global_element_tree_{TREE_NONE};
+  std::map<MeshID, SurfaceTreeID> surface_to_tree_map_;
+  std::map<MeshID, ElementTreeID> point_location_tree_map_;
   std::vector<SurfaceTreeID> surface_trees_;
   std::vector<ElementTreeID> element_trees_;
+  SurfaceTreeID next_surface_tree_id_{0};
+  ElementTreeID next_element_tree_id_{0};
   double numerical_precision_{1e-3};
 };
 
 }  // namespace xdg
+
+#endif  // XDGCU_WITH_XDG_HEADERS
