@@ -73,6 +73,9 @@ BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
 BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
 BYTES_TRI64 = 76            # 72 B FP64 triangle + 4 B id (escalations)
 BYTES_IO = 68               # 48 B origin/dir + 4 B tree id in, 8 B t + 4 B surface + 4 B face out
+GLOBAL_TRACKS = 1_000_000    # tracks of the global track loop (XDG::segments(start, end))
+GLOBAL_CHECK = 2_000         # of them repeated by the oracle's track loop
+GLOBAL_WORKLOAD = "3_tet_blocks_30^3x6_jitter0.2_gaps_1e6_tracks_uniform_endpoints"
 WALK_CHECK = 50_000          # C5 tracks walked by the oracle and compared bit for bit
 WALK_CPU_SAMPLE = 1_000_000  # C5 tracks of the walk's CPU baseline (all of them)
 FV_CHECK = 100_000           # headline points whose find_volume the oracle repeats
@@ -615,6 +618,78 @@ def bench_surface_transport(torch, L, x, model, dev, stream, sptr, p, d, trees_h
                                "cores": cores, "kind": "port",
                                "sample": f"first {kc} particles, FP64 particle_sim loop, BVH, "
                                          "OpenMP"}
+    return out
+
+
+def bench_global_segments(torch, L, dev, stream, sptr, args, rank, world):
+    """XDG::segments(start, end) (xdg.cpp:142-198) over three jittered meshed
+    blocks (30^3 x 6 tets each, 486,000 tets) with gaps of implicit
+    complement between them: GLOBAL_TRACKS tracks between uniform points of
+    the box around them, every round of every track in one
+    xdgcu_segments_global call (device arrays), both precisions; the oracle's
+    track loop repeats a sample bit for bit."""
+    from xdg_gb300 import _lib
+    from xdg_gb300.engine import FP64, MIXED, XDG
+    t0 = time.perf_counter()
+    m = synth.tet_blocks([((0.0, 0.0, 0.0), 30, 10.0), ((12.0, 0.0, 0.0), 30, 10.0),
+                          ((24.0, 0.0, 0.0), 30, 10.0)], jitter=0.2, seed=17)
+    x = XDG(m, device=dev.index)
+    x.prepare_raytracer()
+    rng = np.random.default_rng(dist.rank_seed(777, rank))
+    lo, hi = np.array([-3.0, -1.0, -1.0]), np.array([37.0, 11.0, 11.0])
+    a_h = rng.uniform(lo, hi, (GLOBAL_TRACKS, 3))
+    b_h = rng.uniform(lo, hi, (GLOBAL_TRACKS, 3))
+    a, b = torch.from_numpy(a_h).to(dev), torch.from_numpy(b_h).to(dev)
+    ipc = x.volume_to_surface_tree[m.implicit_complement]
+    gt = x.rti.global_element_tree
+    n = GLOBAL_TRACKS
+    off = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+    se0, sl0, off0, _ = x.rti.segments_global(ipc, gt, a, b, 1, precision=MIXED)
+    torch.cuda.synchronize()
+    cap = int(off0[-1].item())
+    se = torch.empty(cap, dtype=torch.int32, device=dev)
+    sl = torch.empty(cap, dtype=torch.float64, device=dev)
+    log(f"[bench] global segments setup {time.perf_counter() - t0:.1f}s, {len(m.tets.conn)} tets")
+
+    def run(prec, e=se, ln=sl, o=off, s_=st):
+        def go():
+            rc = L.xdgcu_segments_global(x.rti.ctx, ipc, gt, n, ctypes.c_void_p(a.data_ptr()),
+                                         ctypes.c_void_p(b.data_ptr()), 4096, 10_000, cap,
+                                         ctypes.c_void_p(e.data_ptr()), ctypes.c_void_p(ln.data_ptr()),
+                                         ctypes.c_void_p(o.data_ptr()), ctypes.c_void_p(s_.data_ptr()),
+                                         prec, sptr)
+            _lib.check(rc, x.rti.ctx, "segments_global")
+        return go
+
+    ms = timed(torch, run(MIXED), max(3, args.steps // 4), 2, world, stream)
+    ref = (se.clone(), sl.clone(), off.clone())
+    se64, sl64 = torch.empty_like(se), torch.empty_like(sl)
+    off64, st64 = torch.empty_like(off), torch.empty_like(st)
+    ms64 = timed(torch, run(FP64, se64, sl64, off64, st64), 3, 1, world, stream)
+    same = bool(torch.equal(off64, ref[2]) and torch.equal(se64, ref[0]) and torch.equal(sl64, ref[1]))
+    segs = int(ref[2][-1].item())
+    out = {"workload": GLOBAL_WORKLOAD, "tracks": n, "tets": int(len(m.tets.conn)),
+           "segments": segs, "unit": "Msegs/s",
+           "value": dist.sum_over_ranks(segs, world) / (ms / 1e3) / 1e6,
+           "fp64_value": dist.sum_over_ranks(segs, world) / (ms64 / 1e3) / 1e6,
+           "ms_per_step": ms, "fp64_ms_per_step": ms64, "mixed_equals_fp64": same,
+           "tracks_with_status": int((st != 0).sum().item()),
+           "step": "one xdgcu_segments_global call (all rounds: find_element, implicit-complement "
+                   "ray_fire + boundary-face re-entry, packed walk)"}
+    if rank == 0 and not args.no_oracle:
+        from oracle import oracle as xo
+        xo.build()
+        g = xo.GlobalTracker(m)
+        ksel = np.arange(0, n, max(1, n // GLOBAL_CHECK))
+        oh = ref[2].cpu().numpy()
+        eh, lh = ref[0].cpu().numpy(), ref[1].cpu().numpy()
+        mism = 0
+        for i in ksel:
+            oe, ol = g.segments(a_h[i], b_h[i])
+            e_i, l_i = eh[oh[i]:oh[i + 1]], lh[oh[i]:oh[i + 1]]
+            mism += int(not (np.array_equal(e_i, oe) and np.array_equal(l_i, ol)))
+        out["oracle_check"] = {"tracks": int(len(ksel)), "tracks_differing": mism}
     return out
 
 
@@ -1167,6 +1242,7 @@ def run_engine(args, rank, world, local):
         log(f"[bench] walk oracle check + cpu baseline {time.perf_counter() - t1:.1f}s")
 
     # ---- device particle loop (walk_elements tool) over the same mesh ------
+    global_segments = bench_global_segments(torch, L, dev, stream, sptr, args, rank, world)
     transport = bench_transport(torch, L, wr, dev, stream, sptr, ws, wu, we_idx, tm, args, rank,
                                 world)
 
@@ -1255,6 +1331,7 @@ def run_engine(args, rank, world, local):
         "configs_small": small_configs,
         "overlap_check": overlap,
         "transport": transport,
+        "global_segments": global_segments,
         "surface_transport": surface_transport,
         "many_surfaces": many,
         "tuning": tuning,
@@ -1337,6 +1414,11 @@ def run_engine(args, rank, world, local):
                 "walk": (walk_oracle["count_mismatches"] + walk_oracle["element_mismatches"]
                          + walk_oracle["length_mismatches"] + walk_oracle["status_mismatches"]
                          + walk_oracle["find_element_mismatches"]) if walk_oracle else None},
+            "global_segments_Msegs_s": {
+                "mixed": round(global_segments["value"], 1),
+                "fp64": round(global_segments["fp64_value"], 1),
+                "oracle_tracks_differing": (global_segments.get("oracle_check") or {}).get(
+                    "tracks_differing")},
             "mixed_vs_fp64_mismatches": {"ray_fire": id_mism + t_mism,
                                          "walk": walk_elem_mism + walk_len_mism},
         },

@@ -265,6 +265,38 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* ctx, int64_t n, const int32_t* start_i
                                double* seg_len, int64_t* offsets, int32_t* status,
                                int32_t precision, void* stream);
 
+/* MeshManager::get_boundary_face_element (mesh_manager_interface.h:153-157)
+ * for the global track loop below: face_ids[k] (surface face mesh ids, as
+ * ray_fire returns them) -> elem_index[k], the tet index behind the face
+ * (-1: none).  Replaces any earlier map.  Host arrays; needs the tet mesh. */
+int xdgcu_set_boundary_face_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* face_ids,
+                                     const int32_t* elem_index);
+
+/* XDG::segments(start, end) (xdg.cpp:142-198) for n tracks, on the device:
+ * u = (end - start) / |end - start|; while distance remains, find_element(r)
+ * in `element_tree` (the global element tree in the reference), ignoring the
+ * element of the last segment (the track sits on its face); outside the mesh
+ * ray_fire(EXITING) in `ipc_tree` (the implicit complement's surface tree)
+ * from r + u * TINY_BIT, stop on a miss or a hit beyond the distance, else
+ * step to the hit plus TINY_BIT and re-enter through the boundary face's
+ * element (xdgcu_set_boundary_face_elements; none: stop); walk_elements;
+ * r += u * segment_sum, distance -= segment_sum.  All tracks advance
+ * together: each round is one find_element, one ray_fire and one packed walk
+ * launch over the active tracks, with the bookkeeping in device kernels.
+ * Output as xdgcu_walk_elements_packed: track i's segments (element MESH
+ * ids, lengths) at offsets[i] .. offsets[i+1]-1 of arrays of `capacity`
+ * entries; a track that does not fit is not written (XDGCU_RAY_OUTPUT_FULL).
+ * max_segs caps one walk of a track and max_rounds the rounds: a track cut
+ * short by either gets XDGCU_RAY_WALK_LIMIT (the reference has no limit).
+ * status (may be NULL) also records XDGCU_RAY_NO_EXIT_FACE (the track went
+ * on, as the reference's does) and XDGCU_RAY_INVALID (non-finite input).
+ * Host or device arrays (not mixed); scratch is allocated on `stream` with
+ * cudaMallocAsync, and the call waits for a few counters per round. */
+int xdgcu_segments_global(xdgcu_ctx* ctx, int32_t ipc_tree, int32_t element_tree, int64_t n,
+                          const double* starts, const double* ends, int32_t max_segs,
+                          int32_t max_rounds, int64_t capacity, int32_t* seg_elem, double* seg_len,
+                          int64_t* offsets, int32_t* status, int32_t precision, void* stream);
+
 /* Fills states[0..n) (host memory) with independent random stream states
  * for the particle loops: SplitMix64's output function of
  * seed + (i + 1) * 0x9E3779B97F4A7C15.  No counterpart in the reference,

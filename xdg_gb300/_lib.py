@@ -59,6 +59,9 @@ SIGNATURES = {
                                           _VP, _VP, _i32, _VP]),
     "xdgcu_walk_elements_packed_noalloc": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _i32, _i64,
                                                   _VP, _VP, _VP, _VP, _i32, _VP]),
+    "xdgcu_set_boundary_face_elements": (_int, [_VP, _i64, _VP, _VP]),
+    "xdgcu_segments_global": (_int, [_VP, _i32, _i32, _i64, _VP, _VP, _i32, _i32, _i64, _VP, _VP,
+                                     _VP, _VP, _i32, _VP]),
     "xdgcu_point_in_volumes": (_int, [_VP, _i64, _VP, _VP, _i32, _VP, _VP, _VP, _i32, _VP]),
     "xdgcu_set_surface_boundary": (_int, [_VP, _i32, _VP, _VP]),
     "xdgcu_transport_surfaces": (_int, [_VP, _i64, _VP, _VP, _VP, _VP, _dbl, _i32, _i32, _i32,

@@ -26,7 +26,8 @@ LIB = os.path.join(OUT_DIR, "libxdgcu.so")
 # throughput microbenchmarks for the roofline denominators (not the engine)
 PEAKS_SRC = "peaks.cu"
 PEAKS_LIB = os.path.join(OUT_DIR, "libxdgpeaks.so")
-SOURCES = ["api.cu", "bvh.cu", "noalloc.cu", "order.cu", "queries.cu", "trace.cu", "tune.cu", "walk.cu"]
+SOURCES = ["api.cu", "bvh.cu", "noalloc.cu", "order.cu", "queries.cu", "segments.cu", "trace.cu", "tune.cu",
+           "walk.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", os.path.join(HERE, "..", "include")]

@@ -176,124 +176,34 @@ TrackSegments track_segments(CudaRayTracer& rt, const MeshManager& mm, TreeID ip
                              size_t n, const double* starts, const double* ends, int max_rounds) {
   xdgcu_ctx* ctx = rt.context();
   const int prec = rt.precision();
-  const TreeID gtree = rt.global_element_tree_id();
-  // u = end - start; distance = u.length(); u /= distance (xdg.cpp:150-153)
-  std::vector<double> r(starts, starts + 3 * n), u(3 * n), dist(n);
-  for (size_t i = 0; i < n; ++i) {
-    double d[3];
-    for (int c = 0; c < 3; ++c) d[c] = ends[3 * i + c] - starts[3 * i + c];
-    dist[i] = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    for (int c = 0; c < 3; ++c) u[3 * i + c] = d[c] / dist[i];
-  }
-  std::vector<std::vector<std::pair<MeshID, double>>> segs(n);
-  std::vector<size_t> active;
-  for (size_t i = 0; i < n; ++i)
-    if (dist[i] > 0) active.push_back(i);
-  for (int round = 0; round < max_rounds && !active.empty(); ++round) {
-    const size_t m = active.size();
-    std::vector<double> q(3 * m);
-    for (size_t j = 0; j < m; ++j)
-      for (int c = 0; c < 3; ++c) q[3 * j + c] = r[3 * active[j] + c];
-    std::vector<int32_t> eid(m), cur(m);
-    rt.check(xdgcu_find_element(ctx, gtree, nullptr, (int64_t)m, q.data(), eid.data(), cur.data(),
-                                nullptr, prec, nullptr),
-             "find_element");
-    // on the face of the element the last walk ended in: not inside it
-    // (xdg.cpp:161-162)
-    std::vector<size_t> out;
-    for (size_t j = 0; j < m; ++j) {
-      const auto& s = segs[active[j]];
-      if (!s.empty() && eid[j] == s.back().first) cur[j] = -1;
-      if (cur[j] < 0) out.push_back(j);
+  // MeshManager::get_boundary_face_element of every surface face, as tet
+  // indices of the engine's mesh
+  std::vector<int32_t> faces, elems;
+  for (MeshID s : mm.surfaces())
+    for (MeshID f : mm.get_surface_faces(s)) {
+      const MeshID be = mm.get_boundary_face_element(f);
+      faces.push_back(f);
+      elems.push_back(be == ID_NONE ? -1 : rt.tet_index(be));
     }
-    std::vector<char> keep(m, 1);
-    if (!out.empty()) {
-      // implicit-complement ray to the next mesh boundary (xdg.cpp:163-184)
-      const size_t k = out.size();
-      std::vector<double> o(3 * k), d(3 * k), t(k);
-      std::vector<int32_t> surf(k), face(k);
-      for (size_t a = 0; a < k; ++a) {
-        const size_t i = active[out[a]];
-        for (int c = 0; c < 3; ++c) {
-          o[3 * a + c] = r[3 * i + c] + u[3 * i + c] * TINY_BIT;
-          d[3 * a + c] = u[3 * i + c];
-        }
-      }
-      rt.check(xdgcu_ray_fire(ctx, ipc_surface_tree, nullptr, (int64_t)k, o.data(), d.data(),
-                              nullptr, XDGCU_EXITING, nullptr, nullptr, t.data(), surf.data(),
-                              face.data(), nullptr, prec, nullptr),
-               "ray_fire");
-      for (size_t a = 0; a < k; ++a) {
-        const size_t j = out[a], i = active[j];
-        if (surf[a] == ID_NONE || t[a] > dist[i]) {
-          keep[j] = 0;
-          continue;
-        }
-        const double hd = t[a] + TINY_BIT;
-        for (int c = 0; c < 3; ++c) r[3 * i + c] = r[3 * i + c] + u[3 * i + c] * hd;
-        dist[i] = dist[i] - hd;
-        const MeshID be = mm.get_boundary_face_element(face[a]);
-        cur[j] = be == ID_NONE ? -1 : rt.tet_index(be);
-        if (cur[j] < 0) keep[j] = 0;  // no element behind the face
-      }
-    }
-    std::vector<size_t> walkers;
-    std::vector<int32_t> start;
-    for (size_t j = 0; j < m; ++j)
-      if (keep[j]) {
-        walkers.push_back(active[j]);
-        start.push_back(cur[j]);
-      }
-    const size_t w = walkers.size();
-    if (w == 0) break;
-    std::vector<double> wr(3 * w), wu(3 * w), wd(w);
-    for (size_t j = 0; j < w; ++j) {
-      const size_t i = walkers[j];
-      for (int c = 0; c < 3; ++c) {
-        wr[3 * j + c] = r[3 * i + c];
-        wu[3 * j + c] = u[3 * i + c];
-      }
-      wd[j] = dist[i];
-    }
-    // walk_elements from each element (xdg.cpp:187-189), packed; sized
-    // again when the first guess of the output size is too small
-    int64_t cap = std::max<int64_t>(1024, 64 * (int64_t)w);
-    std::vector<int32_t> se, st(w);
-    std::vector<double> sl;
-    std::vector<int64_t> off(w + 1);
-    for (int attempt = 0; attempt < 2; ++attempt) {
-      se.resize(cap);
-      sl.resize(cap);
-      rt.check(xdgcu_walk_elements_packed(ctx, (int64_t)w, start.data(), wr.data(), wu.data(),
-                                          wd.data(), 4096, cap, se.data(), sl.data(), off.data(),
-                                          st.data(), prec, nullptr),
-               "walk_elements_packed");
-      if (off[w] <= cap) break;
-      cap = off[w];
-    }
-    std::vector<size_t> next;
-    for (size_t j = 0; j < w; ++j) {
-      const size_t i = walkers[j];
-      double sum = 0.0;  // std::accumulate from 0.0, in order (xdg.cpp:190-191)
-      for (int64_t s = off[j]; s < off[j + 1]; ++s) {
-        segs[i].emplace_back(se[s], sl[s]);
-        sum = sum + sl[s];
-      }
-      for (int c = 0; c < 3; ++c) r[3 * i + c] = r[3 * i + c] + u[3 * i + c] * sum;
-      dist[i] = dist[i] - sum;
-      if (dist[i] > 0) next.push_back(i);
-    }
-    active.swap(next);
-  }
+  rt.check(xdgcu_set_boundary_face_elements(ctx, (int64_t)faces.size(), faces.data(), elems.data()),
+           "set_boundary_face_elements");
+  // every round of every track in one call; sized again when the first
+  // guess of the output size is too small
   TrackSegments out;
   out.offsets.assign(n + 1, 0);
-  for (size_t i = 0; i < n; ++i) {
-    for (const auto& s : segs[i]) {
-      out.element.push_back(s.first);
-      out.length.push_back(s.second);
-    }
-    out.offsets[i + 1] = (int64_t)out.element.size();
+  int64_t cap = std::max<int64_t>(1024, 64 * (int64_t)n);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    out.element.resize(cap);
+    out.length.resize(cap);
+    rt.check(xdgcu_segments_global(ctx, ipc_surface_tree, rt.global_element_tree_id(), (int64_t)n,
+                                   starts, ends, 4096, max_rounds, cap, out.element.data(),
+                                   out.length.data(), out.offsets.data(), nullptr, prec, nullptr),
+             "segments_global");
+    if (out.offsets[n] <= cap) break;
+    cap = out.offsets[n];
   }
+  out.element.resize(out.offsets[n]);
+  out.length.resize(out.offsets[n]);
   return out;
 }
 

@@ -69,12 +69,12 @@ struct TrackSegments {
 
 // XDG::segments(start, end) (xdg.cpp:142-198) for the n tracks
 // starts[i] -> ends[i] (3 doubles each) across the meshed volumes and the
-// implicit complement between them.  All tracks advance together: each
-// round locates the active tracks in the global element tree
-// (xdgcu_find_element), fires the implicit-complement rays of the tracks
-// outside the mesh (xdgcu_ray_fire, EXITING) and re-enters through the
-// element behind the hit face (MeshManager::get_boundary_face_element), then
-// walks the rest in one packed launch (xdgcu_walk_elements_packed).
+// implicit complement between them, on the device (xdgcu_segments_global):
+// each round locates the active tracks in the global element tree, fires the
+// implicit-complement rays of the tracks outside the mesh (EXITING) and
+// re-enters through the element behind the hit face
+// (MeshManager::get_boundary_face_element, handed to the engine with
+// xdgcu_set_boundary_face_elements), then walks the rest in one packed launch.
 TrackSegments track_segments(CudaRayTracer& rt, const MeshManager& mm, TreeID ipc_surface_tree,
                              size_t n, const double* starts, const double* ends,
                              int max_rounds = 10000);

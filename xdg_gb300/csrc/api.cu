@@ -29,6 +29,7 @@
 #include "bvh.h"
 #include "cbound.h"
 #include "queries.h"
+#include "segments.h"
 #include "walk.h"
 
 using namespace xdgcu;
@@ -363,6 +364,10 @@ struct xdgcu_ctx {
   DevMem<int32_t> d_elem_ids;
   int32_t face[12] = {0};
   int face_order = 0;
+  // MeshManager::get_boundary_face_element for the global track loop:
+  // ascending face ids and the tet index behind each
+  DevMem<int32_t> d_bfe_face, d_bfe_elem;
+  int64_t n_bfe = 0;
   // trees
   std::vector<std::unique_ptr<TreeHost>> surf_trees, elem_trees;
   DevMem<TreeDev> d_surf_trees, d_elem_trees;
@@ -838,6 +843,33 @@ int with_length_order(xdgcu_ctx* c, WalkArgs& a, cudaStream_t s, Body body) {
   a.order = nullptr;
   cudaFreeAsync(buf, s);
   return rc;
+}
+
+// Stream-ordered scratch of one call, freed on every return path.
+struct CallScratch {
+  cudaStream_t st;
+  std::vector<void*> ptrs;
+  explicit CallScratch(cudaStream_t s) : st(s) {}
+  ~CallScratch() {
+    for (void* p : ptrs) cudaFreeAsync(p, st);
+  }
+  template <typename T>
+  cudaError_t get(T** out, int64_t count) {
+    *out = nullptr;
+    void* p = nullptr;
+    const cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (size_t)std::max<int64_t>(1, count), st);
+    if (e != cudaSuccess) return e;
+    ptrs.push_back(p);
+    *out = static_cast<T*>(p);
+    return cudaSuccess;
+  }
+};
+
+// D2H of one counter, waited for.
+cudaError_t read_count(const int32_t* d, int32_t* h, cudaStream_t st) {
+  cudaError_t e = cudaMemcpyAsync(h, d, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e;
 }
 
 // Enqueues one traversal launch with the context's work distribution: when
@@ -1845,6 +1877,255 @@ int xdgcu_walk_elements(xdgcu_ctx* c, int64_t n, const int32_t* start_index, con
                         int32_t precision, void* stream) {
   return walk_query(c, true, n, start_index, start, u, distance, max_segs, seg_elem, seg_len,
                     seg_count, nullptr, nullptr, status, precision, stream);
+}
+
+int xdgcu_set_boundary_face_elements(xdgcu_ctx* c, int64_t n, const int32_t* face_ids,
+                                     const int32_t* elem_index) {
+  CHECK_CTX(c);
+  if (n < 0 || (n > 0 && (!face_ids || !elem_index)))
+    return set_err(XDGCU_ERR_INVALID_ARG, "set_boundary_face_elements: bad arguments");
+  if (!c->has_tets) return set_err(XDGCU_ERR_STATE, "set_boundary_face_elements: no tet mesh set");
+  std::vector<std::pair<int32_t, int32_t>> m;
+  m.reserve((size_t)n);
+  for (int64_t k = 0; k < n; ++k) {
+    if (elem_index[k] < -1 || elem_index[k] >= c->n_tet)
+      return set_err(XDGCU_ERR_INVALID_ARG, "set_boundary_face_elements: tet index out of range");
+    if (elem_index[k] >= 0) m.emplace_back(face_ids[k], elem_index[k]);
+  }
+  std::sort(m.begin(), m.end());
+  for (size_t k = 1; k < m.size(); ++k)
+    if (m[k].first == m[k - 1].first)
+      return set_err(XDGCU_ERR_INVALID_ARG, "set_boundary_face_elements: face id given twice");
+  std::vector<int32_t> f(m.size()), e(m.size());
+  for (size_t k = 0; k < m.size(); ++k) {
+    f[k] = m[k].first;
+    e[k] = m[k].second;
+  }
+  std::lock_guard<std::mutex> g(c->mu);
+  const int64_t cnt = std::max<int64_t>(1, (int64_t)m.size());
+  API_CUDA(c->d_bfe_face.alloc(cnt), "alloc boundary faces");
+  API_CUDA(c->d_bfe_elem.alloc(cnt), "alloc boundary faces");
+  if (!m.empty()) {
+    API_CUDA(cudaMemcpy(c->d_bfe_face.p, f.data(), sizeof(int32_t) * m.size(), cudaMemcpyHostToDevice),
+             "upload boundary faces");
+    API_CUDA(cudaMemcpy(c->d_bfe_elem.p, e.data(), sizeof(int32_t) * m.size(), cudaMemcpyHostToDevice),
+             "upload boundary faces");
+  }
+  c->n_bfe = (int64_t)m.size();
+  return XDGCU_OK;
+}
+
+int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, int64_t n,
+                          const double* starts, const double* ends, int32_t max_segs,
+                          int32_t max_rounds, int64_t capacity, int32_t* seg_elem, double* seg_len,
+                          int64_t* offsets, int32_t* status, int32_t precision, void* stream) {
+  CHECK_CTX(c);
+  if (n < 0 || capacity < 0) return set_err(XDGCU_ERR_INVALID_ARG, "negative size");
+  if (n >= ((int64_t)1 << 31)) return set_err(XDGCU_ERR_INVALID_ARG, "segments_global: n >= 2^31");
+  if (precision != XDGCU_FP64 && precision != XDGCU_MIXED)
+    return set_err(XDGCU_ERR_INVALID_ARG, "precision must be XDGCU_FP64 or XDGCU_MIXED");
+  if (!c->has_tets) return set_err(XDGCU_ERR_STATE, "no tet mesh set");
+  if (!offsets) return set_err(XDGCU_ERR_INVALID_ARG, "segments_global: offsets required");
+  if (max_segs <= 0 || max_rounds <= 0)
+    return set_err(XDGCU_ERR_INVALID_ARG, "segments_global: max_segs and max_rounds must be > 0");
+  if (n > 0 && (!starts || !ends)) return set_err(XDGCU_ERR_INVALID_ARG, "segments_global: null inputs");
+  if (capacity > 0 && (!seg_elem || !seg_len))
+    return set_err(XDGCU_ERR_INVALID_ARG, "segments_global: null segment arrays");
+  if (ipc_tree < 1 || ipc_tree > (int32_t)c->surf_trees.size())
+    return set_err(XDGCU_ERR_NOT_FOUND, "segments_global: no such surface tree");
+  if (element_tree < 1 || element_tree > (int32_t)c->elem_trees.size())
+    return set_err(XDGCU_ERR_NOT_FOUND, "segments_global: no such element tree");
+  const int kind = classify({starts, ends, seg_elem, seg_len, offsets, status});
+  if (kind < 0) return set_err(XDGCU_ERR_INVALID_ARG, "host and device pointers mixed in one call");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 0 && !st) {
+    Slot* sl = get_slot(c);
+    if (!sl) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+    st = sl->stream;
+  }
+  if (n == 0) {
+    if (kind == 0) {
+      offsets[0] = 0;
+      return XDGCU_OK;
+    }
+    API_CUDA(cudaMemsetAsync(offsets, 0, sizeof(int64_t), st), "memset");
+    return XDGCU_OK;
+  }
+  const bool mixed = precision == XDGCU_MIXED;
+  CallScratch S(st);
+  // the caller's arrays, or device images of host arrays
+  const double* d_starts = starts;
+  const double* d_ends = ends;
+  int64_t* d_off = offsets;
+  int32_t* d_status = status;
+  int32_t* d_se = seg_elem;
+  double* d_sl = seg_len;
+  if (kind == 0) {
+    double *ps = nullptr, *pe = nullptr;
+    API_CUDA(S.get(&ps, 3 * n), "segments scratch");
+    API_CUDA(S.get(&pe, 3 * n), "segments scratch");
+    API_CUDA(cudaMemcpyAsync(ps, starts, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st), "H2D");
+    API_CUDA(cudaMemcpyAsync(pe, ends, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st), "H2D");
+    d_starts = ps;
+    d_ends = pe;
+    API_CUDA(S.get(&d_off, n + 1), "segments scratch");
+    d_status = nullptr;
+    API_CUDA(S.get(&d_se, capacity), "segments scratch");
+    API_CUDA(S.get(&d_sl, capacity), "segments scratch");
+  }
+  if (!d_status) API_CUDA(S.get(&d_status, n), "segments scratch");
+  SegState ss{};
+  ss.n = n;
+  ss.status = d_status;
+  API_CUDA(S.get(&ss.r, 3 * n), "segments scratch");
+  API_CUDA(S.get(&ss.u, 3 * n), "segments scratch");
+  API_CUDA(S.get(&ss.dist, n), "segments scratch");
+  API_CUDA(S.get(&ss.written, n), "segments scratch");
+  API_CUDA(S.get(&ss.last, n), "segments scratch");
+  API_CUDA(S.get(&ss.stopped, n), "segments scratch");
+  int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *eid = nullptr, *eidx = nullptr;
+  int32_t *walk_t = nullptr, *walk_start = nullptr, *out_t = nullptr, *surf = nullptr, *face = nullptr;
+  int32_t* wst = nullptr;
+  double *pts = nullptr, *ray_org = nullptr, *ray_dir = nullptr, *t_hit = nullptr;
+  double *wr = nullptr, *wu = nullptr, *wd = nullptr;
+  API_CUDA(S.get(&act, n), "segments scratch");
+  API_CUDA(S.get(&act_next, n), "segments scratch");
+  API_CUDA(S.get(&counters, 4), "segments scratch");
+  API_CUDA(S.get(&eid, n), "segments scratch");
+  API_CUDA(S.get(&eidx, n), "segments scratch");
+  API_CUDA(S.get(&walk_t, n), "segments scratch");
+  API_CUDA(S.get(&walk_start, n), "segments scratch");
+  API_CUDA(S.get(&out_t, n), "segments scratch");
+  API_CUDA(S.get(&surf, n), "segments scratch");
+  API_CUDA(S.get(&face, n), "segments scratch");
+  API_CUDA(S.get(&wst, n), "segments scratch");
+  API_CUDA(S.get(&pts, 3 * n), "segments scratch");
+  API_CUDA(S.get(&ray_org, 3 * n), "segments scratch");
+  API_CUDA(S.get(&ray_dir, 3 * n), "segments scratch");
+  API_CUDA(S.get(&t_hit, n), "segments scratch");
+  API_CUDA(S.get(&wr, 3 * n), "segments scratch");
+  API_CUDA(S.get(&wu, 3 * n), "segments scratch");
+  API_CUDA(S.get(&wd, n), "segments scratch");
+  int32_t* n_act = counters;
+  int32_t* n_walk = counters + 1;
+  int32_t* n_out = counters + 2;
+  // one record per round for the final placement of its segments
+  struct Round {
+    int64_t m, total;
+    int32_t* walk_t;
+    int64_t *off, *dst_rel;
+    int32_t* seg_elem;
+    double* seg_len;
+  };
+  std::vector<Round> rounds;
+  API_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(int32_t), st), "memset");
+  API_CUDA(seg_init(ss, d_starts, d_ends, act, n_act, st), "segments init");
+  int32_t m = 0;
+  API_CUDA(read_count(n_act, &m, st), "segments count");
+  WalkArgs geo{};
+  {
+    int fo = 0, dev = 0;
+    if (const char* msg = walk_args_for(c, &geo, &fo, &dev)) return set_err(XDGCU_ERR_STATE, msg);
+  }
+  int32_t round = 0;
+  for (; m > 0 && round < max_rounds; ++round) {
+    // find_element(r) in the element tree
+    API_CUDA(seg_gather_points(ss, act, m, pts, st), "segments gather");
+    int rc = xdgcu_find_element(c, element_tree, nullptr, m, pts, eid, eidx, nullptr, precision, st);
+    if (rc) return rc;
+    API_CUDA(cudaMemsetAsync(counters + 1, 0, 2 * sizeof(int32_t), st), "memset");
+    API_CUDA(seg_decide(ss, act, m, eid, eidx, walk_t, walk_start, n_walk, out_t, ray_org, ray_dir,
+                        n_out, st),
+             "segments decide");
+    int32_t h2[2] = {0, 0};
+    API_CUDA(cudaMemcpyAsync(h2, counters + 1, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "D2H");
+    API_CUDA(cudaStreamSynchronize(st), "sync");
+    int32_t m_walk = h2[0];
+    const int32_t m_out = h2[1];
+    if (m_out > 0) {
+      // ray_fire(ipc, r + u * TINY_BIT, u, INFTY, EXITING), then re-entry
+      rc = xdgcu_ray_fire(c, ipc_tree, nullptr, m_out, ray_org, ray_dir, nullptr, XDGCU_EXITING,
+                          nullptr, nullptr, t_hit, surf, face, nullptr, precision, st);
+      if (rc) return rc;
+      API_CUDA(seg_reenter(ss, out_t, m_out, t_hit, surf, face, c->d_bfe_face.p, c->d_bfe_elem.p,
+                           c->n_bfe, (int32_t)c->n_tet, walk_t, walk_start, n_walk, st),
+               "segments re-entry");
+      API_CUDA(read_count(n_walk, &m_walk, st), "segments count");
+    }
+    API_CUDA(cudaMemsetAsync(n_act, 0, sizeof(int32_t), st), "memset");
+    if (m_walk > 0) {
+      Round R{};
+      R.m = m_walk;
+      API_CUDA(S.get(&R.walk_t, m_walk), "segments scratch");
+      API_CUDA(S.get(&R.off, (int64_t)m_walk + 1), "segments scratch");
+      API_CUDA(S.get(&R.dst_rel, m_walk), "segments scratch");
+      API_CUDA(cudaMemcpyAsync(R.walk_t, walk_t, sizeof(int32_t) * m_walk, cudaMemcpyDeviceToDevice, st),
+               "D2D");
+      API_CUDA(seg_walk_inputs(ss, walk_t, m_walk, wr, wu, wd, st), "segments walk inputs");
+      // walk_elements(element, r, u, distance) of the round, packed
+      WalkArgs a = geo;
+      a.n = m_walk;
+      a.start = walk_start;
+      a.org = wr;
+      a.dir = wu;
+      a.dist = wd;
+      a.max_segs = max_segs;
+      a.status = wst;
+      a.offsets = R.off;
+      rc = with_length_order(c, a, st, [&]() -> int {
+        a.out_mode = WALK_COUNT;
+        API_CUDA(launch_walk(mixed, c->face_order, a, st), "walk (count)");
+        int64_t* sums = nullptr;
+        API_CUDA(S.get(&sums, scan_scratch_entries(m_walk)), "scan scratch");
+        API_CUDA(scan_offsets(R.off, m_walk, sums, st), "scan");
+        API_CUDA(cudaMemcpyAsync(&R.total, R.off + m_walk, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
+                 "D2H");
+        API_CUDA(cudaStreamSynchronize(st), "sync");
+        API_CUDA(S.get(&R.seg_elem, R.total), "segments scratch");
+        API_CUDA(S.get(&R.seg_len, R.total), "segments scratch");
+        a.seg_elem = R.seg_elem;
+        a.seg_len = R.seg_len;
+        a.capacity = R.total;
+        a.out_mode = WALK_PACKED;
+        API_CUDA(launch_walk(mixed, c->face_order, a, st), "walk (emit)");
+        return XDGCU_OK;
+      });
+      if (rc) return rc;
+      API_CUDA(seg_advance(ss, R.walk_t, m_walk, R.off, R.seg_elem, R.seg_len, wst, R.dst_rel,
+                           act_next, n_act, st),
+               "segments advance");
+      rounds.push_back(R);
+    }
+    API_CUDA(read_count(n_act, &m, st), "segments count");
+    std::swap(act, act_next);
+  }
+  if (m > 0) API_CUDA(seg_stop_active(ss, act, m, XDGCU_RAY_WALK_LIMIT, st), "segments stop");
+  // offsets from the per-track totals, then every round's segments to their place
+  API_CUDA(seg_counts(ss, d_off, st), "segments counts");
+  {
+    int64_t* sums = nullptr;
+    API_CUDA(S.get(&sums, scan_scratch_entries(n)), "scan scratch");
+    API_CUDA(scan_offsets(d_off, n, sums, st), "scan");
+  }
+  API_CUDA(seg_mark_full(ss, d_off, capacity, st), "segments capacity");
+  for (const Round& R : rounds)
+    API_CUDA(seg_scatter(ss, R.walk_t, R.m, R.off, R.dst_rel, R.seg_elem, R.seg_len, d_off, capacity,
+                         d_se, d_sl, st),
+             "segments scatter");
+  if (kind == 0) {
+    API_CUDA(cudaMemcpyAsync(offsets, d_off, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, st),
+             "D2H");
+    if (status)
+      API_CUDA(cudaMemcpyAsync(status, d_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st), "D2H");
+    API_CUDA(cudaStreamSynchronize(st), "sync");
+    const int64_t used = std::min(offsets[n], capacity);
+    if (used > 0) {
+      API_CUDA(cudaMemcpyAsync(seg_elem, d_se, sizeof(int32_t) * used, cudaMemcpyDeviceToHost, st), "D2H");
+      API_CUDA(cudaMemcpyAsync(seg_len, d_sl, sizeof(double) * used, cudaMemcpyDeviceToHost, st), "D2H");
+      API_CUDA(cudaStreamSynchronize(st), "sync");
+    }
+  }
+  return XDGCU_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -530,6 +530,33 @@ class CudaRayTracer:
         return se, sl, off, st
 
 
+    def set_boundary_face_elements(self, face_ids, elem_index):
+        """MeshManager::get_boundary_face_element for the global track loop:
+        face mesh id -> tet index behind it (-1: none)."""
+        f = _host(face_ids, np.int32)
+        e = _host(elem_index, np.int32)
+        self._check(self.L.xdgcu_set_boundary_face_elements(self.ctx, len(f), _addr(f), _addr(e)),
+                    "set_boundary_face_elements")
+
+    def segments_global(self, ipc_tree, element_tree, starts, ends, capacity, max_segs=4096,
+                        max_rounds=10_000, precision=MIXED, stream=None):
+        """xdgcu_segments_global: XDG::segments(start, end) for n tracks on the
+        device.  Returns (seg_elem [capacity], seg_len, offsets [n+1], status)."""
+        s = _prep(starts, np.float64, 3)
+        e = _prep(ends, np.float64, 3)
+        n = s.shape[0]
+        out = _Out(s)
+        se, sl, st = out.i32(max(1, capacity)), out.f64(max(1, capacity)), out.i32(n)
+        off = out.empty(n + 1, out._torch.int64 if out.torch else np.int64)
+        self._check(self.L.xdgcu_segments_global(self.ctx, int(ipc_tree), int(element_tree), n,
+                                                 _addr(s), _addr(e), int(max_segs), int(max_rounds),
+                                                 int(capacity), _addr(se), _addr(sl), _addr(off),
+                                                 _addr(st), int(precision),
+                                                 stream if stream is not None else out.stream()),
+                    "segments_global")
+        return se, sl, off, st
+
+
 class XDG:
     """The XDG facade (src/xdg.cpp) over a model and the CUDA ray tracer."""
 
@@ -550,12 +577,18 @@ class XDG:
         self.volume_to_point_location_tree[volume] = et
 
     def prepare_raytracer(self):
-        """xdg.cpp:37-47."""
+        """xdg.cpp:37-47; also hands the engine the mesh's boundary-face
+        elements (MeshManager::get_boundary_face_element) for the global
+        track loop."""
         for v in self.model.volumes:
             self.prepare_volume_for_raytracing(v)
         self.rti.create_global_element_tree()
         self.rti.create_global_surface_tree()
         self.rti.init()
+        bfe = self.model.boundary_face_element
+        if bfe is not None and self.model.tets is not None and len(bfe):
+            bfe = np.asarray(bfe, dtype=np.int32)
+            self.rti.set_boundary_face_elements(np.arange(len(bfe), dtype=np.int32), bfe)
 
     def _trees(self, volumes):
         """Surface tree of each ray's volume (NumPy, or a torch tensor on the
@@ -678,82 +711,26 @@ class XDG:
         return out
 
 
-    def segments_global(self, starts, ends, precision=MIXED, max_rounds=10_000):
+    def segments_global(self, starts, ends, precision=MIXED, max_rounds=10_000, max_segs=4096):
         """XDG::segments(start, end) (xdg.cpp:142-198) for n tracks: walks the
         tet mesh from element to element and, where the track leaves the mesh,
         fires a ray in the implicit complement to the next boundary face and
         re-enters through the element behind it
-        (MeshManager::get_boundary_face_element).
-
-        All tracks advance together: each round locates the active tracks,
-        fires the implicit-complement rays of those outside the mesh, and
-        walks the rest in one batch.  Returns (elements, lengths, offsets):
-        the segments of track i are [offsets[i], offsets[i+1])."""
-        s = _host(starts, np.float64, (-1, 3))
-        e = _host(ends, np.float64, (-1, 3))
-        n = len(s)
-        bfe = self.model.boundary_face_element
+        (MeshManager::get_boundary_face_element).  One device call
+        (xdgcu_segments_global) runs every round of every track.  Returns
+        (elements, lengths, offsets): the segments of track i are
+        [offsets[i], offsets[i+1]); device arrays for CUDA tensor inputs."""
         ipc_tree = self.volume_to_surface_tree[self.model.implicit_complement]
         gtree = self.rti.global_element_tree
-        # Direction u = end - start; distance = u.length(); u /= distance
-        u = e - s
-        dist = np.sqrt(u[:, 0] * u[:, 0] + u[:, 1] * u[:, 1] + u[:, 2] * u[:, 2])
-        with np.errstate(invalid="ignore", divide="ignore"):
-            u = u / dist[:, None]
-        r = s.copy()
-        last = np.full(n, -2, dtype=np.int64)  # mesh id of the last segment, -2: none yet
-        active = np.nonzero(dist > 0)[0]
-        pieces = []  # (round, track index, element ids, lengths)
-        rnd = 0
-        while len(active) and rnd < max_rounds:
-            eid, eidx = self.rti.find_element(gtree, r[active], precision)
-            cur = np.asarray(eidx, dtype=np.int64).copy()
-            cur[(last[active] != -2) & (np.asarray(eid) == last[active])] = -1
-            out = np.nonzero(cur < 0)[0]
-            keep = np.ones(len(active), dtype=bool)
-            if len(out):
-                j = active[out]
-                o = r[j] + u[j] * TINY_BIT
-                t, surf, face = self.rti.ray_fire(ipc_tree, o, u[j], None, EXITING,
-                                                  [[] for _ in range(len(j))], precision)
-                stop = (surf == ID_NONE) | (t > dist[j])
-                keep[out[stop]] = False
-                ok = np.nonzero(~stop)[0]
-                hd = t[ok] + TINY_BIT
-                jj = j[ok]
-                r[jj] = r[jj] + u[jj] * hd[:, None]
-                dist[jj] = dist[jj] - hd
-                nb = bfe[face[ok]] if bfe is not None else np.full(len(ok), -1)
-                cur[out[ok]] = nb
-                keep[out[ok][nb < 0]] = False  # hit a face with no element behind it
-            w = np.nonzero(keep)[0]
-            active = active[w]
-            cur = cur[w]
-            if len(active) == 0:
-                break
-            se, sl, off = self._walk_packed(cur, r[active], u[active], dist[active], precision)
-            cnt = np.diff(off)
-            # segment_sum: std::accumulate over this walk's segments, in order
-            ssum = np.zeros(len(active))
-            for k in range(int(cnt.max()) if len(cnt) else 0):
-                has = np.nonzero(cnt > k)[0]
-                ssum[has] = ssum[has] + sl[off[has] + k]
-            pieces.append((np.repeat(active, cnt), se, sl))
-            r[active] = r[active] + u[active] * ssum[:, None]
-            dist[active] = dist[active] - ssum
-            if len(se):
-                last[active] = np.where(cnt > 0, se[np.maximum(off[1:] - 1, 0)], last[active])
-            active = active[dist[active] > 0]
-            rnd += 1
-        if not pieces:
-            return (np.zeros(0, dtype=np.int32), np.zeros(0), np.zeros(n + 1, dtype=np.int64))
-        trk = np.concatenate([p[0] for p in pieces])
-        order = np.argsort(trk, kind="stable")
-        el = np.concatenate([p[1] for p in pieces])[order]
-        ln = np.concatenate([p[2] for p in pieces])[order]
-        offsets = np.zeros(n + 1, dtype=np.int64)
-        offsets[1:] = np.cumsum(np.bincount(trk, minlength=n))
-        return el, ln, offsets
+        n = len(starts)
+        cap = max(1024, 64 * n)
+        args = (ipc_tree, gtree, starts, ends)
+        se, sl, off, st = self.rti.segments_global(*args, cap, max_segs, max_rounds, precision)
+        total = int(off[-1])
+        if total > cap:
+            se, sl, off, st = self.rti.segments_global(*args, total, max_segs, max_rounds,
+                                                       precision)
+        return se[:total], sl[:total], off
 
     def walk_particles(self, elem_index, pos, dirs, rng, mfp=1.0, max_events=1_000_000,
                        precision=MIXED, tally=False, max_reentries=64):
@@ -946,19 +923,6 @@ class XDG:
                                     org[2] + th * dirv[2]])
                     found.setdefault(frozenset({parents[int(sh_all[j])][0], pf}), loc)
         return found
-
-    def _walk_packed(self, elem_index, r, u, dist, precision):
-        """Packed walk of host arrays sized in one pass when the first guess
-        of the output size is too small.  Returns (mesh ids, lengths, offsets)."""
-        n = len(r)
-        cap = max(1024, 64 * n)
-        se, sl, off, st = self.rti.walk_elements_packed(elem_index, r, u, dist, cap,
-                                                        precision=precision)
-        if off[-1] > cap:
-            cap = int(off[-1])
-            se, sl, off, st = self.rti.walk_elements_packed(elem_index, r, u, dist, cap,
-                                                            precision=precision)
-        return se[:off[-1]], sl[:off[-1]], off
 
 
 def _normalize_rows(v):
