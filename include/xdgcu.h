@@ -460,6 +460,14 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      default 2)
  *   "node_width"       children per BVH node for trees built (or rebuilt,
  *                      xdgcu_rebuild_trees) afterwards: 4 (default) or 8
+ *   "bvh_sah"          how trees built afterwards group the binary tree's
+ *                      nodes into wide nodes: 1 (default) at the least
+ *                      surface-area cost (a dynamic program over the binary
+ *                      tree), 0 greedily opening the largest child.  Results
+ *                      do not depend on it
+ *   "bvh_prim_cost"    cost of one primitive test relative to one wide-node
+ *                      visit in that surface-area cost, in thousandths
+ *                      (1..100000, default 300)
  *   "walk_queue"       mixed-precision walk: 1 runs the FP64 face tests of a
  *                      warp's tracks 32 at a time from a per-warp queue, 0
  *                      (default) lets each lane evaluate its own faces

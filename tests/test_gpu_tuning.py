@@ -123,7 +123,8 @@ def test_bad_settings_rejected(nested):
     _, x, _, _, _ = nested
     for k, v in [("trace_stack", 12), ("trace_stack", 50), ("trace_stack", 72),
                  ("trace_grab", 33), ("trace_grab", -32), ("trace_sort_min", -1),
-                 ("closest_bound", 2), ("trace_edge_table", -1)]:
+                 ("closest_bound", 2), ("trace_edge_table", -1), ("bvh_sah", 2),
+                 ("bvh_prim_cost", 0)]:
         with pytest.raises(Exception):
             x.rti.set_tuning(k, v)
     assert set(x.rti.tuning()) == set(TUNING_KEYS)
@@ -228,6 +229,66 @@ def test_node_width_8(cuda, oracle, prec):
     assert x8.rti.tree_info(1)["width"] == 4
     for a, b, what in zip(x8.ray_fire(vols, p, d, precision=prec), r4, ("t", "surface", "face")):
         assert_same(a, b, "rebuilt " + what)
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+@pytest.mark.parametrize("width", [4, 8])
+def test_sah_and_greedy_collapse(cuda, oracle, prec, width):
+    """Trees whose wide nodes are chosen by the surface-area cost (bvh_sah 1,
+    the default, at two primitive costs) and greedily (bvh_sah 0) give the
+    same ids and distances for every query, equal to the oracle; the SAH
+    trees visit fewer nodes."""
+    m = synth.nested_spheres(n=8, level=4, jitter=1e-3, seed=7)
+    rng = np.random.default_rng(29)
+    n = 60_000
+    p = rng.uniform(-9, 9, (n, 3))
+    d = synth.isotropic_dirs(rng, n)
+    res = {}
+    nodes = {}
+    for sah, cost in ((0, 300), (1, 300), (1, 1500)):
+        x = XDG(m)
+        x.rti.set_tuning("node_width", width)
+        x.rti.set_tuning("bvh_sah", sah)
+        x.rti.set_tuning("bvh_prim_cost", cost)
+        x.prepare_raytracer()
+        vols = x.find_volume(p, d, precision=prec)
+        x.rti.set_counting(True)
+        rf = x.ray_fire(vols, p, d, precision=prec)
+        nodes[(sah, cost)] = x.rti.counters()["node"]
+        x.rti.set_counting(False)
+        res[(sah, cost)] = (vols, rf, x.point_in_volume(5, p, precision=prec),
+                            x.closest(3, p[:5000], precision=prec),
+                            x.occluded(2, p, d, precision=prec))
+    ref = res[(0, 300)]
+    for key, r in res.items():
+        assert_same(r[0], ref[0], f"find_volume {key}")
+        for a, b, what in zip(r[1], ref[1], ("t", "surface", "face")):
+            assert_same(a, b, f"{what} {key}")
+        assert_same(r[2], ref[2], f"piv {key}")
+        assert_same(r[3][0], ref[3][0], f"closest distance {key}")
+        assert_same(r[3][1], ref[3][1], f"closest face {key}")
+        assert_same(r[4][0], ref[4][0], f"occluded {key}")
+    vols = ref[0]
+    k = np.nonzero(vols[:5000] == 4)[0]
+    ot, os_, of = oracle.volume_tree(m, 4).ray_fire(p[k], d[k])
+    assert_same(res[(1, 300)][1][0][k], ot, "t vs oracle")
+    assert_same(res[(1, 300)][1][2][k], of, "face vs oracle")
+    assert nodes[(1, 300)] < nodes[(0, 300)]
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_sah_element_trees(cuda, prec):
+    tm = synth.tet_cube(n=12, size=10.0, jitter=0.2, seed=11)
+    m = synth.model_from_tets(tm, np.ones(len(tm.conn), dtype=np.int32))
+    out = []
+    for sah in (0, 1):
+        x = XDG(m)
+        x.rti.set_tuning("bvh_sah", sah)
+        x.prepare_raytracer()
+        rng = np.random.default_rng(5)
+        out.append(x.find_element(rng.uniform(-0.5, 10.5, (50_000, 3)), precision=prec))
+    assert_same(out[0][0], out[1][0], "element id")
+    assert_same(out[0][1], out[1][1], "element index")
 
 
 @pytest.mark.parametrize("prec", [FP64, MIXED])

@@ -390,6 +390,8 @@ struct xdgcu_ctx {
   int32_t transport_event_wait = 4;  // walk_elements tool loop (mixed): the same
   int32_t leaf_max = 2;
   int32_t node_width = 4;        // children per BVH node (4 or 8) of trees built afterwards
+  int32_t bvh_sah = 1;           // trees built afterwards: SAH collapse (1) or greedy (0)
+  int32_t bvh_prim_cost = 300;   // SAH: primitive test / wide-node visit, in thousandths
   int32_t walk_queue = 0;
   int32_t walk_flush_wait = 8;
   // host arrays the kernels address directly instead of staging them:
@@ -537,7 +539,10 @@ int build_surface_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tri
     API_CUDA(cudaGetLastError(), "triangle boxes");
   }
   BuiltTree b;
-  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, st, &b), "bvh build");
+  const BvhCost cost{1.0, c->bvh_prim_cost * 1e-3};
+  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, c->bvh_sah ? &cost : nullptr,
+                          st, &b),
+           "bvh build");
   API_CUDA(t.prim32.alloc(3 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim64.alloc(kPrim64Stride * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
@@ -567,7 +572,10 @@ int build_element_bvh(xdgcu_ctx* c, TreeHost& t, const std::vector<int32_t>& tet
     API_CUDA(cudaGetLastError(), "tet boxes");
   }
   BuiltTree b;
-  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, st, &b), "bvh build");
+  const BvhCost cost{1.0, c->bvh_prim_cost * 1e-3};
+  API_CUDA(build_wide_bvh(d_box.p, n, c->leaf_max, c->node_width, c->bvh_sah ? &cost : nullptr,
+                          st, &b),
+           "bvh build");
   API_CUDA(t.prim64.alloc(12 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim32.alloc(4 * (int64_t)std::max(1, n)), "alloc prims");
   API_CUDA(t.prim_ref.alloc(std::max(1, n)), "alloc prims");
@@ -1305,6 +1313,13 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "leaf_max") {
     if (value < 1 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "leaf_max must be 1..4");
     c->leaf_max = (int32_t)value;
+  } else if (k == "bvh_sah") {
+    if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "bvh_sah must be 0 or 1");
+    c->bvh_sah = (int32_t)value;
+  } else if (k == "bvh_prim_cost") {
+    if (value < 1 || value > 100000)
+      return set_err(XDGCU_ERR_INVALID_ARG, "bvh_prim_cost must be 1..100000");
+    c->bvh_prim_cost = (int32_t)value;
   } else if (k == "walk_queue") {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "walk_queue must be 0 or 1");
     c->walk_queue = (int32_t)value;
@@ -1346,6 +1361,8 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "transport_event_wait") *value = c->transport_event_wait;
   else if (k == "leaf_max") *value = c->leaf_max;
   else if (k == "node_width") *value = c->node_width;
+  else if (k == "bvh_sah") *value = c->bvh_sah;
+  else if (k == "bvh_prim_cost") *value = c->bvh_prim_cost;
   else if (k == "walk_queue") *value = c->walk_queue;
   else if (k == "walk_flush_wait") *value = c->walk_flush_wait;
   else if (k == "walk_sort_min") *value = c->walk_sort_min;

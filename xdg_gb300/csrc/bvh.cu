@@ -9,12 +9,24 @@
 //      primitive position so the tree is well formed for duplicates
 //   5. bottom-up box refit: one thread per leaf climbs, the second thread to
 //      reach a node computes its box (atomic arrival counter)
-//   6. collapse to W-wide nodes (W = 4 or 8) top-down, one level per launch:
-//      a wide node repeatedly opens the child with the largest surface area
-//      (the SAH weight) until it has W children; subtrees with at most
-//      leaf_max primitives become leaves (they are contiguous in sorted
-//      order).  An 8-wide node is stored as two consecutive 4-wide records
-//      (children 0-3 and 4-7), so node index k occupies records 2k and 2k+1.
+//   6. collapse to W-wide nodes (W = 4 or 8) top-down, one level per launch,
+//      either
+//      (a) by the SAH: a bottom-up dynamic program over the binary tree
+//          (the optimal wide-BVH conversion of Ylitie, Karras and Laine,
+//          "Efficient incoherent ray traversal on GPUs through compressed
+//          wide BVHs", HPG 2017) finds, for every binary node and every
+//          number of child slots k <= W, the cheapest way to cover its
+//          subtree with k slots, each a leaf of <= leaf_max primitives or a
+//          wide node, under the cost  sum over wide nodes of area * C_node
+//          + sum over leaves of area * primitives * C_prim;  the collapse
+//          then reads each wide node's children off the stored decisions;
+//      or (b) greedily: a wide node repeatedly opens the child with the
+//          largest surface area until it has W children; subtrees with at
+//          most leaf_max primitives become leaves.
+//      Leaves are binary subtrees, so their primitives are contiguous in
+//      sorted order.  An 8-wide node is stored as two consecutive 4-wide
+//      records (children 0-3 and 4-7), so node index k occupies records 2k
+//      and 2k+1.
 // Every loop is bounded by the primitive count; no thread waits on another.
 #include <cub/device/device_radix_sort.cuh>
 
@@ -188,9 +200,156 @@ __device__ __forceinline__ double half_area(const double* b) {
   return dx * dy + dy * dz + dz * dx;
 }
 
+// ---- SAH collapse ------------------------------------------------------
+//
+// Per binary node c (inner c < n-1, leaf n-1+j) and k = 1..W slots:
+//   S[c][k-1]  the least cost of covering c's subtree with at most k slots;
+//   dec[c][k-1] for k = 1: 1 when c is best a wide node, 0 a leaf; for k >= 2:
+//              0 when S[c][k-1] = S[c][k-2] (fewer slots suffice), else the
+//              number of slots j (1..k-1) given to the left child (the rest to
+//              the right).
+// For a wide node at c the children are the slots of (left, j), (right, W-j)
+// with j = split[c], the best division of W slots.
+constexpr int kSahW = 8;
+constexpr float kInfCost = 3.0e38f;
+
+struct SahArgs {
+  const int32_t* left;
+  const int32_t* right;
+  const int32_t* parent;
+  const int32_t* first;
+  const int32_t* last;
+  const double* nbox;
+  int32_t n;
+  int32_t leaf_max;
+  int32_t width;
+  float c_node, c_prim;
+  float* S;         // width per binary node
+  uint8_t* dec;     // width per binary node
+  uint8_t* split;   // per inner node: slots of the left child in a wide node at it
+  int32_t* flag;
+};
+
+__device__ __forceinline__ float node_area(const double* nbox, int32_t c) {
+  const double* b = nbox + 6 * (int64_t)c;
+  const double dx = b[3] - b[0], dy = b[4] - b[1], dz = b[5] - b[2];
+  return (float)(dx * dy + dy * dz + dz * dx);
+}
+
+// S and dec of inner node p from its children's tables (already complete).
+__device__ void sah_node(const SahArgs& A, int32_t p) {
+  const int W = A.width;
+  const int32_t l = A.left[p], r = A.right[p];
+  float Sl[kSahW], Sr[kSahW];
+  for (int k = 0; k < W; ++k) {
+    Sl[k] = __ldcg(&A.S[(int64_t)l * W + k]);
+    Sr[k] = __ldcg(&A.S[(int64_t)r * W + k]);
+  }
+  // D[j-1]: best cost of spreading p's subtree over exactly-at-most j >= 2
+  // slots, j1[j-1] the left child's share
+  float D[kSahW];
+  uint8_t j1[kSahW];
+  for (int j = 2; j <= W; ++j) {
+    float best = kInfCost;
+    int bk = 1;
+    for (int k = 1; k < j; ++k) {
+      const float v = Sl[k - 1] + Sr[j - k - 1];
+      if (v < best) {
+        best = v;
+        bk = k;
+      }
+    }
+    D[j - 1] = best;
+    j1[j - 1] = (uint8_t)bk;
+  }
+  const float area = node_area(A.nbox, p);
+  const int32_t cnt = A.last[p] - A.first[p] + 1;
+  const float c_leaf = cnt <= A.leaf_max ? area * A.c_prim * (float)cnt : kInfCost;
+  const float c_wide = area * A.c_node + D[W - 1];
+  float Sp[kSahW];
+  uint8_t dp[kSahW];
+  Sp[0] = c_leaf <= c_wide ? c_leaf : c_wide;
+  dp[0] = c_leaf <= c_wide ? 0 : 1;
+  for (int k = 2; k <= W; ++k) {
+    if (D[k - 1] < Sp[k - 2]) {
+      Sp[k - 1] = D[k - 1];
+      dp[k - 1] = j1[k - 1];
+    } else {
+      Sp[k - 1] = Sp[k - 2];
+      dp[k - 1] = 0;
+    }
+  }
+  for (int k = 0; k < W; ++k) {
+    __stcg(&A.S[(int64_t)p * W + k], Sp[k]);
+    A.dec[(int64_t)p * W + k] = dp[k];
+  }
+  A.split[p] = j1[W - 1];
+}
+
+// Bottom-up over the binary tree, one thread per leaf; the second thread to
+// reach a node evaluates it (as k_refit).
+__global__ void k_sah(SahArgs A) {
+  const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= A.n) return;
+  const int W = A.width;
+  const int32_t leaf = A.n - 1 + j;
+  const float c = node_area(A.nbox, leaf) * A.c_prim;
+  for (int k = 0; k < W; ++k) {
+    __stcg(&A.S[(int64_t)leaf * W + k], c);
+    A.dec[(int64_t)leaf * W + k] = 0;
+  }
+  __threadfence();
+  int32_t p = A.parent[leaf];
+  while (p >= 0) {
+    if (atomicAdd(&A.flag[p], 1) == 0) return;
+    __threadfence();
+    sah_node(A, p);
+    __threadfence();
+    p = A.parent[p];
+  }
+}
+
+// The children of a wide node at binary node b: the slots of (left, split)
+// and (right, W - split), each expanded by the stored decisions.
+template <int W>
+__device__ int sah_children(const SahArgs& A, int32_t b, int32_t* ch) {
+  int32_t sn[2 * W];
+  int sk[2 * W];
+  int top = 0, cnt = 0;
+  const int s = A.split[b];
+  sn[top] = A.right[b];
+  sk[top++] = W - s;
+  sn[top] = A.left[b];
+  sk[top++] = s;
+  while (top > 0 && cnt < W) {
+    int32_t c = sn[--top];
+    int k = sk[top];
+    while (true) {
+      if (c >= A.n - 1 || k <= 1) {  // a binary leaf, or one slot: c itself
+        ch[cnt++] = c;
+        break;
+      }
+      const int d = A.dec[(int64_t)c * W + (k - 1)];
+      if (d == 0) {  // fewer slots are as cheap
+        --k;
+        continue;
+      }
+      if (top + 1 >= 2 * W) {  // cannot happen: each expansion adds one slot
+        ch[cnt++] = c;
+        break;
+      }
+      sn[top] = A.right[c];
+      sk[top++] = k - d;
+      c = A.left[c];
+      k = d;
+    }
+  }
+  return cnt;
+}
+
 template <int W>
 __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t n_in,
-                           int2* __restrict__ out) {
+                           int2* __restrict__ out, SahArgs sah, int use_sah) {
   int32_t it = blockIdx.x * blockDim.x + threadIdx.x;
   if (it >= n_in) return;
   const int32_t b = in[it].x, w = in[it].y;
@@ -201,7 +360,8 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t 
   int cnt = 2;
   ch[0] = A.left[b];
   ch[1] = A.right[b];
-  while (cnt < W) {
+  if (use_sah) cnt = sah_children<W>(sah, b, ch);
+  while (!use_sah && cnt < W) {
     int best = -1;
     double best_area = -1.0;
     for (int k = 0; k < cnt; ++k) {
@@ -237,7 +397,9 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t 
         f32[2 * a + 1][kk] = __double2float_ru(bx[3 + a]);
       }
       const int32_t cc = count_of(c);
-      if (!is_inner(c) || cc <= A.leaf_max) {
+      const bool leaf = use_sah ? (!is_inner(c) || sah.dec[(int64_t)c * W] == 0)
+                                : (!is_inner(c) || cc <= A.leaf_max);
+      if (leaf) {
         const int32_t f = is_inner(c) ? A.first[c] : c - (n - 1);
         refs[kk] = make_leaf(f, cc);
       } else {
@@ -272,7 +434,7 @@ __global__ void k_collapse(CollapseArgs A, const int2* __restrict__ in, int32_t 
   } while (0)
 
 cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, int32_t width,
-                           cudaStream_t st, BuiltTree* out) {
+                           const BvhCost* sah_cost, cudaStream_t st, BuiltTree* out) {
   if (width != 4 && width != 8) return cudaErrorInvalidValue;
   out->width = width;
   out->n32 = nullptr;
@@ -368,6 +530,25 @@ cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, i
     return cudaSuccess;
   }
 
+  // SAH costs of every binary node (bottom-up), when the collapse uses them
+  const bool use_sah = sah_cost != nullptr;
+  DevMem<float> sahS(use_sah ? (int64_t)nb * width : 0);
+  DevMem<uint8_t> sahD(use_sah ? (int64_t)nb * width : 0), sahSplit(use_sah ? n - 1 : 0);
+  DevMem<int32_t> flag2(use_sah ? n - 1 : 0);
+  SahArgs sah{};
+  if (use_sah) {
+    BVH_CHECK(sahS.alloc());
+    BVH_CHECK(sahD.alloc());
+    BVH_CHECK(sahSplit.alloc());
+    BVH_CHECK(flag2.alloc());
+    BVH_CHECK(cudaMemsetAsync(flag2.p, 0, sizeof(int32_t) * (n - 1), st));
+    sah = SahArgs{left.p, right.p, parent.p, first.p, last.p, nbox.p, n, leaf_max, width,
+                  (float)sah_cost->node, (float)sah_cost->prim, sahS.p, sahD.p, sahSplit.p,
+                  flag2.p};
+    k_sah<<<G, B, 0, st>>>(sah);
+    BVH_CHECK(cudaGetLastError());
+  }
+
   // collapse, level by level
   const int32_t cap = n;  // inner wide nodes < n
   const int64_t recs = (int64_t)cap * (width / kWidth);
@@ -391,9 +572,9 @@ cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, i
   while (n_in > 0) {
     BVH_CHECK(cudaMemsetAsync(counters.p + 1, 0, sizeof(int32_t), st));
     if (width == 8)
-      k_collapse<8><<<(n_in + 127) / 128, 128, 0, st>>>(A, qin, n_in, qout);
+      k_collapse<8><<<(n_in + 127) / 128, 128, 0, st>>>(A, qin, n_in, qout, sah, use_sah ? 1 : 0);
     else
-      k_collapse<4><<<(n_in + 127) / 128, 128, 0, st>>>(A, qin, n_in, qout);
+      k_collapse<4><<<(n_in + 127) / 128, 128, 0, st>>>(A, qin, n_in, qout, sah, use_sah ? 1 : 0);
     BVH_CHECK(cudaGetLastError());
     BVH_CHECK(cudaMemcpyAsync(hc, counters.p, sizeof hc, cudaMemcpyDeviceToHost, st));
     BVH_CHECK(cudaStreamSynchronize(st));

@@ -65,8 +65,17 @@ struct BuiltTree {
   double bounds[6];  // union of the primitive boxes
 };
 
+// Cost weights of the SAH collapse: a wide node visited (node) and a
+// primitive tested (prim), per unit of surface area.
+struct BvhCost {
+  double node;
+  double prim;
+};
+
 // d_boxes: 6 doubles per primitive (lo.xyz, hi.xyz), already dilated.
+// sah_cost: collapse by the SAH (bvh.cu, step 6a), or nullptr for the greedy
+// largest-area collapse (6b).
 cudaError_t build_wide_bvh(const double* d_boxes, int32_t n, int32_t leaf_max, int32_t width,
-                           cudaStream_t st, BuiltTree* out);
+                           const BvhCost* sah_cost, cudaStream_t st, BuiltTree* out);
 
 }  // namespace xdgcu
