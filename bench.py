@@ -1040,12 +1040,22 @@ def run_engine(args, rank, world, local):
         return dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world)
 
     e2e_steps = max(3, args.steps // 2)
-    e2e_transfer = ("page-locked host arrays read and written in place by the kernel over the "
-                    "host link (the library's default, host_direct=2)")
+    hd_default = rti.get_tuning("host_direct")
+    e2e_transfer = {
+        0: "page-locked host arrays staged through device memory in overlapping chunks",
+        2: "page-locked host arrays read and written in place by the kernel over the host link",
+        3: "page-locked host arrays staged in overlapping chunks (large calls)",
+        4: "page-locked inputs copied to device memory a chunk ahead of the kernels, outputs "
+           "written in place over the host link",
+    }.get(hd_default, f"host_direct={hd_default}") + f" (the library's default, host_direct={hd_default})"
     pinned = (tr_h, org_h, dir_h, to_h, so_h, fo_h)
     ms_e2e = e2e_ms(pinned, rti.get_tuning("host_direct"))
     e2e_ok = bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
     ms_e2e_staged = e2e_ms(pinned, 0)
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_in_staged = e2e_ms(pinned, 4)  # inputs staged a chunk ahead, outputs in place
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_in_place = e2e_ms(pinned, 2)
     e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
     del org_h, dir_h, tr_h, to_h, so_h, fo_h
     # the same call on pageable NumPy arrays
@@ -1323,6 +1333,8 @@ def run_engine(args, rank, world, local):
                 "matches_device_path": e2e_ok,
                 "transfer": e2e_transfer,
                 "staged_value": total_rays / (ms_e2e_staged / 1e3) / 1e6,
+                "inputs_staged_outputs_in_place_value": total_rays / (ms_e2e_in_staged / 1e3) / 1e6,
+                "in_place_value": total_rays / (ms_e2e_in_place / 1e3) / 1e6,
                 "pageable_staged_value": total_rays / (ms_e2e_pageable / 1e3) / 1e6,
                 "pageable_direct_value": (total_rays / (ms_e2e_pageable_direct / 1e3) / 1e6
                                           if ms_e2e_pageable_direct else None)},

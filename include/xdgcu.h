@@ -508,7 +508,12 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      default); 3 keeps pageable arrays in place and
  *                      page-locked arrays in place unless the call is large
  *                      enough (more than 2 chunks of 2^21 rays) for the
- *                      staged pipeline to overlap its copies.  Tallies
+ *                      staged pipeline to overlap its copies; 4 is 2 except
+ *                      that such a large call stages its page-locked inputs
+ *                      (the copy engines fill device memory a chunk ahead of
+ *                      the kernels) and still writes its outputs in place.
+ *                      Staged chunks' kernels alternate between two streams
+ *                      so that one launch's tail overlaps the next.  Tallies
  *                      updated atomically are always staged.  Results do not
  *                      depend on it. */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);

@@ -5,8 +5,10 @@ and as device arrays.
 ray_fire runs on 4.5e6 rays (more than two staging chunks) with the inputs
 and outputs in page-locked memory, pageable memory, or page-locked inputs
 with pageable outputs (some arrays in place, the rest staged), under each
-host_direct setting (2, the default, keeps both kinds in place; 3 stages
-the page-locked arrays of this large call in overlapping chunks).  The
+host_direct setting (2 keeps both kinds in place; 3 stages the page-locked
+arrays of this large call in overlapping chunks; 4 stages only its
+page-locked inputs and writes the outputs in place; staged chunks' kernels
+alternate between two streams).  The
 packed tet walk and the walk_elements particle loop
 (whose atomic tally is always staged) are checked the same way.
 """
@@ -87,7 +89,7 @@ def test_ray_fire_host_buffers(cuda, rays, prec):
         ref = fire("device", 1)
         assert (ref[1] >= 0).mean() > 0.5
         for kind in ("pinned", "pageable", "mixed"):
-            for direct in (0, 1, 2, 3):
+            for direct in (0, 1, 2, 3, 4):
                 got = fire(kind, direct)
                 for a, b, what in zip(got, ref, ("t", "surface", "face", "status")):
                     assert np.array_equal(a, b), f"{kind} host_direct={direct}: {what}"
@@ -137,7 +139,7 @@ def test_walk_and_transport_host_buffers(cuda):
         ref_t = transport("device")
         assert ref_w[2][-1] > n and (ref_t[5] > 0).all()
         for kind in ("pinned", "pageable"):
-            for direct in (0, 1, 2, 3):
+            for direct in (0, 1, 2, 3, 4):
                 rti.set_tuning("host_direct", direct)
                 for a, b in zip(walk(kind), ref_w):
                     assert np.array_equal(a, b), f"walk {kind} host_direct={direct}"

@@ -73,6 +73,7 @@ struct TreeHost {
 // overlap.
 struct Slot {
   cudaStream_t stream = nullptr;    // compute
+  cudaStream_t stream2 = nullptr;   // compute, odd chunks of a staged call
   cudaStream_t copy_in = nullptr;
   cudaStream_t copy_out = nullptr;
   std::vector<cudaEvent_t> ev;
@@ -80,6 +81,7 @@ struct Slot {
   ~Slot() {
     for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
+    if (stream2) cudaStreamDestroy(stream2);
     if (copy_in) cudaStreamDestroy(copy_in);
     if (copy_out) cudaStreamDestroy(copy_out);
   }
@@ -615,15 +617,19 @@ struct Arr {
 // one process: page-locked 1319 Mrays/s in place against 1241 staged,
 // pageable 1334 in place against 846 staged (the default, 2, keeps both in
 // place).
-void* direct_ptr(const xdgcu_ctx* c, const void* p, bool pipelined) {
+// Under host_direct 4 a pipelined call stages its page-locked inputs
+// (`input`) and keeps its outputs in place.
+void* direct_ptr(const xdgcu_ctx* c, const void* p, bool pipelined, bool input = true) {
   if (!p || c->host_direct <= 0) return nullptr;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
-  if (at.type == cudaMemoryTypeHost)
-    return (c->host_direct == 3 && pipelined) ? nullptr : at.devicePointer;
+  if (at.type == cudaMemoryTypeHost) {
+    const bool staged = pipelined && (c->host_direct == 3 || (c->host_direct == 4 && input));
+    return staged ? nullptr : at.devicePointer;
+  }
   if (at.type == cudaMemoryTypeUnregistered && c->host_direct >= 2 && c->pageable_direct)
     return const_cast<void*>(p);
   return nullptr;
@@ -660,6 +666,7 @@ Slot* get_slot(xdgcu_ctx* c) {
   if (!s) {
     s.reset(new Slot());
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&s->copy_out, cudaStreamNonBlocking) != cudaSuccess) {
       s.reset();
@@ -728,7 +735,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
     const void* p = r->host_in ? r->host_in : r->host_out;
     void* d = (r->host_in && r->host_out && r->host_in != r->host_out)
                   ? nullptr
-                  : direct_ptr(c, p, pipelined);
+                  : direct_ptr(c, p, pipelined, r->host_in != nullptr);
     if (d) {
       r->dev = (char*)d;
       r->direct = true;
@@ -773,7 +780,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
     for (int64_t k = 0; k <= chunks; ++k) starts.push_back(std::min<int64_t>(n, f + k * per2));
   }
   const int64_t nch = (int64_t)starts.size() - 1;
-  if (!s->events((size_t)(2 * nch + 1))) return set_err(XDGCU_ERR_CUDA, "event creation");
+  if (!s->events((size_t)(2 * nch + 2))) return set_err(XDGCU_ERR_CUDA, "event creation");
   // order after the caller's stream (if any)
   if (user) {
     API_CUDA(cudaEventRecord(s->ev[2 * nch], user), "event");
@@ -785,10 +792,17 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
                "H2D");
   int rc = begin_query(c, s->stream, counters);
   if (rc) return rc;
+  // consecutive chunks' kernels alternate between two compute streams, so
+  // the tail of one launch (its last, slow rays) overlaps the next launch
+  if (nch > 1) {
+    API_CUDA(cudaEventRecord(s->ev[2 * nch + 1], s->stream), "event");
+    API_CUDA(cudaStreamWaitEvent(s->stream2, s->ev[2 * nch + 1], 0), "event wait");
+  }
   for (int64_t k = 0; k < nch; ++k) {
     const int64_t first = starts[k];
     const int64_t cnt = starts[k + 1] - first;
     if (cnt <= 0) continue;
+    cudaStream_t cs = (k & 1) ? s->stream2 : s->stream;
     for (RayArr* r : rays)
       if (r->host_in && r->per_ray && !r->direct)
         API_CUDA(cudaMemcpyAsync(r->dev + r->per_ray * first,
@@ -796,9 +810,9 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
                                  cudaMemcpyHostToDevice, s->copy_in),
                  "H2D");
     API_CUDA(cudaEventRecord(s->ev[2 * k], s->copy_in), "event");
-    API_CUDA(cudaStreamWaitEvent(s->stream, s->ev[2 * k], 0), "event wait");
-    API_CUDA(launch(first, cnt, s->stream), "query launch");
-    API_CUDA(cudaEventRecord(s->ev[2 * k + 1], s->stream), "event");
+    API_CUDA(cudaStreamWaitEvent(cs, s->ev[2 * k], 0), "event wait");
+    API_CUDA(launch(first, cnt, cs), "query launch");
+    API_CUDA(cudaEventRecord(s->ev[2 * k + 1], cs), "event");
     API_CUDA(cudaStreamWaitEvent(s->copy_out, s->ev[2 * k + 1], 0), "event wait");
     for (RayArr* r : rays)
       if (r->host_out && r->per_ray && !r->direct)
@@ -809,6 +823,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
   }
   API_CUDA(cudaStreamSynchronize(s->copy_out), "sync");
   API_CUDA(cudaStreamSynchronize(s->stream), "sync");
+  API_CUDA(cudaStreamSynchronize(s->stream2), "sync");
   API_CUDA(cudaStreamSynchronize(s->copy_in), "sync");
   return XDGCU_OK;
 }
@@ -1339,7 +1354,7 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "walk_edge_table must be 0 or 1");
     c->walk_edge_table = (int32_t)value;
   } else if (k == "host_direct") {
-    if (value < 0 || value > 3) return set_err(XDGCU_ERR_INVALID_ARG, "host_direct must be 0..3");
+    if (value < 0 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "host_direct must be 0..4");
     c->host_direct = (int32_t)value;
   } else {
     return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
