@@ -617,8 +617,8 @@ struct Arr {
 // one process: page-locked 1319 Mrays/s in place against 1241 staged,
 // pageable 1334 in place against 846 staged (the default, 2, keeps both in
 // place).
-// Under host_direct 4 a pipelined call stages its page-locked inputs
-// (`input`) and keeps its outputs in place.
+// Under host_direct 4 a pipelined call reads its page-locked inputs in place
+// and stages its outputs (`input` false).
 void* direct_ptr(const xdgcu_ctx* c, const void* p, bool pipelined, bool input = true) {
   if (!p || c->host_direct <= 0) return nullptr;
   cudaPointerAttributes at;
@@ -627,7 +627,7 @@ void* direct_ptr(const xdgcu_ctx* c, const void* p, bool pipelined, bool input =
     return nullptr;
   }
   if (at.type == cudaMemoryTypeHost) {
-    const bool staged = pipelined && (c->host_direct == 3 || (c->host_direct == 4 && input));
+    const bool staged = pipelined && (c->host_direct == 3 || (c->host_direct == 4 && !input));
     return staged ? nullptr : at.devicePointer;
   }
   if (at.type == cudaMemoryTypeUnregistered && c->host_direct >= 2 && c->pageable_direct)
@@ -711,6 +711,8 @@ struct RayArr {
 // in 12.6 ms (each chunk's launch ends with a tail of a few slow rays).
 constexpr int64_t kChunkRays = 1 << 21;
 constexpr int64_t kMaxChunks = 16;
+// work-queue grab of a chunk's traversal launch (when a call runs in chunks)
+constexpr int32_t kChunkGrab = 64;
 
 // Runs a per-ray query over host arrays in chunks: the inputs of chunk k+1
 // are copied in while chunk k computes and chunk k-1 is copied out.  `whole`
@@ -811,7 +813,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
                  "H2D");
     API_CUDA(cudaEventRecord(s->ev[2 * k], s->copy_in), "event");
     API_CUDA(cudaStreamWaitEvent(cs, s->ev[2 * k], 0), "event wait");
-    API_CUDA(launch(first, cnt, cs), "query launch");
+    API_CUDA(launch(first, cnt, cs, nch > 1), "query launch");
     API_CUDA(cudaEventRecord(s->ev[2 * k + 1], cs), "event");
     API_CUDA(cudaStreamWaitEvent(s->copy_out, s->ev[2 * k + 1], 0), "event wait");
     for (RayArr* r : rays)
@@ -1517,7 +1519,7 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
   return run_staged(
       c, s, st, n, {&A_eo, &A_ei},
       {&R_trees, &R_org, &R_dir, &R_tmax, &R_t, &R_s, &R_f, &R_fl, &R_d, &R_st}, &a.counters,
-      [&](int64_t first, int64_t cnt, cudaStream_t cs) {
+      [&](int64_t first, int64_t cnt, cudaStream_t cs, bool chunked) {
         SurfArgs b = a;
         b.n = cnt;
         b.ray_trees = (const int32_t*)at(R_trees, first);
@@ -1532,7 +1534,8 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
         b.flag_out = (int32_t*)at(R_fl, first);
         b.dist_out = (double*)at(R_d, first);
         b.status = (int32_t*)at(R_st, first);
-        return launch_trace(c, mode, mixed, b, extent, cs);
+        // a chunk's launch takes rays from the work queue, so its tail is short
+        return launch_trace(c, mode, mixed, b, extent, cs, chunked ? kChunkGrab : 0);
       });
 }
 
@@ -1664,7 +1667,7 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
     return r.dev ? r.dev + r.per_ray * first : nullptr;
   };
   return run_staged(c, s, st, n, {}, {&R_trees, &R_p, &R_d, &R_i, &R_x, &R_st}, &a.counters,
-                    [&](int64_t first, int64_t cnt, cudaStream_t cs) {
+                    [&](int64_t first, int64_t cnt, cudaStream_t cs, bool) {
                       PointArgs b = a;
                       b.n = cnt;
                       b.ray_trees = (const int32_t*)at(R_trees, first);
@@ -2239,14 +2242,15 @@ int xdgcu_point_in_volumes(xdgcu_ctx* c, int64_t n, const double* points,
     return r.dev ? r.dev + r.per_ray * first : nullptr;
   };
   rc = run_staged(c, s, st, n, {}, {&R_p, &R_d, &R_in, &R_st}, &a.counters,
-                  [&](int64_t first, int64_t cnt, cudaStream_t cs) {
+                  [&](int64_t first, int64_t cnt, cudaStream_t cs, bool chunked) {
                     SurfArgs b = a;
                     b.n = cnt;
                     b.org = (const double*)at(R_p, first);
                     b.dir = (const double*)at(R_d, first);
                     b.vol_inside = (uint8_t*)at(R_in, first);
                     b.status = (int32_t*)at(R_st, first);
-                    return launch_trace(c, MODE_ALL_VOLUMES, mixed, b, extent, cs);
+                    return launch_trace(c, MODE_ALL_VOLUMES, mixed, b, extent, cs,
+                                        chunked ? kChunkGrab : 0);
                   });
   cudaFreeAsync(d_list, s->stream);
   return rc;
