@@ -859,6 +859,74 @@ def run_engine(args, rank, world, local):
         if bool(hitm.any()) else 0.0
     hit_frac = float((s_mixed >= 0).float().mean().item())
 
+    # ---- e2e through the C ABI with pinned host buffers ------------------
+    # (measured right after the device timing, before the host cores run the
+    # oracle legs)
+    org_h = torch.empty((N_RAYS, 3), dtype=torch.float64, pin_memory=True)
+    dir_h = torch.empty((N_RAYS, 3), dtype=torch.float64, pin_memory=True)
+    tr_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
+    org_h.copy_(torch.from_numpy(p_h))
+    dir_h.copy_(torch.from_numpy(d_h))
+    tr_h.copy_(torch.from_numpy(trees_h))
+    to_h = torch.empty(N_RAYS, dtype=torch.float64, pin_memory=True)
+    so_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
+    fo_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
+
+    def e2e_call(bufs):
+        tr, org, dr, to, so, fo = (ctypes.c_void_p(b.data_ptr()) if hasattr(b, "data_ptr")
+                                   else b.ctypes.data_as(ctypes.c_void_p) for b in bufs)
+        rc = L.xdgcu_ray_fire(rti.ctx, 0, tr, N_RAYS, org, dr, None, 0, None, None, to, so, fo,
+                              None, MIXED, None)
+        _lib.check(rc, rti.ctx, "ray_fire (host buffers)")
+
+    def e2e_ms(bufs, host_direct):
+        # host_direct 0: staged copies in chunks; 1: page-locked arrays read
+        # and written in place by the kernel; 2 (the default): pageable
+        # arrays in place too; 3: page-locked arrays staged in overlapping
+        # chunks when the batch is large
+        old_hd = rti.get_tuning("host_direct")
+        rti.set_tuning("host_direct", host_direct)
+        for _ in range(2):
+            e2e_call(bufs)
+        torch.cuda.synchronize()
+        dist.barrier(world)
+        te = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_call(bufs)
+        torch.cuda.synchronize()
+        rti.set_tuning("host_direct", old_hd)
+        return dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world)
+
+    e2e_steps = max(3, args.steps // 2)
+    hd_default = rti.get_tuning("host_direct")
+    e2e_transfer = {
+        0: "page-locked host arrays staged through device memory in overlapping chunks",
+        2: "page-locked host arrays read and written in place by the kernel over the host link",
+        3: "page-locked host arrays staged in overlapping chunks (large calls)",
+        4: "page-locked inputs copied to device memory a chunk ahead of the kernels, outputs "
+           "written in place over the host link",
+    }.get(hd_default, f"host_direct={hd_default}") + f" (the library's default, host_direct={hd_default})"
+    pinned = (tr_h, org_h, dir_h, to_h, so_h, fo_h)
+    ms_e2e = e2e_ms(pinned, rti.get_tuning("host_direct"))
+    e2e_ok = bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_staged = e2e_ms(pinned, 0)
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_in_staged = e2e_ms(pinned, 4)  # inputs staged a chunk ahead, outputs in place
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_in_place = e2e_ms(pinned, 2)
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    del org_h, dir_h, tr_h, to_h, so_h, fo_h
+    # the same call on pageable NumPy arrays
+    pg = (np.ascontiguousarray(trees_h), np.ascontiguousarray(p_h), np.ascontiguousarray(d_h),
+          np.empty(N_RAYS), np.empty(N_RAYS, np.int32), np.empty(N_RAYS, np.int32))
+    ms_e2e_pageable = e2e_ms(pg, 0)  # pageable arrays staged
+    e2e_ok = e2e_ok and bool(np.array_equal(pg[4], s_mixed.cpu().numpy()))
+    pageable_direct = bool(rti.get_tuning("pageable_direct"))
+    ms_e2e_pageable_direct = e2e_ms(pg, 3) if pageable_direct else None
+    e2e_ok = e2e_ok and bool(np.array_equal(pg[4], s_mixed.cpu().numpy()))
+    del pg
+
+
     # point_in_volume of the same points in their own volume (all must be inside)
     piv_out = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
 
@@ -1002,71 +1070,6 @@ def run_engine(args, rank, world, local):
         cpu_baseline = {"value": cs / dtc / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
                         "sample": f"first {cs} rays of the workload, FP64, BVH, OpenMP"}
         log(f"[bench] oracle check + cpu baseline {time.perf_counter() - t1:.1f}s")
-
-    # ---- e2e through the C ABI with pinned host buffers ------------------
-    org_h = torch.empty((N_RAYS, 3), dtype=torch.float64, pin_memory=True)
-    dir_h = torch.empty((N_RAYS, 3), dtype=torch.float64, pin_memory=True)
-    tr_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
-    org_h.copy_(torch.from_numpy(p_h))
-    dir_h.copy_(torch.from_numpy(d_h))
-    tr_h.copy_(torch.from_numpy(trees_h))
-    to_h = torch.empty(N_RAYS, dtype=torch.float64, pin_memory=True)
-    so_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
-    fo_h = torch.empty(N_RAYS, dtype=torch.int32, pin_memory=True)
-
-    def e2e_call(bufs):
-        tr, org, dr, to, so, fo = (ctypes.c_void_p(b.data_ptr()) if hasattr(b, "data_ptr")
-                                   else b.ctypes.data_as(ctypes.c_void_p) for b in bufs)
-        rc = L.xdgcu_ray_fire(rti.ctx, 0, tr, N_RAYS, org, dr, None, 0, None, None, to, so, fo,
-                              None, MIXED, None)
-        _lib.check(rc, rti.ctx, "ray_fire (host buffers)")
-
-    def e2e_ms(bufs, host_direct):
-        # host_direct 0: staged copies in chunks; 1: page-locked arrays read
-        # and written in place by the kernel; 2 (the default): pageable
-        # arrays in place too; 3: page-locked arrays staged in overlapping
-        # chunks when the batch is large
-        old_hd = rti.get_tuning("host_direct")
-        rti.set_tuning("host_direct", host_direct)
-        for _ in range(2):
-            e2e_call(bufs)
-        torch.cuda.synchronize()
-        dist.barrier(world)
-        te = time.perf_counter()
-        for _ in range(e2e_steps):
-            e2e_call(bufs)
-        torch.cuda.synchronize()
-        rti.set_tuning("host_direct", old_hd)
-        return dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world)
-
-    e2e_steps = max(3, args.steps // 2)
-    hd_default = rti.get_tuning("host_direct")
-    e2e_transfer = {
-        0: "page-locked host arrays staged through device memory in overlapping chunks",
-        2: "page-locked host arrays read and written in place by the kernel over the host link",
-        3: "page-locked host arrays staged in overlapping chunks (large calls)",
-        4: "page-locked inputs copied to device memory a chunk ahead of the kernels, outputs "
-           "written in place over the host link",
-    }.get(hd_default, f"host_direct={hd_default}") + f" (the library's default, host_direct={hd_default})"
-    pinned = (tr_h, org_h, dir_h, to_h, so_h, fo_h)
-    ms_e2e = e2e_ms(pinned, rti.get_tuning("host_direct"))
-    e2e_ok = bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
-    ms_e2e_staged = e2e_ms(pinned, 0)
-    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
-    ms_e2e_in_staged = e2e_ms(pinned, 4)  # inputs staged a chunk ahead, outputs in place
-    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
-    ms_e2e_in_place = e2e_ms(pinned, 2)
-    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
-    del org_h, dir_h, tr_h, to_h, so_h, fo_h
-    # the same call on pageable NumPy arrays
-    pg = (np.ascontiguousarray(trees_h), np.ascontiguousarray(p_h), np.ascontiguousarray(d_h),
-          np.empty(N_RAYS), np.empty(N_RAYS, np.int32), np.empty(N_RAYS, np.int32))
-    ms_e2e_pageable = e2e_ms(pg, 0)  # pageable arrays staged
-    e2e_ok = e2e_ok and bool(np.array_equal(pg[4], s_mixed.cpu().numpy()))
-    pageable_direct = bool(rti.get_tuning("pageable_direct"))
-    ms_e2e_pageable_direct = e2e_ms(pg, 3) if pageable_direct else None
-    e2e_ok = e2e_ok and bool(np.array_equal(pg[4], s_mixed.cpu().numpy()))
-    del pg
 
     # ---- C5: tet walk ------------------------------------------------------
     t0 = time.perf_counter()
