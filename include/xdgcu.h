@@ -24,10 +24,11 @@
  * the caller's arrays).  The two kinds may not be mixed within one call.
  * Host arrays are read and written in place by the kernels where the device
  * can address them (page-locked memory, and pageable memory on systems whose
- * GPU walks the host page tables, such as Grace): the default tuning
- * `host_direct` = 2.  Memory the device cannot address, or any host array
- * under `host_direct` = 0, is staged through a per-thread device workspace in
- * overlapping chunks.
+ * GPU walks the host page tables, such as Grace), except that by default
+ * (`host_direct` = 5) a large call's page-locked arrays are staged when
+ * timing the first large calls found staging faster.  Memory the device
+ * cannot address, or any host array under `host_direct` = 0, is staged
+ * through a per-thread device workspace in overlapping chunks.
  *
  * Precision: XDGCU_FP64 evaluates everything in double precision (the plain
  * drop-in); XDGCU_MIXED runs FP32 box tests, an FP32 Plucker pre-filter (the
@@ -504,18 +505,25 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      host link once, inside the kernel); 2 does the same
  *                      for pageable memory too when the device reads it
  *                      through the host's page tables (read-only key
- *                      "pageable_direct" = 1, as on Grace systems; the
- *                      default); 3 keeps pageable arrays in place and
+ *                      "pageable_direct" = 1, as on Grace systems); 3
+ *                      keeps pageable arrays in place and
  *                      page-locked arrays in place unless the call is large
  *                      enough (more than 2 chunks of 2^21 rays) for the
  *                      staged pipeline to overlap its copies; 4 is 2 except
- *                      that such a large call stages its page-locked inputs
- *                      (the copy engines fill device memory a chunk ahead of
- *                      the kernels) and still writes its outputs in place.
- *                      Staged chunks' kernels alternate between two streams
- *                      so that one launch's tail overlaps the next.  Tallies
- *                      updated atomically are always staged.  Results do not
- *                      depend on it. */
+ *                      that such a large call reads its page-locked inputs
+ *                      in place and stages its outputs; 5 (the default)
+ *                      chooses between 2 and 3 by measurement: the first
+ *                      four large calls with host arrays alternate between
+ *                      them and are timed, and every later large call takes
+ *                      the faster (read-only key "host_direct_choice": -1
+ *                      while undecided, then 2 or 3; setting host_direct to
+ *                      5 again starts a new choice).  Which is faster depends
+ *                      on the machine and the launch settings.  Staged
+ *                      chunks' kernels alternate between two streams and take
+ *                      their rays from the device work queue, so that one
+ *                      launch's tail overlaps the next.  Tallies updated
+ *                      atomically are always staged.  Results do not depend
+ *                      on it. */
 int xdgcu_set_tuning(xdgcu_ctx* ctx, const char* key, int64_t value);
 int xdgcu_get_tuning(const xdgcu_ctx* ctx, const char* key, int64_t* value);
 

@@ -8,7 +8,8 @@ with pageable outputs (some arrays in place, the rest staged), under each
 host_direct setting (2 keeps both kinds in place; 3 stages the page-locked
 arrays of this large call in overlapping chunks; 4 stages only its
 page-locked inputs and writes the outputs in place; staged chunks' kernels
-alternate between two streams).  The
+alternate between two streams; 5, the default, picks 2 or 3 by timing the
+first large calls).  The
 packed tet walk and the walk_elements particle loop
 (whose atomic tally is always staged) are checked the same way.
 """
@@ -89,10 +90,42 @@ def test_ray_fire_host_buffers(cuda, rays, prec):
         ref = fire("device", 1)
         assert (ref[1] >= 0).mean() > 0.5
         for kind in ("pinned", "pageable", "mixed"):
-            for direct in (0, 1, 2, 3, 4):
+            for direct in (0, 1, 2, 3, 4, 5):
                 got = fire(kind, direct)
                 for a, b, what in zip(got, ref, ("t", "surface", "face", "status")):
                     assert np.array_equal(a, b), f"{kind} host_direct={direct}: {what}"
+    finally:
+        rti.set_tuning("host_direct", old)
+
+
+def test_automatic_policy_choice(cuda, rays):
+    """host_direct 5 times the first four large page-locked calls (two in
+    place, two staged), then keeps the faster; every call gives the same
+    results, and setting 5 again starts a new choice."""
+    torch = cuda
+    x, p, d, trees = rays
+    rti = x.rti
+    L = _lib.load()
+    n = len(p)
+    old = rti.get_tuning("host_direct")
+    try:
+        rti.set_tuning("host_direct", 5)
+        assert rti.get_tuning("host_direct_choice") == -1
+        (tr, o, u), outs = _buffers(torch, "pinned", n, [trees, p, d])
+        ref = None
+        for call in range(6):
+            rc = L.xdgcu_ray_fire(rti.ctx, 0, _ptr(tr), n, _ptr(o), _ptr(u), None, 0, None, None,
+                                  *[_ptr(t) for t in outs], MIXED, None)
+            _lib.check(rc, rti.ctx, "ray_fire")
+            got = [t.clone() for t in outs]
+            if ref is None:
+                ref = got
+            else:
+                assert all(bool(torch.equal(a, b)) for a, b in zip(got, ref)), call
+            choice = rti.get_tuning("host_direct_choice")
+            assert choice == (-1 if call < 3 else choice) and (call < 3 or choice in (2, 3))
+        rti.set_tuning("host_direct", 5)
+        assert rti.get_tuning("host_direct_choice") == -1
     finally:
         rti.set_tuning("host_direct", old)
 
@@ -139,7 +172,7 @@ def test_walk_and_transport_host_buffers(cuda):
         ref_t = transport("device")
         assert ref_w[2][-1] > n and (ref_t[5] > 0).all()
         for kind in ("pinned", "pageable"):
-            for direct in (0, 1, 2, 3, 4):
+            for direct in (0, 1, 2, 3, 4, 5):
                 rti.set_tuning("host_direct", direct)
                 for a, b in zip(walk(kind), ref_w):
                     assert np.array_equal(a, b), f"walk {kind} host_direct={direct}"

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -398,12 +399,21 @@ struct xdgcu_ctx {
   int32_t walk_flush_wait = 8;
   // host arrays the kernels address directly instead of staging them:
   // 0 none, 1 page-locked memory, 2 also pageable memory when the device
-  // reads it through the host's page tables (pageable_direct)
-  int32_t host_direct = 2;
+  // reads it through the host's page tables (pageable_direct), 3 / 4 stage
+  // all / the outputs of large calls' page-locked arrays, 5 (default) picks
+  // 2 or 3 for large calls by timing both (xdgcu_set_tuning)
+  int32_t host_direct = 5;
   int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
   int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from d_tri_prime
   int32_t closest_bound = 1;     // mixed closest: FP32 triangle bound from d_tri_cb
   bool pageable_direct = false;
+  // host_direct 5: trial calls of in place (0) and staged (1), their summed
+  // seconds per ray, and the policy chosen (-1 until both have kAutoTrials)
+  std::mutex hd_mu;
+  int32_t hd_trials = 0;
+  int32_t hd_timed[2] = {0, 0};
+  double hd_sec_per_ray[2] = {0.0, 0.0};
+  int32_t hd_choice = -1;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
   bool counting = false;
@@ -613,35 +623,39 @@ struct Arr {
 // host link once, inside the kernel, with no staging copies or chunking.
 // `pipelined`: the call is large enough for the staged chunk pipeline to
 // overlap its copies with compute; under host_direct 3 page-locked arrays
-// are staged then.  Measured on ray_fire over 1e7 host rays, interleaved in
-// one process: page-locked 1319 Mrays/s in place against 1241 staged,
-// pageable 1334 in place against 846 staged (the default, 2, keeps both in
-// place).
-// Under host_direct 4 a pipelined call reads its page-locked inputs in place
-// and stages its outputs (`input` false).
-void* direct_ptr(const xdgcu_ctx* c, const void* p, bool pipelined, bool input = true) {
-  if (!p || c->host_direct <= 0) return nullptr;
+// are staged then, under host_direct 4 only its outputs (`input` false).
+// `hd` is the policy in force for the call (host_direct, or under 5 the
+// policy the automatic choice picked for it).  Measured on ray_fire over
+// 1e7 host rays with the bench's launch settings, the policies interleaved
+// in one process (medians of 24 calls each): page-locked in place 8.14 ms,
+// staged 7.44 ms, inputs in place and outputs staged 7.65 ms, against 6.73
+// ms for device arrays; with the default launch settings in place was ahead
+// (7.55 against 7.70 ms), hence the automatic choice.
+void* direct_ptr(const xdgcu_ctx* c, const void* p, bool pipelined, bool input = true,
+                 int hd = -1) {
+  if (hd < 0) hd = c->host_direct == 5 ? 2 : c->host_direct;
+  if (!p || hd <= 0) return nullptr;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
   if (at.type == cudaMemoryTypeHost) {
-    const bool staged = pipelined && (c->host_direct == 3 || (c->host_direct == 4 && !input));
+    const bool staged = pipelined && (hd == 3 || (hd == 4 && !input));
     return staged ? nullptr : at.devicePointer;
   }
-  if (at.type == cudaMemoryTypeUnregistered && c->host_direct >= 2 && c->pageable_direct)
+  if (at.type == cudaMemoryTypeUnregistered && hd >= 2 && c->pageable_direct)
     return const_cast<void*>(p);
   return nullptr;
 }
 
 // Marks the arrays the kernels address in place (direct_ptr); an array that
 // is both read and written must be addressable for both.
-void resolve_direct(const xdgcu_ctx* c, Arr* a, bool pipelined = false) {
+void resolve_direct(const xdgcu_ctx* c, Arr* a, bool pipelined = false, int hd = -1) {
   if (a->no_direct || a->bytes == 0) return;
   const void* p = a->host_in ? a->host_in : a->host_out;
   if (!p || (a->host_in && a->host_out && a->host_in != a->host_out)) return;
-  void* d = direct_ptr(c, p, pipelined);
+  void* d = direct_ptr(c, p, pipelined, true, hd);
   if (d) {
     a->dev = d;
     a->direct = true;
@@ -711,6 +725,8 @@ struct RayArr {
 // in 12.6 ms (each chunk's launch ends with a tail of a few slow rays).
 constexpr int64_t kChunkRays = 1 << 21;
 constexpr int64_t kMaxChunks = 16;
+// host_direct 5: timed calls of each policy before the choice
+constexpr int kAutoTrials = 2;
 // work-queue grab of a chunk's traversal launch (when a call runs in chunks)
 constexpr int32_t kChunkGrab = 64;
 
@@ -727,9 +743,26 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
                std::vector<RayArr*> rays, unsigned long long** counters, Launch launch) {
   // arrays the kernels address in place take no workspace and no copies
   const bool pipelined = n > 2 * kChunkRays;
+  // host_direct 5: the first large calls alternate between in place (2) and
+  // staged (3) and are timed; then every large call takes the faster
+  int hd = c->host_direct;
+  int trial = -1;
+  if (hd == 5) {
+    hd = 2;
+    if (pipelined) {
+      std::lock_guard<std::mutex> g(c->hd_mu);
+      if (c->hd_choice >= 0) {
+        hd = c->hd_choice;
+      } else {
+        trial = c->hd_trials++ & 1;
+        hd = trial ? 3 : 2;
+      }
+    }
+  }
+  const auto t_start = std::chrono::steady_clock::now();
   bool all_direct = true;
   for (Arr* a : whole) {
-    resolve_direct(c, a, pipelined);
+    resolve_direct(c, a, pipelined, hd);
     if (a->bytes && !a->direct) all_direct = false;
   }
   for (RayArr* r : rays) {
@@ -737,7 +770,7 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
     const void* p = r->host_in ? r->host_in : r->host_out;
     void* d = (r->host_in && r->host_out && r->host_in != r->host_out)
                   ? nullptr
-                  : direct_ptr(c, p, pipelined, r->host_in != nullptr);
+                  : direct_ptr(c, p, pipelined, r->host_in != nullptr, hd);
     if (d) {
       r->dev = (char*)d;
       r->direct = true;
@@ -827,6 +860,17 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
   API_CUDA(cudaStreamSynchronize(s->stream), "sync");
   API_CUDA(cudaStreamSynchronize(s->stream2), "sync");
   API_CUDA(cudaStreamSynchronize(s->copy_in), "sync");
+  if (trial >= 0) {
+    const double sec =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    std::lock_guard<std::mutex> g(c->hd_mu);
+    c->hd_sec_per_ray[trial] += sec / (double)n;
+    c->hd_timed[trial]++;
+    if (c->hd_choice < 0 && c->hd_timed[0] >= kAutoTrials && c->hd_timed[1] >= kAutoTrials)
+      c->hd_choice = c->hd_sec_per_ray[1] / c->hd_timed[1] < c->hd_sec_per_ray[0] / c->hd_timed[0]
+                         ? 3
+                         : 2;
+  }
   return XDGCU_OK;
 }
 
@@ -1356,8 +1400,15 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "walk_edge_table must be 0 or 1");
     c->walk_edge_table = (int32_t)value;
   } else if (k == "host_direct") {
-    if (value < 0 || value > 4) return set_err(XDGCU_ERR_INVALID_ARG, "host_direct must be 0..4");
+    if (value < 0 || value > 5) return set_err(XDGCU_ERR_INVALID_ARG, "host_direct must be 0..5");
     c->host_direct = (int32_t)value;
+    if (value == 5) {  // a fresh choice
+      std::lock_guard<std::mutex> g(c->hd_mu);
+      c->hd_trials = 0;
+      c->hd_timed[0] = c->hd_timed[1] = 0;
+      c->hd_sec_per_ray[0] = c->hd_sec_per_ray[1] = 0.0;
+      c->hd_choice = -1;
+    }
   } else {
     return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   }
@@ -1389,6 +1440,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "closest_bound") *value = c->closest_bound;
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
+  else if (k == "host_direct_choice") *value = c->hd_choice;
   else return set_err(XDGCU_ERR_NOT_FOUND, "unknown tuning key " + k);
   return XDGCU_OK;
 }
