@@ -492,6 +492,10 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      when the surfaces are uploaded) proves farther than the
  *                      nearest so far; 0 tests every triangle the box pruning
  *                      reaches.  Results do not depend on it
+ *   "closest_node_steps"  closest, mixed: inner-node steps each lane takes
+ *                      before the warp's lanes bound and test the triangles of
+ *                      the leaves they hold together (1..64, default 8)
+ *   "closest_node_steps_fp64"  the same for the all-FP64 closest (default 1)
  *   "walk_edge_table"  mixed walk: 1 (default) takes the FP64 Plucker
  *                      coordinates of a face's edges from the edge table built
  *                      with the mesh (each edge's e and e x lo evaluated once,

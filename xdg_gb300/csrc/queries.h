@@ -100,6 +100,7 @@ struct PointArgs {
   // distance (w = NaN for degenerate triangles: never pruned)
   const float4* tri_cb;
   const int32_t* elem_ids;   // find_element: element mesh ids
+  int32_t node_steps;        // closest: inner-node steps per lane between leaf phases (1..64)
   double* dist_out;
   int32_t* id_out;
   int32_t* index_out;
