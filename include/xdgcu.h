@@ -496,6 +496,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      before the warp's lanes bound and test the triangles of
  *                      the leaves they hold together (1..64, default 8)
  *   "closest_node_steps_fp64"  the same for the all-FP64 closest (default 1)
+ *   "find_node_steps_fp64"  the same for the all-FP64 find_element (default
+ *                      16; the mixed find_element runs one lane per point
+ *                      on its own)
  *   "walk_edge_table"  mixed walk: 1 (default) takes the FP64 Plucker
  *                      coordinates of a face's edges from the edge table built
  *                      with the mesh (each edge's e and e x lo evaluated once,

@@ -408,6 +408,7 @@ struct xdgcu_ctx {
   int32_t closest_bound = 1;     // mixed closest: FP32 triangle bound from d_tri_cb
   int32_t closest_node_steps = 8;       // closest: inner-node steps between leaf phases (mixed)
   int32_t closest_node_steps_fp64 = 1;  // the same, all-FP64 path
+  int32_t find_node_steps_fp64 = 16;    // find_element, all-FP64 path: the same
   bool pageable_direct = false;
   // host_direct 5: trial calls of in place (0) and staged (1), their summed
   // seconds per ray, and the policy chosen (-1 until both have kAutoTrials)
@@ -1395,11 +1396,13 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
   } else if (k == "trace_edge_table") {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "trace_edge_table must be 0 or 1");
     c->trace_edge_table = (int32_t)value;
-  } else if (k == "closest_node_steps" || k == "closest_node_steps_fp64") {
+  } else if (k == "closest_node_steps" || k == "closest_node_steps_fp64" ||
+             k == "find_node_steps_fp64") {
     if (value < 1 || value > 64)
       return set_err(XDGCU_ERR_INVALID_ARG, k + " must be 1..64");
-    (k == "closest_node_steps" ? c->closest_node_steps : c->closest_node_steps_fp64) =
-        (int32_t)value;
+    (k == "closest_node_steps"        ? c->closest_node_steps
+     : k == "closest_node_steps_fp64" ? c->closest_node_steps_fp64
+                                      : c->find_node_steps_fp64) = (int32_t)value;
   } else if (k == "closest_bound") {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "closest_bound must be 0 or 1");
     c->closest_bound = (int32_t)value;
@@ -1447,6 +1450,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "closest_bound") *value = c->closest_bound;
   else if (k == "closest_node_steps") *value = c->closest_node_steps;
   else if (k == "closest_node_steps_fp64") *value = c->closest_node_steps_fp64;
+  else if (k == "find_node_steps_fp64") *value = c->find_node_steps_fp64;
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else if (k == "host_direct_choice") *value = c->hd_choice;
@@ -1698,7 +1702,9 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
   a.n = n;
   a.tri_face = c->d_tri_face.p;
   a.tri_cb = closest && c->closest_bound ? c->d_tri_cb.p : nullptr;
-  a.node_steps = precision == XDGCU_MIXED ? c->closest_node_steps : c->closest_node_steps_fp64;
+  a.node_steps = closest ? (precision == XDGCU_MIXED ? c->closest_node_steps
+                                                     : c->closest_node_steps_fp64)
+                         : c->find_node_steps_fp64;  // the mixed find_element runs per lane
   a.elem_ids = c->d_elem_ids.p;
   cudaStream_t st = (cudaStream_t)stream;
   auto launch = [&]() -> cudaError_t {

@@ -264,8 +264,11 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
 // find_element (embree/ray_tracer.cpp:226-257 + tetrahedron_contain.cpp:94-114)
 // ---------------------------------------------------------------------------
 
+// One thread per point, each on its own: the mixed path, whose FP32 filter
+// decides nearly every tet, runs faster this way (1403 against at best 1357
+// Mpoints/s in warp-synchronous phases, 1e6 points on the 750,000-tet cube).
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
+__global__ void __launch_bounds__(kBlock) k_find_element_lane(PointArgs a) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   Counters cnt = {0, 0, 0, 0};
   if (i < a.n) {
@@ -375,6 +378,156 @@ __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
   if (a.counters) flush_counters(a.counters, cnt, i < a.n ? 1ull : 0ull);
 }
 
+// As closest: one lane per point, the warp in step -- up to a.node_steps
+// inner-node steps for the lanes without a leaf in hand, then the leaves'
+// tets (FP32 containment filter in the mixed path), then the exact FP64
+// containment tests of all the warp's lanes together.  Every containing tet
+// is visited (the lowest element id wins), so no entry is pruned.  The
+// all-FP64 path, where every tet of a leaf takes the exact test, runs this
+// way: 76.5 -> 114 Mpoints/s with 16 node steps (1e6 points, 750,000 tets).
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  Counters cnt = {0, 0, 0, 0};
+  int32_t best_id = -1, best_idx = -1;
+  int32_t st = RAY_OK;
+  TreeDev T{};
+  d3 p = mk3(0.0, 0.0, 0.0);
+  float px = 0.0f, py = 0.0f, pz = 0.0f, pabs = 0.0f;
+  int32_t ref = CHILD_EMPTY;
+  bool run = false;
+  if (i < a.n) {
+    const int32_t tid = a.ray_trees ? a.ray_trees[i] : a.tree;
+    p = load3(a.pts, i);
+    if (tid < 1 || tid > a.n_trees || !finite3(p)) {
+      st = RAY_INVALID;
+    } else {
+      T = a.trees[tid - 1];
+      // rounding a point to FP32 is monotone, so fl32(p) inside an outward
+      // rounded box is implied by p inside the exact box: the test is
+      // conservative
+      px = __double2float_rn(p.x);
+      py = __double2float_rn(p.y);
+      pz = __double2float_rn(p.z);
+      pabs = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
+      ref = T.root;
+      run = ref != CHILD_EMPTY;
+    }
+  }
+  int32_t stack[kStackSize];
+  int sp = 0;
+  auto pop = [&]() {
+    if (sp == 0) {
+      run = false;
+      return;
+    }
+    ref = stack[--sp];
+  };
+  auto take = [&](int32_t idx) {
+    const int32_t id = __ldg(&a.elem_ids[idx]);
+    if (best_idx < 0 || id < best_id) {  // tie rule: lowest element id
+      best_id = id;
+      best_idx = idx;
+    }
+  };
+
+  while (__any_sync(kFullMask, run)) {
+    // ---- inner nodes ----
+    for (int it = 0; it < a.node_steps; ++it) {
+      const bool want = run && !ref_is_leaf(ref);
+      if (!__any_sync(kFullMask, want)) break;
+      if (!want) continue;
+      const int nrec = T.width / kWidth;
+      bool overflow = false;
+      for (int rec = 0; rec < nrec; ++rec) {
+        cnt.node++;
+        cnt.box += 4;
+        int32_t cr[4];
+        int nhit = 0;
+        if (MIXED) {
+          const Node32* np = T.n32 + (int64_t)ref * nrec + rec;
+          const float4 lx = __ldg(&np->lox), hx = __ldg(&np->hix), ly = __ldg(&np->loy),
+                       hy = __ldg(&np->hiy), lz = __ldg(&np->loz), hz = __ldg(&np->hiz);
+          const int4 c = __ldg(&np->child);
+          const bool in[4] = {
+              px >= lx.x && px <= hx.x && py >= ly.x && py <= hy.x && pz >= lz.x && pz <= hz.x,
+              px >= lx.y && px <= hx.y && py >= ly.y && py <= hy.y && pz >= lz.y && pz <= hz.y,
+              px >= lx.z && px <= hx.z && py >= ly.z && py <= hy.z && pz >= lz.z && pz <= hz.z,
+              px >= lx.w && px <= hx.w && py >= ly.w && py <= hy.w && pz >= lz.w && pz <= hz.w};
+          const int32_t ca[4] = {c.x, c.y, c.z, c.w};
+          for (int k = 0; k < 4; ++k)
+            if (in[k]) cr[nhit++] = ca[k];
+        } else {
+          const Node64* np = T.n64 + (int64_t)ref * nrec + rec;
+          const int4 c = __ldg(&np->child);
+          const int32_t ca[4] = {c.x, c.y, c.z, c.w};
+          for (int k = 0; k < 4; ++k) {
+            const bool in = p.x >= __ldg(np->lox + k) && p.x <= __ldg(np->hix + k) &&
+                            p.y >= __ldg(np->loy + k) && p.y <= __ldg(np->hiy + k) &&
+                            p.z >= __ldg(np->loz + k) && p.z <= __ldg(np->hiz + k);
+            if (in) cr[nhit++] = ca[k];
+          }
+        }
+        if (sp + nhit > kStackSize) {
+          overflow = true;
+          break;
+        }
+        for (int k = nhit - 1; k >= 0; --k) stack[sp++] = cr[k];
+      }
+      if (overflow) {
+        st = RAY_STACK_OVERFLOW;
+        run = false;
+      } else {
+        pop();
+      }
+    }
+
+    // ---- leaves: the FP32 filter decides what it can ----
+    const bool leaf = run && ref_is_leaf(ref);
+    int32_t first = 0;
+    unsigned need = 0u;  // tets of the leaf that take the exact test
+    if (leaf) {
+      first = leaf_first(ref);
+      const int32_t count = leaf_count(ref);
+      for (int32_t q = 0; q < count; ++q) {
+        cnt.prim++;
+        if (MIXED) {
+          const float4* f = T.prim32 + 4 * (int64_t)(first + q);
+          const int c = tet_filter32(px, py, pz, pabs, __ldg(f), __ldg(f + 1), __ldg(f + 2),
+                                     __ldg(f + 3));
+          if (c < 0) continue;
+          if (c > 0) {
+            take(__ldg(&T.prim_ref[first + q]));
+            continue;
+          }
+          cnt.esc++;
+        }
+        need |= 1u << q;
+      }
+    }
+    // ---- the exact tests, every lane's next pending tet at once ----
+    while (__any_sync(kFullMask, need != 0u)) {
+      if (need != 0u) {
+        const int q = __ffs(need) - 1;
+        need &= need - 1u;
+        const double* v = T.prim64 + 12 * (int64_t)(first + q);
+        const d3 v0 = mk3(__ldg(v + 0), __ldg(v + 1), __ldg(v + 2));
+        const d3 v1 = mk3(__ldg(v + 3), __ldg(v + 4), __ldg(v + 5));
+        const d3 v2 = mk3(__ldg(v + 6), __ldg(v + 7), __ldg(v + 8));
+        const d3 v3 = mk3(__ldg(v + 9), __ldg(v + 10), __ldg(v + 11));
+        if (tet_contains64(p, v0, v1, v2, v3)) take(__ldg(&T.prim_ref[first + q]));
+      }
+    }
+    if (leaf) pop();
+  }
+  if (i < a.n) {
+    if (a.id_out) a.id_out[i] = best_id;
+    if (a.index_out) a.index_out[i] = best_idx;
+    if (a.status) a.status[i] = st;
+  }
+  if (a.counters) flush_counters(a.counters, cnt, i < a.n ? 1ull : 0ull);
+}
+
 inline unsigned grid_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
 }  // namespace
@@ -391,7 +544,7 @@ cudaError_t launch_closest(bool mixed, const PointArgs& a, cudaStream_t st) {
 cudaError_t launch_find_element(bool mixed, const PointArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
   if (mixed)
-    k_find_element<true><<<grid_for(a.n), kBlock, 0, st>>>(a);
+    k_find_element_lane<true><<<grid_for(a.n), kBlock, 0, st>>>(a);
   else
     k_find_element<false><<<grid_for(a.n), kBlock, 0, st>>>(a);
   return cudaGetLastError();
