@@ -66,3 +66,68 @@ def test_single_rank_is_identity(n):
     from xdg_gb300 import dist as xd
     assert xd.max_over_ranks(3.5, 1) == 3.5
     assert xd.sum_over_ranks(3.5, 1) == 3.5
+
+
+def _split_worker(rank, world, port, q):
+    """One rank of a sharded ray_fire: the rank traces its shard_range slice of
+    a shared batch (here with the CPU oracle, standing in for the engine on a
+    rank's GPU) and the slices are gathered by rank order."""
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from oracle import oracle as xo
+    from xdg_gb300 import dist as xd
+    from xdg_gb300 import synth
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        r, w, _ = xd.env_rank()
+        m = synth.single_sphere_in_box(level=3)
+        o, d = synth.lcg_ball_rays(3001, 9.9, seed=12345)
+        lo, hi = xd.shard_range(len(o), r, w)
+        t, s, f = xo.volume_tree(m, 1).ray_fire(o[lo:hi], d[lo:hi], threads=1)
+        # gather the slices (sizes differ by at most one): pad, all_gather, trim
+        cap = xd.shard_range(len(o), 0, w)[1]
+        buf = torch.full((cap, 3), -2.0, dtype=torch.float64)
+        buf[:hi - lo, 0] = torch.from_numpy(t)
+        buf[:hi - lo, 1] = torch.from_numpy(s.astype(np.float64))
+        buf[:hi - lo, 2] = torch.from_numpy(f.astype(np.float64))
+        parts = [torch.empty_like(buf) for _ in range(w)]
+        dist.all_gather(parts, buf)
+        if r == 0:
+            rows = [parts[k][:xd.shard_range(len(o), k, w)[1] - xd.shard_range(len(o), k, w)[0]]
+                    for k in range(w)]
+            q.put(torch.cat(rows).numpy())
+        else:
+            q.put(None)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_batch_equals_one_rank():
+    """A batch split with shard_range over two gloo ranks, each tracing its own
+    slice, gives the single-process results once gathered in rank order."""
+    import numpy as np
+    import torch.multiprocessing as mp
+    from oracle import oracle as xo
+    from xdg_gb300 import synth
+    xo.build()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_split_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=180) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    got = next(x for x in res if x is not None)
+    m = synth.single_sphere_in_box(level=3)
+    o, d = synth.lcg_ball_rays(3001, 9.9, seed=12345)
+    t, s, f = xo.volume_tree(m, 1).ray_fire(o, d, threads=1)
+    assert got.shape == (3001, 3)
+    assert np.array_equal(got[:, 0], t)
+    assert np.array_equal(got[:, 1].astype(np.int32), s)
+    assert np.array_equal(got[:, 2].astype(np.int32), f)
