@@ -676,7 +676,7 @@ def bench_global_segments(torch, L, dev, stream, sptr, args, rank, world):
            "ms_per_step": ms, "fp64_ms_per_step": ms64, "mixed_equals_fp64": same,
            "tracks_with_status": int((st != 0).sum().item()),
            "step": "one xdgcu_segments_global call (all rounds: find_element, implicit-complement "
-                   "ray_fire + boundary-face re-entry, packed walk)"}
+                   "ray_fire + boundary-face re-entry, single-pass walk resumed across rounds)"}
     if rank == 0 and not args.no_oracle:
         from oracle import oracle as xo
         xo.build()

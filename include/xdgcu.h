@@ -282,13 +282,18 @@ int xdgcu_set_boundary_face_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* f
  * step to the hit plus TINY_BIT and re-enter through the boundary face's
  * element (xdgcu_set_boundary_face_elements; none: stop); walk_elements;
  * r += u * segment_sum, distance -= segment_sum.  All tracks advance
- * together: each round is one find_element, one ray_fire and one packed walk
- * launch over the active tracks, with the bookkeeping in device kernels.
+ * together: each round is one find_element launch for the tracks to locate,
+ * one ray_fire launch for those outside the mesh and one walk launch, with
+ * the bookkeeping in device kernels.  A round's walk emits at most K
+ * segments per track (K = 16..256, chosen so the round buffer stays near
+ * 1 GiB); a longer walk pauses and the next round resumes it from where it
+ * stopped, with the same operations as one uninterrupted walk.
  * Output as xdgcu_walk_elements_packed: track i's segments (element MESH
  * ids, lengths) at offsets[i] .. offsets[i+1]-1 of arrays of `capacity`
  * entries; a track that does not fit is not written (XDGCU_RAY_OUTPUT_FULL).
- * max_segs caps one walk of a track and max_rounds the rounds: a track cut
- * short by either gets XDGCU_RAY_WALK_LIMIT (the reference has no limit).
+ * max_segs caps one walk of a track and max_rounds the rounds (a paused
+ * walk's resumption takes a round): a track cut short by either gets
+ * XDGCU_RAY_WALK_LIMIT (the reference has no limit).
  * status (may be NULL) also records XDGCU_RAY_NO_EXIT_FACE (the track went
  * on, as the reference's does) and XDGCU_RAY_INVALID (non-finite input).
  * Host or device arrays (not mixed); scratch is allocated on `stream` with

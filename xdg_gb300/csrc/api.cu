@@ -937,6 +937,10 @@ struct CallScratch {
   }
 };
 
+// The K-strided walk buffer of xdgcu_segments_global (12 bytes per slot)
+// holds at most about this many bytes.
+constexpr int64_t kSegStridedBytes = int64_t(1) << 30;
+
 // D2H of one counter, waited for.
 cudaError_t read_count(const int32_t* d, int32_t* h, cudaStream_t st) {
   cudaError_t e = cudaMemcpyAsync(h, d, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
@@ -2086,11 +2090,22 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   API_CUDA(S.get(&ss.written, n), "segments scratch");
   API_CUDA(S.get(&ss.last, n), "segments scratch");
   API_CUDA(S.get(&ss.stopped, n), "segments scratch");
+  API_CUDA(S.get(&ss.wr, 3 * n), "segments scratch");
+  API_CUDA(S.get(&ss.wd, n), "segments scratch");
+  API_CUDA(S.get(&ss.wsum, n), "segments scratch");
+  API_CUDA(S.get(&ss.wcount, n), "segments scratch");
+  API_CUDA(S.get(&ss.welem, n), "segments scratch");
+  API_CUDA(S.get(&ss.paused, n), "segments scratch");
+  // segments per track and round of the single-pass walk: the K-strided
+  // buffer of one round holds at most about kSegStridedBytes
+  int32_t K = 256;
+  while (K > 16 && (int64_t)K * n * 12 > kSegStridedBytes) K >>= 1;
+  K = std::min(K, max_segs);
   int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *eid = nullptr, *eidx = nullptr;
   int32_t *walk_t = nullptr, *walk_start = nullptr, *out_t = nullptr, *surf = nullptr, *face = nullptr;
-  int32_t* wst = nullptr;
+  int32_t *wst = nullptr, *wcnt = nullptr, *wstop = nullptr, *loc = nullptr, *sk_elem = nullptr;
   double *pts = nullptr, *ray_org = nullptr, *ray_dir = nullptr, *t_hit = nullptr;
-  double *wr = nullptr, *wu = nullptr, *wd = nullptr;
+  double *wr = nullptr, *wu = nullptr, *wd = nullptr, *sk_len = nullptr;
   API_CUDA(S.get(&act, n), "segments scratch");
   API_CUDA(S.get(&act_next, n), "segments scratch");
   API_CUDA(S.get(&counters, 4), "segments scratch");
@@ -2102,6 +2117,11 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   API_CUDA(S.get(&surf, n), "segments scratch");
   API_CUDA(S.get(&face, n), "segments scratch");
   API_CUDA(S.get(&wst, n), "segments scratch");
+  API_CUDA(S.get(&wcnt, n), "segments scratch");
+  API_CUDA(S.get(&wstop, n), "segments scratch");
+  API_CUDA(S.get(&loc, n), "segments scratch");
+  API_CUDA(S.get(&sk_elem, (int64_t)K * n), "segments scratch");
+  API_CUDA(S.get(&sk_len, (int64_t)K * n), "segments scratch");
   API_CUDA(S.get(&pts, 3 * n), "segments scratch");
   API_CUDA(S.get(&ray_org, 3 * n), "segments scratch");
   API_CUDA(S.get(&ray_dir, 3 * n), "segments scratch");
@@ -2112,6 +2132,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   int32_t* n_act = counters;
   int32_t* n_walk = counters + 1;
   int32_t* n_out = counters + 2;
+  int32_t* n_loc = counters + 3;
   // one record per round for the final placement of its segments
   struct Round {
     int64_t m, total;
@@ -2132,28 +2153,39 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   }
   int32_t round = 0;
   for (; m > 0 && round < max_rounds; ++round) {
-    // find_element(r) in the element tree
-    API_CUDA(seg_gather_points(ss, act, m, pts, st), "segments gather");
-    int rc = xdgcu_find_element(c, element_tree, nullptr, m, pts, eid, eidx, nullptr, precision, st);
-    if (rc) return rc;
-    API_CUDA(cudaMemsetAsync(counters + 1, 0, 2 * sizeof(int32_t), st), "memset");
-    API_CUDA(seg_decide(ss, act, m, eid, eidx, walk_t, walk_start, n_walk, out_t, ray_org, ray_dir,
-                        n_out, st),
-             "segments decide");
-    int32_t h2[2] = {0, 0};
-    API_CUDA(cudaMemcpyAsync(h2, counters + 1, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "D2H");
+    // paused walks resume; the other active tracks are located
+    API_CUDA(cudaMemsetAsync(counters + 1, 0, 3 * sizeof(int32_t), st), "memset");
+    API_CUDA(seg_split(ss, act, m, walk_t, walk_start, n_walk, loc, n_loc, st), "segments split");
+    int32_t h3[3] = {0, 0, 0};  // n_walk, n_out, n_loc
+    API_CUDA(cudaMemcpyAsync(h3, counters + 1, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "D2H");
     API_CUDA(cudaStreamSynchronize(st), "sync");
-    int32_t m_walk = h2[0];
-    const int32_t m_out = h2[1];
-    if (m_out > 0) {
-      // ray_fire(ipc, r + u * TINY_BIT, u, INFTY, EXITING), then re-entry
-      rc = xdgcu_ray_fire(c, ipc_tree, nullptr, m_out, ray_org, ray_dir, nullptr, XDGCU_EXITING,
-                          nullptr, nullptr, t_hit, surf, face, nullptr, precision, st);
+    int32_t m_walk = h3[0];
+    const int32_t m_loc = h3[2];
+    int rc = XDGCU_OK;
+    if (m_loc > 0) {
+      // find_element(r) in the element tree
+      API_CUDA(seg_gather_points(ss, loc, m_loc, pts, st), "segments gather");
+      rc = xdgcu_find_element(c, element_tree, nullptr, m_loc, pts, eid, eidx, nullptr, precision, st);
       if (rc) return rc;
-      API_CUDA(seg_reenter(ss, out_t, m_out, t_hit, surf, face, c->d_bfe_face.p, c->d_bfe_elem.p,
-                           c->n_bfe, (int32_t)c->n_tet, walk_t, walk_start, n_walk, st),
-               "segments re-entry");
-      API_CUDA(read_count(n_walk, &m_walk, st), "segments count");
+      API_CUDA(seg_decide(ss, loc, m_loc, eid, eidx, walk_t, walk_start, n_walk, out_t, ray_org,
+                          ray_dir, n_out, st),
+               "segments decide");
+      int32_t h2[2] = {0, 0};
+      API_CUDA(cudaMemcpyAsync(h2, counters + 1, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
+               "D2H");
+      API_CUDA(cudaStreamSynchronize(st), "sync");
+      m_walk = h2[0];
+      const int32_t m_out = h2[1];
+      if (m_out > 0) {
+        // ray_fire(ipc, r + u * TINY_BIT, u, INFTY, EXITING), then re-entry
+        rc = xdgcu_ray_fire(c, ipc_tree, nullptr, m_out, ray_org, ray_dir, nullptr, XDGCU_EXITING,
+                            nullptr, nullptr, t_hit, surf, face, nullptr, precision, st);
+        if (rc) return rc;
+        API_CUDA(seg_reenter(ss, out_t, m_out, t_hit, surf, face, c->d_bfe_face.p, c->d_bfe_elem.p,
+                             c->n_bfe, (int32_t)c->n_tet, walk_t, walk_start, n_walk, st),
+                 "segments re-entry");
+        API_CUDA(read_count(n_walk, &m_walk, st), "segments count");
+      }
     }
     API_CUDA(cudaMemsetAsync(n_act, 0, sizeof(int32_t), st), "memset");
     if (m_walk > 0) {
@@ -2165,37 +2197,38 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
       API_CUDA(cudaMemcpyAsync(R.walk_t, walk_t, sizeof(int32_t) * m_walk, cudaMemcpyDeviceToDevice, st),
                "D2D");
       API_CUDA(seg_walk_inputs(ss, walk_t, m_walk, wr, wu, wd, st), "segments walk inputs");
-      // walk_elements(element, r, u, distance) of the round, packed
+      // walk_elements(element, r, u, distance) of the round, one pass, at
+      // most K segments per track into the K-strided buffer
       WalkArgs a = geo;
       a.n = m_walk;
       a.start = walk_start;
       a.org = wr;
       a.dir = wu;
       a.dist = wd;
-      a.max_segs = max_segs;
+      a.max_segs = K;
       a.status = wst;
-      a.offsets = R.off;
+      a.seg_count = wcnt;
+      a.stop_elem = wstop;
+      a.seg_elem = sk_elem;
+      a.seg_len = sk_len;
+      a.out_mode = WALK_STRIDED;
       rc = with_length_order(c, a, st, [&]() -> int {
-        a.out_mode = WALK_COUNT;
-        API_CUDA(launch_walk(mixed, c->face_order, a, st), "walk (count)");
-        int64_t* sums = nullptr;
-        API_CUDA(S.get(&sums, scan_scratch_entries(m_walk)), "scan scratch");
-        API_CUDA(scan_offsets(R.off, m_walk, sums, st), "scan");
-        API_CUDA(cudaMemcpyAsync(&R.total, R.off + m_walk, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
-                 "D2H");
-        API_CUDA(cudaStreamSynchronize(st), "sync");
-        API_CUDA(S.get(&R.seg_elem, R.total), "segments scratch");
-        API_CUDA(S.get(&R.seg_len, R.total), "segments scratch");
-        a.seg_elem = R.seg_elem;
-        a.seg_len = R.seg_len;
-        a.capacity = R.total;
-        a.out_mode = WALK_PACKED;
-        API_CUDA(launch_walk(mixed, c->face_order, a, st), "walk (emit)");
+        API_CUDA(launch_walk(mixed, c->face_order, a, st), "walk");
         return XDGCU_OK;
       });
       if (rc) return rc;
-      API_CUDA(seg_advance(ss, R.walk_t, m_walk, R.off, R.seg_elem, R.seg_len, wst, R.dst_rel,
-                           act_next, n_act, st),
+      // the segments each track keeps (max_segs per walk), packed
+      API_CUDA(seg_round_counts(ss, R.walk_t, m_walk, wcnt, max_segs, R.off, st), "segments counts");
+      int64_t* sums = nullptr;
+      API_CUDA(S.get(&sums, scan_scratch_entries(m_walk)), "scan scratch");
+      API_CUDA(scan_offsets(R.off, m_walk, sums, st), "scan");
+      API_CUDA(cudaMemcpyAsync(&R.total, R.off + m_walk, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
+               "D2H");
+      API_CUDA(cudaStreamSynchronize(st), "sync");
+      API_CUDA(S.get(&R.seg_elem, R.total), "segments scratch");
+      API_CUDA(S.get(&R.seg_len, R.total), "segments scratch");
+      API_CUDA(seg_advance(ss, R.walk_t, m_walk, K, sk_elem, sk_len, wcnt, wst, wstop, max_segs,
+                           R.off, R.seg_elem, R.seg_len, R.dst_rel, act_next, n_act, st),
                "segments advance");
       rounds.push_back(R);
     }

@@ -38,6 +38,7 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_init(SegState s, const double
   s.last[t] = -1;
   s.status[t] = RAY_OK;
   s.stopped[t] = 0;
+  s.paused[t] = 0;
   store3(s.r, t, a);
   if (!finite3(a) || !finite3(b)) {
     s.status[t] = RAY_INVALID;
@@ -57,6 +58,32 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_init(SegState s, const double
   }
   store3(s.u, t, mk3(w.x / len, w.y / len, w.z / len));
   act[atomicAdd(n_act, 1)] = (int32_t)t;
+}
+
+// A new walk of track t from its current r and distance (xdg.cpp:187).
+__device__ __forceinline__ void start_walk(const SegState& s, int32_t t) {
+  store3(s.wr, t, load3(s.r, t));
+  s.wd[t] = s.dist[t];
+  s.wsum[t] = 0.0;
+  s.wcount[t] = 0;
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_seg_split(SegState s, const int32_t* __restrict__ act,
+                                                          int64_t m, int32_t* __restrict__ walk_t,
+                                                          int32_t* __restrict__ walk_start,
+                                                          int32_t* __restrict__ n_walk,
+                                                          int32_t* __restrict__ loc,
+                                                          int32_t* __restrict__ n_loc) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const int32_t t = act[k];
+  if (s.paused[t]) {
+    const int32_t w = atomicAdd(n_walk, 1);
+    walk_t[w] = t;
+    walk_start[w] = s.welem[t];
+  } else {
+    loc[atomicAdd(n_loc, 1)] = t;
+  }
 }
 
 __global__ void __launch_bounds__(kSegBlock) k_seg_gather_points(SegState s,
@@ -79,6 +106,7 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_decide(
   // on the face of the element just walked: not inside it (xdg.cpp:161-162)
   if (s.written[t] > 0 && eid[k] == s.last[t]) cur = -1;
   if (cur >= 0) {
+    start_walk(s, t);
     const int32_t w = atomicAdd(n_walk, 1);
     walk_t[w] = t;
     walk_start[w] = cur;
@@ -129,6 +157,7 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_reenter(
     s.stopped[t] = 1;
     return;
   }
+  start_walk(s, t);
   const int32_t w = atomicAdd(n_walk, 1);
   walk_t[w] = t;
   walk_start[w] = e;
@@ -142,41 +171,84 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_walk_inputs(SegState s,
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= m) return;
   const int32_t t = walk_t[k];
-  store3(wr, k, load3(s.r, t));
+  store3(wr, k, load3(s.wr, t));
   store3(wu, k, load3(s.u, t));
-  wd[k] = s.dist[t];
+  wd[k] = s.wd[t];
+}
+
+__global__ void __launch_bounds__(kSegBlock) k_seg_round_counts(SegState s,
+                                                                 const int32_t* __restrict__ walk_t,
+                                                                 int64_t m,
+                                                                 const int32_t* __restrict__ cnt,
+                                                                 int32_t max_segs,
+                                                                 int64_t* __restrict__ off) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const int32_t left = max(0, max_segs - s.wcount[walk_t[k]]);
+  off[k] = min(cnt[k], left);
 }
 
 __global__ void __launch_bounds__(kSegBlock) k_seg_advance(
-    SegState s, const int32_t* __restrict__ walk_t, int64_t m, const int64_t* __restrict__ off,
+    SegState s, const int32_t* __restrict__ walk_t, int64_t m, int32_t K,
     const int32_t* __restrict__ seg_elem, const double* __restrict__ seg_len,
-    const int32_t* __restrict__ wst, int64_t* __restrict__ dst_rel, int32_t* __restrict__ act_next,
-    int32_t* __restrict__ n_act) {
+    const int32_t* __restrict__ cnt, const int32_t* __restrict__ wst,
+    const int32_t* __restrict__ wstop, int32_t max_segs, const int64_t* __restrict__ off,
+    int32_t* __restrict__ out_elem, double* __restrict__ out_len, int64_t* __restrict__ dst_rel,
+    int32_t* __restrict__ act_next, int32_t* __restrict__ n_act) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= m) return;
   const int32_t t = walk_t[k];
-  const int64_t o0 = off[k], o1 = off[k + 1];
-  // std::accumulate(vol_segments, 0.0, total + segment.second), in order
-  double sum = 0.0;
-  for (int64_t q = o0; q < o1; ++q) sum = sum + seg_len[q];
-  // r += u * segment_sum; distance -= segment_sum;
-  store3(s.r, t, advance3(load3(s.r, t), load3(s.u, t), sum));
+  const int64_t o = off[k], kept = off[k + 1] - o;
+  const int32_t* se = seg_elem + k * (int64_t)K;
+  const double* sl = seg_len + k * (int64_t)K;
+  // the walk's own updates per segment (walk.cu: distance -= len, r += len *
+  // u), and std::accumulate(vol_segments, 0.0, ...) continued across pauses
+  const d3 u = load3(s.u, t);
+  d3 wr = load3(s.wr, t);
+  double wd = s.wd[t], sum = s.wsum[t];
+  for (int64_t q = 0; q < kept; ++q) {
+    const double len = sl[q];
+    out_elem[o + q] = se[q];
+    out_len[o + q] = len;
+    sum = sum + len;
+    wd -= len;
+    wr = mk3(wr.x + len * u.x, wr.y + len * u.y, wr.z + len * u.z);
+  }
+  dst_rel[k] = s.written[t];
+  s.written[t] += kept;
+  if (kept > 0) s.last[t] = se[kept - 1];
+  const int32_t wc = s.wcount[t] + (int32_t)kept;
+  s.wcount[t] = wc;
+  const int32_t st = wst[k];
+  if (kept < cnt[k] || (st == RAY_WALK_LIMIT && wc >= max_segs)) {
+    // the walk passes max_segs segments: the track stops there
+    if (s.status[t] == RAY_OK) s.status[t] = RAY_WALK_LIMIT;
+    s.stopped[t] = 1;
+    s.paused[t] = 0;
+    return;
+  }
+  if (st == RAY_WALK_LIMIT) {  // paused at K segments: resumes next round
+    store3(s.wr, t, wr);
+    s.wd[t] = wd;
+    s.wsum[t] = sum;
+    s.welem[t] = wstop[k];
+    s.paused[t] = 1;
+    act_next[atomicAdd(n_act, 1)] = t;
+    return;
+  }
+  // the walk has ended: r += u * segment_sum; distance -= segment_sum;
+  s.paused[t] = 0;
+  store3(s.r, t, advance3(load3(s.r, t), u, sum));
   const double dist = s.dist[t] - sum;
   s.dist[t] = dist;
-  dst_rel[k] = s.written[t];
-  s.written[t] += o1 - o0;
-  if (o1 > o0) s.last[t] = seg_elem[o1 - 1];
-  const int32_t st = wst[k];
-  bool stop = false;
   if (st != RAY_OK) {
     if (s.status[t] == RAY_OK) s.status[t] = st;
-    // a walk cut short by the segment limit or invalid data does not go on;
-    // a walk that found no exit face ended as the reference's does
-    stop = st != RAY_NO_EXIT_FACE;
-  }
-  if (stop) {
-    s.stopped[t] = 1;
-    return;
+    // a walk that found no exit face ended as the reference's does; invalid
+    // data does not go on
+    if (st != RAY_NO_EXIT_FACE) {
+      s.stopped[t] = 1;
+      return;
+    }
   }
   if (gt0(dist)) act_next[atomicAdd(n_act, 1)] = t;  // while (distance > 0)
 }
@@ -232,6 +304,21 @@ cudaError_t seg_init(const SegState& s, const double* starts, const double* ends
   return cudaGetLastError();
 }
 
+cudaError_t seg_split(const SegState& s, const int32_t* act, int64_t m, int32_t* walk_t,
+                      int32_t* walk_start, int32_t* n_walk, int32_t* loc, int32_t* n_loc,
+                      cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  k_seg_split<<<seg_grid(m), kSegBlock, 0, st>>>(s, act, m, walk_t, walk_start, n_walk, loc, n_loc);
+  return cudaGetLastError();
+}
+
+cudaError_t seg_round_counts(const SegState& s, const int32_t* walk_t, int64_t m,
+                             const int32_t* cnt, int32_t max_segs, int64_t* off, cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  k_seg_round_counts<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, cnt, max_segs, off);
+  return cudaGetLastError();
+}
+
 cudaError_t seg_gather_points(const SegState& s, const int32_t* act, int64_t m, double* pts,
                               cudaStream_t st) {
   if (m <= 0) return cudaSuccess;
@@ -267,11 +354,14 @@ cudaError_t seg_walk_inputs(const SegState& s, const int32_t* walk_t, int64_t m,
   return cudaGetLastError();
 }
 
-cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, const int64_t* off,
-                        const int32_t* seg_elem, const double* seg_len, const int32_t* wst,
-                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st) {
+cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, int32_t K,
+                        const int32_t* seg_elem, const double* seg_len, const int32_t* cnt,
+                        const int32_t* wst, const int32_t* wstop, int32_t max_segs,
+                        const int64_t* off, int32_t* out_elem, double* out_len, int64_t* dst_rel,
+                        int32_t* act_next, int32_t* n_act, cudaStream_t st) {
   if (m <= 0) return cudaSuccess;
-  k_seg_advance<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, off, seg_elem, seg_len, wst,
+  k_seg_advance<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, K, seg_elem, seg_len, cnt, wst,
+                                                    wstop, max_segs, off, out_elem, out_len,
                                                     dst_rel, act_next, n_act);
   return cudaGetLastError();
 }

@@ -15,11 +15,16 @@
 //            plus TINY_BIT and continues in the element behind the hit face
 //            (get_boundary_face_element); a miss, a hit beyond the distance or
 //            a face without an element ends the track (xdg.cpp:166-183);
-//   walk     walk_elements(element, r, u, distance) of the walk list (packed,
-//            one buffer per round);
-//   advance  segment_sum = the round's lengths summed in order, r += u *
-//            segment_sum, distance -= segment_sum (xdg.cpp:188-193); tracks
-//            with distance > 0 stay active.
+//   walk     walk_elements(element, r, u, distance) of the walk list, at most
+//            K segments per track and round (one pass, K-strided buffer): a
+//            walk that reaches K pauses, and the next round resumes it where
+//            it stopped (the element the walk kernel reports, the position
+//            and remaining distance rebuilt from the emitted lengths with the
+//            walk's own operations) without locating the track again;
+//   advance  the round's segments packed into a buffer of the round, the
+//            walk's segment_sum summed in order across its pauses; when the
+//            walk ends, r += u * segment_sum and distance -= segment_sum
+//            (xdg.cpp:188-193); tracks with distance > 0 stay active.
 // When no track is active, the per-track totals are scanned into the output
 // offsets and every round's segments are copied to their place.
 #pragma once
@@ -39,12 +44,28 @@ struct SegState {
   int32_t* last;     // mesh id of the last segment (valid when written > 0)
   int32_t* status;   // per track: XDGCU_RAY_* (OK until something stops it)
   int8_t* stopped;   // the track's loop has returned
+  // the walk in progress (walk_elements(element, r, u, distance) of one
+  // iteration of the loop): its own position and remaining distance, the
+  // sum of its segments so far, their number, where it resumes, and whether
+  // it is paused at the per-round segment cap
+  double* wr;        // 3 per track
+  double* wd;
+  double* wsum;
+  int32_t* wcount;
+  int32_t* welem;
+  int8_t* paused;
 };
 
 // u = (end - start) / |end - start|, distance = |end - start|, r = start
 // (xdg.cpp:148-153); tracks with distance > 0 are appended to `act`.
 cudaError_t seg_init(const SegState& s, const double* starts, const double* ends, int32_t* act,
                      int32_t* n_act, cudaStream_t st);
+
+// The active tracks: paused walks to the walk list (resumed at welem), the
+// others to `loc` (to be located).
+cudaError_t seg_split(const SegState& s, const int32_t* act, int64_t m, int32_t* walk_t,
+                      int32_t* walk_start, int32_t* n_walk, int32_t* loc, int32_t* n_loc,
+                      cudaStream_t st);
 
 // pts[k] = r[act[k]]
 cudaError_t seg_gather_points(const SegState& s, const int32_t* act, int64_t m, double* pts,
@@ -66,17 +87,27 @@ cudaError_t seg_reenter(const SegState& s, const int32_t* out_t, int64_t m, cons
                         const int32_t* bfe_elem, int64_t n_bfe, int32_t n_tets, int32_t* walk_t,
                         int32_t* walk_start, int32_t* n_walk, cudaStream_t st);
 
-// The walk's inputs for the walk list: wr[k] = r[t], wu[k] = u[t], wd[k] = dist[t].
-cudaError_t seg_walk_inputs(const SegState& s, const int32_t* walk_t, int64_t m, double* wr,
-                            double* wu, double* wd, cudaStream_t st);
+// The walk's inputs for the walk list, from each track's walk state:
+// xr[k] = wr[t], xu[k] = u[t], xd[k] = wd[t].
+cudaError_t seg_walk_inputs(const SegState& s, const int32_t* walk_t, int64_t m, double* xr,
+                            double* xu, double* xd, cudaStream_t st);
 
-// After the round's packed walk (offsets off[0..m], segments seg_elem /
-// seg_len, per-entry status wst): segment_sum, the position and distance
-// updates, dst_rel[k] = the track's segments written before this round; the
-// tracks still active are appended to act_next.
-cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, const int64_t* off,
-                        const int32_t* seg_elem, const double* seg_len, const int32_t* wst,
-                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st);
+// off[k] = the segments of walk entry k this round keeps: its count, cut
+// where the walk would pass max_segs segments.
+cudaError_t seg_round_counts(const SegState& s, const int32_t* walk_t, int64_t m,
+                             const int32_t* cnt, int32_t max_segs, int64_t* off, cudaStream_t st);
+
+// After the round's walk (K-strided segments seg_elem / seg_len, counts cnt,
+// statuses wst, resume elements wstop) and the scan of the kept counts into
+// off[0..m]: the kept segments to out_elem / out_len at off[k], the walk
+// state advanced, dst_rel[k] = the track's segments written before this
+// round; a walk that ends applies segment_sum to r and distance; the tracks
+// still active (paused or with distance left) are appended to act_next.
+cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, int32_t K,
+                        const int32_t* seg_elem, const double* seg_len, const int32_t* cnt,
+                        const int32_t* wst, const int32_t* wstop, int32_t max_segs,
+                        const int64_t* off, int32_t* out_elem, double* out_len, int64_t* dst_rel,
+                        int32_t* act_next, int32_t* n_act, cudaStream_t st);
 
 // Tracks still active after the last allowed round end with `code`.
 cudaError_t seg_stop_active(const SegState& s, const int32_t* act, int64_t m, int32_t code,

@@ -341,6 +341,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
           if (a.out_mode == WALK_PACKED && !oe && k > 0 && st == RAY_OK) st = RAY_OUTPUT_FULL;
         }
         if (a.status) a.status[i] = st;
+        if (a.stop_elem) a.stop_elem[i] = elem;  // where a capped walk resumes
         has = false;
         tracks++;
       }
@@ -559,6 +560,7 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
           if (a.out_mode == WALK_PACKED && !oe && k > 0 && st == RAY_OK) st = RAY_OUTPUT_FULL;
         }
         if (a.status) a.status[i] = st;
+        if (a.stop_elem) a.stop_elem[i] = elem;  // where a capped walk resumes
         has = false;
         tracks++;
       } else {
@@ -701,6 +703,7 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
           if (a.out_mode == WALK_PACKED && !oe && k > 0 && st == RAY_OK) st = RAY_OUTPUT_FULL;
         }
         if (a.status) a.status[i] = st;
+        if (a.stop_elem) a.stop_elem[i] = elem;  // where a capped walk resumes
         has = false;
         tracks++;
       }

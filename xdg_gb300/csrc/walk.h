@@ -33,6 +33,9 @@ struct WalkArgs {
   int32_t* status;
   int32_t* next_out;     // next_element mode
   double* dist_out;
+  // walk modes, optional: the tet index a track stopped in (-1 when it left
+  // the mesh); for a track stopped by max_segs, where its walk goes on
+  int32_t* stop_elem;
   unsigned long long* counters;
   // output layout: 0 = track-major with stride max_segs; 1 = count only
   // (offsets[i] = number of segments of track i); 2 = packed, track i's
