@@ -170,3 +170,30 @@ def test_tet_cube_tracks_leaving_the_mesh(cuda, oracle, prec):
     a = np.concatenate([rng.uniform(0.2, 7.8, (n // 2, 3)), rng.uniform(-6, 14, (n // 2, 3))])
     b = rng.uniform(-6, 14, (n, 3))
     compare(oracle, m, a, b, prec)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_paused_walks_resume_exactly(cuda, oracle, prec):
+    """Walks capped at 1, 3 and 8 segments per round pause and resume across
+    many rounds; the segments equal the uncapped loop's and the oracle's."""
+    m = _gapped_blocks()
+    x = XDG(m)
+    x.prepare_raytracer()
+    rng = np.random.default_rng(41)
+    n = 600
+    a = rng.uniform([-4, -4, -4], [26, 23, 14], (n, 3))
+    b = rng.uniform([-4, -4, -4], [26, 23, 14], (n, 3))
+    ref = x.segments_global(a, b, precision=prec)
+    try:
+        for cap in (1, 3, 8):
+            x.rti.set_tuning("segments_walk_cap", cap)
+            got = x.segments_global(a, b, precision=prec)
+            for u, v, what in zip(got, ref, ("elements", "lengths", "offsets")):
+                assert np.array_equal(u, v), f"cap {cap}: {what}"
+    finally:
+        x.rti.set_tuning("segments_walk_cap", 0)
+    g = oracle.GlobalTracker(m)
+    el, ln, off = ref
+    for i in range(0, n, 7):
+        oe, ol = g.segments(a[i], b[i])
+        assert np.array_equal(el[off[i]:off[i + 1]], oe) and np.array_equal(ln[off[i]:off[i + 1]], ol)

@@ -409,6 +409,7 @@ struct xdgcu_ctx {
   int32_t closest_node_steps = 8;       // closest: inner-node steps between leaf phases (mixed)
   int32_t closest_node_steps_fp64 = 1;  // the same, all-FP64 path
   int32_t find_node_steps_fp64 = 16;    // find_element, all-FP64 path: the same
+  int32_t segments_walk_cap = 0;  // segments_global: segments per walk and round (0 = automatic)
   bool pageable_direct = false;
   // host_direct 5: trial calls of in place (0) and staged (1), their summed
   // seconds per ray, and the policy chosen (-1 until both have kAutoTrials)
@@ -1407,6 +1408,10 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     (k == "closest_node_steps"        ? c->closest_node_steps
      : k == "closest_node_steps_fp64" ? c->closest_node_steps_fp64
                                       : c->find_node_steps_fp64) = (int32_t)value;
+  } else if (k == "segments_walk_cap") {
+    if (value < 0 || value > 1024)
+      return set_err(XDGCU_ERR_INVALID_ARG, "segments_walk_cap must be 0..1024");
+    c->segments_walk_cap = (int32_t)value;
   } else if (k == "closest_bound") {
     if (value < 0 || value > 1) return set_err(XDGCU_ERR_INVALID_ARG, "closest_bound must be 0 or 1");
     c->closest_bound = (int32_t)value;
@@ -1455,6 +1460,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "closest_node_steps") *value = c->closest_node_steps;
   else if (k == "closest_node_steps_fp64") *value = c->closest_node_steps_fp64;
   else if (k == "find_node_steps_fp64") *value = c->find_node_steps_fp64;
+  else if (k == "segments_walk_cap") *value = c->segments_walk_cap;
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else if (k == "host_direct_choice") *value = c->hd_choice;
@@ -2100,6 +2106,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   // buffer of one round holds at most about kSegStridedBytes
   int32_t K = 256;
   while (K > 16 && (int64_t)K * n * 12 > kSegStridedBytes) K >>= 1;
+  if (c->segments_walk_cap > 0) K = c->segments_walk_cap;
   K = std::min(K, max_segs);
   int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *eid = nullptr, *eidx = nullptr;
   int32_t *walk_t = nullptr, *walk_start = nullptr, *out_t = nullptr, *surf = nullptr, *face = nullptr;
