@@ -69,6 +69,8 @@ SURF_CHECK = 1_000
 SURF_CPU_SAMPLE = 20_000
 REF_STEP_SAMPLE = 1_000_000  # rays per step of --impl reference
 CLOSEST_POINTS = 1_000_000   # closest-facet queries (the first points of the ray origins)
+QUERY_CHECK = 100_000        # headline points whose point_in_volume / occluded the oracle repeats
+CLOSEST_CHECK = 20_000       # of the closest queries, repeated by the oracle
 BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
 BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
 BYTES_TRI64 = 76            # 72 B FP64 triangle + 4 B id (escalations)
@@ -272,6 +274,49 @@ def oracle_find_volume(trees, model, p, d, cores):
         vols[todo[ins]] = v
         todo = todo[~ins]
     return vols
+
+
+def oracle_queries(trees, model, p, d, vols, piv, occ, occ_dist, clo_d, clo_f, cores):
+    """point_in_volume, occluded and closest of the headline workload repeated
+    by the oracle on evenly spaced samples (each point in the volume it was
+    queried in), compared with the mixed-precision results bit for bit.  The
+    same oracle calls, timed on every host core, give each query's CPU
+    baseline."""
+    out = {}
+    n = len(p)
+    qsel = np.arange(0, n, max(1, n // QUERY_CHECK))
+    csel = np.arange(0, len(clo_d), max(1, len(clo_d) // CLOSEST_CHECK))
+
+    def per_volume(sel, fn):
+        """[(indices, oracle result)] per volume, and the oracle's seconds."""
+        parts, secs = [], 0.0
+        for v in model.volumes:
+            s = sel[vols[sel] == v]
+            if len(s):
+                t0 = time.perf_counter()
+                res = fn(trees[v], s)
+                secs += time.perf_counter() - t0
+                parts.append((s, res))
+        return parts, secs
+
+    parts, secs = per_volume(qsel, lambda t, s: t.point_in_volume(p[s], d[s], threads=cores))
+    out["point_in_volume"] = {
+        "points": int(len(qsel)),
+        "mismatches": sum(int((res != piv[s]).sum()) for s, res in parts),
+        "cpu_Mpoints_s": len(qsel) / secs / 1e6}
+    parts, secs = per_volume(qsel, lambda t, s: t.occluded(p[s], d[s], threads=cores))
+    out["occluded"] = {
+        "rays": int(len(qsel)),
+        "flag_mismatches": sum(int((res[0] != occ[s]).sum()) for s, res in parts),
+        "distance_mismatches": sum(int((res[1] != occ_dist[s]).sum()) for s, res in parts),
+        "cpu_Mrays_s": len(qsel) / secs / 1e6}
+    parts, secs = per_volume(csel, lambda t, s: t.closest(p[s], threads=cores))
+    out["closest"] = {
+        "points": int(len(csel)),
+        "distance_mismatches": sum(int((res[0] != clo_d[s]).sum()) for s, res in parts),
+        "face_mismatches": sum(int((res[1] != clo_f[s]).sum()) for s, res in parts),
+        "cpu_Mpoints_s": len(csel) / secs / 1e6}
+    return out
 
 
 # --------------------------------------------------------------------------
@@ -899,7 +944,9 @@ def run_engine(args, rank, world, local):
         rti.set_tuning("host_direct", old_hd)
         return dist.max_over_ranks((time.perf_counter() - te) / e2e_steps * 1e3, world), choice
 
-    e2e_steps = max(3, args.steps // 2)
+    # one call is ~7.5 ms: 20 or more keep a single slow call from moving the
+    # figure by more than a few tenths of a percent
+    e2e_steps = max(20, args.steps)
     hd_default = rti.get_tuning("host_direct")
     pinned = (tr_h, org_h, dir_h, to_h, so_h, fo_h)
     ms_e2e, hd_choice = e2e_ms(pinned, hd_default)
@@ -948,24 +995,30 @@ def run_engine(args, rank, world, local):
     ipc = model.implicit_complement
     not_ipc = torch.from_numpy(vols_h != ipc).to(dev)
     piv_inside_frac = float(piv_out[not_ipc].float().mean().item()) if not_ipc.any() else 1.0
+    piv_h = piv_out.cpu().numpy()
     ms_piv64 = timed(torch, piv(FP64), 3, 1, world, stream)
+    piv_same = bool(np.array_equal(piv_out.cpu().numpy(), piv_h))
 
     # occluded (any hit, embree/ray_tracer.cpp:347-370) of the same rays, and
     # closest (the nearest facet, :328-345) of the first CLOSEST_POINTS points
     occ_out = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+    occ_dist = torch.empty(N_RAYS, dtype=torch.float64, device=dev)
 
     def occ(prec):
         def go():
             rc = L.xdgcu_occluded(rti.ctx, 0, ctypes.c_void_p(trees.data_ptr()), N_RAYS,
                                   ctypes.c_void_p(p.data_ptr()), ctypes.c_void_p(d.data_ptr()),
-                                  ctypes.c_void_p(occ_out.data_ptr()), None, None, prec, sptr)
+                                  ctypes.c_void_p(occ_out.data_ptr()),
+                                  ctypes.c_void_p(occ_dist.data_ptr()), None, prec, sptr)
             _lib.check(rc, rti.ctx, "occluded")
         return go
 
     ms_occ = timed(torch, occ(MIXED), max(3, args.steps // 4), 2, world, stream)
     occ_mixed = occ_out.clone()
+    occ_h, occ_dist_h = occ_out.cpu().numpy(), occ_dist.cpu().numpy()
     ms_occ64 = timed(torch, occ(FP64), 3, 1, world, stream)
     occ_same = bool(torch.equal(occ_out, occ_mixed))
+    del occ_dist
     n_clo = min(N_RAYS, CLOSEST_POINTS)
     clo_d = torch.empty(n_clo, dtype=torch.float64, device=dev)
     clo_f = torch.empty(n_clo, dtype=torch.int32, device=dev)
@@ -980,6 +1033,7 @@ def run_engine(args, rank, world, local):
 
     ms_clo = timed(torch, clo(MIXED), 3, 2, world, stream)
     clo_mixed = (clo_d.clone(), clo_f.clone())
+    clo_d_h, clo_f_h = clo_d.cpu().numpy(), clo_f.cpu().numpy()
     ms_clo64 = timed(torch, clo(FP64), 3, 1, world, stream)
     clo_same = bool(torch.equal(clo_d, clo_mixed[0]) and torch.equal(clo_f, clo_mixed[1]))
     rti.set_tuning("closest_bound", 0)
@@ -1040,6 +1094,7 @@ def run_engine(args, rank, world, local):
     # oracle agreement on a sample (rank 0)
     oracle_mism = None
     fv_oracle = None
+    query_oracle = {}
     cpu_baseline = None
     if rank == 0 and not args.no_oracle:
         from oracle import oracle as xo
@@ -1064,6 +1119,8 @@ def run_engine(args, rank, world, local):
         fv_oracle = {"points": int(len(fsel)), "mismatches": int((ovols != fv_h).sum()),
                      "host_path_mismatches": int((ovols != vols_h[fsel]).sum()),
                      "volumes_seen": int(len(np.unique(ovols)))}
+        query_oracle = oracle_queries(otrees, model, p_h, d_h, vols_h, piv_h, occ_h, occ_dist_h,
+                                      clo_d_h, clo_f_h, cores)
         # CPU baseline: the oracle (C restatement of the FP64 path) on the host cores
         cs = min(CPU_SAMPLE, N_RAYS)
         tc = time.perf_counter()
@@ -1363,11 +1420,14 @@ def run_engine(args, rank, world, local):
             "value": total_rays / (ms_piv / 1e3) / 1e6, "unit": "Mpoints/s",
             "fp64_value": total_rays / (ms_piv64 / 1e3) / 1e6,
             "inside_fraction_own_volume": piv_inside_frac,
+            "mixed_equals_fp64": piv_same,
+            "oracle_check": query_oracle.get("point_in_volume"),
         },
         "occluded": {
             "value": total_rays / (ms_occ / 1e3) / 1e6, "unit": "Mrays/s",
             "fp64_value": total_rays / (ms_occ64 / 1e3) / 1e6,
             "mixed_equals_fp64": occ_same,
+            "oracle_check": query_oracle.get("occluded"),
         },
         "closest": {
             "points": n_clo, "unit": "Mpoints/s",
@@ -1375,6 +1435,7 @@ def run_engine(args, rank, world, local):
             "fp64_value": dist.sum_over_ranks(n_clo, world) / (ms_clo64 / 1e3) / 1e6,
             "value_without_triangle_bound": dist.sum_over_ranks(n_clo, world) / (ms_clo_nb / 1e3) / 1e6,
             "mixed_equals_fp64": clo_same,
+            "oracle_check": query_oracle.get("closest"),
         },
         "find_volume": {
             "value": total_rays / (ms_fv / 1e3) / 1e6, "unit": "Mpoints/s",
@@ -1434,7 +1495,14 @@ def run_engine(args, rank, world, local):
                 "find_volume": fv_oracle["mismatches"] if fv_oracle else None,
                 "walk": (walk_oracle["count_mismatches"] + walk_oracle["element_mismatches"]
                          + walk_oracle["length_mismatches"] + walk_oracle["status_mismatches"]
-                         + walk_oracle["find_element_mismatches"]) if walk_oracle else None},
+                         + walk_oracle["find_element_mismatches"]) if walk_oracle else None,
+                "point_in_volume": (query_oracle["point_in_volume"]["mismatches"]
+                                    if query_oracle else None),
+                "occluded": (query_oracle["occluded"]["flag_mismatches"]
+                             + query_oracle["occluded"]["distance_mismatches"]
+                             if query_oracle else None),
+                "closest": (query_oracle["closest"]["distance_mismatches"]
+                            + query_oracle["closest"]["face_mismatches"] if query_oracle else None)},
             "global_segments_Msegs_s": {
                 "mixed": round(global_segments["value"], 1),
                 "fp64": round(global_segments["fp64_value"], 1),

@@ -726,7 +726,8 @@ struct RayArr {
 
 // Staged calls run in chunks of this many rays, at most kMaxChunks: 2^21 per
 // chunk ran ray_fire over 1e7 host rays in 10.1 ms, 2^20 in 10.7 ms and 2^19
-// in 12.6 ms (each chunk's launch ends with a tail of a few slow rays).
+// in 12.6 ms with one launch stream (each chunk's launch ends with a tail of
+// a few slow rays); two alternating streams overlap those tails.
 constexpr int64_t kChunkRays = 1 << 21;
 constexpr int64_t kMaxChunks = 16;
 // host_direct 5: timed calls of each policy before the choice
@@ -808,11 +809,14 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
   // chunk k covers rays [starts[k], starts[k+1]).  With more than one, a
   // first chunk of a quarter of the others starts the kernels after a short
   // copy (ray_fire over 1e7 page-locked host rays: 1202 -> 1246 Mrays/s).
-  const int64_t per = (n + chunks - 1) / chunks;
+  // Shorter first and last chunks (2^17 rays doubling up to 2^21 and back)
+  // were slower, 7.55 against 7.40 ms per call: a small chunk's launch is
+  // as long as its slowest rays, and two streams overlap only two launches.
   std::vector<int64_t> starts;
   if (chunks == 1) {
     starts = {0, n};
   } else {
+    const int64_t per = (n + chunks - 1) / chunks;
     const int64_t f = std::max<int64_t>(1 << 18, per / 4);
     const int64_t per2 = (n - f + chunks - 1) / chunks;
     starts.push_back(0);
