@@ -2117,6 +2117,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   int32_t *wst = nullptr, *wcnt = nullptr, *wstop = nullptr, *loc = nullptr, *sk_elem = nullptr;
   double *pts = nullptr, *ray_org = nullptr, *ray_dir = nullptr, *t_hit = nullptr;
   double *wr = nullptr, *wu = nullptr, *wd = nullptr, *sk_len = nullptr;
+  double *wsum_in = nullptr, *wsum_out = nullptr, *wend_r = nullptr, *wend_d = nullptr;
   API_CUDA(S.get(&act, n), "segments scratch");
   API_CUDA(S.get(&act_next, n), "segments scratch");
   API_CUDA(S.get(&counters, 4), "segments scratch");
@@ -2140,6 +2141,10 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   API_CUDA(S.get(&wr, 3 * n), "segments scratch");
   API_CUDA(S.get(&wu, 3 * n), "segments scratch");
   API_CUDA(S.get(&wd, n), "segments scratch");
+  API_CUDA(S.get(&wsum_in, n), "segments scratch");
+  API_CUDA(S.get(&wsum_out, n), "segments scratch");
+  API_CUDA(S.get(&wend_r, 3 * n), "segments scratch");
+  API_CUDA(S.get(&wend_d, n), "segments scratch");
   int32_t* n_act = counters;
   int32_t* n_walk = counters + 1;
   int32_t* n_out = counters + 2;
@@ -2207,9 +2212,10 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
       API_CUDA(S.get(&R.dst_rel, m_walk), "segments scratch");
       API_CUDA(cudaMemcpyAsync(R.walk_t, walk_t, sizeof(int32_t) * m_walk, cudaMemcpyDeviceToDevice, st),
                "D2D");
-      API_CUDA(seg_walk_inputs(ss, walk_t, m_walk, wr, wu, wd, st), "segments walk inputs");
+      API_CUDA(seg_walk_inputs(ss, walk_t, m_walk, wr, wu, wd, wsum_in, st), "segments walk inputs");
       // walk_elements(element, r, u, distance) of the round, one pass, at
-      // most K segments per track into the K-strided buffer
+      // most K segments per track into the K-strided buffer; the walk reports
+      // where it stopped and continues each track's sum of lengths
       WalkArgs a = geo;
       a.n = m_walk;
       a.start = walk_start;
@@ -2220,6 +2226,10 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
       a.status = wst;
       a.seg_count = wcnt;
       a.stop_elem = wstop;
+      a.sum_in = wsum_in;
+      a.sum_out = wsum_out;
+      a.end_r = wend_r;
+      a.end_dist = wend_d;
       a.seg_elem = sk_elem;
       a.seg_len = sk_len;
       a.out_mode = WALK_STRIDED;
@@ -2238,8 +2248,10 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
       API_CUDA(cudaStreamSynchronize(st), "sync");
       API_CUDA(S.get(&R.seg_elem, R.total), "segments scratch");
       API_CUDA(S.get(&R.seg_len, R.total), "segments scratch");
-      API_CUDA(seg_advance(ss, R.walk_t, m_walk, K, sk_elem, sk_len, wcnt, wst, wstop, max_segs,
-                           R.off, R.seg_elem, R.seg_len, R.dst_rel, act_next, n_act, st),
+      API_CUDA(seg_pack(m_walk, K, sk_elem, sk_len, R.off, R.seg_elem, R.seg_len, st),
+               "segments pack");
+      API_CUDA(seg_advance(ss, R.walk_t, m_walk, K, sk_elem, wcnt, wst, wstop, wend_r, wend_d,
+                           wsum_out, max_segs, R.off, R.dst_rel, act_next, n_act, st),
                "segments advance");
       rounds.push_back(R);
     }

@@ -4,6 +4,8 @@
 // (-fmad=false).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "internal.cuh"
 #include "segments.h"
 
@@ -167,13 +169,15 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_walk_inputs(SegState s,
                                                                 const int32_t* __restrict__ walk_t,
                                                                 int64_t m, double* __restrict__ wr,
                                                                 double* __restrict__ wu,
-                                                                double* __restrict__ wd) {
+                                                                double* __restrict__ wd,
+                                                                double* __restrict__ wsum) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= m) return;
   const int32_t t = walk_t[k];
   store3(wr, k, load3(s.wr, t));
   store3(wu, k, load3(s.u, t));
   wd[k] = s.wd[t];
+  wsum[k] = s.wsum[t];
 }
 
 __global__ void __launch_bounds__(kSegBlock) k_seg_round_counts(SegState s,
@@ -188,35 +192,44 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_round_counts(SegState s,
   off[k] = min(cnt[k], left);
 }
 
+// Warp-per-row copy: row k's kept entries, read from the K-strided buffer and
+// written contiguously, 32 at a time.
+__global__ void __launch_bounds__(kSegBlock) k_seg_pack(int64_t m, int32_t K,
+                                                         const int32_t* __restrict__ seg_elem,
+                                                         const double* __restrict__ seg_len,
+                                                         const int64_t* __restrict__ off,
+                                                         int32_t* __restrict__ out_elem,
+                                                         double* __restrict__ out_len) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; k < m; k += nw) {
+    const int64_t o = off[k], kept = off[k + 1] - o;
+    const int32_t* se = seg_elem + k * (int64_t)K;
+    const double* sl = seg_len + k * (int64_t)K;
+    for (int64_t q = lane; q < kept; q += 32) {
+      out_elem[o + q] = se[q];
+      out_len[o + q] = sl[q];
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kSegBlock) k_seg_advance(
     SegState s, const int32_t* __restrict__ walk_t, int64_t m, int32_t K,
-    const int32_t* __restrict__ seg_elem, const double* __restrict__ seg_len,
-    const int32_t* __restrict__ cnt, const int32_t* __restrict__ wst,
-    const int32_t* __restrict__ wstop, int32_t max_segs, const int64_t* __restrict__ off,
-    int32_t* __restrict__ out_elem, double* __restrict__ out_len, int64_t* __restrict__ dst_rel,
-    int32_t* __restrict__ act_next, int32_t* __restrict__ n_act) {
+    const int32_t* __restrict__ seg_elem, const int32_t* __restrict__ cnt,
+    const int32_t* __restrict__ wst, const int32_t* __restrict__ wstop,
+    const double* __restrict__ wend_r, const double* __restrict__ wend_d,
+    const double* __restrict__ wsum, int32_t max_segs, const int64_t* __restrict__ off,
+    int64_t* __restrict__ dst_rel, int32_t* __restrict__ act_next, int32_t* __restrict__ n_act) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= m) return;
   const int32_t t = walk_t[k];
-  const int64_t o = off[k], kept = off[k + 1] - o;
-  const int32_t* se = seg_elem + k * (int64_t)K;
-  const double* sl = seg_len + k * (int64_t)K;
-  // the walk's own updates per segment (walk.cu: distance -= len, r += len *
-  // u), and std::accumulate(vol_segments, 0.0, ...) continued across pauses
-  const d3 u = load3(s.u, t);
-  d3 wr = load3(s.wr, t);
-  double wd = s.wd[t], sum = s.wsum[t];
-  for (int64_t q = 0; q < kept; ++q) {
-    const double len = sl[q];
-    out_elem[o + q] = se[q];
-    out_len[o + q] = len;
-    sum = sum + len;
-    wd -= len;
-    wr = mk3(wr.x + len * u.x, wr.y + len * u.y, wr.z + len * u.z);
-  }
+  const int64_t kept = off[k + 1] - off[k];
+  // std::accumulate(vol_segments, 0.0, ...) continued across pauses: the walk
+  // kernel added this round's lengths, in order, to the sum it was given
+  const double sum = wsum[k];
   dst_rel[k] = s.written[t];
   s.written[t] += kept;
-  if (kept > 0) s.last[t] = se[kept - 1];
+  if (kept > 0) s.last[t] = seg_elem[k * (int64_t)K + kept - 1];
   const int32_t wc = s.wcount[t] + (int32_t)kept;
   s.wcount[t] = wc;
   const int32_t st = wst[k];
@@ -228,8 +241,9 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_advance(
     return;
   }
   if (st == RAY_WALK_LIMIT) {  // paused at K segments: resumes next round
-    store3(s.wr, t, wr);
-    s.wd[t] = wd;
+    // where the walk's own steps left it (distance -= len, r += len * u)
+    store3(s.wr, t, load3(wend_r, k));
+    s.wd[t] = wend_d[k];
     s.wsum[t] = sum;
     s.welem[t] = wstop[k];
     s.paused[t] = 1;
@@ -238,6 +252,7 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_advance(
   }
   // the walk has ended: r += u * segment_sum; distance -= segment_sum;
   s.paused[t] = 0;
+  const d3 u = load3(s.u, t);
   store3(s.r, t, advance3(load3(s.r, t), u, sum));
   const double dist = s.dist[t] - sum;
   s.dist[t] = dist;
@@ -283,16 +298,24 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_scatter(
     const int64_t* __restrict__ dst_rel, const int32_t* __restrict__ seg_elem,
     const double* __restrict__ seg_len, const int64_t* __restrict__ offsets, int64_t capacity,
     int32_t* __restrict__ out_elem, double* __restrict__ out_len) {
-  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= m) return;
-  const int32_t t = walk_t[k];
-  if (offsets[t + 1] > capacity) return;  // the track does not fit: nothing is written
-  const int64_t o0 = off[k], o1 = off[k + 1];
-  const int64_t d = offsets[t] + dst_rel[k] - o0;
-  for (int64_t q = o0; q < o1; ++q) {
-    out_elem[d + q] = seg_elem[q];
-    out_len[d + q] = seg_len[q];
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; k < m; k += nw) {
+    const int32_t t = walk_t[k];
+    if (offsets[t + 1] > capacity) continue;  // the track does not fit: nothing is written
+    const int64_t o0 = off[k], o1 = off[k + 1];
+    const int64_t d = offsets[t] + dst_rel[k] - o0;
+    for (int64_t q = o0 + lane; q < o1; q += 32) {
+      out_elem[d + q] = seg_elem[q];
+      out_len[d + q] = seg_len[q];
+    }
   }
+}
+
+// grid of the warp-per-row kernels: a few blocks per SM, rows strided
+inline unsigned seg_warp_grid(int64_t rows) {
+  const int64_t need = (rows + kSegBlock / 32 - 1) / (kSegBlock / 32);
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)device_sm_count() * 8));
 }
 
 }  // namespace
@@ -348,21 +371,29 @@ cudaError_t seg_reenter(const SegState& s, const int32_t* out_t, int64_t m, cons
 }
 
 cudaError_t seg_walk_inputs(const SegState& s, const int32_t* walk_t, int64_t m, double* wr,
-                            double* wu, double* wd, cudaStream_t st) {
+                            double* wu, double* wd, double* wsum, cudaStream_t st) {
   if (m <= 0) return cudaSuccess;
-  k_seg_walk_inputs<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, wr, wu, wd);
+  k_seg_walk_inputs<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, wr, wu, wd, wsum);
+  return cudaGetLastError();
+}
+
+cudaError_t seg_pack(int64_t m, int32_t K, const int32_t* seg_elem, const double* seg_len,
+                     const int64_t* off, int32_t* out_elem, double* out_len, cudaStream_t st) {
+  if (m <= 0) return cudaSuccess;
+  k_seg_pack<<<seg_warp_grid(m), kSegBlock, 0, st>>>(m, K, seg_elem, seg_len, off, out_elem,
+                                                      out_len);
   return cudaGetLastError();
 }
 
 cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, int32_t K,
-                        const int32_t* seg_elem, const double* seg_len, const int32_t* cnt,
-                        const int32_t* wst, const int32_t* wstop, int32_t max_segs,
-                        const int64_t* off, int32_t* out_elem, double* out_len, int64_t* dst_rel,
-                        int32_t* act_next, int32_t* n_act, cudaStream_t st) {
+                        const int32_t* seg_elem, const int32_t* cnt, const int32_t* wst,
+                        const int32_t* wstop, const double* wend_r, const double* wend_d,
+                        const double* wsum, int32_t max_segs, const int64_t* off,
+                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st) {
   if (m <= 0) return cudaSuccess;
-  k_seg_advance<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, K, seg_elem, seg_len, cnt, wst,
-                                                    wstop, max_segs, off, out_elem, out_len,
-                                                    dst_rel, act_next, n_act);
+  k_seg_advance<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, K, seg_elem, cnt, wst, wstop,
+                                                    wend_r, wend_d, wsum, max_segs, off, dst_rel,
+                                                    act_next, n_act);
   return cudaGetLastError();
 }
 
@@ -392,7 +423,7 @@ cudaError_t seg_scatter(const SegState& s, const int32_t* walk_t, int64_t m, con
                         double* out_len, cudaStream_t st) {
   (void)s;
   if (m <= 0) return cudaSuccess;
-  k_seg_scatter<<<seg_grid(m), kSegBlock, 0, st>>>(walk_t, m, off, dst_rel, seg_elem, seg_len,
+  k_seg_scatter<<<seg_warp_grid(m), kSegBlock, 0, st>>>(walk_t, m, off, dst_rel, seg_elem, seg_len,
                                                     offsets, capacity, out_elem, out_len);
   return cudaGetLastError();
 }

@@ -18,13 +18,15 @@
 //   walk     walk_elements(element, r, u, distance) of the walk list, at most
 //            K segments per track and round (one pass, K-strided buffer): a
 //            walk that reaches K pauses, and the next round resumes it where
-//            it stopped (the element the walk kernel reports, the position
-//            and remaining distance rebuilt from the emitted lengths with the
-//            walk's own operations) without locating the track again;
-//   advance  the round's segments packed into a buffer of the round, the
-//            walk's segment_sum summed in order across its pauses; when the
-//            walk ends, r += u * segment_sum and distance -= segment_sum
-//            (xdg.cpp:188-193); tracks with distance > 0 stay active.
+//            it stopped (the element, position and remaining distance the
+//            walk kernel reports, as its own steps computed them) without
+//            locating the track again.  The walk kernel also sums the lengths
+//            it emits, in order, continuing the sum of the walk's earlier
+//            rounds (std::accumulate across the pauses);
+//   advance  the round's segments packed into a buffer of the round (one warp
+//            per track); when the walk ends, r += u * segment_sum and
+//            distance -= segment_sum (xdg.cpp:188-193); tracks with
+//            distance > 0 stay active.
 // When no track is active, the per-track totals are scanned into the output
 // offsets and every round's segments are copied to their place.
 #pragma once
@@ -88,26 +90,32 @@ cudaError_t seg_reenter(const SegState& s, const int32_t* out_t, int64_t m, cons
                         int32_t* walk_start, int32_t* n_walk, cudaStream_t st);
 
 // The walk's inputs for the walk list, from each track's walk state:
-// xr[k] = wr[t], xu[k] = u[t], xd[k] = wd[t].
+// xr[k] = wr[t], xu[k] = u[t], xd[k] = wd[t], xsum[k] = wsum[t].
 cudaError_t seg_walk_inputs(const SegState& s, const int32_t* walk_t, int64_t m, double* xr,
-                            double* xu, double* xd, cudaStream_t st);
+                            double* xu, double* xd, double* xsum, cudaStream_t st);
 
 // off[k] = the segments of walk entry k this round keeps: its count, cut
 // where the walk would pass max_segs segments.
 cudaError_t seg_round_counts(const SegState& s, const int32_t* walk_t, int64_t m,
                              const int32_t* cnt, int32_t max_segs, int64_t* off, cudaStream_t st);
 
-// After the round's walk (K-strided segments seg_elem / seg_len, counts cnt,
-// statuses wst, resume elements wstop) and the scan of the kept counts into
-// off[0..m]: the kept segments to out_elem / out_len at off[k], the walk
-// state advanced, dst_rel[k] = the track's segments written before this
-// round; a walk that ends applies segment_sum to r and distance; the tracks
-// still active (paused or with distance left) are appended to act_next.
+// The kept segments of the round's walk (rows of K in seg_elem / seg_len) to
+// out_elem / out_len at off[k] .. off[k+1]-1, one warp per walk entry.
+cudaError_t seg_pack(int64_t m, int32_t K, const int32_t* seg_elem, const double* seg_len,
+                     const int64_t* off, int32_t* out_elem, double* out_len, cudaStream_t st);
+
+// After the round's walk (K-strided segments seg_elem, counts cnt, statuses
+// wst, and per walk entry where it stopped: element wstop, position wend_r,
+// distance left wend_d, running length sum wsum) and the scan of the kept
+// counts into off[0..m]: the walk state advanced, dst_rel[k] = the track's
+// segments written before this round; a walk that ends applies segment_sum
+// to r and distance; the tracks still active (paused or with distance left)
+// are appended to act_next.
 cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, int32_t K,
-                        const int32_t* seg_elem, const double* seg_len, const int32_t* cnt,
-                        const int32_t* wst, const int32_t* wstop, int32_t max_segs,
-                        const int64_t* off, int32_t* out_elem, double* out_len, int64_t* dst_rel,
-                        int32_t* act_next, int32_t* n_act, cudaStream_t st);
+                        const int32_t* seg_elem, const int32_t* cnt, const int32_t* wst,
+                        const int32_t* wstop, const double* wend_r, const double* wend_d,
+                        const double* wsum, int32_t max_segs, const int64_t* off,
+                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st);
 
 // Tracks still active after the last allowed round end with `code`.
 cudaError_t seg_stop_active(const SegState& s, const int32_t* act, int64_t m, int32_t code,
@@ -122,7 +130,8 @@ cudaError_t seg_mark_full(const SegState& s, const int64_t* offsets, int64_t cap
 
 // One round's segments to their final place: track t's k-th segment of the
 // round goes to offsets[t] + dst_rel + k when the track's segments fit in
-// `capacity`; nothing is written for a track that does not fit.
+// `capacity`; nothing is written for a track that does not fit.  One warp
+// per walk entry.
 cudaError_t seg_scatter(const SegState& s, const int32_t* walk_t, int64_t m, const int64_t* off,
                         const int64_t* dst_rel, const int32_t* seg_elem, const double* seg_len,
                         const int64_t* offsets, int64_t capacity, int32_t* out_elem,

@@ -230,6 +230,19 @@ __device__ __forceinline__ void flush(unsigned long long* g, const StepCnt& c, u
   }
 }
 
+// The optional end state of track i's walk (WalkArgs::sum_out, end_r,
+// end_dist): the running length sum, the position and the distance left.
+__device__ __forceinline__ void walk_end_state(const WalkArgs& a, int64_t i, d3 r, double dist,
+                                               double sum) {
+  if (a.sum_out) a.sum_out[i] = sum;
+  if (a.end_r) {
+    a.end_r[3 * i] = r.x;
+    a.end_r[3 * i + 1] = r.y;
+    a.end_r[3 * i + 2] = r.z;
+  }
+  if (a.end_dist) a.end_dist[i] = dist;
+}
+
 // Persistent walk: each warp owns a contiguous chunk of tracks; a lane whose
 // track has ended takes the next track of the chunk, so a warp keeps all 32
 // lanes stepping until its chunk is exhausted (track lengths are
@@ -253,7 +266,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
   bool has = false;
   int64_t i = 0;
   d3 r = mk3(0, 0, 0), u = mk3(0, 0, 0);
-  double dist = 0.0;
+  double dist = 0.0, sum = 0.0;
   int32_t elem = -1, k = 0, st = RAY_OK;
   int32_t* oe = nullptr;
   double* ol = nullptr;
@@ -271,6 +284,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
           r = load3(a.org, i);
           u = load3(a.dir, i);
           dist = a.dist[i];
+          sum = a.sum_in ? a.sum_in[i] : 0.0;
           elem = a.start[i];
           k = 0;
           st = RAY_OK;
@@ -319,6 +333,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
         }
         ex = dlt(dist, ex) ? dist : ex;  // std::min(exit, distance)
         dist -= ex;
+        if (a.sum_out) sum = sum + ex;
         if (oe) {
           oe[k] = __ldg(&a.elem_ids[elem]);
           ol[k] = ex;
@@ -342,6 +357,7 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
         }
         if (a.status) a.status[i] = st;
         if (a.stop_elem) a.stop_elem[i] = elem;  // where a capped walk resumes
+        walk_end_state(a, i, r, dist, sum);
         has = false;
         tracks++;
       }
@@ -481,7 +497,7 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
   bool has = false;
   int64_t i = 0;
   d3 r = mk3(0, 0, 0), u = mk3(0, 0, 0);
-  double dist = 0.0;
+  double dist = 0.0, sum = 0.0;
   int32_t elem = -1, k = 0, st = RAY_OK;
   int32_t* oe = nullptr;
   double* ol = nullptr;
@@ -510,6 +526,7 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
           r = load3(a.org, i);
           u = load3(a.dir, i);
           dist = a.dist[i];
+          sum = a.sum_in ? a.sum_in[i] : 0.0;
           elem = a.start[i];
           k = 0;
           st = RAY_OK;
@@ -561,6 +578,7 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
         }
         if (a.status) a.status[i] = st;
         if (a.stop_elem) a.stop_elem[i] = elem;  // where a capped walk resumes
+        walk_end_state(a, i, r, dist, sum);
         has = false;
         tracks++;
       } else {
@@ -681,6 +699,7 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
       }
       ex = dlt(dist, ex) ? dist : ex;  // std::min(exit, distance)
       dist -= ex;
+      if (a.sum_out) sum = sum + ex;
       if (oe) {
         oe[k] = __ldg(&a.elem_ids[elem]);
         ol[k] = ex;
@@ -704,6 +723,7 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
         }
         if (a.status) a.status[i] = st;
         if (a.stop_elem) a.stop_elem[i] = elem;  // where a capped walk resumes
+        walk_end_state(a, i, r, dist, sum);
         has = false;
         tracks++;
       }

@@ -36,6 +36,15 @@ struct WalkArgs {
   // walk modes, optional: the tet index a track stopped in (-1 when it left
   // the mesh); for a track stopped by max_segs, where its walk goes on
   int32_t* stop_elem;
+  // walk modes, optional (the global track loop): the running sum of a
+  // track's segment lengths, added in segment order from sum_in[i] (0 when
+  // null) and written to sum_out[i]; and the position (3 doubles at end_r)
+  // and distance left (end_dist) where the walk stopped, as its own steps
+  // computed them (r += len * u, distance -= len)
+  const double* sum_in;
+  double* sum_out;
+  double* end_r;
+  double* end_dist;
   unsigned long long* counters;
   // output layout: 0 = track-major with stride max_segs; 1 = count only
   // (offsets[i] = number of segments of track i); 2 = packed, track i's
