@@ -502,8 +502,17 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      the leaves they hold together (1..64, default 8)
  *   "closest_node_steps_fp64"  the same for the all-FP64 closest (default 1)
  *   "find_node_steps_fp64"  the same for the all-FP64 find_element (default
- *                      16; the mixed find_element runs one lane per point
- *                      on its own)
+ *                      16), and for the mixed one when it runs in phases
+ *   "find_element_phased"  mixed find_element: 0 (default) runs one lane per
+ *                      point on its own, the faster for points inside tets
+ *                      (1409 against 1249 Mpoints/s on 1e6 uniform points of
+ *                      a 750,000-tet cube); 1 runs the warp's lanes in step
+ *                      with their exact FP64 tests together, the faster for
+ *                      points on tet faces, where the FP32 filter decides
+ *                      little (445 against 198 Mpoints/s on the cube's faces).
+ *                      xdgcu_segments_global locates in phases after its
+ *                      first round whatever this says.  Results do not
+ *                      depend on it
  *   "segments_walk_cap"  xdgcu_segments_global: segments a walk emits per
  *                      round before it pauses (1..1024; 0, the default, picks
  *                      16..256 so that a round's buffer stays near 1 GiB).

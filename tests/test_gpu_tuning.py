@@ -308,6 +308,36 @@ def test_node_width_8_elements(cuda, prec):
     assert (a[0] >= 0).sum() > 35_000  # (10/11)^3 of the points lie in the cube
 
 
+def test_find_element_phased(cuda, oracle):
+    """The mixed find_element one lane per point (find_element_phased 0) and
+    in warp-synchronous phases (1) give the oracle's element ids and indices,
+    for points inside the cube, on its faces, and on mesh vertices (on the
+    faces of many tets at once, where the lowest element id decides)."""
+    tm = synth.tet_cube(n=12, size=10.0, jitter=0.2, seed=11)
+    m = synth.model_from_tets(tm, np.ones(len(tm.conn), dtype=np.int32))
+    x = XDG(m)
+    x.prepare_raytracer()
+    rng = np.random.default_rng(9)
+    inner = rng.uniform(-0.5, 10.5, (30_000, 3))
+    face = rng.uniform(0.0, 10.0, (30_000, 3))
+    face[np.arange(len(face)), rng.integers(0, 3, len(face))] = rng.choice([0.0, 10.0], len(face))
+    verts = tm.vertices[rng.integers(0, len(tm.vertices), 10_000)]
+    p = np.concatenate([inner, face, verts])
+    oid, oidx = oracle.TetTree(tm.tet_xyz(), tm.elem_ids).find_element(p)
+    assert x.rti.get_tuning("find_element_phased") == 0
+    try:
+        for phased in (0, 1):
+            x.rti.set_tuning("find_element_phased", phased)
+            eid, eidx = x.find_element(p, precision=MIXED)
+            assert_same(eid, oid, f"element id, phased={phased}")
+            assert_same(eidx, oidx, f"element index, phased={phased}")
+        with pytest.raises(Exception):
+            x.rti.set_tuning("find_element_phased", 2)
+    finally:
+        x.rti.set_tuning("find_element_phased", 0)
+    assert (oid >= 0).sum() > 50_000
+
+
 def test_autotune_width(nested):
     """The tree-shape search rebuilds the trees and keeps results unchanged."""
     import torch

@@ -265,8 +265,10 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
 // ---------------------------------------------------------------------------
 
 // One thread per point, each on its own: the mixed path, whose FP32 filter
-// decides nearly every tet, runs faster this way (1403 against at best 1357
-// Mpoints/s in warp-synchronous phases, 1e6 points on the 750,000-tet cube).
+// decides nearly every tet of an interior point, runs faster this way (1409
+// against 1249 Mpoints/s in warp-synchronous phases, 1e6 uniform points in
+// the 750,000-tet cube).  For points on the cube's faces, where most tets
+// take the exact test, the phases win: 445 against 198 Mpoints/s.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_find_element_lane(PointArgs a) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -384,7 +386,8 @@ __global__ void __launch_bounds__(kBlock) k_find_element_lane(PointArgs a) {
 // containment tests of all the warp's lanes together.  Every containing tet
 // is visited (the lowest element id wins), so no entry is pruned.  The
 // all-FP64 path, where every tet of a leaf takes the exact test, runs this
-// way: 76.5 -> 114 Mpoints/s with 16 node steps (1e6 points, 750,000 tets).
+// way: 76.5 -> 114 Mpoints/s with 16 node steps (1e6 points, 750,000 tets);
+// so does the mixed path for points on tet faces (launch_find_element).
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -541,9 +544,11 @@ cudaError_t launch_closest(bool mixed, const PointArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_find_element(bool mixed, const PointArgs& a, cudaStream_t st) {
+cudaError_t launch_find_element(bool mixed, const PointArgs& a, cudaStream_t st, bool phased) {
   if (a.n <= 0) return cudaSuccess;
-  if (mixed)
+  if (mixed && phased)
+    k_find_element<true><<<grid_for(a.n), kBlock, 0, st>>>(a);
+  else if (mixed)
     k_find_element_lane<true><<<grid_for(a.n), kBlock, 0, st>>>(a);
   else
     k_find_element<false><<<grid_for(a.n), kBlock, 0, st>>>(a);

@@ -118,6 +118,11 @@ cudaError_t ray_order(const double* org, const double* dir, const int32_t* ray_t
                       int32_t n_trees, int64_t n, double extent, int32_t* order, void* scratch,
                       size_t scratch_bytes, cudaStream_t st);
 cudaError_t launch_closest(bool mixed, const PointArgs& a, cudaStream_t st);
-cudaError_t launch_find_element(bool mixed, const PointArgs& a, cudaStream_t st);
+// The mixed find_element runs one lane per point on its own unless `phased`
+// (warp-synchronous phases, as the all-FP64 path always runs): the faster
+// for points on or near tet faces, where the FP32 filter leaves most tets to
+// the exact test.
+cudaError_t launch_find_element(bool mixed, const PointArgs& a, cudaStream_t st,
+                                bool phased = false);
 
 }  // namespace xdgcu
