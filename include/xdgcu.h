@@ -515,8 +515,10 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      depend on it
  *   "segments_walk_cap"  xdgcu_segments_global: segments a walk emits per
  *                      round before it pauses (1..1024; 0, the default, picks
- *                      16..256 so that a round's buffer stays near 1 GiB).
- *                      Results do not depend on it
+ *                      per round the largest power of two in 16..256 for which
+ *                      that round's walks fit a buffer of about 1 GiB, so
+ *                      rounds with fewer walks pause fewer of them).  Results
+ *                      do not depend on it
  *   "walk_edge_table"  mixed walk: 1 (default) takes the FP64 Plucker
  *                      coordinates of a face's edges from the edge table built
  *                      with the mesh (each edge's e and e x lo evaluated once,

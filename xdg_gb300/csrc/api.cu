@@ -2117,11 +2117,19 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   API_CUDA(S.get(&ss.welem, n), "segments scratch");
   API_CUDA(S.get(&ss.paused, n), "segments scratch");
   // segments per track and round of the single-pass walk: the K-strided
-  // buffer of one round holds at most about kSegStridedBytes
-  int32_t K = 256;
-  while (K > 16 && (int64_t)K * n * 12 > kSegStridedBytes) K >>= 1;
-  if (c->segments_walk_cap > 0) K = c->segments_walk_cap;
-  K = std::min(K, max_segs);
+  // buffer holds strided_cap entries, about kSegStridedBytes (at least 16
+  // per track), and each round takes the largest K <= 256 (a power of two)
+  // that fits its walks, so that rounds with fewer walks pause fewer of
+  // them; segments_walk_cap fixes K instead
+  const int64_t fixed_k = c->segments_walk_cap;
+  const int64_t strided_cap =
+      fixed_k > 0 ? fixed_k * n
+                  : std::max<int64_t>(16 * n, std::min<int64_t>(256 * n, kSegStridedBytes / 12));
+  auto round_k = [&](int64_t walks) -> int32_t {
+    int32_t K = (int32_t)(fixed_k > 0 ? fixed_k : 256);
+    while (fixed_k <= 0 && K > 16 && (int64_t)K * walks > strided_cap) K >>= 1;
+    return std::min(K, max_segs);
+  };
   int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *eid = nullptr, *eidx = nullptr;
   int32_t *walk_t = nullptr, *walk_start = nullptr, *out_t = nullptr, *surf = nullptr, *face = nullptr;
   int32_t *wst = nullptr, *wcnt = nullptr, *wstop = nullptr, *loc = nullptr, *sk_elem = nullptr;
@@ -2142,8 +2150,8 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   API_CUDA(S.get(&wcnt, n), "segments scratch");
   API_CUDA(S.get(&wstop, n), "segments scratch");
   API_CUDA(S.get(&loc, n), "segments scratch");
-  API_CUDA(S.get(&sk_elem, (int64_t)K * n), "segments scratch");
-  API_CUDA(S.get(&sk_len, (int64_t)K * n), "segments scratch");
+  API_CUDA(S.get(&sk_elem, strided_cap), "segments scratch");
+  API_CUDA(S.get(&sk_len, strided_cap), "segments scratch");
   API_CUDA(S.get(&pts, 3 * n), "segments scratch");
   API_CUDA(S.get(&ray_org, 3 * n), "segments scratch");
   API_CUDA(S.get(&ray_dir, 3 * n), "segments scratch");
@@ -2219,6 +2227,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
     }
     API_CUDA(cudaMemsetAsync(n_act, 0, sizeof(int32_t), st), "memset");
     if (m_walk > 0) {
+      const int32_t K = round_k(m_walk);
       Round R{};
       R.m = m_walk;
       API_CUDA(S.get(&R.walk_t, m_walk), "segments scratch");
