@@ -1228,7 +1228,8 @@ def run_engine(args, rank, world, local):
         ((seg_e64 != seg_e) & valid).sum().item())
     walk_len_mism = int(((seg_l64 != seg_l) & valid).sum().item())
     del seg_e64, seg_l64, seg_c64, valid
-    # the packed walk (count, scan, emit) and its allocation-free variant
+    # the packed walk (one walk in resumed rounds; count + emit walks beside
+    # it) and its allocation-free variant
     cap = int(n_segs + N_TRACKS)
     pk_e = torch.empty(cap, dtype=torch.int32, device=dev)
     pk_l = torch.empty(cap, dtype=torch.float64, device=dev)
@@ -1248,6 +1249,13 @@ def run_engine(args, rank, world, local):
     ms_packed = timed(torch, packed(L.xdgcu_walk_elements_packed), max(3, args.steps // 4), 2,
                       world, stream)
     pk_ref = (pk_e[:n_segs].clone(), pk_l[:n_segs].clone(), pk_off.clone())
+    # the same entry point walking every track twice (count, then emit)
+    wr.rti.set_tuning("packed_walk_passes", 2)
+    ms_packed2 = timed(torch, packed(L.xdgcu_walk_elements_packed), max(3, args.steps // 4), 2,
+                       world, stream)
+    wr.rti.set_tuning("packed_walk_passes", 1)
+    packed2_same = (bool(torch.equal(pk_off, pk_ref[2])) and bool(torch.equal(pk_e[:n_segs], pk_ref[0]))
+                    and bool(torch.equal(pk_l[:n_segs], pk_ref[1])))
     ms_packed_na = (timed(torch, packed(L.xdgcu_walk_elements_packed_noalloc),
                           max(3, args.steps // 4), 2, world, stream)
                     if N_TRACKS <= NOALLOC_MAX_TRACKS else None)
@@ -1463,6 +1471,8 @@ def run_engine(args, rank, world, local):
             "value_without_edge_table": total_segs / (ms_walk_noedge / 1e3) / 1e6,
             "edge_table_same_segments": walk_edge_table_same,
             "packed_value": total_segs / (ms_packed / 1e3) / 1e6,
+            "packed_two_pass_value": total_segs / (ms_packed2 / 1e3) / 1e6,
+            "packed_two_pass_equals_packed": packed2_same,
             "packed_noalloc_value": (total_segs / (ms_packed_na / 1e3) / 1e6
                                      if ms_packed_na else None),
             "packed_noalloc_equals_packed": packed_same,

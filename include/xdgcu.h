@@ -257,9 +257,15 @@ int xdgcu_walk_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
  * n+1 entries and offsets[n] is the total.  Arrays hold `capacity` entries:
  * a track whose segments do not fit is not written and gets
  * XDGCU_RAY_OUTPUT_FULL (call again with capacity >= offsets[n]).  max_segs
- * caps the segments of one track (XDGCU_RAY_WALK_LIMIT).  The tracks are
- * walked twice (count, then emit at the scanned offsets); the scan's scratch
- * is allocated on `stream` with cudaMallocAsync. */
+ * caps the segments of one track (XDGCU_RAY_WALK_LIMIT).  Each track is
+ * walked once, in rounds of walks capped at 16..256 segments per track: a
+ * walk that reaches the cap pauses and the next round resumes it where it
+ * stopped; each round's segments wait in temporary device memory (about the
+ * output's size, plus a buffer of up to 1 GiB, allocated on `stream` with
+ * cudaMallocAsync) until the offsets are known.  Where that memory cannot be
+ * had, or with the tuning key "packed_walk_passes" = 2, the tracks are walked
+ * twice instead (count, then emit at the scanned offsets), which needs only
+ * the scan's scratch.  The results are the same either way. */
 int xdgcu_walk_elements_packed(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
                                const double* start, const double* u, const double* distance,
                                int32_t max_segs, int64_t capacity, int32_t* seg_elem,
@@ -503,6 +509,10 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *   "closest_node_steps_fp64"  the same for the all-FP64 closest (default 1)
  *   "find_node_steps_fp64"  the same for the all-FP64 find_element (default
  *                      16), and for the mixed one when it runs in phases
+ *   "packed_walk_passes"  xdgcu_walk_elements_packed: 1 (default) walks each
+ *                      track once, in resumed rounds; 2 walks it twice (a
+ *                      count walk, then an emit walk), without the temporary
+ *                      memory of the rounds.  Results do not depend on it
  *   "find_element_phased"  mixed find_element: 0 (default) runs one lane per
  *                      point on its own, the faster for points inside tets
  *                      (1409 against 1249 Mpoints/s on 1e6 uniform points of
@@ -513,7 +523,8 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      xdgcu_segments_global locates in phases after its
  *                      first round whatever this says.  Results do not
  *                      depend on it
- *   "segments_walk_cap"  xdgcu_segments_global: segments a walk emits per
+ *   "segments_walk_cap"  xdgcu_segments_global and the packed walk's rounds:
+ *                      segments a walk emits per
  *                      round before it pauses (1..1024; 0, the default, picks
  *                      per round the largest power of two in 16..256 for which
  *                      that round's walks fit a buffer of about 1 GiB, so

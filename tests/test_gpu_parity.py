@@ -371,6 +371,48 @@ def test_packed_walk_matches_strided(cuda, tet_model, prec):
     assert len(off0) == 1 and off0[0] == 0
 
 
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_packed_walk_rounds(cuda, tet_model, prec):
+    """The packed walk walked once in resumed rounds (packed_walk_passes 1,
+    rounds capped at 1, 3 and 8 segments per track or automatically) and
+    walked twice (2: count, then emit) gives the strided walk's segments,
+    offsets and statuses, with tracks stopped at max_segs among them."""
+    from xdg_gb300._lib import RAY_WALK_LIMIT
+    tm = tet_model
+    rti = CudaRayTracer()
+    rti.set_tet_mesh(tm)
+    m = synth.Model(volumes=[1], tets=tm, elements={1: np.arange(len(tm.conn), dtype=np.int32)})
+    et = rti.create_element_tree(m, 1)
+    rng = np.random.default_rng(41)
+    n = 3000
+    start = rng.uniform(0, 10, (n, 3))
+    u = synth.isotropic_dirs(rng, n)
+    length = np.minimum(rng.exponential(8.0, n), _exit_distance(start, u, 0.0, 10.0))
+    _, idx = rti.find_element(et, start, prec)
+    try:
+        for max_segs in (512, 12):
+            se, sl, sc, st = rti.walk_elements(idx, start, u, length, max_segs, prec)
+            keep = np.arange(max_segs)[None, :] < sc[:, None]
+            total = int(sc.sum())
+            if max_segs == 12:
+                assert (st == RAY_WALK_LIMIT).sum() > 100
+            for passes, cap in ((1, 0), (1, 1), (1, 3), (1, 8), (2, 0)):
+                rti.set_tuning("packed_walk_passes", passes)
+                rti.set_tuning("segments_walk_cap", cap)
+                pe, pl, off, pst = rti.walk_elements_packed(idx, start, u, length, total, max_segs,
+                                                            prec)
+                what = f"max_segs={max_segs} passes={passes} cap={cap}"
+                assert off[0] == 0 and np.array_equal(np.diff(off), sc), what
+                assert np.array_equal(pst, st), what
+                assert np.array_equal(pe[:total], se[keep]), what
+                assert np.array_equal(pl[:total], sl[keep]), what
+        with pytest.raises(Exception):
+            rti.set_tuning("packed_walk_passes", 3)
+    finally:
+        rti.set_tuning("packed_walk_passes", 1)
+        rti.set_tuning("segments_walk_cap", 0)
+
+
 @pytest.mark.parametrize("shift", [0.0, 3.0e4])
 def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
     """closest in mixed precision (an FP32 bound that skips the FP64 test of

@@ -410,6 +410,7 @@ struct xdgcu_ctx {
   int32_t closest_node_steps_fp64 = 1;  // the same, all-FP64 path
   int32_t find_node_steps_fp64 = 16;    // find_element in phases (all-FP64, or find_phased): the same
   int32_t find_phased = 0;  // mixed find_element: 1 runs warp-synchronous phases, 0 one lane per point
+  int32_t packed_passes = 1;  // packed walk: 1 walk in resumed rounds, 2 a count walk and an emit walk
   int32_t segments_walk_cap = 0;  // segments_global: segments per walk and round (0 = automatic)
   bool pageable_direct = false;
   // host_direct 5: trial calls of in place (0) and staged (1), their summed
@@ -954,6 +955,170 @@ cudaError_t read_count(const int32_t* d, int32_t* h, cudaStream_t st) {
   return e;
 }
 
+// Rounds of single-pass walks (the global track loop and the packed walk):
+// the K-strided buffer of n tracks holds seg_strided_cap entries, about
+// kSegStridedBytes (at least 16 per track, 256 at most), or fixed_k per track
+// when that is set; a round of `walks` walks takes the largest K <= 256 (a
+// power of two) that fits, so rounds with fewer walks pause fewer of them.
+int64_t seg_strided_cap(int64_t n, int64_t fixed_k) {
+  return fixed_k > 0 ? fixed_k * n
+                     : std::max<int64_t>(16 * n, std::min<int64_t>(256 * n, kSegStridedBytes / 12));
+}
+int32_t seg_round_k(int64_t walks, int64_t cap, int64_t fixed_k, int32_t max_segs) {
+  int32_t K = (int32_t)(fixed_k > 0 ? fixed_k : 256);
+  while (fixed_k <= 0 && K > 16 && (int64_t)K * walks > cap) K >>= 1;
+  return std::min(K, max_segs);
+}
+
+// One round's walked tracks and where their kept segments wait, packed, for
+// the final placement.
+struct SegRound {
+  int64_t m, total;
+  int32_t* walk_t;
+  int64_t *off, *dst_rel;
+  int32_t* seg_elem;
+  double* seg_len;
+};
+
+// xdgcu_walk_elements_packed with one walk of every track instead of a count
+// walk and an emit walk: rounds of single-pass walks capped at K segments per
+// track (as the global track loop's walk step), each round's kept segments
+// packed into a buffer of the round; a track that reaches K pauses and the
+// next round resumes it where the walk kernel stopped (same element, position
+// and distance, so the same segments).  The tracks' totals then give the
+// offsets, and every round's segments go to their place.  Statuses follow the
+// two-pass walk: RAY_WALK_LIMIT past max_segs, RAY_OUTPUT_FULL (replacing OK)
+// for a track with segments that do not fit in `capacity`.  `a` holds device
+// arrays.  Sets *no_memory when a temporary buffer could not be allocated (about the
+// output's size plus the strided buffer); nothing has then been written that
+// the two-pass walk does not overwrite.
+int walk_packed_rounds(xdgcu_ctx* c, bool mixed, const WalkArgs& a, cudaStream_t st,
+                       bool* no_memory) {
+  *no_memory = false;
+  const int64_t n = a.n;
+  CallScratch S(st);
+  bool ok = true;
+  auto get = [&](auto** p, int64_t count) {
+    if (ok && S.get(p, count) != cudaSuccess) {
+      ok = false;
+      *no_memory = true;
+      cudaGetLastError();  // the failed allocation is not a pending launch error
+    }
+  };
+  SegState ss{};
+  ss.n = n;
+  ss.status = a.status;
+  if (!ss.status) get(&ss.status, n);
+  get(&ss.written, n);
+  get(&ss.last, n);
+  get(&ss.stopped, n);
+  get(&ss.u, 3 * n);
+  get(&ss.wr, 3 * n);
+  get(&ss.wd, n);
+  get(&ss.wsum, n);
+  get(&ss.wcount, n);
+  get(&ss.welem, n);
+  get(&ss.paused, n);
+  int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *walk_t = nullptr;
+  int32_t *walk_start = nullptr, *wst = nullptr, *wcnt = nullptr, *wstop = nullptr;
+  int32_t *loc = nullptr, *sk_elem = nullptr;
+  double *wr = nullptr, *wu = nullptr, *wd = nullptr, *sk_len = nullptr;
+  double *wsum_in = nullptr, *wsum_out = nullptr, *wend_r = nullptr, *wend_d = nullptr;
+  get(&act, n);
+  get(&act_next, n);
+  get(&counters, 4);
+  get(&walk_t, n);
+  get(&walk_start, n);
+  get(&wst, n);
+  get(&wcnt, n);
+  get(&wstop, n);
+  get(&loc, n);
+  get(&wr, 3 * n);
+  get(&wu, 3 * n);
+  get(&wd, n);
+  get(&wsum_in, n);
+  get(&wsum_out, n);
+  get(&wend_r, 3 * n);
+  get(&wend_d, n);
+  const int64_t cap = seg_strided_cap(n, c->segments_walk_cap);
+  get(&sk_elem, cap);
+  get(&sk_len, cap);
+  if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
+  int32_t* n_act = counters;
+  int32_t* n_walk = counters + 1;
+  int32_t* n_loc = counters + 3;
+  API_CUDA(seg_walk_init(ss, a.start, a.org, a.dir, a.dist, act, st), "packed walk init");
+  std::vector<SegRound> rounds;
+  int32_t m = (int32_t)n;
+  while (m > 0) {
+    // every active track is a paused walk: all go to the walk list
+    API_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(int32_t), st), "memset");
+    API_CUDA(seg_split(ss, act, m, walk_t, walk_start, n_walk, loc, n_loc, st), "packed walk split");
+    const int32_t K = seg_round_k(m, cap, c->segments_walk_cap, a.max_segs);
+    SegRound R{};
+    R.m = m;
+    get(&R.walk_t, m);
+    get(&R.off, (int64_t)m + 1);
+    get(&R.dst_rel, m);
+    if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
+    API_CUDA(cudaMemcpyAsync(R.walk_t, walk_t, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, st),
+             "D2D");
+    API_CUDA(seg_walk_inputs(ss, walk_t, m, wr, wu, wd, wsum_in, st), "packed walk inputs");
+    WalkArgs w = a;
+    w.n = m;
+    w.start = walk_start;
+    w.org = wr;
+    w.dir = wu;
+    w.dist = wd;
+    w.max_segs = K;
+    w.status = wst;
+    w.seg_count = wcnt;
+    w.stop_elem = wstop;
+    w.sum_in = wsum_in;
+    w.sum_out = wsum_out;
+    w.end_r = wend_r;
+    w.end_dist = wend_d;
+    w.seg_elem = sk_elem;
+    w.seg_len = sk_len;
+    w.offsets = nullptr;
+    w.out_mode = WALK_STRIDED;
+    int rc = with_length_order(c, w, st, [&]() -> int {
+      API_CUDA(launch_walk(mixed, c->face_order, w, st), "walk");
+      return XDGCU_OK;
+    });
+    if (rc) return rc;
+    API_CUDA(seg_round_counts(ss, R.walk_t, m, wcnt, a.max_segs, R.off, st), "packed walk counts");
+    int64_t* sums = nullptr;
+    get(&sums, scan_scratch_entries(m));
+    if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
+    API_CUDA(scan_offsets(R.off, m, sums, st), "scan");
+    API_CUDA(cudaMemcpyAsync(&R.total, R.off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "D2H");
+    API_CUDA(cudaStreamSynchronize(st), "sync");
+    get(&R.seg_elem, R.total);
+    get(&R.seg_len, R.total);
+    if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
+    API_CUDA(seg_pack(m, K, sk_elem, sk_len, R.off, R.seg_elem, R.seg_len, st), "packed walk pack");
+    API_CUDA(seg_advance(ss, R.walk_t, m, K, sk_elem, wcnt, wst, wstop, wend_r, wend_d, wsum_out,
+                         a.max_segs, R.off, R.dst_rel, act_next, n_act, st, true),
+             "packed walk advance");
+    rounds.push_back(R);
+    API_CUDA(read_count(n_act, &m, st), "packed walk count");
+    std::swap(act, act_next);
+  }
+  // offsets from the tracks' totals, then every round's segments to their place
+  API_CUDA(seg_counts(ss, a.offsets, st), "packed walk totals");
+  int64_t* sums = nullptr;
+  get(&sums, scan_scratch_entries(n));
+  if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
+  API_CUDA(scan_offsets(a.offsets, n, sums, st), "scan");
+  API_CUDA(seg_mark_full(ss, a.offsets, a.capacity, st), "packed walk capacity");
+  for (const SegRound& R : rounds)
+    API_CUDA(seg_scatter(ss, R.walk_t, R.m, R.off, R.dst_rel, R.seg_elem, R.seg_len, a.offsets,
+                         a.capacity, a.seg_elem, a.seg_len, st),
+             "packed walk scatter");
+  return XDGCU_OK;
+}
+
 // Enqueues one traversal launch with the context's work distribution: when
 // the device work queue is on (trace_grab > 0) a zeroed cursor, and when the
 // batch is large enough (trace_sort_min) a coherent ray order, both in one
@@ -1413,6 +1578,9 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     (k == "closest_node_steps"        ? c->closest_node_steps
      : k == "closest_node_steps_fp64" ? c->closest_node_steps_fp64
                                       : c->find_node_steps_fp64) = (int32_t)value;
+  } else if (k == "packed_walk_passes") {
+    if (value != 1 && value != 2) return set_err(XDGCU_ERR_INVALID_ARG, "packed_walk_passes must be 1 or 2");
+    c->packed_passes = (int32_t)value;
   } else if (k == "find_element_phased") {
     if (value < 0 || value > 1)
       return set_err(XDGCU_ERR_INVALID_ARG, "find_element_phased must be 0 or 1");
@@ -1471,6 +1639,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "find_node_steps_fp64") *value = c->find_node_steps_fp64;
   else if (k == "segments_walk_cap") *value = c->segments_walk_cap;
   else if (k == "find_element_phased") *value = c->find_phased;
+  else if (k == "packed_walk_passes") *value = c->packed_passes;
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else if (k == "host_direct_choice") *value = c->hd_choice;
@@ -1924,6 +2093,12 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* c, int64_t n, const int32_t* start_ind
   cudaStream_t st = (cudaStream_t)stream;
   const bool mixed = precision == XDGCU_MIXED;
   auto run = [&](cudaStream_t s) -> int {
+    if (c->packed_passes == 1 && n < ((int64_t)1 << 31)) {
+      bool no_memory = false;
+      const int rc = walk_packed_rounds(c, mixed, a, s, &no_memory);
+      if (!no_memory) return rc;
+    }
+    // (or without the temporary memory): a count walk, the scan, an emit walk
     return with_length_order(c, a, s, [&]() -> int {
       a.out_mode = WALK_COUNT;
       API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (count)");
@@ -2116,19 +2291,10 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   API_CUDA(S.get(&ss.wcount, n), "segments scratch");
   API_CUDA(S.get(&ss.welem, n), "segments scratch");
   API_CUDA(S.get(&ss.paused, n), "segments scratch");
-  // segments per track and round of the single-pass walk: the K-strided
-  // buffer holds strided_cap entries, about kSegStridedBytes (at least 16
-  // per track), and each round takes the largest K <= 256 (a power of two)
-  // that fits its walks, so that rounds with fewer walks pause fewer of
-  // them; segments_walk_cap fixes K instead
-  const int64_t fixed_k = c->segments_walk_cap;
-  const int64_t strided_cap =
-      fixed_k > 0 ? fixed_k * n
-                  : std::max<int64_t>(16 * n, std::min<int64_t>(256 * n, kSegStridedBytes / 12));
+  // segments per track and round of the single-pass walk (seg_round_k)
+  const int64_t strided_cap = seg_strided_cap(n, c->segments_walk_cap);
   auto round_k = [&](int64_t walks) -> int32_t {
-    int32_t K = (int32_t)(fixed_k > 0 ? fixed_k : 256);
-    while (fixed_k <= 0 && K > 16 && (int64_t)K * walks > strided_cap) K >>= 1;
-    return std::min(K, max_segs);
+    return seg_round_k(walks, strided_cap, c->segments_walk_cap, max_segs);
   };
   int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *eid = nullptr, *eidx = nullptr;
   int32_t *walk_t = nullptr, *walk_start = nullptr, *out_t = nullptr, *surf = nullptr, *face = nullptr;
@@ -2168,14 +2334,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   int32_t* n_out = counters + 2;
   int32_t* n_loc = counters + 3;
   // one record per round for the final placement of its segments
-  struct Round {
-    int64_t m, total;
-    int32_t* walk_t;
-    int64_t *off, *dst_rel;
-    int32_t* seg_elem;
-    double* seg_len;
-  };
-  std::vector<Round> rounds;
+  std::vector<SegRound> rounds;
   API_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(int32_t), st), "memset");
   API_CUDA(seg_init(ss, d_starts, d_ends, act, n_act, st), "segments init");
   int32_t m = 0;
@@ -2228,7 +2387,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
     API_CUDA(cudaMemsetAsync(n_act, 0, sizeof(int32_t), st), "memset");
     if (m_walk > 0) {
       const int32_t K = round_k(m_walk);
-      Round R{};
+      SegRound R{};
       R.m = m_walk;
       API_CUDA(S.get(&R.walk_t, m_walk), "segments scratch");
       API_CUDA(S.get(&R.off, (int64_t)m_walk + 1), "segments scratch");
@@ -2290,7 +2449,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
     API_CUDA(scan_offsets(d_off, n, sums, st), "scan");
   }
   API_CUDA(seg_mark_full(ss, d_off, capacity, st), "segments capacity");
-  for (const Round& R : rounds)
+  for (const SegRound& R : rounds)
     API_CUDA(seg_scatter(ss, R.walk_t, R.m, R.off, R.dst_rel, R.seg_elem, R.seg_len, d_off, capacity,
                          d_se, d_sl, st),
              "segments scatter");

@@ -62,6 +62,29 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_init(SegState s, const double
   act[atomicAdd(n_act, 1)] = (int32_t)t;
 }
 
+// walk_elements of every track in rounds (the packed walk): each track starts
+// as a walk paused at its start element, position and distance.
+__global__ void __launch_bounds__(kSegBlock) k_seg_walk_init(SegState s, const int32_t* __restrict__ start,
+                                                              const double* __restrict__ org,
+                                                              const double* __restrict__ dir,
+                                                              const double* __restrict__ dist,
+                                                              int32_t* __restrict__ act) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= s.n) return;
+  s.written[t] = 0;
+  s.last[t] = -1;
+  s.status[t] = RAY_OK;
+  s.stopped[t] = 0;
+  s.paused[t] = 1;
+  s.welem[t] = start[t];
+  store3(s.wr, t, load3(org, t));
+  store3(s.u, t, load3(dir, t));
+  s.wd[t] = dist[t];
+  s.wsum[t] = 0.0;
+  s.wcount[t] = 0;
+  act[t] = (int32_t)t;
+}
+
 // A new walk of track t from its current r and distance (xdg.cpp:187).
 __device__ __forceinline__ void start_walk(const SegState& s, int32_t t) {
   store3(s.wr, t, load3(s.r, t));
@@ -219,7 +242,8 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_advance(
     const int32_t* __restrict__ wst, const int32_t* __restrict__ wstop,
     const double* __restrict__ wend_r, const double* __restrict__ wend_d,
     const double* __restrict__ wsum, int32_t max_segs, const int64_t* __restrict__ off,
-    int64_t* __restrict__ dst_rel, int32_t* __restrict__ act_next, int32_t* __restrict__ n_act) {
+    int64_t* __restrict__ dst_rel, int32_t* __restrict__ act_next, int32_t* __restrict__ n_act,
+    int walk_only) {
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= m) return;
   const int32_t t = walk_t[k];
@@ -250,8 +274,13 @@ __global__ void __launch_bounds__(kSegBlock) k_seg_advance(
     act_next[atomicAdd(n_act, 1)] = t;
     return;
   }
-  // the walk has ended: r += u * segment_sum; distance -= segment_sum;
   s.paused[t] = 0;
+  if (walk_only) {  // the packed walk: the track's walk_elements is done
+    if (st != RAY_OK && s.status[t] == RAY_OK) s.status[t] = st;
+    s.stopped[t] = 1;
+    return;
+  }
+  // the walk has ended: r += u * segment_sum; distance -= segment_sum;
   const d3 u = load3(s.u, t);
   store3(s.r, t, advance3(load3(s.r, t), u, sum));
   const double dist = s.dist[t] - sum;
@@ -327,6 +356,13 @@ cudaError_t seg_init(const SegState& s, const double* starts, const double* ends
   return cudaGetLastError();
 }
 
+cudaError_t seg_walk_init(const SegState& s, const int32_t* start, const double* org,
+                          const double* dir, const double* dist, int32_t* act, cudaStream_t st) {
+  if (s.n <= 0) return cudaSuccess;
+  k_seg_walk_init<<<seg_grid(s.n), kSegBlock, 0, st>>>(s, start, org, dir, dist, act);
+  return cudaGetLastError();
+}
+
 cudaError_t seg_split(const SegState& s, const int32_t* act, int64_t m, int32_t* walk_t,
                       int32_t* walk_start, int32_t* n_walk, int32_t* loc, int32_t* n_loc,
                       cudaStream_t st) {
@@ -389,11 +425,12 @@ cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, int
                         const int32_t* seg_elem, const int32_t* cnt, const int32_t* wst,
                         const int32_t* wstop, const double* wend_r, const double* wend_d,
                         const double* wsum, int32_t max_segs, const int64_t* off,
-                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st) {
+                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st,
+                        bool walk_only) {
   if (m <= 0) return cudaSuccess;
   k_seg_advance<<<seg_grid(m), kSegBlock, 0, st>>>(s, walk_t, m, K, seg_elem, cnt, wst, wstop,
                                                     wend_r, wend_d, wsum, max_segs, off, dst_rel,
-                                                    act_next, n_act);
+                                                    act_next, n_act, walk_only ? 1 : 0);
   return cudaGetLastError();
 }
 

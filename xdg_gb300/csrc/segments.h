@@ -63,6 +63,13 @@ struct SegState {
 cudaError_t seg_init(const SegState& s, const double* starts, const double* ends, int32_t* act,
                      int32_t* n_act, cudaStream_t st);
 
+// The packed walk (walk_elements of every track, no global loop around it):
+// track t starts as a walk paused at element start[t], position org[t],
+// direction dir[t] and distance dist[t]; act[t] = t.  State r and dist are
+// not used.
+cudaError_t seg_walk_init(const SegState& s, const int32_t* start, const double* org,
+                          const double* dir, const double* dist, int32_t* act, cudaStream_t st);
+
 // The active tracks: paused walks to the walk list (resumed at welem), the
 // others to `loc` (to be located).
 cudaError_t seg_split(const SegState& s, const int32_t* act, int64_t m, int32_t* walk_t,
@@ -110,12 +117,14 @@ cudaError_t seg_pack(int64_t m, int32_t K, const int32_t* seg_elem, const double
 // counts into off[0..m]: the walk state advanced, dst_rel[k] = the track's
 // segments written before this round; a walk that ends applies segment_sum
 // to r and distance; the tracks still active (paused or with distance left)
-// are appended to act_next.
+// are appended to act_next.  With walk_only (the packed walk) a walk that
+// ends finishes its track, with the walk's status.
 cudaError_t seg_advance(const SegState& s, const int32_t* walk_t, int64_t m, int32_t K,
                         const int32_t* seg_elem, const int32_t* cnt, const int32_t* wst,
                         const int32_t* wstop, const double* wend_r, const double* wend_d,
                         const double* wsum, int32_t max_segs, const int64_t* off,
-                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st);
+                        int64_t* dst_rel, int32_t* act_next, int32_t* n_act, cudaStream_t st,
+                        bool walk_only = false);
 
 // Tracks still active after the last allowed round end with `code`.
 cudaError_t seg_stop_active(const SegState& s, const int32_t* act, int64_t m, int32_t code,
