@@ -507,6 +507,15 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      before the warp's lanes bound and test the triangles of
  *                      the leaves they hold together (1..64, default 8)
  *   "closest_node_steps_fp64"  the same for the all-FP64 closest (default 1)
+ *   "closest_step_budget"  closest: node records and triangles a lane visits
+ *                      for one point (default 1024; 0 = no limit) before the
+ *                      point is left to a second kernel that searches it with
+ *                      a whole warp.  A point almost equidistant from many
+ *                      triangles (the centre of a sphere) otherwise holds one
+ *                      lane, and the launch, for thousands of steps (1e6
+ *                      points of the nested spheres: 25.8 -> 32.0 Mpoints/s
+ *                      mixed, 4.45 -> 6.23 FP64).  Results do not depend on
+ *                      it
  *   "find_node_steps_fp64"  the same for the all-FP64 find_element (default
  *                      16), and for the mixed one when it runs in phases
  *   "packed_walk_passes"  xdgcu_walk_elements_packed: 1 (default) walks each

@@ -419,7 +419,11 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
     triangles proven farther than the best so far) gives the FP64 answer bit
     for bit and the oracle's: lattice points with exact ties between the two
     triangles of a box face and between faces, points within 1e-9 of a
-    jittered sphere, and the same model moved far from the origin."""
+    jittered sphere, points at and near the sphere's centre (nearly
+    equidistant from all its triangles), and the same model moved far from
+    the origin.  Also with the step budget after which a warp finishes a
+    point's search at 1 and 16 steps (nearly every point searched by a warp)
+    and off."""
     c = np.array([shift, -0.5 * shift, 0.25 * shift])
     m = synth.Model()
     v, f = synth.icosphere(4, 3.0, center=tuple(c), jitter=1e-3, seed=21)
@@ -436,7 +440,10 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
     dirs = synth.isotropic_dirs(rng, 3000)
     r = np.linalg.norm(v - c, axis=1).mean()
     near = c + dirs * (r + rng.choice([-1e-9, 0.0, 1e-9], 3000))[:, None]
-    p = np.concatenate([lat + c, near, c + rng.uniform(-12, 12, (3000, 3))])
+    centre = c + rng.uniform(-0.05, 0.05, (200, 3))
+    p = np.concatenate([lat + c, near, c + rng.uniform(-12, 12, (3000, 3)), centre, c[None, :]])
+    budget = x.rti.get_tuning("closest_step_budget")
+    assert budget > 0
     for vol in (1, 2, 3):
         ocd, ocf = oracle.volume_tree(m, vol).closest(p)
         res = {prec: x.closest(vol, p, prec) for prec in PRECISIONS}
@@ -445,6 +452,13 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
             res["mixed, no bound"] = x.closest(vol, p, MIXED)
         finally:
             x.rti.set_tuning("closest_bound", 1)
+        try:
+            for b in (1, 16, 0):
+                x.rti.set_tuning("closest_step_budget", b)
+                for prec in PRECISIONS:
+                    res[f"{prec}, budget {b}"] = x.closest(vol, p, prec)
+        finally:
+            x.rti.set_tuning("closest_step_budget", budget)
         for prec, (cd, cf) in res.items():
             assert_same(cf, ocf, f"closest face vol {vol} prec {prec}")
             assert_same(cd, ocd, f"closest distance vol {vol} prec {prec}")

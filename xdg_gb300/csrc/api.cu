@@ -411,6 +411,7 @@ struct xdgcu_ctx {
   int32_t find_node_steps_fp64 = 16;    // find_element in phases (all-FP64, or find_phased): the same
   int32_t find_phased = 0;  // mixed find_element: 1 runs warp-synchronous phases, 0 one lane per point
   int32_t packed_passes = 1;  // packed walk: 1 walk in resumed rounds, 2 a count walk and an emit walk
+  int32_t closest_budget = 1024;  // closest: steps of one lane before a warp takes the point (0: never)
   int32_t segments_walk_cap = 0;  // segments_global: segments per walk and round (0 = automatic)
   bool pageable_direct = false;
   // host_direct 5: trial calls of in place (0) and staged (1), their summed
@@ -1578,6 +1579,10 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     (k == "closest_node_steps"        ? c->closest_node_steps
      : k == "closest_node_steps_fp64" ? c->closest_node_steps_fp64
                                       : c->find_node_steps_fp64) = (int32_t)value;
+  } else if (k == "closest_step_budget") {
+    if (value < 0 || value > (1 << 30))
+      return set_err(XDGCU_ERR_INVALID_ARG, "closest_step_budget must be 0..2^30");
+    c->closest_budget = (int32_t)value;
   } else if (k == "packed_walk_passes") {
     if (value != 1 && value != 2) return set_err(XDGCU_ERR_INVALID_ARG, "packed_walk_passes must be 1 or 2");
     c->packed_passes = (int32_t)value;
@@ -1640,6 +1645,7 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "segments_walk_cap") *value = c->segments_walk_cap;
   else if (k == "find_element_phased") *value = c->find_phased;
   else if (k == "packed_walk_passes") *value = c->packed_passes;
+  else if (k == "closest_step_budget") *value = c->closest_budget;
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else if (k == "host_direct_choice") *value = c->hd_choice;
@@ -1900,6 +1906,17 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
   phased = phased || c->find_phased != 0;
   a.elem_ids = c->d_elem_ids.p;
   cudaStream_t st = (cudaStream_t)stream;
+  // closest: a point's search passing closest_step_budget steps is finished
+  // by a whole warp; its flag and best so far live in scratch of n entries,
+  // allocated on the stream the kernels are ordered after
+  auto defer_scratch = [&](CallScratch& S) -> cudaError_t {
+    if (!closest || c->closest_budget <= 0) return cudaSuccess;
+    cudaError_t e = S.get(&a.deferred, n);
+    if (e == cudaSuccess) e = S.get(&a.def_best, n);
+    if (e == cudaSuccess) e = S.get(&a.def_face, n);
+    if (e == cudaSuccess) a.step_budget = c->closest_budget;
+    return e;
+  };
   auto launch = [&]() -> cudaError_t {
     return closest ? launch_closest(precision == XDGCU_MIXED, a, st)
                    : launch_find_element(precision == XDGCU_MIXED, a, st, phased);
@@ -1913,11 +1930,17 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
     a.status = status;
     int rc = begin_query(c, st, &a.counters);
     if (rc) return rc;
+    CallScratch S(st);
+    API_CUDA(defer_scratch(S), "closest scratch");
     API_CUDA(launch(), "query launch");
     return XDGCU_OK;
   }
   Slot* s = get_slot(c);
   if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
+  // (the chunks' launches alternate between the slot's streams; the second
+  // waits for the first before its first launch)
+  CallScratch S(s->stream);
+  API_CUDA(defer_scratch(S), "closest scratch");
   RayArr R_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) : 0};
   RayArr R_p{pts, nullptr, sizeof(double) * 3};
   RayArr R_d{nullptr, dist_out, dist_out ? sizeof(double) : 0};
@@ -1937,6 +1960,11 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
                       b.id_out = (int32_t*)at(R_i, first);
                       b.index_out = (int32_t*)at(R_x, first);
                       b.status = (int32_t*)at(R_st, first);
+                      if (a.deferred) {  // this chunk's slice of the closest scratch
+                        b.deferred = a.deferred + first;
+                        b.def_best = a.def_best + first;
+                        b.def_face = a.def_face + first;
+                      }
                       return closest ? launch_closest(precision == XDGCU_MIXED, b, cs)
                                      : launch_find_element(precision == XDGCU_MIXED, b, cs, phased);
                     });

@@ -8,6 +8,8 @@
 // point rounded to FP32 stays inside any FP32 box that contains it -- and the
 // per-primitive tests (closest point on a triangle, tet containment) are the
 // reference's FP64 formulas from geom.cuh, so results are bit-identical.
+#include <algorithm>
+
 #include "queries.h"
 #include "traverse.cuh"
 
@@ -22,6 +24,126 @@ constexpr int kBlock = 128;
 // ---------------------------------------------------------------------------
 
 constexpr unsigned kFullMask = 0xffffffffu;
+
+// The children of record `rec` of inner node `ref` that may hold a facet no
+// farther than `best`: their references in cr and lower bounds of the
+// point's distance to their boxes in ck (FP32, rounded down; 0 where FP32
+// cannot prune), nearest first.  Returns their number.
+template <bool MIXED>
+__device__ __forceinline__ int closest_children(const TreeDev& T, int32_t ref, int rec, d3 p,
+                                                float px, float py, float pz, float pabs,
+                                                bool f32ok, double best, int32_t cr[4],
+                                                float ck[4]) {
+  const int nrec = T.width / kWidth;
+  int nhit = 0;
+  if (MIXED) {
+    const Node32* np = T.n32 + (int64_t)ref * nrec + rec;
+    const float4 lx = __ldg(&np->lox), hx = __ldg(&np->hix), ly = __ldg(&np->loy),
+                 hy = __ldg(&np->hiy), lz = __ldg(&np->loz), hz = __ldg(&np->hiz);
+    const int4 c = __ldg(&np->child);
+    const float la[3][4] = {{lx.x, lx.y, lx.z, lx.w}, {ly.x, ly.y, ly.z, ly.w},
+                            {lz.x, lz.y, lz.z, lz.w}};
+    const float ha[3][4] = {{hx.x, hx.y, hx.z, hx.w}, {hy.x, hy.y, hy.z, hy.w},
+                            {hz.x, hz.y, hz.z, hz.w}};
+    const float pa[3] = {px, py, pz};
+    const int32_t ca[4] = {c.x, c.y, c.z, c.w};
+    // prune only when the FP32 distance, shrunk by its error bound,
+    // exceeds the current best (rounded up to float)
+    const float bestf = __double2float_ru(best);
+    float key[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float s2 = 0.0f;
+      bool empty = false;
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) {
+        empty |= !(la[ax][k] <= ha[ax][k]);
+        const float e = fmaxf(fmaxf(la[ax][k] - pa[ax], pa[ax] - ha[ax][k]), 0.0f);
+        s2 += e * e;
+      }
+      const float dist = sqrtf(s2);
+      const float lb = dist * (1.0f - 8.0f * kU32) - 4.0f * kU32 * pabs;
+      // the key is the lower bound itself (0 where FP32 cannot prune)
+      key[k] = (!empty && (lb <= bestf || !f32ok)) ? (f32ok ? fmaxf(lb, 0.0f) : 0.0f) : INFINITY;
+      cr[k] = ca[k];
+    }
+    sort4(key, cr);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      nhit += key[k] < INFINITY ? 1 : 0;
+      ck[k] = key[k];
+    }
+  } else {
+    const Node64* np = T.n64 + (int64_t)ref * nrec + rec;
+    const int4 c = __ldg(&np->child);
+    const int32_t ca[4] = {c.x, c.y, c.z, c.w};
+    double key[4];
+    const double pa[3] = {p.x, p.y, p.z};
+    const double* lo[3] = {np->lox, np->loy, np->loz};
+    const double* hi[3] = {np->hix, np->hiy, np->hiz};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      double s2 = 0.0;
+      bool empty = false;
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) {
+        const double l = __ldg(lo[ax] + k), u = __ldg(hi[ax] + k);
+        empty |= !(l <= u);
+        const double e = fmax(fmax(l - pa[ax], pa[ax] - u), 0.0);
+        s2 += e * e;
+      }
+      const double dist = sqrt(s2);
+      key[k] = (!empty && dist * (1.0 - 1e-12) <= best) ? dist : INFINITY;
+      cr[k] = ca[k];
+    }
+    sort4d(key, cr);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      nhit += key[k] < INFINITY ? 1 : 0;
+      // rounded down: a lower bound of dist * (1 - 1e-12)
+      ck[k] = key[k] < INFINITY ? __double2float_rd(key[k] * (1.0 - 1e-12)) : INFINITY;
+    }
+  }
+  return nhit;
+}
+
+// Whether the triangle `gtri` may be no farther than `bestf` (the best
+// distance rounded up to FP32) by the certified FP32 lower bound of
+// the point's distance to it (planes from tri_cbound): sqrt(h^2 + m^2) with
+// h the distance to its face plane and m the largest distance beyond one of
+// its edge planes.  With p exact, the triangle lies within 8 u M of the face
+// plane and inside the edge planes, and the rows are orthonormal to 4 u, so
+// the distance is at least that root less 8 u M, over 1 + 6 u.  The FP32
+// evaluation (p's rounding and three FMAs) is within about 7 u (|p| + M) of h
+// and of each edge distance (M = max_abs).  The bound, less 48 u (|p| + M)
+// (cmargin) and the rounding of the root, undershoots the distance by at
+// least 20 u (|p| + M), far beyond the FP64 rounding of the exact test; the
+// triangle is skipped only when it still exceeds the best distance rounded
+// up, so neither the minimum nor its tie rule can change.
+__device__ __forceinline__ bool closest_may_win(const float4* __restrict__ tri_cb, int32_t gtri,
+                                                float px, float py, float pz, float cmargin,
+                                                float bestf) {
+  const float4* cb = tri_cb + 4 * (int64_t)gtri;
+  const float4 pn = __ldg(cb), e0 = __ldg(cb + 1), e1 = __ldg(cb + 2), e2 = __ldg(cb + 3);
+  const float h = fabsf(__fmaf_rn(pn.x, px, __fmaf_rn(pn.y, py, __fmaf_rn(pn.z, pz, -pn.w))));
+  const float s0 = __fmaf_rn(e0.x, px, __fmaf_rn(e0.y, py, __fmaf_rn(e0.z, pz, -e0.w)));
+  const float s1 = __fmaf_rn(e1.x, px, __fmaf_rn(e1.y, py, __fmaf_rn(e1.z, pz, -e1.w)));
+  const float s2 = __fmaf_rn(e2.x, px, __fmaf_rn(e2.y, py, __fmaf_rn(e2.z, pz, -e2.w)));
+  const float mo = fmaxf(fmaxf(fmaxf(s0, s1), s2), 0.0f);
+  const float lb = __fsqrt_rn(__fmaf_rn(h, h, mo * mo));
+  return !(lb * (1.0f - 8.0f * kU32) - cmargin > bestf);
+}
+
+// Whether (d, face) replaces (best, best_face): triangle_intersect.cpp:126-133
+// keeps a strictly nearer facet (strict <), and of facets at the same
+// distance the lowest face id wins.  (best, best_face) starts at (INFTY, -1),
+// so for face ids >= 0 the result is the lexicographic minimum, whatever the
+// order the candidates come in.
+__device__ __forceinline__ bool closest_better(double d, int32_t face, double best,
+                                               int32_t best_face) {
+  return d < best || (d == best && best_face >= 0 && face < best_face);
+}
+
 // One lane per point, the warp in step: each round, every lane without a
 // leaf in hand takes up to a.node_steps inner-node steps, then the lanes
 // holding a leaf bound its triangles in FP32 together, then the exact FP64
@@ -46,7 +168,8 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
   float px = 0.0f, py = 0.0f, pz = 0.0f, pabs = 0.0f, cmargin = 0.0f;
   bool f32ok = false, cbound = false;
   int32_t ref = CHILD_EMPTY;
-  bool run = false;
+  bool run = false, deferred = false;
+  int32_t steps = 0;  // node records and triangles of this point (a.step_budget)
   if (i < a.n) {
     const int32_t tid = a.ray_trees ? a.ray_trees[i] : a.tree;
     p = load3(a.pts, i);
@@ -87,6 +210,11 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
   };
 
   while (__any_sync(kFullMask, run)) {
+    // a point past its step budget stops here; k_closest_coop finishes it
+    if (run && a.step_budget > 0 && steps >= a.step_budget) {
+      run = false;
+      deferred = true;
+    }
     // ---- inner nodes: lanes without a leaf in hand descend ----
     for (int it = 0; it < a.node_steps; ++it) {
       const bool want = run && (ref == CHILD_EMPTY || !ref_is_leaf(ref));
@@ -103,78 +231,10 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
       for (int rec = 0; rec < nrec; ++rec) {
         cnt.node++;
         cnt.box += 4;
+        ++steps;
         int32_t cr[4];
         float ck[4];
-        int nhit = 0;
-        if (MIXED) {
-          const Node32* np = T.n32 + (int64_t)ref * nrec + rec;
-          const float4 lx = __ldg(&np->lox), hx = __ldg(&np->hix), ly = __ldg(&np->loy),
-                       hy = __ldg(&np->hiy), lz = __ldg(&np->loz), hz = __ldg(&np->hiz);
-          const int4 c = __ldg(&np->child);
-          const float la[3][4] = {{lx.x, lx.y, lx.z, lx.w}, {ly.x, ly.y, ly.z, ly.w},
-                                  {lz.x, lz.y, lz.z, lz.w}};
-          const float ha[3][4] = {{hx.x, hx.y, hx.z, hx.w}, {hy.x, hy.y, hy.z, hy.w},
-                                  {hz.x, hz.y, hz.z, hz.w}};
-          const float pa[3] = {px, py, pz};
-          const int32_t ca[4] = {c.x, c.y, c.z, c.w};
-          // prune only when the FP32 distance, shrunk by its error bound,
-          // exceeds the current best (rounded up to float)
-          const float bestf = __double2float_ru(best);
-          float key[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            float s2 = 0.0f;
-            bool empty = false;
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) {
-              empty |= !(la[ax][k] <= ha[ax][k]);
-              const float e = fmaxf(fmaxf(la[ax][k] - pa[ax], pa[ax] - ha[ax][k]), 0.0f);
-              s2 += e * e;
-            }
-            const float dist = sqrtf(s2);
-            const float lb = dist * (1.0f - 8.0f * kU32) - 4.0f * kU32 * pabs;
-            // the key is the lower bound itself (0 where FP32 cannot prune)
-            key[k] = (!empty && (lb <= bestf || !f32ok)) ? (f32ok ? fmaxf(lb, 0.0f) : 0.0f)
-                                                         : INFINITY;
-            cr[k] = ca[k];
-          }
-          sort4(key, cr);
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            nhit += key[k] < INFINITY ? 1 : 0;
-            ck[k] = key[k];
-          }
-        } else {
-          const Node64* np = T.n64 + (int64_t)ref * nrec + rec;
-          const int4 c = __ldg(&np->child);
-          const int32_t ca[4] = {c.x, c.y, c.z, c.w};
-          double key[4];
-          const double pa[3] = {p.x, p.y, p.z};
-          const double* lo[3] = {np->lox, np->loy, np->loz};
-          const double* hi[3] = {np->hix, np->hiy, np->hiz};
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            double s2 = 0.0;
-            bool empty = false;
-#pragma unroll
-            for (int ax = 0; ax < 3; ++ax) {
-              const double l = __ldg(lo[ax] + k), u = __ldg(hi[ax] + k);
-              empty |= !(l <= u);
-              const double e = fmax(fmax(l - pa[ax], pa[ax] - u), 0.0);
-              s2 += e * e;
-            }
-            const double dist = sqrt(s2);
-            key[k] = (!empty && dist * (1.0 - 1e-12) <= best) ? dist : INFINITY;
-            cr[k] = ca[k];
-          }
-          sort4d(key, cr);
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            nhit += key[k] < INFINITY ? 1 : 0;
-            // rounded down: a lower bound of dist * (1 - 1e-12)
-            ck[k] = key[k] < INFINITY ? __double2float_rd(key[k] * (1.0 - 1e-12)) : INFINITY;
-          }
-        }
+        const int nhit = closest_children<MIXED>(T, ref, rec, p, px, py, pz, pabs, f32ok, best, cr, ck);
         if (sp + nhit > kStackSize) {
           overflow = true;
           break;
@@ -202,31 +262,10 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
       const float bestf = __double2float_ru(best);
       for (int32_t q = 0; q < count; ++q) {
         cnt.prim++;
+        ++steps;
         if (cbound) {
-          // Certified FP32 lower bound of the distance to the triangle
-          // (planes from tri_cbound): sqrt(h^2 + m^2) with h the distance to
-          // its face plane and m the largest distance beyond one of its edge
-          // planes.  With p exact, the triangle lies within 8 u M of the face
-          // plane and inside the edge planes, and the rows are orthonormal to
-          // 4 u, so the distance is at least that root less 8 u M, over 1 +
-          // 6 u.  The FP32 evaluation (p's rounding and three FMAs) is within
-          // about 7 u (|p| + M) of h and of each edge distance (M = max_abs).
-          // The bound, less 48 u (|p| + M) and the rounding of the root,
-          // undershoots the distance by at least 20 u (|p| + M), far beyond
-          // the FP64 rounding of the exact test; the triangle is skipped only
-          // when it still exceeds the best distance rounded up, so neither
-          // the minimum nor its tie rule can change.
-          const int32_t gtri = __ldg(&T.prim_ref[first + q]);
-          const float4* cb = a.tri_cb + 4 * (int64_t)gtri;
-          const float4 pn = __ldg(cb), e0 = __ldg(cb + 1), e1 = __ldg(cb + 2),
-                       e2 = __ldg(cb + 3);
-          const float h = fabsf(__fmaf_rn(pn.x, px, __fmaf_rn(pn.y, py, __fmaf_rn(pn.z, pz, -pn.w))));
-          const float s0 = __fmaf_rn(e0.x, px, __fmaf_rn(e0.y, py, __fmaf_rn(e0.z, pz, -e0.w)));
-          const float s1 = __fmaf_rn(e1.x, px, __fmaf_rn(e1.y, py, __fmaf_rn(e1.z, pz, -e1.w)));
-          const float s2 = __fmaf_rn(e2.x, px, __fmaf_rn(e2.y, py, __fmaf_rn(e2.z, pz, -e2.w)));
-          const float mo = fmaxf(fmaxf(fmaxf(s0, s1), s2), 0.0f);
-          const float lb = __fsqrt_rn(__fmaf_rn(h, h, mo * mo));
-          if (lb * (1.0f - 8.0f * kU32) - cmargin > bestf) continue;
+          if (!closest_may_win(a.tri_cb, __ldg(&T.prim_ref[first + q]), px, py, pz, cmargin, bestf))
+            continue;
           cnt.esc++;
         }
         need |= 1u << q;
@@ -243,8 +282,7 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
         const d3 r = closest64(v0, v1, v2, p);
         const double dd = dist64(r, p);
         const int32_t fid = __ldg(&a.tri_face[__ldg(&T.prim_ref[qq])]);
-        // triangle_intersect.cpp:126-133 (strict <) plus the tie rule
-        if (dd < best || (dd == best && best_face >= 0 && fid < best_face)) {
+        if (closest_better(dd, fid, best, best_face)) {
           best = dd;
           best_face = fid;
         }
@@ -253,11 +291,172 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
     if (leaf) pop();
   }
   if (i < a.n) {
-    a.dist_out[i] = best_face >= 0 ? best : INFTY;
-    if (a.id_out) a.id_out[i] = best_face;
-    if (a.status) a.status[i] = st;
+    if (a.deferred) a.deferred[i] = deferred ? 1 : 0;
+    if (deferred) {
+      a.def_best[i] = best;
+      a.def_face[i] = best_face;
+    } else {
+      a.dist_out[i] = best_face >= 0 ? best : INFTY;
+      if (a.id_out) a.id_out[i] = best_face;
+      if (a.status) a.status[i] = st;
+    }
   }
   if (a.counters) flush_counters(a.counters, cnt, i < a.n ? 1ull : 0ull);
+}
+
+// A point whose search passed k_closest's step budget (a.deferred[i] = 1),
+// searched by a whole warp.  Each round the lanes take the top 32 entries of
+// a shared stack of subtrees, push the children that may hold a facet no
+// farther than the warp's best (closest_children), or bound and test their
+// leaf's triangles (closest_may_win, then the exact FP64 closest point); the
+// lanes' bests are then merged by closest_better.  The search starts from
+// the best k_closest had found (a real candidate: nothing nearer is lost),
+// and every facet that may be no farther than the final best takes the exact
+// test, so the result is k_closest's: the strictly nearest facet, of equally
+// near ones the lowest face id.  A point at the centre of a sphere is nearly
+// equidistant from all its triangles and bounds most of them: one lane took
+// about 20 ms on such a point of the nested spheres, the warp shares it.
+constexpr int kCoopStack = 4096;
+
+template <bool MIXED>
+__global__ void __launch_bounds__(32) k_closest_coop(PointArgs a) {
+  __shared__ int32_t sref[kCoopStack];
+  __shared__ float skey[kCoopStack];
+  const int lane = threadIdx.x;
+  Counters cnt = {0, 0, 0, 0};
+  for (int64_t base = (int64_t)blockIdx.x * 32; base < a.n; base += (int64_t)gridDim.x * 32) {
+    const int64_t j = base + lane;
+    unsigned todo = __ballot_sync(kFullMask, j < a.n && a.deferred[j] != 0);
+    while (todo) {
+      const int64_t i = base + __ffs(todo) - 1;
+      todo &= todo - 1u;
+      // (k_closest checked the tree id and the point)
+      const int32_t tid = a.ray_trees ? a.ray_trees[i] : a.tree;
+      const TreeDev T = a.trees[tid - 1];
+      const d3 p = load3(a.pts, i);
+      const float px = __double2float_rn(p.x), py = __double2float_rn(p.y),
+                  pz = __double2float_rn(p.z);
+      const float pabs = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
+      const bool f32ok = pabs + T.max_abs < 1e18f;
+      const bool cbound = MIXED && a.tri_cb && f32ok;
+      const float cmargin = 48.0f * kU32 * (pabs + T.max_abs);
+      double best = a.def_best[i];
+      int32_t best_face = a.def_face[i];
+      int32_t st = RAY_OK;
+      int top = 0;
+      if (T.root != CHILD_EMPTY) {
+        if (lane == 0) {
+          sref[0] = T.root;
+          skey[0] = 0.0f;
+        }
+        top = 1;
+      }
+      __syncwarp();
+      while (top > 0) {
+        // the top entries, one per lane; an entry whose bound is above the
+        // best (rounded up) holds no facet that could win
+        const int take = min(top, 32);
+        int32_t ref = CHILD_EMPTY;
+        if (lane < take && !(skey[top - 1 - lane] > __double2float_ru(best)))
+          ref = sref[top - 1 - lane];
+        top -= take;
+        __syncwarp();  // every entry read before the pushes below reuse the slots
+        int32_t cr[8];
+        float ck[8];
+        int nc = 0;
+        double lbest = best;
+        int32_t lface = best_face;
+        if (ref != CHILD_EMPTY && !ref_is_leaf(ref)) {
+          const int nrec = T.width / kWidth;
+          for (int rec = 0; rec < nrec; ++rec) {
+            cnt.node++;
+            cnt.box += 4;
+            int32_t c4[4];
+            float k4[4];
+            const int nh = closest_children<MIXED>(T, ref, rec, p, px, py, pz, pabs, f32ok, best,
+                                                   c4, k4);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              if (k < nh) {
+                cr[rec * 4 + k] = c4[k];
+                ck[rec * 4 + k] = k4[k];
+              } else {
+                cr[rec * 4 + k] = CHILD_EMPTY;
+              }
+            }
+            nc = rec * 4 + 4;
+          }
+        } else if (ref != CHILD_EMPTY) {
+          const int32_t first = leaf_first(ref), count = leaf_count(ref);
+          const float bestf = __double2float_ru(best);
+          for (int32_t q = 0; q < count; ++q) {
+            cnt.prim++;
+            const int32_t qq = first + q;
+            if (cbound) {
+              if (!closest_may_win(a.tri_cb, __ldg(&T.prim_ref[qq]), px, py, pz, cmargin, bestf))
+                continue;
+              cnt.esc++;
+            }
+            d3 v0, v1, v2;
+            load_tri64(T.prim64 + kPrim64Stride * (int64_t)qq, v0, v1, v2);
+            const double dd = dist64(closest64(v0, v1, v2, p), p);
+            const int32_t fid = __ldg(&a.tri_face[__ldg(&T.prim_ref[qq])]);
+            if (closest_better(dd, fid, lbest, lface)) {
+              lbest = dd;
+              lface = fid;
+            }
+          }
+        }
+        // the children to push (slots of cr holding CHILD_EMPTY are gaps)
+        int mine = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) mine += (k < nc && cr[k] != CHILD_EMPTY) ? 1 : 0;
+        int incl = mine;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const int y = __shfl_up_sync(kFullMask, incl, off);
+          if (lane >= off) incl += y;
+        }
+        const int total = __shfl_sync(kFullMask, incl, 31);
+        if (top + total > kCoopStack) {
+          st = RAY_STACK_OVERFLOW;  // (warp-uniform)
+        } else {
+          // each record's children nearest last, so the nearest is taken first
+          int pos = top + incl - mine;
+#pragma unroll
+          for (int k = 7; k >= 0; --k) {
+            if (k < nc && cr[k] != CHILD_EMPTY) {
+              sref[pos] = cr[k];
+              skey[pos] = ck[k];
+              ++pos;
+            }
+          }
+          top += total;
+        }
+        __syncwarp();
+        // the warp's best: the lanes' candidates merged, then lane 0's taken
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const double od = __shfl_xor_sync(kFullMask, lbest, off);
+          const int32_t of = __shfl_xor_sync(kFullMask, lface, off);
+          if (closest_better(od, of, lbest, lface)) {
+            lbest = od;
+            lface = of;
+          }
+        }
+        best = __shfl_sync(kFullMask, lbest, 0);
+        best_face = __shfl_sync(kFullMask, lface, 0);
+        if (st != RAY_OK) break;
+      }
+      if (lane == 0) {
+        a.dist_out[i] = best_face >= 0 ? best : INFTY;
+        if (a.id_out) a.id_out[i] = best_face;
+        if (a.status) a.status[i] = st;
+      }
+      __syncwarp();
+    }
+  }
+  if (a.counters) flush_counters(a.counters, cnt, 0ull);
 }
 
 // ---------------------------------------------------------------------------
@@ -537,10 +736,24 @@ inline unsigned grid_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBloc
 
 cudaError_t launch_closest(bool mixed, const PointArgs& a, cudaStream_t st) {
   if (a.n <= 0) return cudaSuccess;
+  PointArgs b = a;
+  const bool coop = a.step_budget > 0 && a.deferred && a.def_best && a.def_face;
+  if (!coop) b.step_budget = 0;
   if (mixed)
-    k_closest<true><<<grid_for(a.n), kBlock, 0, st>>>(a);
+    k_closest<true><<<grid_for(a.n), kBlock, 0, st>>>(b);
   else
-    k_closest<false><<<grid_for(a.n), kBlock, 0, st>>>(a);
+    k_closest<false><<<grid_for(a.n), kBlock, 0, st>>>(b);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !coop) return e;
+  // the deferred points, one warp each; blocks of one warp with a 32 KB
+  // stack, at most 7 per SM, each scanning its share of the flags
+  const int64_t need = (a.n + 31) / 32;
+  const unsigned grid = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>(need, (int64_t)device_sm_count() * 7));
+  if (mixed)
+    k_closest_coop<true><<<grid, 32, 0, st>>>(b);
+  else
+    k_closest_coop<false><<<grid, 32, 0, st>>>(b);
   return cudaGetLastError();
 }
 

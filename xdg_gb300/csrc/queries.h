@@ -101,6 +101,14 @@ struct PointArgs {
   const float4* tri_cb;
   const int32_t* elem_ids;   // find_element: element mesh ids
   int32_t node_steps;        // closest: inner-node steps per lane between leaf phases (1..64)
+  // closest, optional: a lane stops a point's search after step_budget node
+  // records and triangles (0: no budget), sets deferred[i] and leaves its
+  // best so far in def_best / def_face; a warp then finishes each such point
+  // (launch_closest).  deferred, def_best and def_face hold n entries.
+  int32_t step_budget;
+  int8_t* deferred;
+  double* def_best;
+  int32_t* def_face;
   double* dist_out;
   int32_t* id_out;
   int32_t* index_out;
