@@ -261,8 +261,9 @@ int xdgcu_walk_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* start_index,
  * walked once, in rounds of walks capped at 16..256 segments per track: a
  * walk that reaches the cap pauses and the next round resumes it where it
  * stopped; each round's segments wait in temporary device memory (about the
- * output's size, plus a buffer of up to 1 GiB, allocated on `stream` with
- * cudaMallocAsync) until the offsets are known.  Where that memory cannot be
+ * output's size, plus a buffer of up to 1 GiB, allocated on `stream` from
+ * the context's scratch pool, "scratch_keep_bytes") until the offsets are
+ * known.  Where that memory cannot be
  * had, or with the tuning key "packed_walk_passes" = 2, the tracks are walked
  * twice instead (count, then emit at the scanned offsets), which needs only
  * the scan's scratch.  The results are the same either way. */
@@ -302,8 +303,9 @@ int xdgcu_set_boundary_face_elements(xdgcu_ctx* ctx, int64_t n, const int32_t* f
  * XDGCU_RAY_WALK_LIMIT (the reference has no limit).
  * status (may be NULL) also records XDGCU_RAY_NO_EXIT_FACE (the track went
  * on, as the reference's does) and XDGCU_RAY_INVALID (non-finite input).
- * Host or device arrays (not mixed); scratch is allocated on `stream` with
- * cudaMallocAsync, and the call waits for a few counters per round. */
+ * Host or device arrays (not mixed); scratch is allocated on `stream` from
+ * the context's scratch pool, and the call waits for a few counters per
+ * round. */
 int xdgcu_segments_global(xdgcu_ctx* ctx, int32_t ipc_tree, int32_t element_tree, int64_t n,
                           const double* starts, const double* ends, int32_t max_segs,
                           int32_t max_rounds, int64_t capacity, int32_t* seg_elem, double* seg_len,
@@ -518,6 +520,17 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      it
  *   "find_node_steps_fp64"  the same for the all-FP64 find_element (default
  *                      16), and for the mixed one when it runs in phases
+ *   "scratch_keep_bytes"  the calls' temporary device memory (allocated on
+ *                      their stream) comes from a memory pool of the
+ *                      context that keeps up to this many bytes of it between
+ *                      calls (default 8 GiB; 0 returns it to the driver at
+ *                      each synchronisation, as the device's default pool
+ *                      does); setting it waits for the device and releases
+ *                      what exceeds it.  The
+ *                      pool is destroyed with the context.  Read-only
+ *                      "scratch_bytes_reserved" is what the pool holds and
+ *                      "scratch_bytes_high" the most it has lent at once
+ *                      (set it to 0 to restart the count)
  *   "packed_walk_passes"  xdgcu_walk_elements_packed: 1 (default) walks each
  *                      track once, in resumed rounds; 2 walks it twice (a
  *                      count walk, then an emit walk), without the temporary

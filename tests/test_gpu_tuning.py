@@ -308,6 +308,32 @@ def test_node_width_8_elements(cuda, prec):
     assert (a[0] >= 0).sum() > 35_000  # (10/11)^3 of the points lie in the cube
 
 
+def test_scratch_pool(nested):
+    """The calls' scratch comes from the context's pool, which keeps up to
+    scratch_keep_bytes of it between calls: after a closest call (its
+    deferral flags and seeds are scratch) the pool holds memory; setting 0
+    releases it at once; results are the same."""
+    _, x, p, _, vols = nested
+    rti = x.rti
+    keep = rti.get_tuning("scratch_keep_bytes")
+    assert keep == 8 << 30
+    ref = x.closest(2, p, MIXED)
+    assert rti.get_tuning("scratch_bytes_reserved") > 0
+    try:
+        rti.set_tuning("scratch_keep_bytes", 0)
+        assert rti.get_tuning("scratch_bytes_reserved") == 0
+        rti.set_tuning("scratch_bytes_high", 0)
+        got = x.closest(2, p, MIXED)
+        assert rti.get_tuning("scratch_bytes_high") > 0
+        assert_same(got[0], ref[0], "closest distance")
+        assert_same(got[1], ref[1], "closest face")
+        for k, v in [("scratch_keep_bytes", -1), ("scratch_bytes_high", 5)]:
+            with pytest.raises(Exception):
+                rti.set_tuning(k, v)
+    finally:
+        rti.set_tuning("scratch_keep_bytes", keep)
+
+
 def test_find_element_phased(cuda, oracle):
     """The mixed find_element one lane per point (find_element_phased 0) and
     in warp-synchronous phases (1) give the oracle's element ids and indices,

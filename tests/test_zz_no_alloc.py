@@ -111,8 +111,9 @@ def test_noalloc_walk_matches_allocating_walk(cuda, prec):
         assert np.array_equal(got[0], ref[0]), call
         assert np.array_equal(got[1], ref[1]), call
 
-    # no allocation inside a call (after the first call's set-up): the pool's
-    # high-water mark and the free memory stay as they were; the same check
+    # no allocation inside a call (after the first call's set-up): the high-
+    # water marks of the device's default pool and of the context's scratch
+    # pool, and the free memory, stay as they were; the scratch pool's mark
     # sees the allocating entry point's scratch
     outs = [torch.empty(total, dtype=torch.int32, device=dev),
             torch.empty(total, dtype=torch.float64, device=dev),
@@ -123,17 +124,20 @@ def test_noalloc_walk_matches_allocating_walk(cuda, prec):
     def call(fn):
         torch.cuda.synchronize()
         base = watch.reset()
+        rti.set_tuning("scratch_bytes_high", 0)
         free0 = torch.cuda.mem_get_info()[0]
         rc = fn(rti.ctx, n, P(idx), P(ts), P(tu), P(tl), max_segs, total, P(outs[0]), P(outs[1]),
                 P(outs[2]), P(outs[3]), prec, stream)
         _lib.check(rc, rti.ctx, fn.__name__)
         torch.cuda.synchronize()
-        return watch.high() - base, free0 - torch.cuda.mem_get_info()[0]
+        return (watch.high() - base, rti.get_tuning("scratch_bytes_high"),
+                free0 - torch.cuda.mem_get_info()[0])
 
-    grew, _ = call(L.xdgcu_walk_elements_packed)
-    assert grew > 0  # the watch sees the allocating walk's cudaMallocAsync
-    grew, used = call(L.xdgcu_walk_elements_packed_noalloc)
-    assert grew == 0 and used == 0
+    _, scratch, _ = call(L.xdgcu_walk_elements_packed)
+    assert scratch > 0  # the context's pool lends the allocating walk its scratch
+    assert rti.get_tuning("scratch_bytes_reserved") > 0  # and keeps it for the next call
+    grew, scratch, used = call(L.xdgcu_walk_elements_packed_noalloc)
+    assert grew == 0 and scratch == 0 and used == 0
     assert np.array_equal(outs[2].cpu().numpy(), ref[2])
 
 

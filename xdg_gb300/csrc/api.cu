@@ -430,9 +430,20 @@ struct xdgcu_ctx {
   std::mutex slot_mu;
   std::unordered_map<std::thread::id, std::unique_ptr<Slot>> slots;
   cudaStream_t build_stream = nullptr;
+  // the calls' stream-ordered scratch comes from this pool, which keeps up to
+  // keep_bytes of freed memory for later calls instead of returning it to the
+  // driver at each synchronisation as the device's default pool does (the
+  // global track loop on 1e6 tracks: 36.7 -> 33.0 ms); null: the default pool
+  cudaMemPool_t pool = nullptr;
+  int64_t keep_bytes = int64_t(8) << 30;
 };
 
 namespace {
+
+// Stream-ordered scratch of a call, from the context's pool.
+cudaError_t scratch_alloc(const xdgcu_ctx* c, void** p, size_t bytes, cudaStream_t s) {
+  return c->pool ? cudaMallocFromPoolAsync(p, bytes, c->pool, s) : cudaMallocAsync(p, bytes, s);
+}
 
 int sync_surfaces(xdgcu_ctx* c) {
   if (c->tri_dirty) {
@@ -912,7 +923,7 @@ int with_length_order(xdgcu_ctx* c, WalkArgs& a, cudaStream_t s, Body body) {
   const size_t ord_bytes = ((sizeof(int32_t) * (size_t)a.n + 255) & ~(size_t)255);
   const size_t scr = walk_order_scratch_bytes(a.n);
   char* buf = nullptr;
-  API_CUDA(cudaMallocAsync((void**)&buf, ord_bytes + scr, s), "walk order scratch");
+  API_CUDA(scratch_alloc(c, (void**)&buf, ord_bytes + scr, s), "walk order scratch");
   cudaError_t e = walk_order(a.dist, a.n, (int32_t*)buf, buf + ord_bytes, scr, s);
   if (e != cudaSuccess) {
     cudaFreeAsync(buf, s);
@@ -928,8 +939,9 @@ int with_length_order(xdgcu_ctx* c, WalkArgs& a, cudaStream_t s, Body body) {
 // Stream-ordered scratch of one call, freed on every return path.
 struct CallScratch {
   cudaStream_t st;
+  cudaMemPool_t pool;
   std::vector<void*> ptrs;
-  explicit CallScratch(cudaStream_t s) : st(s) {}
+  CallScratch(cudaStream_t s, cudaMemPool_t p) : st(s), pool(p) {}
   ~CallScratch() {
     for (void* p : ptrs) cudaFreeAsync(p, st);
   }
@@ -937,7 +949,9 @@ struct CallScratch {
   cudaError_t get(T** out, int64_t count) {
     *out = nullptr;
     void* p = nullptr;
-    const cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (size_t)std::max<int64_t>(1, count), st);
+    const size_t bytes = sizeof(T) * (size_t)std::max<int64_t>(1, count);
+    const cudaError_t e =
+        pool ? cudaMallocFromPoolAsync(&p, bytes, pool, st) : cudaMallocAsync(&p, bytes, st);
     if (e != cudaSuccess) return e;
     ptrs.push_back(p);
     *out = static_cast<T*>(p);
@@ -997,7 +1011,7 @@ int walk_packed_rounds(xdgcu_ctx* c, bool mixed, const WalkArgs& a, cudaStream_t
                        bool* no_memory) {
   *no_memory = false;
   const int64_t n = a.n;
-  CallScratch S(st);
+  CallScratch S(st, c->pool);
   bool ok = true;
   auto get = [&](auto** p, int64_t count) {
     if (ok && S.get(p, count) != cudaSuccess) {
@@ -1144,7 +1158,7 @@ cudaError_t launch_trace(xdgcu_ctx* c, int mode, bool mixed, SurfArgs a, double 
   const size_t ord_bytes = sort ? ((sizeof(int32_t) * (size_t)a.n + 255) & ~(size_t)255) : 0;
   const size_t scr = sort ? ray_order_scratch_bytes(a.n) : 0;
   char* buf = nullptr;
-  cudaError_t e = cudaMallocAsync((void**)&buf, 256 + ord_bytes + scr, s);
+  cudaError_t e = scratch_alloc(c, (void**)&buf, 256 + ord_bytes + scr, s);
   if (e != cudaSuccess) return e;
   if (a.grab > 0) {
     a.work = (unsigned long long*)buf;
@@ -1229,6 +1243,18 @@ int xdgcu_create(xdgcu_ctx** out, int device) {
     delete c;
     return set_err(XDGCU_ERR_CUDA, "stream creation failed");
   }
+  // the scratch pool (without one the calls use the device's default pool)
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = device;
+  if (cudaMemPoolCreate(&c->pool, &props) == cudaSuccess) {
+    uint64_t keep = (uint64_t)c->keep_bytes;
+    cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  } else {
+    cudaGetLastError();
+    c->pool = nullptr;
+  }
   *out = c;
   return XDGCU_OK;
 }
@@ -1238,6 +1264,7 @@ int xdgcu_destroy(xdgcu_ctx* c) {
   DeviceGuard guard(c->device);
   cudaDeviceSynchronize();
   if (c->build_stream) cudaStreamDestroy(c->build_stream);
+  if (c->pool) cudaMemPoolDestroy(c->pool);
   delete c;
   return XDGCU_OK;
 }
@@ -1579,6 +1606,25 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     (k == "closest_node_steps"        ? c->closest_node_steps
      : k == "closest_node_steps_fp64" ? c->closest_node_steps_fp64
                                       : c->find_node_steps_fp64) = (int32_t)value;
+  } else if (k == "scratch_keep_bytes") {
+    if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "scratch_keep_bytes must be >= 0");
+    c->keep_bytes = value;
+    if (c->pool) {
+      uint64_t keep = (uint64_t)value;
+      API_CUDA(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep),
+               "scratch pool");
+      // memory freed on a stream counts as held until the host has seen the
+      // free complete: wait for the device, then release
+      DeviceGuard guard(c->device);
+      API_CUDA(cudaDeviceSynchronize(), "scratch pool");
+      API_CUDA(cudaMemPoolTrimTo(c->pool, (size_t)value), "scratch pool");
+    }
+  } else if (k == "scratch_bytes_high") {
+    if (value != 0) return set_err(XDGCU_ERR_INVALID_ARG, "scratch_bytes_high can only be reset to 0");
+    if (c->pool) {
+      uint64_t zero = 0;
+      API_CUDA(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrUsedMemHigh, &zero), "scratch pool");
+    }
   } else if (k == "closest_step_budget") {
     if (value < 0 || value > (1 << 30))
       return set_err(XDGCU_ERR_INVALID_ARG, "closest_step_budget must be 0..2^30");
@@ -1646,6 +1692,17 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "find_element_phased") *value = c->find_phased;
   else if (k == "packed_walk_passes") *value = c->packed_passes;
   else if (k == "closest_step_budget") *value = c->closest_budget;
+  else if (k == "scratch_keep_bytes") *value = c->keep_bytes;
+  else if (k == "scratch_bytes_reserved" || k == "scratch_bytes_high") {
+    uint64_t v = 0;
+    if (c->pool &&
+        cudaMemPoolGetAttribute(c->pool,
+                                k == "scratch_bytes_high" ? cudaMemPoolAttrUsedMemHigh
+                                                          : cudaMemPoolAttrReservedMemCurrent,
+                                &v) != cudaSuccess)
+      return set_err(XDGCU_ERR_CUDA, "scratch pool");
+    *value = (int64_t)v;
+  }
   else if (k == "walk_edges") *value = c->n_edges;
   else if (k == "pageable_direct") *value = c->pageable_direct ? 1 : 0;
   else if (k == "host_direct_choice") *value = c->hd_choice;
@@ -1930,7 +1987,7 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
     a.status = status;
     int rc = begin_query(c, st, &a.counters);
     if (rc) return rc;
-    CallScratch S(st);
+    CallScratch S(st, c->pool);
     API_CUDA(defer_scratch(S), "closest scratch");
     API_CUDA(launch(), "query launch");
     return XDGCU_OK;
@@ -1939,7 +1996,7 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
   if (!s) return set_err(XDGCU_ERR_CUDA, "staging stream creation failed");
   // (the chunks' launches alternate between the slot's streams; the second
   // waits for the first before its first launch)
-  CallScratch S(s->stream);
+  CallScratch S(s->stream, c->pool);
   API_CUDA(defer_scratch(S), "closest scratch");
   RayArr R_trees{ray_trees, nullptr, ray_trees ? sizeof(int32_t) : 0};
   RayArr R_p{pts, nullptr, sizeof(double) * 3};
@@ -2131,7 +2188,8 @@ int xdgcu_walk_elements_packed(xdgcu_ctx* c, int64_t n, const int32_t* start_ind
       a.out_mode = WALK_COUNT;
       API_CUDA(launch_walk(mixed, c->face_order, a, s), "walk (count)");
       int64_t* sums = nullptr;
-      API_CUDA(cudaMallocAsync(&sums, sizeof(int64_t) * scan_scratch_entries(n), s), "scan scratch");
+      API_CUDA(scratch_alloc(c, (void**)&sums, sizeof(int64_t) * scan_scratch_entries(n), s),
+               "scan scratch");
       cudaError_t e = scan_offsets(a.offsets, n, sums, s);
       cudaFreeAsync(sums, s);
       API_CUDA(e, "scan");
@@ -2282,7 +2340,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
     return XDGCU_OK;
   }
   const bool mixed = precision == XDGCU_MIXED;
-  CallScratch S(st);
+  CallScratch S(st, c->pool);
   // the caller's arrays, or device images of host arrays
   const double* d_starts = starts;
   const double* d_ends = ends;
@@ -2551,7 +2609,7 @@ int xdgcu_point_in_volumes(xdgcu_ctx* c, int64_t n, const double* points,
   // the tree list, in stream order before the launches
   cudaStream_t ls = kind == 1 ? st : s->stream;
   int32_t* d_list = nullptr;
-  API_CUDA(cudaMallocAsync((void**)&d_list, sizeof(int32_t) * n_trees, ls), "tree list");
+  API_CUDA(scratch_alloc(c, (void**)&d_list, sizeof(int32_t) * n_trees, ls), "tree list");
   API_CUDA(cudaMemcpyAsync(d_list, trees, sizeof(int32_t) * n_trees, cudaMemcpyHostToDevice, ls),
            "tree list");
   a.vol_trees = d_list;
