@@ -527,7 +527,11 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      each synchronisation, as the device's default pool
  *                      does); setting it waits for the device and releases
  *                      what exceeds it.  The
- *                      pool is destroyed with the context.  Read-only
+ *                      pool is destroyed with the context; with
+ *                      XDGCU_SCRATCH_POOL=0 in the environment when the
+ *                      context is created, the device's default pool serves
+ *                      instead (for tools that save and restore device
+ *                      memory, such as a profiler's kernel replay).  Read-only
  *                      "scratch_bytes_reserved" is what the pool holds and
  *                      "scratch_bytes_high" the most it has lent at once
  *                      (set it to 0 to restart the count)

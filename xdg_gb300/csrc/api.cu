@@ -17,6 +17,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <chrono>
@@ -1243,12 +1244,18 @@ int xdgcu_create(xdgcu_ctx** out, int device) {
     delete c;
     return set_err(XDGCU_ERR_CUDA, "stream creation failed");
   }
-  // the scratch pool (without one the calls use the device's default pool)
+  // the scratch pool (without one the calls use the device's default pool).
+  // XDGCU_SCRATCH_POOL=0 in the environment leaves it out: a profiler's
+  // kernel replay, which saves and restores the device memory around each
+  // pass, ended in a GPU memory fault in a process with such a pool
   cudaMemPoolProps props{};
   props.allocType = cudaMemAllocationTypePinned;
   props.location.type = cudaMemLocationTypeDevice;
   props.location.id = device;
-  if (cudaMemPoolCreate(&c->pool, &props) == cudaSuccess) {
+  const char* want_pool = std::getenv("XDGCU_SCRATCH_POOL");
+  if (want_pool && std::strcmp(want_pool, "0") == 0) {
+    c->pool = nullptr;
+  } else if (cudaMemPoolCreate(&c->pool, &props) == cudaSuccess) {
     uint64_t keep = (uint64_t)c->keep_bytes;
     cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   } else {

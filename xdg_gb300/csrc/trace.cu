@@ -482,8 +482,8 @@ __global__ void __launch_bounds__(kTBlock, MINB) k_trace(SurfArgs a, int64_t chu
     if (need != 0u && cursor < end) {
       if (!has_ray) {
         const int64_t pos = cursor + __popc(need & lanemask_lt());
-        if (pos < end) {
-          const int64_t idx = a.order ? (int64_t)__ldg(&a.order[pos]) : pos;
+        const int64_t idx = pos < end ? (a.order ? (int64_t)__ldg(&a.order[pos]) : pos) : -1;
+        if (idx >= 0 && idx < a.n) {  // (an order entry out of range names no ray)
           ray = idx;
           has_ray = true;
           status = RAY_OK;

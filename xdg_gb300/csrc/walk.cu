@@ -277,9 +277,10 @@ __global__ void __launch_bounds__(kBlock) k_walk(WalkArgs a, int64_t chunk) {
         unsigned lt;
         asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
         const int64_t kk = cursor + __popc(need & lt);
-        if (kk < end) {
-          const int64_t pos = first + kk * stride;
-          i = a.order ? (int64_t)__ldg(&a.order[pos]) : pos;
+        const int64_t pos = first + kk * stride;
+        const int64_t cand = kk < end ? (a.order ? (int64_t)__ldg(&a.order[pos]) : pos) : -1;
+        if (cand >= 0 && cand < a.n) {  // (an order entry out of range names no track)
+          i = cand;
           has = true;
           r = load3(a.org, i);
           u = load3(a.dir, i);
@@ -518,9 +519,10 @@ __global__ void __launch_bounds__(kBlock) k_walk_q(WalkArgs a, int64_t chunk) {
         unsigned lt;
         asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
         const int64_t kk = cursor + __popc(need & lt);
-        if (kk < end) {
-          const int64_t pos = first + kk * stride;
-          i = a.order ? (int64_t)__ldg(&a.order[pos]) : pos;
+        const int64_t pos = first + kk * stride;
+        const int64_t cand = kk < end ? (a.order ? (int64_t)__ldg(&a.order[pos]) : pos) : -1;
+        if (cand >= 0 && cand < a.n) {  // (an order entry out of range names no track)
+          i = cand;
           has = true;
           in_step = false;
           r = load3(a.org, i);
