@@ -576,12 +576,12 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      staged pipeline to overlap its copies; 4 is 2 except
  *                      that such a large call reads its page-locked inputs
  *                      in place and stages its outputs; 5 (the default)
- *                      chooses between 2 and 3 by measurement: the first
- *                      four large calls with host arrays alternate between
- *                      them and are timed, and every later large call takes
- *                      the faster (read-only key "host_direct_choice": -1
- *                      while undecided, then 2 or 3; setting host_direct to
- *                      5 again starts a new choice).  Which is faster depends
+ *                      chooses among 2, 3 and 4 by measurement: the first
+ *                      six large calls with host arrays take them in turn
+ *                      and are timed, and every later large call takes the
+ *                      fastest (read-only key "host_direct_choice": -1 while
+ *                      undecided, then 2, 3 or 4; setting host_direct to 5
+ *                      again starts a new choice).  Which is faster depends
  *                      on the machine and the launch settings.  Staged
  *                      chunks' kernels alternate between two streams and take
  *                      their rays from the device work queue, so that one

@@ -8,7 +8,7 @@ with pageable outputs (some arrays in place, the rest staged), under each
 host_direct setting (2 keeps both kinds in place; 3 stages the page-locked
 arrays of this large call in overlapping chunks; 4 stages only its
 page-locked inputs and writes the outputs in place; staged chunks' kernels
-alternate between two streams; 5, the default, picks 2 or 3 by timing the
+alternate between two streams; 5, the default, picks 2, 3 or 4 by timing the
 first large calls).  The
 packed tet walk and the walk_elements particle loop
 (whose atomic tally is always staged) are checked the same way.
@@ -99,9 +99,10 @@ def test_ray_fire_host_buffers(cuda, rays, prec):
 
 
 def test_automatic_policy_choice(cuda, rays):
-    """host_direct 5 times the first four large page-locked calls (two in
-    place, two staged), then keeps the faster; every call gives the same
-    results, and setting 5 again starts a new choice."""
+    """host_direct 5 times the first six large page-locked calls (two in
+    place, two staged, two with the inputs in place and the outputs staged),
+    then keeps the fastest; every call gives the same results, and setting 5
+    again starts a new choice."""
     torch = cuda
     x, p, d, trees = rays
     rti = x.rti
@@ -113,7 +114,7 @@ def test_automatic_policy_choice(cuda, rays):
         assert rti.get_tuning("host_direct_choice") == -1
         (tr, o, u), outs = _buffers(torch, "pinned", n, [trees, p, d])
         ref = None
-        for call in range(6):
+        for call in range(8):
             rc = L.xdgcu_ray_fire(rti.ctx, 0, _ptr(tr), n, _ptr(o), _ptr(u), None, 0, None, None,
                                   *[_ptr(t) for t in outs], MIXED, None)
             _lib.check(rc, rti.ctx, "ray_fire")
@@ -123,7 +124,7 @@ def test_automatic_policy_choice(cuda, rays):
             else:
                 assert all(bool(torch.equal(a, b)) for a, b in zip(got, ref)), call
             choice = rti.get_tuning("host_direct_choice")
-            assert choice == (-1 if call < 3 else choice) and (call < 3 or choice in (2, 3))
+            assert (choice == -1) if call < 5 else (choice in (2, 3, 4)), (call, choice)
         rti.set_tuning("host_direct", 5)
         assert rti.get_tuning("host_direct_choice") == -1
     finally:

@@ -402,7 +402,7 @@ struct xdgcu_ctx {
   // 0 none, 1 page-locked memory, 2 also pageable memory when the device
   // reads it through the host's page tables (pageable_direct), 3 / 4 stage
   // all / the outputs of large calls' page-locked arrays, 5 (default) picks
-  // 2 or 3 for large calls by timing both (xdgcu_set_tuning)
+  // 2, 3 or 4 for large calls by timing each (xdgcu_set_tuning)
   int32_t host_direct = 5;
   int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
   int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from d_tri_prime
@@ -415,12 +415,13 @@ struct xdgcu_ctx {
   int32_t closest_budget = 1024;  // closest: steps of one lane before a warp takes the point (0: never)
   int32_t segments_walk_cap = 0;  // segments_global: segments per walk and round (0 = automatic)
   bool pageable_direct = false;
-  // host_direct 5: trial calls of in place (0) and staged (1), their summed
-  // seconds per ray, and the policy chosen (-1 until both have kAutoTrials)
+  // host_direct 5: trial calls of the policies kAutoPolicies (in place,
+  // staged, inputs in place with outputs staged), their summed seconds per
+  // ray, and the policy chosen (-1 until each has kAutoTrials)
   std::mutex hd_mu;
   int32_t hd_trials = 0;
-  int32_t hd_timed[2] = {0, 0};
-  double hd_sec_per_ray[2] = {0.0, 0.0};
+  int32_t hd_timed[3] = {0, 0, 0};
+  double hd_sec_per_ray[3] = {0.0, 0.0, 0.0};
   int32_t hd_choice = -1;
   int64_t walk_sort_min = 16384;  // tracks; 0 disables the length order
   // diagnostics
@@ -747,6 +748,10 @@ constexpr int64_t kChunkRays = 1 << 21;
 constexpr int64_t kMaxChunks = 16;
 // host_direct 5: timed calls of each policy before the choice
 constexpr int kAutoTrials = 2;
+// host_direct 5: the policies it chooses among (the fastest differed from one
+// GB300 machine to another: staged on some, in place or inputs in place with
+// outputs staged on others)
+constexpr int kAutoPolicies[3] = {2, 3, 4};
 // work-queue grab of a chunk's traversal launch (when a call runs in chunks)
 constexpr int32_t kChunkGrab = 64;
 
@@ -763,8 +768,8 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
                std::vector<RayArr*> rays, unsigned long long** counters, Launch launch) {
   // arrays the kernels address in place take no workspace and no copies
   const bool pipelined = n > 2 * kChunkRays;
-  // host_direct 5: the first large calls alternate between in place (2) and
-  // staged (3) and are timed; then every large call takes the faster
+  // host_direct 5: the first large calls take the policies kAutoPolicies in
+  // turn and are timed; then every large call takes the fastest
   int hd = c->host_direct;
   int trial = -1;
   if (hd == 5) {
@@ -774,8 +779,8 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
       if (c->hd_choice >= 0) {
         hd = c->hd_choice;
       } else {
-        trial = c->hd_trials++ & 1;
-        hd = trial ? 3 : 2;
+        trial = c->hd_trials++ % 3;
+        hd = kAutoPolicies[trial];
       }
     }
   }
@@ -889,10 +894,15 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
     std::lock_guard<std::mutex> g(c->hd_mu);
     c->hd_sec_per_ray[trial] += sec / (double)n;
     c->hd_timed[trial]++;
-    if (c->hd_choice < 0 && c->hd_timed[0] >= kAutoTrials && c->hd_timed[1] >= kAutoTrials)
-      c->hd_choice = c->hd_sec_per_ray[1] / c->hd_timed[1] < c->hd_sec_per_ray[0] / c->hd_timed[0]
-                         ? 3
-                         : 2;
+    bool all = c->hd_choice < 0;
+    for (int k = 0; k < 3; ++k) all = all && c->hd_timed[k] >= kAutoTrials;
+    if (all) {
+      int best = 0;
+      for (int k = 1; k < 3; ++k)
+        if (c->hd_sec_per_ray[k] / c->hd_timed[k] < c->hd_sec_per_ray[best] / c->hd_timed[best])
+          best = k;
+      c->hd_choice = kAutoPolicies[best];
+    }
   }
   return XDGCU_OK;
 }
@@ -1659,8 +1669,10 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
     if (value == 5) {  // a fresh choice
       std::lock_guard<std::mutex> g(c->hd_mu);
       c->hd_trials = 0;
-      c->hd_timed[0] = c->hd_timed[1] = 0;
-      c->hd_sec_per_ray[0] = c->hd_sec_per_ray[1] = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        c->hd_timed[k] = 0;
+        c->hd_sec_per_ray[k] = 0.0;
+      }
       c->hd_choice = -1;
     }
   } else {
