@@ -929,10 +929,10 @@ def run_engine(args, rank, world, local):
         # and written in place by the kernel; 2: pageable arrays in place too;
         # 3: page-locked arrays of large calls staged in overlapping chunks;
         # 4: large calls' outputs staged; 5 (the default): 2, 3 or 4, chosen
-        # by timing the first six large calls, which are warm-up calls here
+        # by timing six of the first nine large calls, warm-up calls here
         old_hd = rti.get_tuning("host_direct")
         rti.set_tuning("host_direct", host_direct)
-        for _ in range(2 + (6 if host_direct == 5 else 0)):
+        for _ in range(2 + (9 if host_direct == 5 else 0)):
             e2e_call(bufs)
         torch.cuda.synchronize()
         dist.barrier(world)

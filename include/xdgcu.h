@@ -577,9 +577,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      that such a large call reads its page-locked inputs
  *                      in place and stages its outputs; 5 (the default)
  *                      chooses among 2, 3 and 4 by measurement: the first
- *                      six large calls with host arrays take them in turn
- *                      and are timed, and every later large call takes the
- *                      fastest (read-only key "host_direct_choice": -1 while
+ *                      nine large calls with host arrays take them in turn,
+ *                      the last six are timed, and every later large call
+ *                      takes the fastest (read-only key "host_direct_choice": -1 while
  *                      undecided, then 2, 3 or 4; setting host_direct to 5
  *                      again starts a new choice).  Which is faster depends
  *                      on the machine and the launch settings.  Staged

@@ -99,10 +99,11 @@ def test_ray_fire_host_buffers(cuda, rays, prec):
 
 
 def test_automatic_policy_choice(cuda, rays):
-    """host_direct 5 times the first six large page-locked calls (two in
-    place, two staged, two with the inputs in place and the outputs staged),
-    then keeps the fastest; every call gives the same results, and setting 5
-    again starts a new choice."""
+    """host_direct 5 runs the first nine large page-locked calls in place,
+    staged and with the inputs in place and the outputs staged in turn, times
+    the last six (the first of each pays one-time costs), then keeps the
+    fastest; every call gives the same results, and setting 5 again starts a
+    new choice."""
     torch = cuda
     x, p, d, trees = rays
     rti = x.rti
@@ -114,7 +115,7 @@ def test_automatic_policy_choice(cuda, rays):
         assert rti.get_tuning("host_direct_choice") == -1
         (tr, o, u), outs = _buffers(torch, "pinned", n, [trees, p, d])
         ref = None
-        for call in range(8):
+        for call in range(11):
             rc = L.xdgcu_ray_fire(rti.ctx, 0, _ptr(tr), n, _ptr(o), _ptr(u), None, 0, None, None,
                                   *[_ptr(t) for t in outs], MIXED, None)
             _lib.check(rc, rti.ctx, "ray_fire")
@@ -124,7 +125,7 @@ def test_automatic_policy_choice(cuda, rays):
             else:
                 assert all(bool(torch.equal(a, b)) for a, b in zip(got, ref)), call
             choice = rti.get_tuning("host_direct_choice")
-            assert (choice == -1) if call < 5 else (choice in (2, 3, 4)), (call, choice)
+            assert (choice == -1) if call < 8 else (choice in (2, 3, 4)), (call, choice)
         rti.set_tuning("host_direct", 5)
         assert rti.get_tuning("host_direct_choice") == -1
     finally:

@@ -779,8 +779,11 @@ int run_staged(xdgcu_ctx* c, Slot* s, cudaStream_t user, int64_t n, std::vector<
       if (c->hd_choice >= 0) {
         hd = c->hd_choice;
       } else {
-        trial = c->hd_trials++ % 3;
-        hd = kAutoPolicies[trial];
+        // the first call of each policy is not timed: it pays one-time
+        // costs (the staging workspace's allocation, first touches)
+        const int32_t k = c->hd_trials++;
+        hd = kAutoPolicies[k % 3];
+        trial = k >= 3 ? k % 3 : -1;
       }
     }
   }
