@@ -1,6 +1,6 @@
 // peaks.cu -- throughput microbenchmarks that give the roofline denominators
-// the driver's measured peaks do not include: FP64 and FP32 arithmetic issue
-// rates and the L2 read bandwidth of this GPU.  Built as its own library
+// a copy-bandwidth and GEMM measurement does not: FP64 and FP32 arithmetic
+// issue rates and the L2 read bandwidth of this GPU.  Built as its own library
 // (libxdgpeaks.so), separate from the engine's C ABI; bench.py runs it on the
 // same GPU in the same process as the kernels whose fractions it reports.
 //
