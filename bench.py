@@ -949,8 +949,18 @@ def run_engine(args, rank, world, local):
     e2e_steps = max(20, args.steps)
     hd_default = rti.get_tuning("host_direct")
     pinned = (tr_h, org_h, dir_h, to_h, so_h, fo_h)
-    ms_e2e, hd_choice = e2e_ms(pinned, hd_default)
+    # the explicit policies first, then the default (a fresh automatic
+    # choice): the first host-array measurement after the device timings ran
+    # up to 9 % slow in this process (1243 against 1357 Mrays/s for the same
+    # policy), which a probe of the calls alone did not show
+    ms_e2e_staged, _ = e2e_ms(pinned, 3)
     e2e_ok = bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_out_staged, _ = e2e_ms(pinned, 4)  # inputs read in place, outputs staged
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e_in_place, _ = e2e_ms(pinned, 2)
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
+    ms_e2e, hd_choice = e2e_ms(pinned, hd_default)
+    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
     policy = {
         0: "page-locked host arrays staged through device memory in overlapping chunks",
         2: "page-locked host arrays read and written in place by the kernel over the host link",
@@ -961,12 +971,6 @@ def run_engine(args, rank, world, local):
                     + (f", which timed its first large calls and chose {hd_choice}" if hd_default == 5
                        else "") + "): " + policy.get(hd_choice if hd_default == 5 else hd_default,
                                                      "see host_direct"))
-    ms_e2e_staged, _ = e2e_ms(pinned, 3)
-    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
-    ms_e2e_out_staged, _ = e2e_ms(pinned, 4)  # inputs read in place, outputs staged
-    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
-    ms_e2e_in_place, _ = e2e_ms(pinned, 2)
-    e2e_ok = e2e_ok and bool(np.array_equal(so_h.numpy(), s_mixed.cpu().numpy()))
     del org_h, dir_h, tr_h, to_h, so_h, fo_h
     # the same call on pageable NumPy arrays
     pg = (np.ascontiguousarray(trees_h), np.ascontiguousarray(p_h), np.ascontiguousarray(d_h),
