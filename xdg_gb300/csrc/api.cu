@@ -1009,6 +1009,82 @@ struct SegRound {
   double* seg_len;
 };
 
+// Per-walk-entry buffers of the rounds (n entries each) and the K-strided
+// segment buffer of strided_cap entries: the walk list (track, start
+// element), the walk's inputs from the tracks' walk state, and what the walk
+// kernel reports (status, count, where it stopped, its running length sum).
+struct SegWalkBufs {
+  int32_t *walk_t, *walk_start, *wst, *wcnt, *wstop, *sk_elem;
+  double *wr, *wu, *wd, *wsum_in, *wsum_out, *wend_r, *wend_d, *sk_len;
+  int64_t strided_cap;
+};
+
+// One round of the capped single-pass walk for the m entries of the walk
+// list: walk_elements from each track's walk state, at most K segments per
+// track into the K-strided buffer, the kept counts scanned into R->off, the
+// kept segments packed into a buffer of the round (R, kept for the final
+// placement), the walk state advanced and the tracks still active appended to
+// act_next (seg_advance; walk_only: an ended walk finishes its track).
+// Synchronises `st` once, for the round's total.  On an allocation failure
+// sets *no_memory (when given).
+int seg_walk_round(xdgcu_ctx* c, bool mixed, const SegState& ss, const WalkArgs& geo,
+                   const SegWalkBufs& B, int32_t m, int32_t max_segs, bool walk_only,
+                   int32_t* act_next, int32_t* n_act, CallScratch& S, cudaStream_t st,
+                   bool* no_memory, SegRound* R) {
+  auto get = [&](auto** p, int64_t count) -> bool {
+    if (S.get(p, count) == cudaSuccess) return true;
+    cudaGetLastError();  // the failed allocation is not a pending launch error
+    if (no_memory) *no_memory = true;
+    return false;
+  };
+  const int32_t K = seg_round_k(m, B.strided_cap, c->segments_walk_cap, max_segs);
+  *R = SegRound{};
+  R->m = m;
+  if (!get(&R->walk_t, m) || !get(&R->off, (int64_t)m + 1) || !get(&R->dst_rel, m))
+    return set_err(XDGCU_ERR_CUDA, "walk rounds: temporary memory");
+  API_CUDA(cudaMemcpyAsync(R->walk_t, B.walk_t, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, st),
+           "D2D");
+  API_CUDA(seg_walk_inputs(ss, B.walk_t, m, B.wr, B.wu, B.wd, B.wsum_in, st), "walk inputs");
+  WalkArgs w = geo;
+  w.n = m;
+  w.start = B.walk_start;
+  w.org = B.wr;
+  w.dir = B.wu;
+  w.dist = B.wd;
+  w.max_segs = K;
+  w.status = B.wst;
+  w.seg_count = B.wcnt;
+  w.stop_elem = B.wstop;
+  w.sum_in = B.wsum_in;
+  w.sum_out = B.wsum_out;
+  w.end_r = B.wend_r;
+  w.end_dist = B.wend_d;
+  w.seg_elem = B.sk_elem;
+  w.seg_len = B.sk_len;
+  w.offsets = nullptr;
+  w.out_mode = WALK_STRIDED;
+  int rc = with_length_order(c, w, st, [&]() -> int {
+    API_CUDA(launch_walk(mixed, c->face_order, w, st), "walk");
+    return XDGCU_OK;
+  });
+  if (rc) return rc;
+  // the segments each track keeps (max_segs per walk), packed
+  API_CUDA(seg_round_counts(ss, R->walk_t, m, B.wcnt, max_segs, R->off, st), "walk round counts");
+  int64_t* sums = nullptr;
+  if (!get(&sums, scan_scratch_entries(m))) return set_err(XDGCU_ERR_CUDA, "walk rounds: scan scratch");
+  API_CUDA(scan_offsets(R->off, m, sums, st), "scan");
+  API_CUDA(cudaMemcpyAsync(&R->total, R->off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
+           "D2H");
+  API_CUDA(cudaStreamSynchronize(st), "sync");
+  if (!get(&R->seg_elem, R->total) || !get(&R->seg_len, R->total))
+    return set_err(XDGCU_ERR_CUDA, "walk rounds: temporary memory");
+  API_CUDA(seg_pack(m, K, B.sk_elem, B.sk_len, R->off, R->seg_elem, R->seg_len, st), "walk pack");
+  API_CUDA(seg_advance(ss, R->walk_t, m, K, B.sk_elem, B.wcnt, B.wst, B.wstop, B.wend_r, B.wend_d,
+                       B.wsum_out, max_segs, R->off, R->dst_rel, act_next, n_act, st, walk_only),
+           "walk advance");
+  return XDGCU_OK;
+}
+
 // xdgcu_walk_elements_packed with one walk of every track instead of a count
 // walk and an emit walk: rounds of single-pass walks capped at K segments per
 // track (as the global track loop's walk step), each round's kept segments
@@ -1048,30 +1124,27 @@ int walk_packed_rounds(xdgcu_ctx* c, bool mixed, const WalkArgs& a, cudaStream_t
   get(&ss.wcount, n);
   get(&ss.welem, n);
   get(&ss.paused, n);
-  int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *walk_t = nullptr;
-  int32_t *walk_start = nullptr, *wst = nullptr, *wcnt = nullptr, *wstop = nullptr;
-  int32_t *loc = nullptr, *sk_elem = nullptr;
-  double *wr = nullptr, *wu = nullptr, *wd = nullptr, *sk_len = nullptr;
-  double *wsum_in = nullptr, *wsum_out = nullptr, *wend_r = nullptr, *wend_d = nullptr;
+  int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *loc = nullptr;
   get(&act, n);
   get(&act_next, n);
   get(&counters, 4);
-  get(&walk_t, n);
-  get(&walk_start, n);
-  get(&wst, n);
-  get(&wcnt, n);
-  get(&wstop, n);
   get(&loc, n);
-  get(&wr, 3 * n);
-  get(&wu, 3 * n);
-  get(&wd, n);
-  get(&wsum_in, n);
-  get(&wsum_out, n);
-  get(&wend_r, 3 * n);
-  get(&wend_d, n);
-  const int64_t cap = seg_strided_cap(n, c->segments_walk_cap);
-  get(&sk_elem, cap);
-  get(&sk_len, cap);
+  SegWalkBufs B{};
+  get(&B.walk_t, n);
+  get(&B.walk_start, n);
+  get(&B.wst, n);
+  get(&B.wcnt, n);
+  get(&B.wstop, n);
+  get(&B.wr, 3 * n);
+  get(&B.wu, 3 * n);
+  get(&B.wd, n);
+  get(&B.wsum_in, n);
+  get(&B.wsum_out, n);
+  get(&B.wend_r, 3 * n);
+  get(&B.wend_d, n);
+  B.strided_cap = seg_strided_cap(n, c->segments_walk_cap);
+  get(&B.sk_elem, B.strided_cap);
+  get(&B.sk_len, B.strided_cap);
   if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
   int32_t* n_act = counters;
   int32_t* n_walk = counters + 1;
@@ -1082,54 +1155,12 @@ int walk_packed_rounds(xdgcu_ctx* c, bool mixed, const WalkArgs& a, cudaStream_t
   while (m > 0) {
     // every active track is a paused walk: all go to the walk list
     API_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(int32_t), st), "memset");
-    API_CUDA(seg_split(ss, act, m, walk_t, walk_start, n_walk, loc, n_loc, st), "packed walk split");
-    const int32_t K = seg_round_k(m, cap, c->segments_walk_cap, a.max_segs);
+    API_CUDA(seg_split(ss, act, m, B.walk_t, B.walk_start, n_walk, loc, n_loc, st),
+             "packed walk split");
     SegRound R{};
-    R.m = m;
-    get(&R.walk_t, m);
-    get(&R.off, (int64_t)m + 1);
-    get(&R.dst_rel, m);
-    if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
-    API_CUDA(cudaMemcpyAsync(R.walk_t, walk_t, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, st),
-             "D2D");
-    API_CUDA(seg_walk_inputs(ss, walk_t, m, wr, wu, wd, wsum_in, st), "packed walk inputs");
-    WalkArgs w = a;
-    w.n = m;
-    w.start = walk_start;
-    w.org = wr;
-    w.dir = wu;
-    w.dist = wd;
-    w.max_segs = K;
-    w.status = wst;
-    w.seg_count = wcnt;
-    w.stop_elem = wstop;
-    w.sum_in = wsum_in;
-    w.sum_out = wsum_out;
-    w.end_r = wend_r;
-    w.end_dist = wend_d;
-    w.seg_elem = sk_elem;
-    w.seg_len = sk_len;
-    w.offsets = nullptr;
-    w.out_mode = WALK_STRIDED;
-    int rc = with_length_order(c, w, st, [&]() -> int {
-      API_CUDA(launch_walk(mixed, c->face_order, w, st), "walk");
-      return XDGCU_OK;
-    });
+    const int rc = seg_walk_round(c, mixed, ss, a, B, m, a.max_segs, true, act_next, n_act, S, st,
+                                  no_memory, &R);
     if (rc) return rc;
-    API_CUDA(seg_round_counts(ss, R.walk_t, m, wcnt, a.max_segs, R.off, st), "packed walk counts");
-    int64_t* sums = nullptr;
-    get(&sums, scan_scratch_entries(m));
-    if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
-    API_CUDA(scan_offsets(R.off, m, sums, st), "scan");
-    API_CUDA(cudaMemcpyAsync(&R.total, R.off + m, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "D2H");
-    API_CUDA(cudaStreamSynchronize(st), "sync");
-    get(&R.seg_elem, R.total);
-    get(&R.seg_len, R.total);
-    if (!ok) return set_err(XDGCU_ERR_CUDA, "walk_elements_packed: temporary memory");
-    API_CUDA(seg_pack(m, K, sk_elem, sk_len, R.off, R.seg_elem, R.seg_len, st), "packed walk pack");
-    API_CUDA(seg_advance(ss, R.walk_t, m, K, sk_elem, wcnt, wst, wstop, wend_r, wend_d, wsum_out,
-                         a.max_segs, R.off, R.dst_rel, act_next, n_act, st, true),
-             "packed walk advance");
     rounds.push_back(R);
     API_CUDA(read_count(n_act, &m, st), "packed walk count");
     std::swap(act, act_next);
@@ -2399,44 +2430,39 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   API_CUDA(S.get(&ss.wcount, n), "segments scratch");
   API_CUDA(S.get(&ss.welem, n), "segments scratch");
   API_CUDA(S.get(&ss.paused, n), "segments scratch");
-  // segments per track and round of the single-pass walk (seg_round_k)
-  const int64_t strided_cap = seg_strided_cap(n, c->segments_walk_cap);
-  auto round_k = [&](int64_t walks) -> int32_t {
-    return seg_round_k(walks, strided_cap, c->segments_walk_cap, max_segs);
-  };
   int32_t *act = nullptr, *act_next = nullptr, *counters = nullptr, *eid = nullptr, *eidx = nullptr;
-  int32_t *walk_t = nullptr, *walk_start = nullptr, *out_t = nullptr, *surf = nullptr, *face = nullptr;
-  int32_t *wst = nullptr, *wcnt = nullptr, *wstop = nullptr, *loc = nullptr, *sk_elem = nullptr;
+  int32_t *out_t = nullptr, *surf = nullptr, *face = nullptr, *loc = nullptr;
   double *pts = nullptr, *ray_org = nullptr, *ray_dir = nullptr, *t_hit = nullptr;
-  double *wr = nullptr, *wu = nullptr, *wd = nullptr, *sk_len = nullptr;
-  double *wsum_in = nullptr, *wsum_out = nullptr, *wend_r = nullptr, *wend_d = nullptr;
   API_CUDA(S.get(&act, n), "segments scratch");
   API_CUDA(S.get(&act_next, n), "segments scratch");
   API_CUDA(S.get(&counters, 4), "segments scratch");
   API_CUDA(S.get(&eid, n), "segments scratch");
   API_CUDA(S.get(&eidx, n), "segments scratch");
-  API_CUDA(S.get(&walk_t, n), "segments scratch");
-  API_CUDA(S.get(&walk_start, n), "segments scratch");
   API_CUDA(S.get(&out_t, n), "segments scratch");
   API_CUDA(S.get(&surf, n), "segments scratch");
   API_CUDA(S.get(&face, n), "segments scratch");
-  API_CUDA(S.get(&wst, n), "segments scratch");
-  API_CUDA(S.get(&wcnt, n), "segments scratch");
-  API_CUDA(S.get(&wstop, n), "segments scratch");
   API_CUDA(S.get(&loc, n), "segments scratch");
-  API_CUDA(S.get(&sk_elem, strided_cap), "segments scratch");
-  API_CUDA(S.get(&sk_len, strided_cap), "segments scratch");
   API_CUDA(S.get(&pts, 3 * n), "segments scratch");
   API_CUDA(S.get(&ray_org, 3 * n), "segments scratch");
   API_CUDA(S.get(&ray_dir, 3 * n), "segments scratch");
   API_CUDA(S.get(&t_hit, n), "segments scratch");
-  API_CUDA(S.get(&wr, 3 * n), "segments scratch");
-  API_CUDA(S.get(&wu, 3 * n), "segments scratch");
-  API_CUDA(S.get(&wd, n), "segments scratch");
-  API_CUDA(S.get(&wsum_in, n), "segments scratch");
-  API_CUDA(S.get(&wsum_out, n), "segments scratch");
-  API_CUDA(S.get(&wend_r, 3 * n), "segments scratch");
-  API_CUDA(S.get(&wend_d, n), "segments scratch");
+  // the walk list and the rounds' walk buffers (seg_walk_round)
+  SegWalkBufs B{};
+  B.strided_cap = seg_strided_cap(n, c->segments_walk_cap);
+  API_CUDA(S.get(&B.walk_t, n), "segments scratch");
+  API_CUDA(S.get(&B.walk_start, n), "segments scratch");
+  API_CUDA(S.get(&B.wst, n), "segments scratch");
+  API_CUDA(S.get(&B.wcnt, n), "segments scratch");
+  API_CUDA(S.get(&B.wstop, n), "segments scratch");
+  API_CUDA(S.get(&B.wr, 3 * n), "segments scratch");
+  API_CUDA(S.get(&B.wu, 3 * n), "segments scratch");
+  API_CUDA(S.get(&B.wd, n), "segments scratch");
+  API_CUDA(S.get(&B.wsum_in, n), "segments scratch");
+  API_CUDA(S.get(&B.wsum_out, n), "segments scratch");
+  API_CUDA(S.get(&B.wend_r, 3 * n), "segments scratch");
+  API_CUDA(S.get(&B.wend_d, n), "segments scratch");
+  API_CUDA(S.get(&B.sk_elem, B.strided_cap), "segments scratch");
+  API_CUDA(S.get(&B.sk_len, B.strided_cap), "segments scratch");
   int32_t* n_act = counters;
   int32_t* n_walk = counters + 1;
   int32_t* n_out = counters + 2;
@@ -2456,7 +2482,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
   for (; m > 0 && round < max_rounds; ++round) {
     // paused walks resume; the other active tracks are located
     API_CUDA(cudaMemsetAsync(counters + 1, 0, 3 * sizeof(int32_t), st), "memset");
-    API_CUDA(seg_split(ss, act, m, walk_t, walk_start, n_walk, loc, n_loc, st), "segments split");
+    API_CUDA(seg_split(ss, act, m, B.walk_t, B.walk_start, n_walk, loc, n_loc, st), "segments split");
     int32_t h3[3] = {0, 0, 0};  // n_walk, n_out, n_loc
     API_CUDA(cudaMemcpyAsync(h3, counters + 1, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "D2H");
     API_CUDA(cudaStreamSynchronize(st), "sync");
@@ -2472,7 +2498,7 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
       rc = point_query(c, false, element_tree, nullptr, m_loc, pts, nullptr, eid, eidx, nullptr,
                        precision, st, round > 0);
       if (rc) return rc;
-      API_CUDA(seg_decide(ss, loc, m_loc, eid, eidx, walk_t, walk_start, n_walk, out_t, ray_org,
+      API_CUDA(seg_decide(ss, loc, m_loc, eid, eidx, B.walk_t, B.walk_start, n_walk, out_t, ray_org,
                           ray_dir, n_out, st),
                "segments decide");
       int32_t h2[2] = {0, 0};
@@ -2487,62 +2513,20 @@ int xdgcu_segments_global(xdgcu_ctx* c, int32_t ipc_tree, int32_t element_tree, 
                             nullptr, nullptr, t_hit, surf, face, nullptr, precision, st);
         if (rc) return rc;
         API_CUDA(seg_reenter(ss, out_t, m_out, t_hit, surf, face, c->d_bfe_face.p, c->d_bfe_elem.p,
-                             c->n_bfe, (int32_t)c->n_tet, walk_t, walk_start, n_walk, st),
+                             c->n_bfe, (int32_t)c->n_tet, B.walk_t, B.walk_start, n_walk, st),
                  "segments re-entry");
         API_CUDA(read_count(n_walk, &m_walk, st), "segments count");
       }
     }
     API_CUDA(cudaMemsetAsync(n_act, 0, sizeof(int32_t), st), "memset");
     if (m_walk > 0) {
-      const int32_t K = round_k(m_walk);
-      SegRound R{};
-      R.m = m_walk;
-      API_CUDA(S.get(&R.walk_t, m_walk), "segments scratch");
-      API_CUDA(S.get(&R.off, (int64_t)m_walk + 1), "segments scratch");
-      API_CUDA(S.get(&R.dst_rel, m_walk), "segments scratch");
-      API_CUDA(cudaMemcpyAsync(R.walk_t, walk_t, sizeof(int32_t) * m_walk, cudaMemcpyDeviceToDevice, st),
-               "D2D");
-      API_CUDA(seg_walk_inputs(ss, walk_t, m_walk, wr, wu, wd, wsum_in, st), "segments walk inputs");
       // walk_elements(element, r, u, distance) of the round, one pass, at
-      // most K segments per track into the K-strided buffer; the walk reports
-      // where it stopped and continues each track's sum of lengths
-      WalkArgs a = geo;
-      a.n = m_walk;
-      a.start = walk_start;
-      a.org = wr;
-      a.dir = wu;
-      a.dist = wd;
-      a.max_segs = K;
-      a.status = wst;
-      a.seg_count = wcnt;
-      a.stop_elem = wstop;
-      a.sum_in = wsum_in;
-      a.sum_out = wsum_out;
-      a.end_r = wend_r;
-      a.end_dist = wend_d;
-      a.seg_elem = sk_elem;
-      a.seg_len = sk_len;
-      a.out_mode = WALK_STRIDED;
-      rc = with_length_order(c, a, st, [&]() -> int {
-        API_CUDA(launch_walk(mixed, c->face_order, a, st), "walk");
-        return XDGCU_OK;
-      });
+      // most K segments per track; the walk reports where it stopped and
+      // continues each track's sum of lengths
+      SegRound R{};
+      rc = seg_walk_round(c, mixed, ss, geo, B, m_walk, max_segs, false, act_next, n_act, S, st,
+                          nullptr, &R);
       if (rc) return rc;
-      // the segments each track keeps (max_segs per walk), packed
-      API_CUDA(seg_round_counts(ss, R.walk_t, m_walk, wcnt, max_segs, R.off, st), "segments counts");
-      int64_t* sums = nullptr;
-      API_CUDA(S.get(&sums, scan_scratch_entries(m_walk)), "scan scratch");
-      API_CUDA(scan_offsets(R.off, m_walk, sums, st), "scan");
-      API_CUDA(cudaMemcpyAsync(&R.total, R.off + m_walk, sizeof(int64_t), cudaMemcpyDeviceToHost, st),
-               "D2H");
-      API_CUDA(cudaStreamSynchronize(st), "sync");
-      API_CUDA(S.get(&R.seg_elem, R.total), "segments scratch");
-      API_CUDA(S.get(&R.seg_len, R.total), "segments scratch");
-      API_CUDA(seg_pack(m_walk, K, sk_elem, sk_len, R.off, R.seg_elem, R.seg_len, st),
-               "segments pack");
-      API_CUDA(seg_advance(ss, R.walk_t, m_walk, K, sk_elem, wcnt, wst, wstop, wend_r, wend_d,
-                           wsum_out, max_segs, R.off, R.dst_rel, act_next, n_act, st),
-               "segments advance");
       rounds.push_back(R);
     }
     API_CUDA(read_count(n_act, &m, st), "segments count");
