@@ -405,10 +405,14 @@ int xdgcu_transport_surfaces(xdgcu_ctx* ctx, int64_t n, int32_t* tree, double* p
  *   - n must not exceed XDGCU_NOALLOC_MAX_TRACKS (else XDGCU_ERR_INVALID_ARG);
  *   - all array arguments must be device (or managed) memory;
  *   - all array arguments must be on the context's device;
- *   - it never applies the longest-first track order the allocating walk
- *     uses for batches of at least `walk_sort_min` tracks (that order sorts
- *     the tracks into scratch memory), so `walk_sort_min` has no effect here:
- *     the results are the same, large batches of uneven tracks run slower;
+ *   - it walks every track twice (count, then emit at the scanned offsets:
+ *     the allocating walk's resumed rounds keep their segments in scratch
+ *     memory), and it never applies the longest-first track order the
+ *     allocating walk uses for batches of at least `walk_sort_min` tracks
+ *     (that order sorts the tracks into scratch memory), so
+ *     `walk_sort_min` has no effect here: the results are the same, and
+ *     it runs at about half the allocating walk's rate (2323 against 4664
+ *     Msegs/s on 1e6 tracks of a 750,000-tet cube);
  *   - the first call on a device looks up the static array's device address
  *     (cudaGetSymbolAddress); make that first call before any stream capture.
  *     The address stays valid for the device's primary context: after a
