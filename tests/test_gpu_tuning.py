@@ -221,6 +221,16 @@ def test_node_width_8(cuda, oracle, prec):
     c8, c4 = x8.closest(3, p[:5000], precision=prec), x4.closest(3, p[:5000], precision=prec)
     assert_same(c8[0], c4[0], "closest distance")
     assert_same(c8[1], c4[1], "closest face")
+    # with most points' searches finished by a whole warp (8 children a node)
+    pc = np.concatenate([np.zeros((1, 3)), p[:2000]])
+    x8.rti.set_tuning("closest_step_budget", 4)
+    try:
+        w8 = x8.closest(3, pc, precision=prec)
+    finally:
+        x8.rti.set_tuning("closest_step_budget", 1024)
+    ocd, ocf = oracle.volume_tree(m, 3).closest(pc)
+    assert_same(w8[0], ocd, "closest distance, warp-finished, 8-wide")
+    assert_same(w8[1], ocf, "closest face, warp-finished, 8-wide")
     o8, o4 = x8.occluded(2, p, d, precision=prec), x4.occluded(2, p, d, precision=prec)
     assert_same(o8[0], o4[0], "occluded")
     # back to 4-wide by a rebuild: same results again
