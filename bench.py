@@ -75,6 +75,11 @@ BYTES_NODE = 112            # 4-wide FP32 node: 24 B boxes + 4 B child per child
 BYTES_TRI32 = 40            # 36 B FP32 triangle + 4 B id
 BYTES_TRI64 = 76            # 72 B FP64 triangle + 4 B id (escalations)
 BYTES_IO = 68               # 48 B origin/dir + 4 B tree id in, 8 B t + 4 B surface + 4 B face out
+# FP32 work of one ray (the survey's measurement convention): 110 flops per
+# Plucker triangle test, 12 per box of a W-wide node (slab test)
+FLOPS_TRI = 110
+FLOPS_BOX = 12
+BYTES_IO_ONLY = 64          # the convention's ray I/O: 48 B in, 8 B t + 4 B surface + 4 B status out
 GLOBAL_TRACKS = 1_000_000    # tracks of the global track loop (XDG::segments(start, end))
 GLOBAL_CHECK = 2_000         # of them repeated by the oracle's track loop
 GLOBAL_WORKLOAD = "3_tet_blocks_30^3x6_jitter0.2_gaps_1e6_tracks_uniform_endpoints"
@@ -1362,6 +1367,14 @@ def run_engine(args, rank, world, local):
     fp64_peak = peaks.get("fp64_add_gops")
     walk_fp64_achieved = fp64_ops_per_seg * n_segs / (ms_walk / 1e3) / 1e9
     walk_hbm_achieved = WALK_BYTES_SEG_MIXED * n_segs / (ms_walk / 1e3) / 1e9
+    width = rti.get_tuning("node_width")
+    flops_per_ray = FLOPS_TRI * per_ray["prim"] + FLOPS_BOX * width * per_ray["node"]
+    fp32_peak = 2.0 * peaks["fp32_fma_gops"] / 1e3 if peaks.get("fp32_fma_gops") else None
+    fp32_achieved = flops_per_ray * N_RAYS / (ms_mixed / 1e3) / 1e12
+    fp32_roofline = {"flops_per_ray": flops_per_ray, "achieved": fp32_achieved,
+                     "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": fp32_achieved / fp32_peak if fp32_peak else None,
+                     "peak_kind": "measured in this run: FP32 FMA issue rate x 2 (peaks.cu)"}
     walk_roofline = {
         "bound": "fp64", "kernel": "k_walk<MOAB, mixed>",
         "achieved": walk_fp64_achieved, "peak": fp64_peak, "unit": "GFP64op/s",
@@ -1409,6 +1422,16 @@ def run_engine(args, rank, world, local):
             "peak_kind": f"{peak_kind} HBM copy bandwidth",
             "kernel": f"k_trace<RAY_FIRE, mixed, {rti.get_tuning('trace_occupancy')}>",
             "algorithmic_bytes_per_ray": bytes_per_ray,
+            # the other bounds of the same launch: the algorithmic bytes
+            # against the measured L2 read bandwidth (the tree is served from
+            # L2), FP32 flops against the measured FP32 FMA rate (2 flops
+            # each), and the ray I/O alone
+            "l2": {"achieved": achieved, "peak": peaks.get("l2_read_gbs"), "unit": "GB/s",
+                   "frac": achieved / peaks["l2_read_gbs"] if peaks.get("l2_read_gbs") else None},
+            "fp32": fp32_roofline,
+            "io_only": {"bytes_per_ray": BYTES_IO_ONLY,
+                        "achieved": BYTES_IO_ONLY * N_RAYS / (ms_mixed / 1e3) / 1e9,
+                        "frac": BYTES_IO_ONLY * N_RAYS / (ms_mixed / 1e3) / 1e9 / peak},
         },
         "cpu_baseline": cpu_baseline,
         "e2e": {"value": total_rays / (ms_e2e / 1e3) / 1e6, "unit": "Mrays/s",

@@ -1,6 +1,6 @@
 """IEEE FP32 operations of the kernels, emulated in numpy for the CPU
 certification tests of the mixed path's FP32 filters: correctly rounded
-fused multiply-add, rounding toward zero with flush of subnormals (the
+fused multiply-add (to nearest, and up), rounding toward zero with flush of subnormals (the
 engine's f32_trunc), and directed rounding of FP64 values to FP32."""
 import numpy as np
 
@@ -26,6 +26,24 @@ def fma32(a, b, c):
         mid = np.isfinite(s) & (fd != s) & ((fd + other.astype(np.float64)) * 0.5 == s)
         toward = np.where(err > 0, np.maximum(f, other), np.minimum(f, other))
         return np.where(mid & (err != 0), toward, f).astype(np.float32)
+
+
+def fma32_up(a, b, c):
+    """FP32 fused multiply-add rounded up (__fmaf_ru): the smallest float at
+    or above a b + c.  The FP64 sum s of the exact product and c is within
+    half an FP64 ulp of the exact value; rounding s up is exact unless s is
+    itself a float and the TwoSum error is positive."""
+    a, b, c = (np.asarray(x, dtype=np.float32) for x in (a, b, c))
+    p = a.astype(np.float64) * b.astype(np.float64)
+    c64 = c.astype(np.float64)
+    with np.errstate(over="ignore", invalid="ignore"):
+        s = p + c64
+        bb = s - p
+        err = (p - (s - bb)) + (c64 - bb)
+        f = np.atleast_1d(f32_dir(s, up=True))
+        bump = (f.astype(np.float64) == s) & (err > 0)
+        f[bump] = np.nextafter(f[bump], F(np.inf))
+        return f
 
 
 def f32_trunc(x):

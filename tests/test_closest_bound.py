@@ -25,7 +25,7 @@ from fractions import Fraction
 import numpy as np
 import pytest
 
-from fp32_emul import U, f32_dir, fma32
+from fp32_emul import U, f32_dir, fma32, fma32_up
 
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -137,6 +137,183 @@ def test_bound_never_exceeds_fp64_distance(oracle, cbound):
     assert far.sum() > 1000
     ratio = sv[far] / dd[far]
     assert np.median(ratio) >= 0.9 and np.percentile(ratio, 10) >= 0.5
+
+
+def shaped_flag(v):
+    """The FP32 record's flag (k_tri_gather): |e1 x e2|^2 >= 1e-6 |e1|^2
+    |e2|^2 in the FP64 operations of the build."""
+    e1 = v[:, 1] - v[:, 0]
+    e2 = v[:, 2] - v[:, 0]
+    ss = e1[:, 0] * e1[:, 0] + e1[:, 1] * e1[:, 1] + e1[:, 2] * e1[:, 2]
+    tt = e2[:, 0] * e2[:, 0] + e2[:, 1] * e2[:, 1] + e2[:, 2] * e2[:, 2]
+    st = e1[:, 0] * e2[:, 0] + e1[:, 1] * e2[:, 1] + e1[:, 2] * e2[:, 2]
+    with np.errstate(all="ignore"):
+        det = ss * tt - st * st
+        return (ss * tt > 0) & (ss * tt < 1e300) & (det >= 1e-6 * (ss * tt))
+
+
+def upper_value(pl, v, p, max_abs, edge_check=True, weights=None):
+    """closest_upper_of (queries.cu) restated: the FP32 distance from p to
+    the projection of p onto the triangle clamped into it, from the FP32
+    record (v0 and the FP64 edges rounded to nearest), times 1 + 8u plus the
+    margin, rounded up; given where the triangle is well shaped and p is
+    inside edge plane 0 or 1 by the margin, else +inf.  Also returns the
+    clamped weights."""
+    F = np.float32
+    h, s0, s1, s2 = plane_dists32(pl, p)
+    pabs = np.abs(p.astype(F)).max(1)
+    cmargin = (F(48) * U) * (pabs + max_abs)
+    A = v[:, 0].astype(F)
+    B = (v[:, 1] - v[:, 0]).astype(F)
+    C = (v[:, 2] - v[:, 0]).astype(F)
+    pf = p.astype(F)
+    with np.errstate(all="ignore"):
+        ok = shaped_flag(v) & (h >= 0) & (cmargin > 0)
+        if edge_check:
+            ok &= np.minimum(s0, s1) <= -cmargin
+        w = pf - A
+        dot = lambda a, b: a[:, 0] * b[:, 0] + a[:, 1] * b[:, 1] + a[:, 2] * b[:, 2]  # noqa: E731
+        d11, d12, d22 = dot(B, B), dot(B, C), dot(C, C)
+        w1, w2 = dot(w, B), dot(w, C)
+        den = d11 * d22 - d12 * d12
+        if weights is None:
+            s, t = (d22 * w1 - d12 * w2) / den, (d11 * w2 - d12 * w1) / den
+        else:
+            s, t = weights(A, B, C, pf)
+        s = np.fmax(s, F(0))
+        t = np.fmax(t, F(0))
+        over = ~(fma32_up(s, F(1), t) <= F(1))
+        s2w = np.fmin(s / (s + t), F(1))
+        t2w = f32_dir(F(1) - s2w.astype(np.float64), up=False)
+        s = np.where(over, s2w, s).astype(F)
+        t = np.where(over, t2w, t).astype(F)
+        q = np.stack([fma32(t, C[:, k], fma32(s, B[:, k], A[:, k])) for k in range(3)], 1)
+        d = pf - q
+        d32 = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+        ub = fma32_up(d32, F(1) + F(8) * U, cmargin)
+    return np.where(ok, ub, F(np.inf)).astype(F), s, t
+
+
+def test_upper_bound_never_below_fp64_distance(oracle, cbound):
+    """closest's FP32 upper bound (closest_upper_of), which prunes like a
+    best distance while the exact tests wait, is never below the distance
+    the exact FP64 test (closest.cpp:54-183, through the oracle) gives for
+    the same triangle -- although that test returns a point off the
+    triangle in its region six, where a bound from the geometry alone fails
+    (checked below) -- its weights are a point of the triangle, and it is
+    tight and given for most points over a triangle's face."""
+    rng = np.random.default_rng(31)
+    v, p = _cases(rng, 12000)
+    # degenerate triangles too: repeated vertices, collinear, a point
+    v[:40, 1] = v[:40, 0]
+    v[40:80, 2] = 2 * v[40:80, 1] - v[40:80, 0]
+    v[80:100, 1:] = v[80:100, :1]
+    n = len(v)
+    # points over the face (a third of them near an edge), and points in
+    # v1's wedge beyond edges v0v1 and v1v2 (region six), near its sides
+    w = rng.dirichlet([2, 2, 2], n)
+    ne = rng.random(n) < 0.33
+    w[ne, rng.integers(0, 3, ne.sum())] = 10.0 ** rng.uniform(-9, -2, ne.sum())
+    w /= w.sum(1, keepdims=True)
+    foot = (w[:, :, None] * v).sum(1)
+    nrm = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    with np.errstate(all="ignore"):
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    size = np.abs(v - v.mean(1, keepdims=True)).max((1, 2))
+    over = foot + nrm * (size * 10.0 ** rng.uniform(-3, 1, n))[:, None]
+    over = np.where(np.isfinite(over), over, p)
+    a = rng.uniform(-1.0, 1e-6, n)           # weight of v2, at or below 0
+    b = 1.0 + 10.0 ** rng.uniform(-9, 0, n)  # weights of v1 and v2 summing above 1
+    six = v[:, 0] + (b - a)[:, None] * (v[:, 1] - v[:, 0]) + a[:, None] * (v[:, 2] - v[:, 0])
+    six = six + nrm * (size * 10.0 ** rng.uniform(-6, 0, n))[:, None]
+    six = np.where(np.isfinite(six), six, p)
+    v = np.concatenate([v, v, v])
+    p = np.concatenate([p, over, six])
+    pl = cbound(v)
+    max_abs = np.abs(v).max((1, 2)).astype(np.float32)
+    ub, s, t = upper_value(pl, v, p, max_abs)
+    assert ((s >= 0) & (t >= 0)).all()
+    assert all(Fraction(float(x)) + Fraction(float(y)) <= 1 for x, y in zip(s, t))
+    dd = np.empty(len(v))
+    for i in range(len(v)):
+        r = oracle.closest_on_tri(v[i].reshape(9), p[i])
+        d = r - p[i]
+        dd[i] = np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+    fin = np.isfinite(ub)
+    bad = np.nonzero(fin & ~(ub.astype(np.float64) >= dd))[0]
+    assert len(bad) == 0, f"bound below the distance at {bad[:5]}: {ub[bad[:3]]} vs {dd[bad[:3]]}"
+    for k in range(3):  # degenerate triangles: no bound
+        assert not fin[k * n:k * n + 100].any()
+    # region six is where the exact test is off: the same geometric bound
+    # without the edge condition fails there
+    geo = upper_value(pl, v, p, max_abs, edge_check=False)[0]
+    assert (geo[2 * n:].astype(np.float64) < dd[2 * n:]).sum() >= 5
+    # given for most of the points over well-shaped faces that are large
+    # against the margin, away from the edges, and within 1e-5 (|p| + M)
+    half = slice(n, 2 * n)
+    big = size > 1e-3 * (np.abs(p[half]).max(1) + max_abs[half])
+    good = big & shaped_flag(v[half]) & np.isfinite(pl[half, 0, 3]) & ~ne
+    assert good.sum() > 2000 and fin[half][good].mean() > 0.9
+    slack = (ub[half][fin[half]].astype(np.float64) - dd[half][fin[half]]) / (
+        np.abs(p[half][fin[half]]).max(1) + max_abs[half][fin[half]])
+    assert np.median(slack) < 1e-5
+    # and the exact test does leave the triangle in region six here
+    sx = slice(2 * n, 3 * n)
+    assert (dd[sx] > 1.01 * np.linalg.norm(p[sx] - v[sx, 1], axis=1)).sum() > 100
+
+
+def box_lower_value(v, p, max_abs):
+    """The box bound of closest_record_bounds (queries.cu) restated: the
+    FP32 distance from p to the box of the vertices rebuilt from the FP32
+    record (A, A + B, A + C), times 1 - 8u, less the margin."""
+    F = np.float32
+    A = v[:, 0].astype(F)
+    B = (v[:, 1] - v[:, 0]).astype(F)
+    C = (v[:, 2] - v[:, 0]).astype(F)
+    V1, V2 = A + B, A + C
+    lo = np.minimum(np.minimum(A, V1), V2)
+    hi = np.maximum(np.maximum(A, V1), V2)
+    pf = p.astype(F)
+    with np.errstate(all="ignore"):
+        e = np.maximum(np.maximum(lo - pf, pf - hi), F(0))
+        d = np.sqrt(e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1] + e[:, 2] * e[:, 2])
+        cmargin = (F(48) * U) * (np.abs(pf).max(1) + max_abs)
+        return d * (F(1) - F(8) * U) - cmargin
+
+
+def test_box_lower_bound_never_exceeds_fp64_distance(oracle):
+    """closest's second lower bound (the triangle's box, closest_record_bounds)
+    never exceeds the exact FP64 test's distance (closest.cpp:54-183), in
+    particular in region six, where that test's point is off the triangle;
+    and it is tight for points far from small triangles."""
+    rng = np.random.default_rng(44)
+    v, p = _cases(rng, 12000)
+    n = len(v)
+    nrm = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    with np.errstate(all="ignore"):
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    size = np.abs(v - v.mean(1, keepdims=True)).max((1, 2))
+    a = rng.uniform(-3.0, 1e-6, n)
+    b = 1.0 + 10.0 ** rng.uniform(-9, 0.5, n)
+    six = v[:, 0] + (b - a)[:, None] * (v[:, 1] - v[:, 0]) + a[:, None] * (v[:, 2] - v[:, 0])
+    six = six + nrm * (size * rng.uniform(-2, 2, n))[:, None]
+    six = np.where(np.isfinite(six), six, p)
+    v = np.concatenate([v, v])
+    p = np.concatenate([p, six])
+    max_abs = np.abs(v).max((1, 2)).astype(np.float32)
+    lo = box_lower_value(v, p, max_abs)
+    dd = np.empty(len(v))
+    for i in range(len(v)):
+        r = oracle.closest_on_tri(v[i].reshape(9), p[i])
+        d = r - p[i]
+        dd[i] = np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+    fin = np.isfinite(lo) & np.isfinite(dd)
+    assert fin.mean() > 0.99
+    bad = np.nonzero(fin & (lo.astype(np.float64) > dd))[0]
+    assert len(bad) == 0, f"bound above the distance at {bad[:5]}: {lo[bad[:3]]} vs {dd[bad[:3]]}"
+    size = np.concatenate([size, size])
+    far = fin & (dd > 100 * size) & (dd > 1e3 * U * (np.abs(p).max(1) + max_abs))
+    assert far.sum() > 500 and np.median(lo[far] / dd[far]) > 0.95
 
 
 def test_plane_certificates_exact(cbound):

@@ -161,8 +161,16 @@ __global__ void k_tri_gather(const double* __restrict__ tri_xyz, const int32_t* 
   prim32[3 * (int64_t)j] = make_float4(v0x, v0y, v0z, v0abs);
   prim32[3 * (int64_t)j + 1] = make_float4(__double2float_rn(e1[0]), __double2float_rn(e1[1]),
                                            __double2float_rn(e1[2]), emaxf);
+  // fourth slot: 1 when the triangle is well shaped at v0 for closest's
+  // upper bound, |e1 x e2|^2 >= 1e-6 |e1|^2 |e2|^2 (the determinant of
+  // closest.cpp:60-65 against its two squared lengths)
+  const double ss = e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2];
+  const double tt = e2[0] * e2[0] + e2[1] * e2[1] + e2[2] * e2[2];
+  const double st = e1[0] * e2[0] + e1[1] * e2[1] + e1[2] * e2[2];
+  const double det = ss * tt - st * st;
+  const bool shaped = ss * tt > 0.0 && ss * tt < 1e300 && det >= 1e-6 * (ss * tt);
   prim32[3 * (int64_t)j + 2] = make_float4(__double2float_rn(e2[0]), __double2float_rn(e2[1]),
-                                           __double2float_rn(e2[2]), 0.0f);
+                                           __double2float_rn(e2[2]), shaped ? 1.0f : 0.0f);
 }
 
 // Per global triangle (kTriPrimeStride doubles), the ray-independent terms

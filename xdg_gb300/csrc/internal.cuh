@@ -56,7 +56,8 @@ enum TreeKind : int32_t { TREE_SURFACE = 0, TREE_ELEMENT = 1 };
 // Everything a kernel needs to traverse one tree.  Primitive arrays are in
 // leaf order (the BVH's sorted order):
 //   surface trees: prim32 = 3 float4 per triangle
-//                     (v0.xyz, |v0|_inf), (v1-v0, max edge |.|_inf), (v2-v0, 0)
+//                     (v0.xyz, |v0|_inf), (v1-v0, max edge |.|_inf),
+//                     (v2-v0, 1 if well shaped at v0 for closest's upper bound, else 0)
 //                  prim64 = 10 doubles per triangle (v0, v1, v2, pad)
 //                  prim_ref = global triangle index
 //   element trees: prim64 = 12 doubles per tet (v0..v3), prim_ref = tet index

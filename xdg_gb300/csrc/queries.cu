@@ -24,6 +24,8 @@ constexpr int kBlock = 128;
 // ---------------------------------------------------------------------------
 
 constexpr unsigned kFullMask = 0xffffffffu;
+// closest: candidates a lane keeps for its exact tests after the traversal
+constexpr int kCand = 8;
 
 // The children of record `rec` of inner node `ref` that may hold a facet no
 // farther than `best`: their references in cr and lower bounds of the
@@ -120,18 +122,123 @@ __device__ __forceinline__ int closest_children(const TreeDev& T, int32_t ref, i
 // least 20 u (|p| + M), far beyond the FP64 rounding of the exact test; the
 // triangle is skipped only when it still exceeds the best distance rounded
 // up, so neither the minimum nor its tie rule can change.
+// p's FP32 distances to the face plane (h, unsigned) and beyond the three
+// edge planes (s0..s2, positive outside) of global triangle gtri
+struct PlaneDists {
+  float h, s0, s1, s2;
+};
+__device__ __forceinline__ PlaneDists closest_planes32(const float4* __restrict__ tri_cb,
+                                                       int32_t gtri, float px, float py, float pz) {
+  const float4* cb = tri_cb + 4 * (int64_t)gtri;
+  const float4 pn = __ldg(cb), e0 = __ldg(cb + 1), e1 = __ldg(cb + 2), e2 = __ldg(cb + 3);
+  PlaneDists r;
+  r.h = fabsf(__fmaf_rn(pn.x, px, __fmaf_rn(pn.y, py, __fmaf_rn(pn.z, pz, -pn.w))));
+  r.s0 = __fmaf_rn(e0.x, px, __fmaf_rn(e0.y, py, __fmaf_rn(e0.z, pz, -e0.w)));
+  r.s1 = __fmaf_rn(e1.x, px, __fmaf_rn(e1.y, py, __fmaf_rn(e1.z, pz, -e1.w)));
+  r.s2 = __fmaf_rn(e2.x, px, __fmaf_rn(e2.y, py, __fmaf_rn(e2.z, pz, -e2.w)));
+  return r;
+}
+
+__device__ __forceinline__ float closest_lower_of(const PlaneDists& d, float cmargin) {
+  const float mo = fmaxf(fmaxf(fmaxf(d.s0, d.s1), d.s2), 0.0f);
+  const float lb = __fsqrt_rn(__fmaf_rn(d.h, d.h, mo * mo));
+  return lb * (1.0f - 8.0f * kU32) - cmargin;
+}
+
+__device__ __forceinline__ float closest_lower32(const float4* __restrict__ tri_cb, int32_t gtri,
+                                                 float px, float py, float pz, float cmargin) {
+  return closest_lower_of(closest_planes32(tri_cb, gtri, px, py, pz), cmargin);
+}
+
 __device__ __forceinline__ bool closest_may_win(const float4* __restrict__ tri_cb, int32_t gtri,
                                                 float px, float py, float pz, float cmargin,
                                                 float bestf) {
-  const float4* cb = tri_cb + 4 * (int64_t)gtri;
-  const float4 pn = __ldg(cb), e0 = __ldg(cb + 1), e1 = __ldg(cb + 2), e2 = __ldg(cb + 3);
-  const float h = fabsf(__fmaf_rn(pn.x, px, __fmaf_rn(pn.y, py, __fmaf_rn(pn.z, pz, -pn.w))));
-  const float s0 = __fmaf_rn(e0.x, px, __fmaf_rn(e0.y, py, __fmaf_rn(e0.z, pz, -e0.w)));
-  const float s1 = __fmaf_rn(e1.x, px, __fmaf_rn(e1.y, py, __fmaf_rn(e1.z, pz, -e1.w)));
-  const float s2 = __fmaf_rn(e2.x, px, __fmaf_rn(e2.y, py, __fmaf_rn(e2.z, pz, -e2.w)));
-  const float mo = fmaxf(fmaxf(fmaxf(s0, s1), s2), 0.0f);
-  const float lb = __fsqrt_rn(__fmaf_rn(h, h, mo * mo));
-  return !(lb * (1.0f - 8.0f * kU32) - cmargin > bestf);
+  return !(closest_lower32(tri_cb, gtri, px, py, pz, cmargin) > bestf);
+}
+
+// closest_record_bounds: hi, a certified FP32 upper bound of the distance the exact
+// test (closest_location_on_triangle, closest.cpp:54-183) gives for the
+// leaf-ordered triangle qq, or +inf.  That routine returns the true closest
+// point in its regions zero to five, but in region six (p beyond the edges
+// v0v1 and v1v2 near v1, :155-177) it extrapolates along v1v2 past v1, so a
+// geometric bound does not bound it there.  The bound is given only where
+// the routine certainly does not take region six and computes accurately:
+//  - the triangle is well shaped at v0: (v1-v0)x(v2-v0) squared is at least
+//    1e-6 of |v1-v0|^2 |v2-v0|^2 (a flag in the FP32 record's fourth slot,
+//    set from FP64 at build), so the routine's FP64 region tests and weights
+//    are within about 1e-8 (|p| + M) of exact, in position, and the edge
+//    planes' directions are accurate to about u;
+//  - p's FP32 distance beyond edge plane 0 (v0v1) or 1 (v1v2) is below
+//    -cmargin: with the planes' certificates (face slab 7 u M, the rows
+//    orthonormal to 4 u), the foot of p on the plane is inside that edge's
+//    line by at least 7 u (|p| + M), so the routine's t > 0 or s + t < det
+//    holds in FP64 and region six is not taken.
+// Its result is then the triangle's closest point up to those errors, and
+// any point Q of the triangle bounds it: Q = v0 + s e1 + t e2 with s, t >= 0
+// and s + t <= 1 exactly (the projection of p clamped into the triangle, so
+// that the bound is tight).  The FP32 record holds v0, e1 = v1 - v0 and
+// e2 = v2 - v0 rounded to nearest (each within u |x|, u = 2^-24, |v0| <= M,
+// |e| <= 2M per coordinate, M = max_abs), so Q evaluated by two FMAs is
+// within 9.1 u M of Q per coordinate (16 u M in norm); the FP32 distance is
+// within 3.1 u of |p32 - q32|, and p32 within sqrt(3) u |p| of p.  So
+// d32 (1 + 8u) + 48 u (|p| + M) (cmargin), rounded up, bounds the exact
+// test's distance with about 30 u (|p| + M) to spare.
+//
+// And lo, a certified FP32 lower bound of the same distance from
+// the triangle's bounding box, which the plane bound misses for triangles
+// whose plane passes near p (the "horizon" of a sphere seen from outside:
+// the plane bound there undershoots by a third).  The vertices rebuilt from
+// the FP32 record (A, A + B, A + C) are within 4 u M of the triangle's per
+// coordinate, p32 within u |p| of p, and the FP32 box distance within 3 u of
+// its value, so dist32 (1 - 8u) - cmargin is at most the distance from p to
+// the triangle; and the exact test's point is on the triangle, or in region
+// six farther from p than v1 (the foot of p on the line v1v2 mirrored across
+// v1), so its distance is no smaller.
+struct RecordBounds {
+  float lo, hi;
+};
+__device__ __forceinline__ RecordBounds closest_record_bounds(const PlaneDists& d,
+                                                              const float4* __restrict__ prim32,
+                                                              int32_t qq, float px, float py,
+                                                              float pz, float cmargin) {
+  const float4 A = __ldg(&prim32[3 * (int64_t)qq]);
+  const float4 B = __ldg(&prim32[3 * (int64_t)qq + 1]);
+  const float4 C = __ldg(&prim32[3 * (int64_t)qq + 2]);
+  RecordBounds r;
+  {
+    const float b1x = A.x + B.x, b1y = A.y + B.y, b1z = A.z + B.z;
+    const float b2x = A.x + C.x, b2y = A.y + C.y, b2z = A.z + C.z;
+    const float ex = fmaxf(fmaxf(fminf(fminf(A.x, b1x), b2x) - px, px - fmaxf(fmaxf(A.x, b1x), b2x)), 0.0f);
+    const float ey = fmaxf(fmaxf(fminf(fminf(A.y, b1y), b2y) - py, py - fmaxf(fmaxf(A.y, b1y), b2y)), 0.0f);
+    const float ez = fmaxf(fmaxf(fminf(fminf(A.z, b1z), b2z) - pz, pz - fmaxf(fmaxf(A.z, b1z), b2z)), 0.0f);
+    r.lo = __fsqrt_rn(ex * ex + ey * ey + ez * ez) * (1.0f - 8.0f * kU32) - cmargin;
+  }
+  r.hi = INFINITY;
+  // (a triangle without plane certificates has a NaN face distance)
+  if (!(C.w > 0.0f) || !(d.h >= 0.0f) || !(fminf(d.s0, d.s1) <= -cmargin) || !(cmargin > 0.0f))
+    return r;
+  const float wx = px - A.x, wy = py - A.y, wz = pz - A.z;
+  const float d11 = B.x * B.x + B.y * B.y + B.z * B.z;
+  const float d12 = B.x * C.x + B.y * C.y + B.z * C.z;
+  const float d22 = C.x * C.x + C.y * C.y + C.z * C.z;
+  const float w1 = wx * B.x + wy * B.y + wz * B.z;
+  const float w2 = wx * C.x + wy * C.y + wz * C.z;
+  const float den = d11 * d22 - d12 * d12;
+  // fmaxf of a NaN and 0 is 0
+  float s = fmaxf((d22 * w1 - d12 * w2) / den, 0.0f);
+  float t = fmaxf((d11 * w2 - d12 * w1) / den, 0.0f);
+  // s + t rounded up: at most 1 means the exact sum is too
+  if (!(__fadd_ru(s, t) <= 1.0f)) {
+    s = fminf(s / (s + t), 1.0f);  // (inf / inf is NaN, and fminf gives 1)
+    t = __fsub_rd(1.0f, s);
+  }
+  const float qx = __fmaf_rn(t, C.x, __fmaf_rn(s, B.x, A.x));
+  const float qy = __fmaf_rn(t, C.y, __fmaf_rn(s, B.y, A.y));
+  const float qz = __fmaf_rn(t, C.z, __fmaf_rn(s, B.z, A.z));
+  const float dx = px - qx, dy = py - qy, dz = pz - qz;
+  const float d32 = __fsqrt_rn(dx * dx + dy * dy + dz * dz);
+  r.hi = __fmaf_ru(d32, 1.0f + 8.0f * kU32, cmargin);
+  return r;
 }
 
 // Whether (d, face) replaces (best, best_face): triangle_intersect.cpp:126-133
@@ -155,7 +262,11 @@ __device__ __forceinline__ bool closest_better(double d, int32_t face, double be
 // Mpoints/s with 8 node steps per round; the all-FP64 path, whose every
 // triangle takes the exact test, is best with 1 (4.35 -> 4.5).  Entries
 // popped beyond the best distance are skipped (node visits 74.7 -> 60.5
-// per point).
+// per point).  In the mixed path a triangle's exact test waits, once a
+// certified upper bound of the nearest exact distance is known, until the
+// traversal ends, and runs only if its lower bound is still within the
+// best: most triangles that would have improved the best for a while are
+// never tested.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -197,16 +308,45 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
   // distance has usually shrunk since it was pushed
   float skey[kStackSize];
   int sp = 0;
+  // With the FP32 bounds, the exact tests wait once an upper bound is known:
+  // a triangle whose lower bound is within the bound below joins the lane's
+  // candidates (cl: lower bound, cq: leaf-ordered index), and the
+  // candidates are tested after the traversal, nearest lower bound first.
+  // best_hi, the least certified FP32 upper bound of the candidates' exact
+  // distances (closest_record_bounds), prunes like a best distance: anything
+  // whose lower bound exceeds it is strictly farther than some facet's exact
+  // distance, so it is neither the minimum nor tied with it.  Before any
+  // upper bound, and when the list is full, a triangle takes its exact test
+  // at once.
+  float best_hi = INFINITY;
+  float cl[kCand];
+  int32_t cq[kCand];
+  int nc = 0;
+  // the pruning bound: the best exact distance rounded up, or best_hi
+  auto bound = [&]() { return fminf(__double2float_ru(best), best_hi); };
+  // the exact closest-point test of leaf-ordered triangle qq
+  auto exact = [&](int32_t qq) {
+    if (MIXED) cnt.esc++;
+    d3 v0, v1, v2;
+    load_tri64(T.prim64 + kPrim64Stride * (int64_t)qq, v0, v1, v2);
+    const d3 r = closest64(v0, v1, v2, p);
+    const double dd = dist64(r, p);
+    const int32_t fid = __ldg(&a.tri_face[__ldg(&T.prim_ref[qq])]);
+    if (closest_better(dd, fid, best, best_face)) {
+      best = dd;
+      best_face = fid;
+    }
+  };
   // the next entry; one that can no longer hold a closer facet (its lower
-  // bound above the best distance rounded up to FP32: every facet inside is
-  // strictly farther) becomes CHILD_EMPTY and is skipped
+  // bound above the bound: every facet inside is strictly farther) becomes
+  // CHILD_EMPTY and is skipped
   auto pop = [&]() {
     if (sp == 0) {
       run = false;
       return;
     }
     --sp;
-    ref = skey[sp] > __double2float_ru(best) ? CHILD_EMPTY : stack[sp];
+    ref = skey[sp] > bound() ? CHILD_EMPTY : stack[sp];
   };
 
   while (__any_sync(kFullMask, run)) {
@@ -234,7 +374,8 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
         ++steps;
         int32_t cr[4];
         float ck[4];
-        const int nhit = closest_children<MIXED>(T, ref, rec, p, px, py, pz, pabs, f32ok, best, cr, ck);
+        const int nhit = closest_children<MIXED>(T, ref, rec, p, px, py, pz, pabs, f32ok,
+                                                 fmin(best, (double)best_hi), cr, ck);
         if (sp + nhit > kStackSize) {
           overflow = true;
           break;
@@ -259,14 +400,39 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
     if (leaf) {
       first = leaf_first(ref);
       const int32_t count = leaf_count(ref);
-      const float bestf = __double2float_ru(best);
       for (int32_t q = 0; q < count; ++q) {
         cnt.prim++;
         ++steps;
         if (cbound) {
-          if (!closest_may_win(a.tri_cb, __ldg(&T.prim_ref[first + q]), px, py, pz, cmargin, bestf))
-            continue;
-          cnt.esc++;
+          const int32_t qq = first + q;
+          const PlaneDists pd = closest_planes32(a.tri_cb, __ldg(&T.prim_ref[qq]), px, py, pz);
+          if (closest_lower_of(pd, cmargin) > bound()) continue;
+          const RecordBounds rb = closest_record_bounds(pd, T.prim32, qq, px, py, pz, cmargin);
+          const float lo = fmaxf(closest_lower_of(pd, cmargin), rb.lo);
+          if (lo > bound()) continue;
+          best_hi = fminf(best_hi, rb.hi);
+          // without an upper bound yet the test runs at once: its distance
+          // is the only bound the traversal would have
+          if (best_hi < INFINITY) {
+            if (nc == kCand) {  // drop the candidates the bound now excludes
+              const float b = bound();
+              int w = 0;
+              for (int k = 0; k < kCand; ++k) {
+                if (!(cl[k] > b)) {
+                  cl[w] = cl[k];
+                  cq[w] = cq[k];
+                  ++w;
+                }
+              }
+              nc = w;
+            }
+            if (nc < kCand) {
+              cl[nc] = lo;
+              cq[nc] = qq;
+              ++nc;
+              continue;
+            }
+          }
         }
         need |= 1u << q;
       }
@@ -276,19 +442,38 @@ __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
       if (need != 0u) {
         const int q = __ffs(need) - 1;
         need &= need - 1u;
-        const int32_t qq = first + q;
-        d3 v0, v1, v2;
-        load_tri64(T.prim64 + kPrim64Stride * (int64_t)qq, v0, v1, v2);
-        const d3 r = closest64(v0, v1, v2, p);
-        const double dd = dist64(r, p);
-        const int32_t fid = __ldg(&a.tri_face[__ldg(&T.prim_ref[qq])]);
-        if (closest_better(dd, fid, best, best_face)) {
-          best = dd;
-          best_face = fid;
-        }
+        exact(first + q);
       }
     }
     if (leaf) pop();
+  }
+  // ---- the candidates' exact tests, nearest lower bound first, every
+  // lane's next candidate at once; the rest of a lane's list is dropped at
+  // the first lower bound above the bound ----
+  if (MIXED && __any_sync(kFullMask, nc > 0)) {
+    for (int k = 1; k < nc; ++k) {  // insertion sort by lower bound
+      const float key = cl[k];
+      const int32_t v = cq[k];
+      int j = k - 1;
+      while (j >= 0 && cl[j] > key) {
+        cl[j + 1] = cl[j];
+        cq[j + 1] = cq[j];
+        --j;
+      }
+      cl[j + 1] = key;
+      cq[j + 1] = v;
+    }
+    int nx = 0;
+    while (__any_sync(kFullMask, nx < nc)) {
+      if (nx < nc) {
+        if (cl[nx] > bound()) {
+          nx = nc;
+        } else {
+          exact(cq[nx]);
+          ++nx;
+        }
+      }
+    }
   }
   if (i < a.n) {
     if (a.deferred) a.deferred[i] = deferred ? 1 : 0;
