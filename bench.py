@@ -1055,6 +1055,12 @@ def run_engine(args, rank, world, local):
     ms_clo_lane = timed(torch, clo(MIXED), 3, 1, world, stream)
     rti.set_tuning("closest_step_budget", clo_budget)
     clo_same = clo_same and bool(torch.equal(clo_d, clo_mixed[0]) and torch.equal(clo_f, clo_mixed[1]))
+    # the points in the caller's order instead of the Morton order
+    clo_sort = rti.get_tuning("closest_sort_min")
+    rti.set_tuning("closest_sort_min", 0)
+    ms_clo_unsorted = timed(torch, clo(MIXED), 3, 1, world, stream)
+    rti.set_tuning("closest_sort_min", clo_sort)
+    clo_same = clo_same and bool(torch.equal(clo_d, clo_mixed[0]) and torch.equal(clo_f, clo_mixed[1]))
     del occ_mixed, clo_mixed
 
     # find_volume of the same points: one fused launch vs one launch per volume
@@ -1476,6 +1482,7 @@ def run_engine(args, rank, world, local):
             "fp64_value": dist.sum_over_ranks(n_clo, world) / (ms_clo64 / 1e3) / 1e6,
             "value_without_triangle_bound": dist.sum_over_ranks(n_clo, world) / (ms_clo_nb / 1e3) / 1e6,
             "value_one_lane_per_point": dist.sum_over_ranks(n_clo, world) / (ms_clo_lane / 1e3) / 1e6,
+            "value_caller_order": dist.sum_over_ranks(n_clo, world) / (ms_clo_unsorted / 1e3) / 1e6,
             "mixed_equals_fp64": clo_same,
             "oracle_check": query_oracle.get("closest"),
         },

@@ -522,6 +522,22 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      points of the nested spheres: 25.8 -> 32.0 Mpoints/s
  *                      mixed, 4.45 -> 6.23 FP64).  Results do not depend on
  *                      it
+ *   "closest_sort_min"  closest: batches (or staged chunks) of at least this
+ *                      many points run in the order of [tree | Morton code
+ *                      of the point] (default 65536; 0 = the caller's
+ *                      order), so that the points of a warp share their
+ *                      upper nodes and take similar work; the order is
+ *                      computed in the call's scratch (one radix sort).
+ *                      1e6 points of the nested spheres: 35.9 -> 60.5
+ *                      Mpoints/s mixed, 155 -> 92 ms FP64.  Results do not
+ *                      depend on it
+ *   "find_sort_min"    the same for find_element (default 65536; 1e6 points
+ *                      of the 750,000-tet cube: 0.723 -> 0.700 ms mixed,
+ *                      8.74 -> 8.07 ms FP64).  The ray queries' own order
+ *                      (trace_sort_min) stays off by default: with it,
+ *                      point_in_volume of 1e7 points took 15.9 instead of
+ *                      6.7 ms, the warps' contiguous shares of similar rays
+ *                      being unequal work
  *   "find_node_steps_fp64"  the same for the all-FP64 find_element (default
  *                      16), and for the mixed one when it runs in phases
  *   "scratch_keep_bytes"  the calls' temporary device memory (allocated on

@@ -423,7 +423,7 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
     equidistant from all its triangles), and the same model moved far from
     the origin.  Also with the step budget after which a warp finishes a
     point's search at 1 and 16 steps (nearly every point searched by a warp)
-    and off."""
+    and off, and with the points in Morton order and in the caller's."""
     c = np.array([shift, -0.5 * shift, 0.25 * shift])
     m = synth.Model()
     v, f = synth.icosphere(4, 3.0, center=tuple(c), jitter=1e-3, seed=21)
@@ -459,9 +459,76 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
                     res[f"{prec}, budget {b}"] = x.closest(vol, p, prec)
         finally:
             x.rti.set_tuning("closest_step_budget", budget)
+        # the points in Morton order (every batch) and in the caller's order
+        sort_min = x.rti.get_tuning("closest_sort_min")
+        try:
+            for smin in (1, 0):
+                x.rti.set_tuning("closest_sort_min", smin)
+                for prec in PRECISIONS:
+                    res[f"{prec}, sort_min {smin}"] = x.closest(vol, p, prec)
+        finally:
+            x.rti.set_tuning("closest_sort_min", sort_min)
         for prec, (cd, cf) in res.items():
             assert_same(cf, ocf, f"closest face vol {vol} prec {prec}")
             assert_same(cd, ocd, f"closest distance vol {vol} prec {prec}")
+
+
+def test_closest_triangle_soup_region_six(cuda, oracle):
+    """closest over a soup of random, needle, obtuse and degenerate triangles,
+    with points placed where the reference's closest-point routine leaves the
+    triangle (its region six, beyond edges v0v1 and v1v2 near v1), near
+    vertices and edges, and at random: the mixed path (FP32 lower and upper
+    bounds that defer and skip exact tests) equals FP64 and the oracle bit
+    for bit, so no bound ever prunes the reference's answer."""
+    rng = np.random.default_rng(66)
+    nt = 600
+    c = rng.uniform(-5, 5, (nt, 3))
+    size = 10.0 ** rng.uniform(-1, 0.5, nt)
+    v = c[:, None, :] + rng.normal(size=(nt, 3, 3)) * size[:, None, None]
+    kind = rng.integers(0, 10, nt)
+    t = rng.uniform(0.2, 0.8, nt)
+    nudge = 10.0 ** rng.uniform(-7, -2, nt)
+    needle = kind < 2     # third vertex just off the first edge's line
+    v[needle, 2] = (v[needle, 0] + t[needle, None] * (v[needle, 1] - v[needle, 0])
+                    + (nudge * size)[needle, None] * rng.normal(size=(needle.sum(), 3)))
+    obtuse = kind == 2    # v1 near the middle of v0v2, pushed out a little
+    v[obtuse, 1] = (0.5 * (v[obtuse, 0] + v[obtuse, 2])
+                    + 0.05 * size[obtuse, None] * rng.normal(size=(obtuse.sum(), 3)))
+    degen = kind == 3     # a repeated vertex
+    v[degen, 2] = v[degen, 1]
+    m = synth.Model()
+    verts = v.reshape(-1, 3)
+    faces = np.arange(3 * nt, dtype=np.int32).reshape(nt, 3)
+    m.surfaces.append(synth.Surface(1, verts, faces, np.arange(nt, dtype=np.int32), 1, 2))
+    m.volumes = [1, 2]
+    m.implicit_complement = 2
+    x = XDG(m)
+    x.prepare_raytracer()
+    nrm = np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0])
+    with np.errstate(all="ignore"):
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm = np.where(np.isfinite(nrm), nrm, 0.0)
+    a = rng.uniform(-2.0, 0.0, nt)
+    b = 1.0 + 10.0 ** rng.uniform(-6, 0.3, nt)
+    six = (v[:, 0] + (b - a)[:, None] * (v[:, 1] - v[:, 0]) + a[:, None] * (v[:, 2] - v[:, 0])
+           + nrm * (size * rng.uniform(-1, 1, nt))[:, None])
+    k = rng.integers(0, 3, nt)
+    ends = v[np.arange(nt), k], v[np.arange(nt), (k + 1) % 3]
+    edge = ends[0] + rng.random(nt)[:, None] * (ends[1] - ends[0])
+    off = (size * 10.0 ** rng.uniform(-9, -1, nt))[:, None] * rng.normal(size=(nt, 3))
+    p = np.concatenate([six, v[:, 1] + off, edge + off, rng.uniform(-8, 8, (1500, 3))])
+    ocd, ocf = oracle.volume_tree(m, 1).closest(p)
+    assert (ocf >= 0).all()
+    sort_min = x.rti.get_tuning("closest_sort_min")
+    try:
+        for smin in (1, 0):  # Morton order, and the caller's
+            x.rti.set_tuning("closest_sort_min", smin)
+            for prec in PRECISIONS:
+                cd, cf = x.closest(1, p, prec)
+                assert_same(cf, ocf, f"closest face prec {prec} sort_min {smin}")
+                assert_same(cd, ocd, f"closest distance prec {prec} sort_min {smin}")
+    finally:
+        x.rti.set_tuning("closest_sort_min", sort_min)
 
 
 def test_closest_far_points(cuda, oracle, sphere_box):

@@ -346,9 +346,11 @@ def test_scratch_pool(nested):
 
 def test_find_element_phased(cuda, oracle):
     """The mixed find_element one lane per point (find_element_phased 0) and
-    in warp-synchronous phases (1) give the oracle's element ids and indices,
-    for points inside the cube, on its faces, and on mesh vertices (on the
-    faces of many tets at once, where the lowest element id decides)."""
+    in warp-synchronous phases (1), and both precisions, with the points in
+    Morton order (find_sort_min 1) and in the caller's (0), give the oracle's
+    element ids and indices, for points inside the cube, on its faces, and
+    on mesh vertices (on the faces of many tets at once, where the lowest
+    element id decides)."""
     tm = synth.tet_cube(n=12, size=10.0, jitter=0.2, seed=11)
     m = synth.model_from_tets(tm, np.ones(len(tm.conn), dtype=np.int32))
     x = XDG(m)
@@ -361,16 +363,24 @@ def test_find_element_phased(cuda, oracle):
     p = np.concatenate([inner, face, verts])
     oid, oidx = oracle.TetTree(tm.tet_xyz(), tm.elem_ids).find_element(p)
     assert x.rti.get_tuning("find_element_phased") == 0
+    sort_min = x.rti.get_tuning("find_sort_min")
     try:
         for phased in (0, 1):
             x.rti.set_tuning("find_element_phased", phased)
-            eid, eidx = x.find_element(p, precision=MIXED)
-            assert_same(eid, oid, f"element id, phased={phased}")
-            assert_same(eidx, oidx, f"element index, phased={phased}")
+            for smin in (1, 0):  # the points in Morton order, and in the caller's
+                x.rti.set_tuning("find_sort_min", smin)
+                for prec in (MIXED, FP64):
+                    eid, eidx = x.find_element(p, precision=prec)
+                    what = f"phased={phased} sort_min={smin} {prec}"
+                    assert_same(eid, oid, f"element id, {what}")
+                    assert_same(eidx, oidx, f"element index, {what}")
         with pytest.raises(Exception):
             x.rti.set_tuning("find_element_phased", 2)
+        with pytest.raises(Exception):
+            x.rti.set_tuning("find_sort_min", -1)
     finally:
         x.rti.set_tuning("find_element_phased", 0)
+        x.rti.set_tuning("find_sort_min", sort_min)
     assert (oid >= 0).sum() > 50_000
 
 

@@ -421,6 +421,8 @@ struct xdgcu_ctx {
   int32_t find_phased = 0;  // mixed find_element: 1 runs warp-synchronous phases, 0 one lane per point
   int32_t packed_passes = 1;  // packed walk: 1 walk in resumed rounds, 2 a count walk and an emit walk
   int32_t closest_budget = 1024;  // closest: steps of one lane before a warp takes the point (0: never)
+  int64_t closest_sort_min = 65536;  // closest: batches of at least this many points run in Morton order (0 = never)
+  int64_t find_sort_min = 65536;  // find_element: the same
   int32_t segments_walk_cap = 0;  // segments_global: segments per walk and round (0 = automatic)
   bool pageable_direct = false;
   // host_direct 5: trial calls of the policies kAutoPolicies (in place,
@@ -1684,6 +1686,12 @@ int xdgcu_set_tuning(xdgcu_ctx* c, const char* key, int64_t value) {
       uint64_t zero = 0;
       API_CUDA(cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrUsedMemHigh, &zero), "scratch pool");
     }
+  } else if (k == "closest_sort_min") {
+    if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "closest_sort_min must be >= 0");
+    c->closest_sort_min = value;
+  } else if (k == "find_sort_min") {
+    if (value < 0) return set_err(XDGCU_ERR_INVALID_ARG, "find_sort_min must be >= 0");
+    c->find_sort_min = value;
   } else if (k == "closest_step_budget") {
     if (value < 0 || value > (1 << 30))
       return set_err(XDGCU_ERR_INVALID_ARG, "closest_step_budget must be 0..2^30");
@@ -1753,6 +1761,8 @@ int xdgcu_get_tuning(const xdgcu_ctx* c, const char* key, int64_t* value) {
   else if (k == "find_element_phased") *value = c->find_phased;
   else if (k == "packed_walk_passes") *value = c->packed_passes;
   else if (k == "closest_step_budget") *value = c->closest_budget;
+  else if (k == "closest_sort_min") *value = c->closest_sort_min;
+  else if (k == "find_sort_min") *value = c->find_sort_min;
   else if (k == "scratch_keep_bytes") *value = c->keep_bytes;
   else if (k == "scratch_bytes_reserved" || k == "scratch_bytes_high") {
     uint64_t v = 0;
@@ -1986,6 +1996,33 @@ int xdgcu_occluded(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t
 
 // phased: the mixed find_element in warp-synchronous phases whatever the
 // context's find_element_phased says (points known to lie on tet faces)
+// A closest or find_element launch over one batch: when the batch has at
+// least closest_sort_min (find_sort_min) points, in the order of [tree |
+// Morton code of the point] (ray_order without directions, in
+// stream-ordered scratch freed after the launch), so that the points of a
+// warp share their upper nodes and take similar work.
+static cudaError_t launch_points_ordered(xdgcu_ctx* c, bool closest, bool mixed, PointArgs a,
+                                         double extent, bool phased, cudaStream_t s) {
+  a.order = nullptr;
+  const int64_t smin = closest ? c->closest_sort_min : c->find_sort_min;
+  const bool sort = smin > 0 && a.n >= smin && a.n < ((int64_t)1 << 31) && extent > 0.0;
+  auto launch = [&]() {
+    return closest ? launch_closest(mixed, a, s) : launch_find_element(mixed, a, s, phased);
+  };
+  if (!sort) return launch();
+  const size_t ord_bytes = (sizeof(int32_t) * (size_t)a.n + 255) & ~(size_t)255;
+  const size_t scr = ray_order_scratch_bytes(a.n);
+  char* buf = nullptr;
+  cudaError_t e = scratch_alloc(c, (void**)&buf, ord_bytes + scr, s);
+  if (e != cudaSuccess) return e;
+  e = ray_order(a.pts, nullptr, a.ray_trees, a.n_trees, a.n, extent, (int32_t*)buf,
+                buf + ord_bytes, scr, s);
+  a.order = (const int32_t*)buf;
+  if (e == cudaSuccess) e = launch();
+  const cudaError_t f = cudaFreeAsync(buf, s);
+  return e != cudaSuccess ? e : f;
+}
+
 static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* ray_trees,
                        int64_t n, const double* pts, double* dist_out, int32_t* id_out,
                        int32_t* index_out, int32_t* status, int32_t precision, void* stream,
@@ -2035,9 +2072,18 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
     if (e == cudaSuccess) a.step_budget = c->closest_budget;
     return e;
   };
+  // the bounds of the trees queried, for the points' Morton order
+  double extent = 0.0;
+  {
+    const auto& trees = closest ? c->surf_trees : c->elem_trees;
+    if (ray_trees) {
+      for (auto& t : trees) extent = std::max(extent, (double)t->dev.max_abs);
+    } else {
+      extent = (double)trees[tree - 1]->dev.max_abs;
+    }
+  }
   auto launch = [&]() -> cudaError_t {
-    return closest ? launch_closest(precision == XDGCU_MIXED, a, st)
-                   : launch_find_element(precision == XDGCU_MIXED, a, st, phased);
+    return launch_points_ordered(c, closest, precision == XDGCU_MIXED, a, extent, phased, st);
   };
   if (kind == 1) {
     a.ray_trees = ray_trees;
@@ -2083,8 +2129,8 @@ static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* 
                         b.def_best = a.def_best + first;
                         b.def_face = a.def_face + first;
                       }
-                      return closest ? launch_closest(precision == XDGCU_MIXED, b, cs)
-                                     : launch_find_element(precision == XDGCU_MIXED, b, cs, phased);
+                      return launch_points_ordered(c, closest, precision == XDGCU_MIXED, b,
+                                                   extent, phased, cs);
                     });
 }
 

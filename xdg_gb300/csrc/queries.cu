@@ -24,6 +24,16 @@ constexpr int kBlock = 128;
 // ---------------------------------------------------------------------------
 
 constexpr unsigned kFullMask = 0xffffffffu;
+
+// The point a thread of a point-query launch takes: its position in the
+// launch, or the entry of a.order there (a point index; an entry out of
+// range takes no point).
+__device__ __forceinline__ int64_t point_index(const PointArgs& a) {
+  const int64_t pos = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (!a.order || pos >= a.n) return pos;
+  const int32_t o = __ldg(&a.order[pos]);
+  return o >= 0 ? (int64_t)o : a.n;
+}
 // closest: candidates a lane keeps for its exact tests after the traversal
 constexpr int kCand = 8;
 
@@ -269,7 +279,7 @@ __device__ __forceinline__ bool closest_better(double d, int32_t face, double be
 // never tested.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = point_index(a);
   Counters cnt = {0, 0, 0, 0};
   double best = INFTY;
   int32_t best_face = -1;
@@ -655,7 +665,7 @@ __global__ void __launch_bounds__(32) k_closest_coop(PointArgs a) {
 // take the exact test, the phases win: 445 against 198 Mpoints/s.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_find_element_lane(PointArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = point_index(a);
   Counters cnt = {0, 0, 0, 0};
   if (i < a.n) {
     const int32_t tid = a.ray_trees ? a.ray_trees[i] : a.tree;
@@ -774,7 +784,7 @@ __global__ void __launch_bounds__(kBlock) k_find_element_lane(PointArgs a) {
 // so does the mixed path for points on tet faces (launch_find_element).
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_find_element(PointArgs a) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i = point_index(a);
   Counters cnt = {0, 0, 0, 0};
   int32_t best_id = -1, best_idx = -1;
   int32_t st = RAY_OK;

@@ -109,6 +109,9 @@ struct PointArgs {
   int8_t* deferred;
   double* def_best;
   int32_t* def_face;
+  // optional: position k of the launch takes point order[k] (a permutation
+  // of 0..n-1; closest and find_element); results go to the point's own index
+  const int32_t* order;
   double* dist_out;
   int32_t* id_out;
   int32_t* index_out;
