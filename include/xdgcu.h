@@ -511,7 +511,9 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      reaches.  Results do not depend on it
  *   "closest_node_steps"  closest, mixed: inner-node steps each lane takes
  *                      before the warp's lanes bound and test the triangles of
- *                      the leaves they hold together (1..64, default 8)
+ *                      the leaves they hold together (1..64, default 4;
+ *                      with the points in Morton order 4 ran 1e6 points in
+ *                      15.4 ms, 8 in 16.6, 2 in 15.6, 16 in 17.4)
  *   "closest_node_steps_fp64"  the same for the all-FP64 closest (default 1)
  *   "closest_step_budget"  closest: node records and triangles a lane visits
  *                      for one point (default 1024; 0 = no limit) before the

@@ -415,7 +415,7 @@ struct xdgcu_ctx {
   int32_t walk_edge_table = 1;  // mixed walk: FP64 edge coordinates from the edge table
   int32_t trace_edge_table = 1;  // mixed traversal: FP64 triangle terms from d_tri_prime
   int32_t closest_bound = 1;     // mixed closest: FP32 triangle bound from d_tri_cb
-  int32_t closest_node_steps = 8;       // closest: inner-node steps between leaf phases (mixed)
+  int32_t closest_node_steps = 4;       // closest: inner-node steps between leaf phases (mixed)
   int32_t closest_node_steps_fp64 = 1;  // the same, all-FP64 path
   int32_t find_node_steps_fp64 = 16;    // find_element in phases (all-FP64, or find_phased): the same
   int32_t find_phased = 0;  // mixed find_element: 1 runs warp-synchronous phases, 0 one lane per point
