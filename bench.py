@@ -49,7 +49,10 @@ WORKLOAD = "nested_spheres_8x_icosphere_L6_jitter1e-3_1e7_rays"
 WALK_WORKLOAD = "tet_cube_50^3x6_kuhn_jitter0.2_1e6_tracks_exp5"
 MANY_SURFACES = 256
 MANY_WORKLOAD = "256_surfaces_sphere_torus_tris_10^U(3,5.7)_rays_10^U(3,6)"
-TUNE_RAYS = 1_000_000       # autotuner sample (same distribution, its own seed)
+TUNE_RAYS = 10_000_000      # autotuner sample of the headline: its size and distribution, its own
+                            # seed (on a 1e6 sample static chunks won; on 1e7 rays the work queue
+                            # does, by about 3 %)
+TUNE_RAYS_MANY = 1_000_000  # autotuner sample of the many-surface rays
 TUNE_TRACKS = 1_000_000     # the walk's length order pays off only on large batches
 TRACE_KEYS = ("node_width", "leaf_max", "trace_occupancy", "trace_stack", "trace_node_iters",
               "trace_node_iters_fp64", "trace_flush_wait", "trace_grab", "trace_sort_min")
@@ -379,7 +382,7 @@ def bench_many_surfaces(torch, L, dev, stream, args, rank, world):
     tuned = None
     if args.autotune:
         from xdg_gb300.engine import QUERY_RAY_FIRE
-        sel = torch.arange(0, n, max(1, n // TUNE_RAYS), device=dev)
+        sel = torch.arange(0, n, max(1, n // TUNE_RAYS_MANY), device=dev)
         t1 = time.perf_counter()
         _, tv = rti.autotune_trace(QUERY_RAY_FIRE, 0, o[sel], d[sel], precision=MIXED,
                                    ray_trees=trees[sel], reps=3)
