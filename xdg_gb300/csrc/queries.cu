@@ -276,7 +276,9 @@ __device__ __forceinline__ bool closest_better(double d, int32_t face, double be
 // certified upper bound of the nearest exact distance is known, until the
 // traversal ends, and runs only if its lower bound is still within the
 // best: most triangles that would have improved the best for a while are
-// never tested.
+// never tested.  A lane keeps its point to the end, so a warp takes as long
+// as its slowest point: large batches run in the [tree | Morton code] order
+// a.order gives (point_index), whose neighbouring points take similar work.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock) k_closest(PointArgs a) {
   const int64_t i = point_index(a);
