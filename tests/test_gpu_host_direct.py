@@ -9,8 +9,8 @@ host_direct setting (2 keeps both kinds in place; 3 stages the page-locked
 arrays of this large call in overlapping chunks; 4 stages only its
 page-locked inputs and writes the outputs in place; staged chunks' kernels
 alternate between two streams; 5, the default, picks 2, 3 or 4 by timing the
-first large calls).  The
-packed tet walk and the walk_elements particle loop
+first large calls), and with the node steps of in-place launches
+(trace_node_iters_direct) varied.  The packed tet walk and the walk_elements particle loop
 (whose atomic tally is always staged) are checked the same way.
 """
 import ctypes
@@ -86,6 +86,7 @@ def test_ray_fire_host_buffers(cuda, rays, prec):
         torch.cuda.synchronize()
         return [t.cpu().numpy() for t in outs]
 
+    old_iters = rti.get_tuning("trace_node_iters_direct")
     try:
         ref = fire("device", 1)
         assert (ref[1] >= 0).mean() > 0.5
@@ -94,8 +95,15 @@ def test_ray_fire_host_buffers(cuda, rays, prec):
                 got = fire(kind, direct)
                 for a, b, what in zip(got, ref, ("t", "surface", "face", "status")):
                     assert np.array_equal(a, b), f"{kind} host_direct={direct}: {what}"
+        # the node steps of launches reading their rays in place
+        for iters in (1, 3, 16):
+            rti.set_tuning("trace_node_iters_direct", iters)
+            got = fire("pinned", 2)
+            for a, b, what in zip(got, ref, ("t", "surface", "face", "status")):
+                assert np.array_equal(a, b), f"trace_node_iters_direct={iters}: {what}"
     finally:
         rti.set_tuning("host_direct", old)
+        rti.set_tuning("trace_node_iters_direct", old_iters)
 
 
 def test_automatic_policy_choice(cuda, rays):

@@ -29,7 +29,7 @@ TUNING_KEYS = ("trace_occupancy", "trace_node_iters", "trace_node_iters_fp64",
                "closest_node_steps", "closest_node_steps_fp64", "find_node_steps_fp64",
                "segments_walk_cap", "find_element_phased", "packed_walk_passes",
                "closest_step_budget", "scratch_keep_bytes", "closest_sort_min",
-               "find_sort_min")
+               "find_sort_min", "trace_node_iters_direct")
 
 INFTY = np.finfo(np.float64).max
 TINY_BIT = 1e-10  # constants.h:32
