@@ -450,10 +450,10 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *   "trace_node_iters_fp64"  the same for the all-FP64 path
  *   "trace_node_iters_direct"  the same for mixed calls whose rays the
  *                      kernel reads in place from host memory (host_direct;
- *                      default 8).  The best setting differs: 1e7 rays of
+ *                      default 6).  The best setting differs: 1e7 rays of
  *                      the nested spheres ran 6.45 ms from device arrays
- *                      with 4 steps (6.64 with 8) but 7.08-7.13 ms in place
- *                      with 8 (7.39 with 4)
+ *                      with 4 steps (6.64 with 8) but in place 6.93 ms with
+ *                      6, 7.03 with 8, 7.39 with 4 and 7.48 with 12
  *   "trace_flush_wait" number of lanes (1..32, default 4) whose rays wait
  *                      only on queued FP64 candidate tests before the warp
  *                      drains a partly filled queue

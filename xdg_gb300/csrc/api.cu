@@ -393,7 +393,7 @@ struct xdgcu_ctx {
   int32_t trace_occupancy = 4;
   int32_t trace_node_iters = 8;       // mixed precision
   int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
-  int32_t trace_node_iters_direct = 8;  // mixed launches reading their rays in place from host memory
+  int32_t trace_node_iters_direct = 6;  // mixed launches reading their rays in place from host memory
   int32_t trace_flush_wait = 4;
   int32_t trace_stack = 40;      // shared-memory stack entries per lane
   int32_t trace_grab = 0;        // 0: one contiguous chunk per warp; > 0: device work queue
@@ -1929,8 +1929,8 @@ static int surface_query(xdgcu_ctx* c, int mode, int32_t tree, const int32_t* ra
         b.dist_out = (double*)at(R_d, first);
         b.status = (int32_t*)at(R_st, first);
         // rays read in place from host memory take their own node steps per
-        // leaf phase (1e7 rays: 8 steps 7.08-7.13 ms against 7.39 with 4, the
-        // device arrays' best at 6.45 ms)
+        // leaf phase (1e7 rays: 6 steps 6.93 ms, 8 7.03, 4 7.39, 12 7.48,
+        // while from device arrays 4 steps were best, 6.45 ms)
         if (mixed && R_org.direct) b.node_iters = c->trace_node_iters_direct;
         // a chunk's launch takes rays from the work queue, so its tail is short
         return launch_trace(c, mode, mixed, b, extent, cs, chunked ? kChunkGrab : 0);
