@@ -446,7 +446,12 @@ int xdgcu_get_counters(xdgcu_ctx* ctx, int64_t counters[8]);
  *                      registers)
  *   "trace_node_iters" inner-node steps a lane takes between two leaf phases
  *                      of the warp-synchronous traversal, mixed precision
- *                      (1..64, default 8; the FP64 path's default is 1)
+ *                      (1..64, default 4; the FP64 path's default is 1).  On
+ *                      the nested spheres every query ran fastest with 4 (1e7
+ *                      rays, ms with 2/4/8/16 steps: ray_fire 7.36/6.50/
+ *                      6.70/8.03, point_in_volume 7.05/6.23/6.41/7.71,
+ *                      occluded 5.52/4.90/5.15/6.26, find_volume 22.6/22.1/
+ *                      24.5/29.9)
  *   "trace_node_iters_fp64"  the same for the all-FP64 path
  *   "trace_node_iters_direct"  the same for mixed calls whose rays the
  *                      kernel reads in place from host memory (host_direct;

@@ -391,7 +391,7 @@ struct xdgcu_ctx {
   bool has_volume_map = false;
   // tuning (xdgcu_set_tuning)
   int32_t trace_occupancy = 4;
-  int32_t trace_node_iters = 8;       // mixed precision
+  int32_t trace_node_iters = 4;       // mixed precision
   int32_t trace_node_iters_fp64 = 1;  // all-FP64 path
   int32_t trace_node_iters_direct = 6;  // mixed launches reading their rays in place from host memory
   int32_t trace_flush_wait = 4;
