@@ -2004,8 +2004,6 @@ int xdgcu_occluded(xdgcu_ctx* c, int32_t tree, const int32_t* ray_trees, int64_t
 // point queries
 // ---------------------------------------------------------------------------
 
-// phased: the mixed find_element in warp-synchronous phases whatever the
-// context's find_element_phased says (points known to lie on tet faces)
 // A closest or find_element launch over one batch: when the batch has at
 // least closest_sort_min (find_sort_min) points, in the order of [tree |
 // Morton code of the point] (ray_order without directions, in
@@ -2033,6 +2031,8 @@ static cudaError_t launch_points_ordered(xdgcu_ctx* c, bool closest, bool mixed,
   return e != cudaSuccess ? e : f;
 }
 
+// phased: the mixed find_element in warp-synchronous phases whatever the
+// context's find_element_phased says (points known to lie on tet faces)
 static int point_query(xdgcu_ctx* c, bool closest, int32_t tree, const int32_t* ray_trees,
                        int64_t n, const double* pts, double* dist_out, int32_t* id_out,
                        int32_t* index_out, int32_t* status, int32_t precision, void* stream,
