@@ -119,19 +119,6 @@ __device__ __forceinline__ int closest_children(const TreeDev& T, int32_t ref, i
   return nhit;
 }
 
-// Whether the triangle `gtri` may be no farther than `bestf` (the best
-// distance rounded up to FP32) by the certified FP32 lower bound of
-// the point's distance to it (planes from tri_cbound): sqrt(h^2 + m^2) with
-// h the distance to its face plane and m the largest distance beyond one of
-// its edge planes.  With p exact, the triangle lies within 8 u M of the face
-// plane and inside the edge planes, and the rows are orthonormal to 4 u, so
-// the distance is at least that root less 8 u M, over 1 + 6 u.  The FP32
-// evaluation (p's rounding and three FMAs) is within about 7 u (|p| + M) of h
-// and of each edge distance (M = max_abs).  The bound, less 48 u (|p| + M)
-// (cmargin) and the rounding of the root, undershoots the distance by at
-// least 20 u (|p| + M), far beyond the FP64 rounding of the exact test; the
-// triangle is skipped only when it still exceeds the best distance rounded
-// up, so neither the minimum nor its tie rule can change.
 // p's FP32 distances to the face plane (h, unsigned) and beyond the three
 // edge planes (s0..s2, positive outside) of global triangle gtri
 struct PlaneDists {
@@ -149,6 +136,19 @@ __device__ __forceinline__ PlaneDists closest_planes32(const float4* __restrict_
   return r;
 }
 
+// closest_lower_of: the certified FP32 lower bound of the point's distance
+// to a triangle, and closest_may_win: whether the triangle may be no farther
+// than `bestf` (the best distance rounded up to FP32) by it.  From the planes
+// of tri_cbound: sqrt(h^2 + m^2) with h the distance to its face plane and m
+// the largest distance beyond one of its edge planes.  With p exact, the triangle lies within 8 u M of the face
+// plane and inside the edge planes, and the rows are orthonormal to 4 u, so
+// the distance is at least that root less 8 u M, over 1 + 6 u.  The FP32
+// evaluation (p's rounding and three FMAs) is within about 7 u (|p| + M) of h
+// and of each edge distance (M = max_abs).  The bound, less 48 u (|p| + M)
+// (cmargin) and the rounding of the root, undershoots the distance by at
+// least 20 u (|p| + M), far beyond the FP64 rounding of the exact test; the
+// triangle is skipped only when it still exceeds the best distance rounded
+// up, so neither the minimum nor its tie rule can change.
 __device__ __forceinline__ float closest_lower_of(const PlaneDists& d, float cmargin) {
   const float mo = fmaxf(fmaxf(fmaxf(d.s0, d.s1), d.s2), 0.0f);
   const float lb = __fsqrt_rn(__fmaf_rn(d.h, d.h, mo * mo));
@@ -166,10 +166,10 @@ __device__ __forceinline__ bool closest_may_win(const float4* __restrict__ tri_c
   return !(closest_lower32(tri_cb, gtri, px, py, pz, cmargin) > bestf);
 }
 
-// closest_record_bounds: hi, a certified FP32 upper bound of the distance the exact
-// test (closest_location_on_triangle, closest.cpp:54-183) gives for the
-// leaf-ordered triangle qq, or +inf.  That routine returns the true closest
-// point in its regions zero to five, but in region six (p beyond the edges
+// closest_record_bounds: hi, a certified FP32 upper bound of the distance
+// the exact test (closest_location_on_triangle, closest.cpp:54-183) gives
+// for the leaf-ordered triangle qq, or +inf.  That routine returns the true
+// closest point in its regions zero to five, but in region six (p beyond the edges
 // v0v1 and v1v2 near v1, :155-177) it extrapolates along v1v2 past v1, so a
 // geometric bound does not bound it there.  The bound is given only where
 // the routine certainly does not take region six and computes accurately:
