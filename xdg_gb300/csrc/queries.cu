@@ -136,19 +136,20 @@ __device__ __forceinline__ PlaneDists closest_planes32(const float4* __restrict_
   return r;
 }
 
-// closest_lower_of: the certified FP32 lower bound of the point's distance
-// to a triangle, and closest_may_win: whether the triangle may be no farther
-// than `bestf` (the best distance rounded up to FP32) by it.  From the planes
-// of tri_cbound: sqrt(h^2 + m^2) with h the distance to its face plane and m
-// the largest distance beyond one of its edge planes.  With p exact, the triangle lies within 8 u M of the face
-// plane and inside the edge planes, and the rows are orthonormal to 4 u, so
-// the distance is at least that root less 8 u M, over 1 + 6 u.  The FP32
-// evaluation (p's rounding and three FMAs) is within about 7 u (|p| + M) of h
-// and of each edge distance (M = max_abs).  The bound, less 48 u (|p| + M)
-// (cmargin) and the rounding of the root, undershoots the distance by at
-// least 20 u (|p| + M), far beyond the FP64 rounding of the exact test; the
-// triangle is skipped only when it still exceeds the best distance rounded
-// up, so neither the minimum nor its tie rule can change.
+// closest_lower_of: the certified FP32 lower bound of the point's distance to
+// a triangle, and closest_may_win: whether the triangle may be no farther than
+// `bestf` (the best distance rounded up to FP32) by it.  From the planes of
+// tri_cbound: sqrt(h^2 + m^2) with h the distance to its face plane and m the
+// largest distance beyond one of its edge planes.  With p exact, the triangle
+// lies within 8 u M of the face plane and inside the edge planes, and the rows
+// are orthonormal to 4 u, so the distance is at least that root less 8 u M,
+// over 1 + 6 u.  The FP32 evaluation (p's rounding and three FMAs) is within
+// about 7 u (|p| + M) of h and of each edge distance (M = max_abs).  The
+// bound, less 48 u (|p| + M) (cmargin) and the rounding of the root,
+// undershoots the distance by at least 20 u (|p| + M), far beyond the FP64
+// rounding of the exact test; the triangle is skipped only when it still
+// exceeds the best distance rounded up, so neither the minimum nor its tie
+// rule can change.
 __device__ __forceinline__ float closest_lower_of(const PlaneDists& d, float cmargin) {
   const float mo = fmaxf(fmaxf(fmaxf(d.s0, d.s1), d.s2), 0.0f);
   const float lb = __fsqrt_rn(__fmaf_rn(d.h, d.h, mo * mo));
@@ -218,9 +219,13 @@ __device__ __forceinline__ RecordBounds closest_record_bounds(const PlaneDists& 
   {
     const float b1x = A.x + B.x, b1y = A.y + B.y, b1z = A.z + B.z;
     const float b2x = A.x + C.x, b2y = A.y + C.y, b2z = A.z + C.z;
-    const float ex = fmaxf(fmaxf(fminf(fminf(A.x, b1x), b2x) - px, px - fmaxf(fmaxf(A.x, b1x), b2x)), 0.0f);
-    const float ey = fmaxf(fmaxf(fminf(fminf(A.y, b1y), b2y) - py, py - fmaxf(fmaxf(A.y, b1y), b2y)), 0.0f);
-    const float ez = fmaxf(fmaxf(fminf(fminf(A.z, b1z), b2z) - pz, pz - fmaxf(fmaxf(A.z, b1z), b2z)), 0.0f);
+    // the point's distance beyond the box of the three vertices, per axis
+    auto out = [](float a, float b, float c, float q) {
+      return fmaxf(fmaxf(fminf(fminf(a, b), c) - q, q - fmaxf(fmaxf(a, b), c)), 0.0f);
+    };
+    const float ex = out(A.x, b1x, b2x, px);
+    const float ey = out(A.y, b1y, b2y, py);
+    const float ez = out(A.z, b1z, b2z, pz);
     r.lo = __fsqrt_rn(ex * ex + ey * ey + ez * ez) * (1.0f - 8.0f * kU32) - cmargin;
   }
   r.hi = INFINITY;
