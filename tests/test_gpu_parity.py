@@ -459,15 +459,21 @@ def test_closest_ties_and_offset_mesh(cuda, oracle, shift):
                     res[f"{prec}, budget {b}"] = x.closest(vol, p, prec)
         finally:
             x.rti.set_tuning("closest_step_budget", budget)
-        # the points in Morton order (every batch) and in the caller's order
+        # the points in Morton order (every batch) and in the caller's order,
+        # and in Morton order with nearly every point finished by a warp
         sort_min = x.rti.get_tuning("closest_sort_min")
         try:
             for smin in (1, 0):
                 x.rti.set_tuning("closest_sort_min", smin)
                 for prec in PRECISIONS:
                     res[f"{prec}, sort_min {smin}"] = x.closest(vol, p, prec)
+            x.rti.set_tuning("closest_sort_min", 1)
+            x.rti.set_tuning("closest_step_budget", 1)
+            for prec in PRECISIONS:
+                res[f"{prec}, sort_min 1, budget 1"] = x.closest(vol, p, prec)
         finally:
             x.rti.set_tuning("closest_sort_min", sort_min)
+            x.rti.set_tuning("closest_step_budget", budget)
         for prec, (cd, cf) in res.items():
             assert_same(cf, ocf, f"closest face vol {vol} prec {prec}")
             assert_same(cd, ocd, f"closest distance vol {vol} prec {prec}")
